@@ -1,0 +1,409 @@
+// ggks_api.cu -- contexts, workspace management and the extern "C" entry
+// points declared in include/ggks.h.
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "ggks_internal.h"
+
+namespace ggks {
+
+// ---------------------------------------------------------------------------
+// small kernels owned by this unit
+// ---------------------------------------------------------------------------
+// top-k requests: output i receives the (i+1)-th largest, i.e. ascending rank
+// n-1-i (multiselectTimingFunctions.cu:207-209 builds k = 1..K for this)
+__global__ void k_make_topk_reqs(Req *reqs, uint64_t n, uint32_t K) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < K) {
+    Req r;
+    r.rank = (uint32_t)(n - 1 - i);
+    r.out = i;
+    reqs[i] = r;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// context and workspace
+// ---------------------------------------------------------------------------
+int from_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return GGKS_OK;
+  if (e == cudaErrorMemoryAllocation) return GGKS_OOM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return GGKS_NO_DEVICE;
+  return GGKS_CUDA_ERROR;
+}
+
+Context::~Context() {
+  int cur = -1;
+  cudaGetDevice(&cur);
+  cudaSetDevice(device);
+  child.reset();
+  if (stream) cudaStreamSynchronize(stream);
+  if (arena) cudaFree(arena);
+  if (surv) cudaFree(surv);
+  if (dvec) cudaFree(dvec);
+  if (pin) cudaFreeHost(pin);
+  if (events_ready) {
+    for (int i = 0; i < GGKS_NUM_PASSES; ++i) {
+      cudaEventDestroy(ev0[i]);
+      cudaEventDestroy(ev1[i]);
+    }
+  }
+  if (copy_done) cudaEventDestroy(copy_done);
+  if (stream && depth == 0) cudaStreamDestroy(stream);
+  if (cur >= 0) cudaSetDevice(cur);
+}
+
+int context_init(Context &ctx, int device) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return GGKS_NO_DEVICE;
+  if (device < 0 || device >= count) return GGKS_INVALID_ARG;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return from_cuda(e);
+  ctx.device = device;
+  e = cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&ctx.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx.stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx.copy_done, cudaEventDisableTiming);
+  return from_cuda(e);
+}
+
+static cudaError_t grow(void **p, size_t *have, size_t need, bool zero) {
+  if (need <= *have && *p) return cudaSuccess;
+  size_t want = need + need / 4 + 4096;
+  if (*p) {
+    cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+  }
+  cudaError_t e = cudaMalloc(p, want);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return e;
+  }
+  *have = want;
+  if (zero) e = cudaMemset(*p, 0, want);
+  return e;
+}
+
+cudaError_t ensure_arena(Context &ctx, size_t bytes) {
+  // the arena's head holds state that must start zeroed (look-back flags)
+  if (bytes <= ctx.arena_bytes && ctx.arena) return cudaSuccess;
+  cudaError_t e = cudaStreamSynchronize(ctx.stream);
+  if (e != cudaSuccess) return e;
+  void *p = ctx.arena;
+  e = grow(&p, &ctx.arena_bytes, bytes, true);
+  ctx.arena = static_cast<char *>(p);
+  return e;
+}
+
+cudaError_t ensure_surv(Context &ctx, size_t bytes) {
+  if (bytes <= ctx.surv_bytes && ctx.surv) return cudaSuccess;
+  cudaError_t e = cudaStreamSynchronize(ctx.stream);
+  if (e != cudaSuccess) return e;
+  return grow(&ctx.surv, &ctx.surv_bytes, bytes, false);
+}
+
+cudaError_t ensure_dvec(Context &ctx, size_t bytes) {
+  if (bytes <= ctx.dvec_bytes && ctx.dvec) return cudaSuccess;
+  cudaError_t e = cudaStreamSynchronize(ctx.stream);
+  if (e != cudaSuccess) return e;
+  return grow(&ctx.dvec, &ctx.dvec_bytes, bytes, false);
+}
+
+cudaError_t ensure_pin(Context &ctx, size_t bytes) {
+  if (bytes <= ctx.pin_bytes && ctx.pin) return cudaSuccess;
+  if (ctx.pin) {
+    cudaFreeHost(ctx.pin);
+    ctx.pin = nullptr;
+    ctx.pin_bytes = 0;
+  }
+  size_t want = bytes + bytes / 4 + 4096;
+  void *p = nullptr;
+  cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+  if (e != cudaSuccess) return e;
+  ctx.pin = static_cast<char *>(p);
+  ctx.pin_bytes = want;
+  return cudaSuccess;
+}
+
+Context *child_of(Context &ctx, int *status) {
+  if (!ctx.child) {
+    std::unique_ptr<Context> c(new Context());
+    c->device = ctx.device;
+    c->sm_count = ctx.sm_count;
+    c->smem_optin = ctx.smem_optin;
+    c->stream = ctx.stream;  // borrowed: not destroyed by the child
+    c->depth = ctx.depth + 1;
+    ctx.child = std::move(c);
+  }
+  *status = GGKS_OK;
+  return ctx.child.get();
+}
+
+static std::mutex g_default_mu;
+static Context *g_default[64];
+
+Context *default_context(int device, int *status) {
+  if (device < 0 || device >= 64) {
+    *status = GGKS_INVALID_ARG;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(g_default_mu);
+  if (!g_default[device]) {
+    // default contexts live until process exit (never destroyed: tearing
+    // down CUDA state from a static destructor is unsafe)
+    Context *c = new Context();
+    int st = context_init(*c, device);
+    if (st != GGKS_OK) {
+      c->stream = nullptr;
+      delete c;
+      *status = st;
+      return nullptr;
+    }
+    g_default[device] = c;
+  }
+  *status = GGKS_OK;
+  return g_default[device];
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+static Context *resolve(const ggks_opts *opts, int *status) {
+  if (opts && opts->ctx) {
+    *status = GGKS_OK;
+    return reinterpret_cast<Context *>(opts->ctx);
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    *status = GGKS_NO_DEVICE;
+    return nullptr;
+  }
+  return default_context(dev, status);
+}
+
+// ---------------------------------------------------------------------------
+// API bodies
+// ---------------------------------------------------------------------------
+template <class T>
+static int api_multiselect(const T *vec, uint64_t n, const uint32_t *h_k, uint32_t num_k, T *out,
+                           const ggks_opts *opts, bool host_input) {
+  if (!vec || !h_k || !out || n == 0 || n > GGKS_MAX_N || num_k == 0) return GGKS_INVALID_ARG;
+  if ((uintptr_t)vec % sizeof(T) != 0) return GGKS_INVALID_ARG;
+  for (uint32_t i = 0; i < num_k; ++i)
+    if (h_k[i] < 1 || (uint64_t)h_k[i] > n) return GGKS_INVALID_ARG;
+  int st = GGKS_OK;
+  Context *ctx = resolve(opts, &st);
+  if (!ctx) return st;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  DeviceGuard dg(ctx->device);
+  cudaStream_t s = (opts && opts->stream) ? static_cast<cudaStream_t>(opts->stream) : ctx->stream;
+  const T *d_in = vec;
+  if (host_input) {
+    cudaError_t e = ensure_dvec(*ctx, n * sizeof(T));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->dvec, vec, n * sizeof(T), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return from_cuda(e);
+    d_in = static_cast<const T *>(ctx->dvec);
+  }
+  const bool out_dev = opts && (opts->flags & GGKS_FLAG_OUT_DEVICE);
+  ReqSource src;
+  src.h_k = h_k;
+  const T *hres = nullptr;
+  st = select<T, T>(*ctx, d_in, n, src, num_k, out_dev ? out : nullptr, out_dev ? nullptr : &hres, s);
+  if (st == GGKS_OK) {
+    if (!out_dev) std::memcpy(out, hres, (size_t)num_k * sizeof(T));
+    ctx->stats.calls++;
+    ctx->stats.bytes_in += n * sizeof(T);
+  }
+  return st;
+}
+
+template <class T>
+static int api_topk(const T *vec, uint64_t n, uint32_t K, T *out, const ggks_opts *opts,
+                    bool host_input) {
+  if (!vec || !out || n == 0 || n > GGKS_MAX_N || K == 0 || (uint64_t)K > n) return GGKS_INVALID_ARG;
+  if ((uintptr_t)vec % sizeof(T) != 0) return GGKS_INVALID_ARG;
+  int st = GGKS_OK;
+  Context *ctx = resolve(opts, &st);
+  if (!ctx) return st;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  DeviceGuard dg(ctx->device);
+  cudaStream_t s = (opts && opts->stream) ? static_cast<cudaStream_t>(opts->stream) : ctx->stream;
+  const T *d_in = vec;
+  if (host_input) {
+    cudaError_t e = ensure_dvec(*ctx, n * sizeof(T));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->dvec, vec, n * sizeof(T), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return from_cuda(e);
+    d_in = static_cast<const T *>(ctx->dvec);
+  }
+  const bool out_dev = opts && (opts->flags & GGKS_FLAG_OUT_DEVICE);
+  ReqSource src;
+  src.topk = true;
+  const T *hres = nullptr;
+  st = select<T, T>(*ctx, d_in, n, src, K, out_dev ? out : nullptr, out_dev ? nullptr : &hres, s);
+  if (st == GGKS_OK) {
+    if (!out_dev) std::memcpy(out, hres, (size_t)K * sizeof(T));
+    ctx->stats.calls++;
+    ctx->stats.bytes_in += n * sizeof(T);
+  }
+  return st;
+}
+
+}  // namespace ggks
+
+using namespace ggks;
+
+extern "C" {
+
+int ggks_multiselect_f32(const float *d_vec, uint64_t n, const uint32_t *h_k, uint32_t num_k,
+                         float *h_out, const ggks_opts *opts) {
+  return api_multiselect<float>(d_vec, n, h_k, num_k, h_out, opts, false);
+}
+int ggks_multiselect_f64(const double *d_vec, uint64_t n, const uint32_t *h_k, uint32_t num_k,
+                         double *h_out, const ggks_opts *opts) {
+  return api_multiselect<double>(d_vec, n, h_k, num_k, h_out, opts, false);
+}
+int ggks_multiselect_u32(const uint32_t *d_vec, uint64_t n, const uint32_t *h_k, uint32_t num_k,
+                         uint32_t *h_out, const ggks_opts *opts) {
+  return api_multiselect<uint32_t>(d_vec, n, h_k, num_k, h_out, opts, false);
+}
+int ggks_multiselect_host_f32(const float *h_vec, uint64_t n, const uint32_t *h_k, uint32_t num_k,
+                              float *h_out, const ggks_opts *opts) {
+  return api_multiselect<float>(h_vec, n, h_k, num_k, h_out, opts, true);
+}
+int ggks_multiselect_host_f64(const double *h_vec, uint64_t n, const uint32_t *h_k,
+                              uint32_t num_k, double *h_out, const ggks_opts *opts) {
+  return api_multiselect<double>(h_vec, n, h_k, num_k, h_out, opts, true);
+}
+int ggks_multiselect_host_u32(const uint32_t *h_vec, uint64_t n, const uint32_t *h_k,
+                              uint32_t num_k, uint32_t *h_out, const ggks_opts *opts) {
+  return api_multiselect<uint32_t>(h_vec, n, h_k, num_k, h_out, opts, true);
+}
+int ggks_topk_f32(const float *d_vec, uint64_t n, uint32_t K, float *h_out, const ggks_opts *opts) {
+  return api_topk<float>(d_vec, n, K, h_out, opts, false);
+}
+int ggks_topk_f64(const double *d_vec, uint64_t n, uint32_t K, double *h_out,
+                  const ggks_opts *opts) {
+  return api_topk<double>(d_vec, n, K, h_out, opts, false);
+}
+int ggks_topk_u32(const uint32_t *d_vec, uint64_t n, uint32_t K, uint32_t *h_out,
+                  const ggks_opts *opts) {
+  return api_topk<uint32_t>(d_vec, n, K, h_out, opts, false);
+}
+int ggks_topk_host_f32(const float *h_vec, uint64_t n, uint32_t K, float *h_out,
+                       const ggks_opts *opts) {
+  return api_topk<float>(h_vec, n, K, h_out, opts, true);
+}
+int ggks_topk_host_f64(const double *h_vec, uint64_t n, uint32_t K, double *h_out,
+                       const ggks_opts *opts) {
+  return api_topk<double>(h_vec, n, K, h_out, opts, true);
+}
+int ggks_topk_host_u32(const uint32_t *h_vec, uint64_t n, uint32_t K, uint32_t *h_out,
+                       const ggks_opts *opts) {
+  return api_topk<uint32_t>(h_vec, n, K, h_out, opts, true);
+}
+
+int ggks_context_create(int device, ggks_context **out) {
+  if (!out) return GGKS_INVALID_ARG;
+  *out = nullptr;
+  Context *c = new Context();
+  int cur = -1;
+  cudaGetDevice(&cur);
+  int st = context_init(*c, device);
+  if (cur >= 0) cudaSetDevice(cur);
+  if (st != GGKS_OK) {
+    delete c;
+    return st;
+  }
+  *out = reinterpret_cast<ggks_context *>(c);
+  return GGKS_OK;
+}
+
+int ggks_context_destroy(ggks_context *ctx) {
+  if (!ctx) return GGKS_INVALID_ARG;
+  delete reinterpret_cast<Context *>(ctx);
+  return GGKS_OK;
+}
+
+static Context *ctx_or_default(ggks_context *ctx, int *st) {
+  if (ctx) {
+    *st = GGKS_OK;
+    return reinterpret_cast<Context *>(ctx);
+  }
+  ggks_opts o{};
+  return resolve(&o, st);
+}
+
+int ggks_context_get_stats(ggks_context *ctx, ggks_stats *out) {
+  if (!out) return GGKS_INVALID_ARG;
+  int st = GGKS_OK;
+  Context *c = ctx_or_default(ctx, &st);
+  if (!c) return st;
+  std::lock_guard<std::mutex> lk(c->mu);
+  *out = c->stats;
+  // recursive levels count toward their parent
+  for (Context *ch = c->child.get(); ch; ch = ch->child.get()) {
+    out->launches += ch->stats.launches;
+    for (int i = 0; i < GGKS_NUM_PASSES; ++i) {
+      out->pass_launches[i] += ch->stats.pass_launches[i];
+      out->pass_ms[i] += ch->stats.pass_ms[i];
+    }
+  }
+  return GGKS_OK;
+}
+
+int ggks_context_reset_stats(ggks_context *ctx) {
+  int st = GGKS_OK;
+  Context *c = ctx_or_default(ctx, &st);
+  if (!c) return st;
+  std::lock_guard<std::mutex> lk(c->mu);
+  for (Context *p = c; p; p = p->child.get()) p->stats = ggks_stats{};
+  return GGKS_OK;
+}
+
+int ggks_context_set_profiling(ggks_context *ctx, int on) {
+  int st = GGKS_OK;
+  Context *c = ctx_or_default(ctx, &st);
+  if (!c) return st;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  if (on && !c->events_ready) {
+    for (int i = 0; i < GGKS_NUM_PASSES; ++i) {
+      if (cudaEventCreate(&c->ev0[i]) != cudaSuccess || cudaEventCreate(&c->ev1[i]) != cudaSuccess)
+        return GGKS_CUDA_ERROR;
+    }
+    c->events_ready = true;
+  }
+  c->profiling = on != 0;
+  return GGKS_OK;
+}
+
+const char *ggks_status_string(int status) {
+  switch (status) {
+    case GGKS_OK: return "ok";
+    case GGKS_INVALID_ARG: return "invalid argument";
+    case GGKS_OOM: return "out of memory";
+    case GGKS_CUDA_ERROR: return "CUDA error";
+    case GGKS_TIMEOUT: return "device-side wait timed out";
+    case GGKS_INTERNAL: return "internal consistency check failed";
+    case GGKS_NO_DEVICE: return "no CUDA device";
+    case GGKS_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+int ggks_version(void) { return GGKS_VERSION; }
+
+}  // extern "C"

@@ -1,0 +1,79 @@
+// ggks_internal.h -- host-side context and pipeline driver declarations.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <mutex>
+
+#include "ggks.h"
+#include "ggks_device.cuh"
+
+namespace ggks {
+
+// A context owns one device, one stream, a device arena (per-call scratch), a
+// survivor buffer, a device staging buffer for host-vector inputs, pinned host
+// staging, and a child context for recursive re-selection of oversized
+// segments.
+struct Context {
+  int device = 0;
+  int sm_count = 0;
+  int smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+
+  char *arena = nullptr;  // [tile_state | out | ctrl | reqs | ... ]
+  size_t arena_bytes = 0;
+  void *surv = nullptr;
+  size_t surv_bytes = 0;
+  void *dvec = nullptr;
+  size_t dvec_bytes = 0;
+  char *pin = nullptr;
+  size_t pin_bytes = 0;
+
+  std::unique_ptr<Context> child;
+  int depth = 0;
+
+  ggks_stats stats{};
+  bool profiling = false;
+  bool events_ready = false;
+  cudaEvent_t ev0[GGKS_NUM_PASSES]{}, ev1[GGKS_NUM_PASSES]{};
+  cudaEvent_t copy_done = nullptr;
+
+  ~Context();
+};
+
+// status mapping
+int from_cuda(cudaError_t e);
+
+int context_init(Context &ctx, int device);
+Context *default_context(int device, int *status);
+Context *child_of(Context &ctx, int *status);
+
+cudaError_t ensure_arena(Context &ctx, size_t bytes);
+cudaError_t ensure_surv(Context &ctx, size_t bytes);
+cudaError_t ensure_dvec(Context &ctx, size_t bytes);
+cudaError_t ensure_pin(Context &ctx, size_t bytes);
+
+// fixed-offset persistent state at the start of the arena
+constexpr size_t kTileStateBytes = 4096;  // >= (65536 / kScanTile) * 8
+constexpr uint32_t kMaxNb = 32768;        // shared-memory histogram limit (u32 counters)
+
+// Where the requests of one selection come from.
+struct ReqSource {
+  const uint32_t *h_k = nullptr;  // host k list (k-th largest): rank = n - k
+  const Req *d_reqs = nullptr;    // device requests (recursive levels)
+  bool topk = false;              // ranks n-1 .. n-K into outputs 0 .. K-1
+};
+
+// Run one selection.  Results land in d_out_user (device) or, when it is
+// null, in the context's arena.  If host_results is not null the results are
+// also copied to pinned host memory and *host_results points there (valid
+// until the next call on the context).  The stream is synchronised.
+template <class InT, class OutT>
+int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint32_t num_req,
+           OutT *d_out_user, const OutT **host_results, cudaStream_t s);
+
+}  // namespace ggks

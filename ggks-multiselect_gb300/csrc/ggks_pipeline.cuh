@@ -1,0 +1,325 @@
+// ggks_pipeline.cuh -- host driver of the selection pipeline (templated on the
+// input element type and the output value type).  Included by the
+// per-type instantiation units.
+#pragma once
+
+#include <cstring>
+#include <vector>
+
+#include "ggks_internal.h"
+
+namespace ggks {
+
+template <class T>
+static inline uint32_t cap_keys_for() {
+  return sizeof(typename Traits<T>::K) == 4 ? 16384u : 8192u;
+}
+
+static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+struct Plan {
+  uint64_t n = 0;
+  uint32_t num_req = 0;
+  uint32_t S = 0, sample_grid = 0;
+  uint32_t nb_max = 0;
+  uint32_t G = 0;           // hist / compact grid
+  uint32_t scan_tiles = 0;
+  uint32_t cap_keys = 0;
+  uint32_t fin_grid = 0;
+  uint64_t surv_cap = 0;
+  // arena offsets
+  size_t out = 0, ctrl = 0, reqs = 0, hdr = 0, lut = 0, samples = 0, partials = 0,
+         counts = 0, excl = 0, slot_of = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0,
+         kcur = 0, seg_cursor = 0, deferred = 0, req_bucket = 0, klist = 0, total = 0;
+};
+
+template <class InT, class OutT>
+static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
+  using K = typename Traits<InT>::K;
+  Plan p;
+  p.n = n;
+  p.num_req = num_req;
+  p.S = n <= 65536 ? (uint32_t)n : 65536u;
+  p.sample_grid = (p.S + 1023) / 1024;
+  uint64_t want = n / 32;
+  uint32_t nb = 8192;
+  while (nb < kMaxNb && (uint64_t)nb * 2 <= want) nb *= 2;
+  p.nb_max = nb;
+  uint64_t g = (n + 65535) / 65536;
+  p.G = (uint32_t)(g < 1 ? 1 : (g > (uint64_t)ctx.sm_count ? ctx.sm_count : g));
+  p.scan_tiles = (p.nb_max + kScanTile - 1) / kScanTile;
+  p.cap_keys = cap_keys_for<InT>();
+  uint32_t slots_bound = num_req < p.nb_max ? num_req : p.nb_max;
+  uint32_t fg = 2u * (uint32_t)ctx.sm_count;
+  p.fin_grid = slots_bound < fg ? (slots_bound ? slots_bound : 1) : fg;
+  uint64_t cap = n / 8;
+  p.surv_cap = cap < (1u << 20) ? (1u << 20) : cap;
+  if (p.surv_cap > n) p.surv_cap = n;
+
+  const size_t A = 256;
+  size_t o = kTileStateBytes;
+  p.out = o;
+  o = align_up(o + (size_t)num_req * sizeof(OutT), A);
+  p.ctrl = o;
+  o += A;  // ctrl is followed directly by the requests (one upload)
+  p.reqs = o;
+  o = align_up(o + (size_t)num_req * sizeof(Req), A);
+  p.hdr = o;
+  o = align_up(o + sizeof(LutHeader<K>), A);
+  p.lut = o;
+  o = align_up(o + (kLutEntries + 1) * sizeof(uint2), A);
+  p.samples = o;
+  o = align_up(o + (size_t)p.S * sizeof(K), A);
+  p.partials = o;
+  o = align_up(o + (size_t)p.G * p.nb_max * sizeof(uint32_t), A);
+  auto arr = [&](size_t &off, size_t elems, size_t esz) {
+    off = o;
+    o = align_up(o + elems * esz, A);
+  };
+  arr(p.counts, p.nb_max, 4);
+  arr(p.excl, p.nb_max, 4);
+  arr(p.slot_of, p.nb_max, 4);
+  arr(p.seg_off, p.nb_max, 8);
+  arr(p.seg_size, p.nb_max, 4);
+  arr(p.kstart, p.nb_max, 4);
+  arr(p.kcnt, p.nb_max, 4);
+  arr(p.kcur, p.nb_max, 4);
+  arr(p.seg_cursor, p.nb_max, 4);
+  arr(p.deferred, p.nb_max, 4);
+  arr(p.req_bucket, num_req, 4);
+  arr(p.klist, num_req, sizeof(Req));
+  p.total = o;
+  return p;
+}
+
+// Raise a kernel's dynamic shared-memory limit once per process (thread-safe
+// static initialisation; one GPU per process).
+template <auto F>
+static void set_smem_max(int bytes) {
+  static const bool done = [bytes]() {
+    cudaFuncSetAttribute((const void *)F, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return true;
+  }();
+  (void)done;
+}
+
+struct PassTimer {
+  Context &ctx;
+  cudaStream_t s;
+  int pass;
+  PassTimer(Context &c, cudaStream_t st, int p) : ctx(c), s(st), pass(p) {
+    if (ctx.profiling) cudaEventRecord(ctx.ev0[pass], s);
+  }
+  ~PassTimer() {
+    if (ctx.profiling) cudaEventRecord(ctx.ev1[pass], s);
+    ctx.stats.launches++;
+    ctx.stats.pass_launches[pass]++;
+  }
+};
+
+static void collect_pass_times(Context &ctx, const bool *ran) {
+  if (!ctx.profiling) return;
+  for (int i = 0; i < GGKS_NUM_PASSES; ++i) {
+    if (!ran[i]) continue;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx.ev0[i], ctx.ev1[i]) == cudaSuccess) ctx.stats.pass_ms[i] += ms;
+  }
+}
+
+__global__ void k_make_topk_reqs(Req *reqs, uint64_t n, uint32_t K);
+
+template <class InT, class OutT>
+int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint32_t num_req,
+           OutT *d_out_user, const OutT **host_results, cudaStream_t s) {
+  using K = typename Traits<InT>::K;
+  constexpr int UNROLL = 4;
+  if (ctx.depth > 12) return GGKS_INTERNAL;
+  const Plan p = make_plan<InT, OutT>(ctx, n, num_req);
+  cudaError_t e = ensure_arena(ctx, p.total);
+  if (e != cudaSuccess) return from_cuda(e);
+  e = ensure_surv(ctx, (size_t)p.surv_cap * sizeof(K));
+  if (e != cudaSuccess) return from_cuda(e);
+  char *A = ctx.arena;
+  Ctrl *ctrl = reinterpret_cast<Ctrl *>(A + p.ctrl);
+  Req *reqs = reinterpret_cast<Req *>(A + p.reqs);
+  LutHeader<K> *hdr = reinterpret_cast<LutHeader<K> *>(A + p.hdr);
+  uint2 *lut = reinterpret_cast<uint2 *>(A + p.lut);
+  K *samples = reinterpret_cast<K *>(A + p.samples);
+  uint32_t *partials = reinterpret_cast<uint32_t *>(A + p.partials);
+  uint32_t *counts = reinterpret_cast<uint32_t *>(A + p.counts);
+  uint32_t *excl = reinterpret_cast<uint32_t *>(A + p.excl);
+  uint64_t *tile_state = reinterpret_cast<uint64_t *>(A);
+  uint32_t *slot_of = reinterpret_cast<uint32_t *>(A + p.slot_of);
+  uint64_t *seg_off = reinterpret_cast<uint64_t *>(A + p.seg_off);
+  uint32_t *seg_size = reinterpret_cast<uint32_t *>(A + p.seg_size);
+  uint32_t *kstart = reinterpret_cast<uint32_t *>(A + p.kstart);
+  uint32_t *kcnt = reinterpret_cast<uint32_t *>(A + p.kcnt);
+  uint32_t *kcur = reinterpret_cast<uint32_t *>(A + p.kcur);
+  uint32_t *seg_cursor = reinterpret_cast<uint32_t *>(A + p.seg_cursor);
+  uint32_t *deferred = reinterpret_cast<uint32_t *>(A + p.deferred);
+  uint32_t *req_bucket = reinterpret_cast<uint32_t *>(A + p.req_bucket);
+  Req *klist = reinterpret_cast<Req *>(A + p.klist);
+  K *surv = reinterpret_cast<K *>(ctx.surv);
+  OutT *d_out = d_out_user ? d_out_user : reinterpret_cast<OutT *>(A + p.out);
+  const bool out_in_arena = d_out_user == nullptr;
+
+  // pinned staging: [ctrl image | host requests] up, [out | pad | ctrl] down
+  const size_t up_bytes = 256 + (src.h_k ? (size_t)num_req * sizeof(Req) : 0);
+  const size_t out_span = p.ctrl - p.out;  // == align_up(num_req * sizeof(OutT), 256)
+  const size_t down_off = align_up(up_bytes, 256);
+  e = ensure_pin(ctx, down_off + out_span + 256);
+  if (e != cudaSuccess) return from_cuda(e);
+  char *pin_up = ctx.pin;
+  char *pin_down = ctx.pin + down_off;
+  Ctrl *h_ctrl = reinterpret_cast<Ctrl *>(pin_down + out_span);
+  // every call ends with a stream synchronisation, so no earlier copy still
+  // reads the pinned buffer here
+  std::memset(pin_up, 0, 256);
+  if (src.h_k) {
+    Req *hr = reinterpret_cast<Req *>(pin_up + 256);
+    for (uint32_t i = 0; i < num_req; ++i) {
+      hr[i].rank = (uint32_t)(n - src.h_k[i]);
+      hr[i].out = i;
+    }
+  }
+  e = cudaMemcpyAsync(ctrl, pin_up, up_bytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return from_cuda(e);
+  const Req *rq = src.d_reqs ? src.d_reqs : reqs;
+  bool ran[GGKS_NUM_PASSES] = {false, false, false, false, false, false};
+  if (src.topk) {
+    k_make_topk_reqs<<<(num_req + 255) / 256, 256, 0, s>>>(reqs, n, num_req);
+    ctx.stats.launches++;
+  }
+
+  // ---- (b) sample + splitter table
+  {
+    PassTimer t(ctx, s, GGKS_PASS_SAMPLE);
+    k_sample_lut<InT><<<p.sample_grid, 1024, 0, s>>>(d_in, n, p.S, 0x5EEDu, samples, ctrl, hdr,
+                                                      lut, p.nb_max);
+    ran[GGKS_PASS_SAMPLE] = true;
+  }
+  // ---- (c) histogram
+  {
+    const int smem = (int)((kLutEntries + 1) * sizeof(uint2) + (size_t)p.nb_max * 4);
+    set_smem_max<k_hist<InT, UNROLL>>((int)((kLutEntries + 1) * sizeof(uint2) + (size_t)kMaxNb * 4));
+    PassTimer t(ctx, s, GGKS_PASS_HIST);
+    k_hist<InT, UNROLL><<<p.G, 1024, smem, s>>>(d_in, n, hdr, lut, partials, p.nb_max, ctrl);
+    ran[GGKS_PASS_HIST] = true;
+  }
+  // ---- (d) reduce + decoupled look-back scan
+  {
+    PassTimer t(ctx, s, GGKS_PASS_SCAN);
+    k_scan<K><<<p.scan_tiles, kScanTile, 0, s>>>(partials, p.G, p.nb_max, hdr, counts, excl,
+                                                  tile_state, ctrl);
+    ran[GGKS_PASS_SCAN] = true;
+  }
+  // ---- (e) plan
+  {
+    const int smem =
+        (int)((kLutEntries + 1) * sizeof(uint2) + (size_t)p.nb_max * 4 + (size_t)p.nb_max);
+    set_smem_max<k_plan<InT, OutT>>((int)((kLutEntries + 1) * sizeof(uint2) + (size_t)kMaxNb * 5));
+    PassTimer t(ctx, s, GGKS_PASS_PLAN);
+    k_plan<InT, OutT><<<1, 1024, smem, s>>>(hdr, lut, counts, excl, n, rq, num_req, p.nb_max, ctrl,
+                                             tile_state, p.scan_tiles, slot_of, seg_off, seg_size,
+                                             kstart, kcnt, kcur, seg_cursor, req_bucket, klist,
+                                             p.surv_cap, d_out);
+    ran[GGKS_PASS_PLAN] = true;
+  }
+  auto launch_tail = [&]() {
+    {
+      const int smem = (int)((kLutEntries + 1) * sizeof(uint2) + (size_t)(p.nb_max / 32 + 1) * 4);
+      set_smem_max<k_compact<InT, UNROLL>>((int)((kLutEntries + 1) * sizeof(uint2) + (size_t)(kMaxNb / 32 + 1) * 4));
+      PassTimer t(ctx, s, GGKS_PASS_COMPACT);
+      k_compact<InT, UNROLL><<<p.G, 1024, smem, s>>>(d_in, n, hdr, lut, slot_of, seg_off,
+                                                     seg_size, seg_cursor, surv, p.nb_max, ctrl);
+      ran[GGKS_PASS_COMPACT] = true;
+    }
+    {
+      const int smem = (int)((size_t)p.cap_keys * sizeof(K));
+      set_smem_max<k_finish<K, OutT>>(smem);
+      PassTimer t(ctx, s, GGKS_PASS_FINISH);
+      k_finish<K, OutT><<<p.fin_grid, 1024, smem, s>>>(surv, ctrl, seg_off, seg_size, kstart, kcnt,
+                                                       klist, deferred, p.cap_keys, d_out);
+      ran[GGKS_PASS_FINISH] = true;
+    }
+  };
+  launch_tail();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return from_cuda(e);
+
+  // results and control block come back in one copy when the output is ours
+  auto pull = [&](bool with_out) -> cudaError_t {
+    cudaError_t r;
+    if (with_out && out_in_arena)
+      r = cudaMemcpyAsync(pin_down, A + p.out, out_span + sizeof(Ctrl), cudaMemcpyDeviceToHost, s);
+    else
+      r = cudaMemcpyAsync(h_ctrl, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s);
+    if (r == cudaSuccess && with_out && !out_in_arena)
+      r = cudaMemcpyAsync(pin_down, d_out, (size_t)num_req * sizeof(OutT), cudaMemcpyDeviceToHost, s);
+    if (r != cudaSuccess) return r;
+    return cudaStreamSynchronize(s);
+  };
+  const bool want_host = host_results != nullptr;
+  e = pull(want_host);
+  if (e != cudaSuccess) return from_cuda(e);
+  collect_pass_times(ctx, ran);
+
+  for (int round = 0; round < 4; ++round) {
+    const Ctrl c = *h_ctrl;
+    if (c.status & ST_FATAL) {
+      cudaMemsetAsync(tile_state, 0, kTileStateBytes, s);
+      cudaStreamSynchronize(s);
+      return (c.status & ST_TIMEOUT) ? GGKS_TIMEOUT : GGKS_INTERNAL;
+    }
+    if (c.status & ST_OVERFLOW) {
+      // survivors did not fit: grow the buffer, re-run compaction + finish
+      const uint64_t need = c.cap_needed + (c.cap_needed >> 3);
+      e = ensure_surv(ctx, (size_t)need * sizeof(K));
+      if (e != cudaSuccess) return from_cuda(e);
+      surv = reinterpret_cast<K *>(ctx.surv);
+      ctx.stats.retries++;
+      e = cudaMemsetAsync(&ctrl->status, 0, sizeof(uint32_t), s);
+      if (e != cudaSuccess) return from_cuda(e);
+      for (int i = 0; i < GGKS_NUM_PASSES; ++i) ran[i] = false;
+      launch_tail();
+      e = pull(want_host);
+      if (e != cudaSuccess) return from_cuda(e);
+      collect_pass_times(ctx, ran);
+      continue;
+    }
+    if (c.status & ST_DEFERRED) {
+      // oversized segments: select each again, recursively, on its keys
+      const uint32_t D = c.deferred_count, ns = c.num_slots;
+      std::vector<uint32_t> dl(D), sz(ns), ks(ns), kc(ns);
+      std::vector<uint64_t> so(ns);
+      e = cudaMemcpyAsync(dl.data(), deferred, D * 4, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(sz.data(), seg_size, ns * 4, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(so.data(), seg_off, ns * 8, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(ks.data(), kstart, ns * 4, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(kc.data(), kcnt, ns * 4, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) return from_cuda(e);
+      int st = GGKS_OK;
+      Context *ch = child_of(ctx, &st);
+      if (!ch) return st;
+      for (uint32_t d = 0; d < D; ++d) {
+        const uint32_t slot = dl[d];
+        ReqSource cs;
+        cs.d_reqs = klist + ks[slot];
+        ctx.stats.recursions++;
+        st = select<K, OutT>(*ch, surv + so[slot], sz[slot], cs, kc[slot], d_out, nullptr, s);
+        if (st != GGKS_OK) return st;
+      }
+      if (want_host) {
+        e = pull(true);
+        if (e != cudaSuccess) return from_cuda(e);
+      }
+    }
+    break;
+  }
+  ctx.stats.survivors += h_ctrl->total_surv;
+  if (want_host) *host_results = reinterpret_cast<const OutT *>(pin_down);
+  return GGKS_OK;
+}
+
+}  // namespace ggks

@@ -1,0 +1,314 @@
+"""Python binding (ctypes) of libggks_gb300.so, the GB300 GGKS bucket
+multiselect / top-k library, plus Python mirrors of the reference's host-side
+interface for this path:
+
+* ``bucketMultiselectWrapper``   -- BucketMultiselect::bucketMultiselectWrapper
+  (bucketMultiselect.cu:837-871): device vector, k list (k-th largest),
+  outputs in k order; blocks/threads accepted and ignored.
+* ``timeBucketMultiselect`` / ``timeBucketTopkselect`` -- the timing adapters
+  of multiselectTimingFunctions.cu:100-122 and :205-231, returning a
+  ``Results`` (time in ms, values) like ``results_t<T>`` (:11-14).
+
+The CUDA library must be built (``ggks_build.build()``); importing this module
+without it raises -- there is no CPU fallback.
+"""
+import ctypes
+import os
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libggks_gb300.so")
+
+OK, INVALID_ARG, OOM, CUDA_ERROR, TIMEOUT, INTERNAL, NO_DEVICE, UNSUPPORTED = range(8)
+FLAG_OUT_DEVICE = 1
+NUM_PASSES = 6
+PASS_NAMES = ("sample", "hist", "scan", "plan", "compact", "finish")
+
+_SFX = {np.dtype(np.float32): "f32", np.dtype(np.float64): "f64", np.dtype(np.uint32): "u32"}
+
+
+class GgksError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        super().__init__(f"{what}: ggks status {status} ({status_string(status)})")
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("ctx", ctypes.c_void_p), ("stream", ctypes.c_void_p),
+                ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("calls", ctypes.c_uint64), ("launches", ctypes.c_uint64),
+                ("pass_launches", ctypes.c_uint64 * NUM_PASSES),
+                ("pass_ms", ctypes.c_double * NUM_PASSES),
+                ("bytes_in", ctypes.c_uint64), ("survivors", ctypes.c_uint64),
+                ("retries", ctypes.c_uint64), ("recursions", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {"calls": self.calls, "launches": self.launches,
+                "pass_launches": dict(zip(PASS_NAMES, list(self.pass_launches))),
+                "pass_ms": dict(zip(PASS_NAMES, list(self.pass_ms))),
+                "bytes_in": self.bytes_in, "survivors": self.survivors,
+                "retries": self.retries, "recursions": self.recursions}
+
+
+# every symbol declared in include/ggks.h
+EXPORTS = [
+    "ggks_multiselect_f32", "ggks_multiselect_f64", "ggks_multiselect_u32",
+    "ggks_multiselect_host_f32", "ggks_multiselect_host_f64", "ggks_multiselect_host_u32",
+    "ggks_topk_f32", "ggks_topk_f64", "ggks_topk_u32",
+    "ggks_topk_host_f32", "ggks_topk_host_f64", "ggks_topk_host_u32",
+    "ggks_context_create", "ggks_context_destroy", "ggks_context_get_stats",
+    "ggks_context_reset_stats", "ggks_context_set_profiling", "ggks_status_string",
+    "ggks_version",
+]
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with ggks_build.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    P, U64, U32 = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32
+    for sfx in ("f32", "f64", "u32"):
+        for nm in ("ggks_multiselect_", "ggks_multiselect_host_"):
+            f = getattr(L, nm + sfx)
+            f.argtypes = [P, U64, P, U32, P, ctypes.POINTER(Opts)]
+            f.restype = ctypes.c_int
+        for nm in ("ggks_topk_", "ggks_topk_host_"):
+            f = getattr(L, nm + sfx)
+            f.argtypes = [P, U64, U32, P, ctypes.POINTER(Opts)]
+            f.restype = ctypes.c_int
+    L.ggks_context_create.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+    L.ggks_context_destroy.argtypes = [P]
+    L.ggks_context_get_stats.argtypes = [P, ctypes.POINTER(Stats)]
+    L.ggks_context_reset_stats.argtypes = [P]
+    L.ggks_context_set_profiling.argtypes = [P, ctypes.c_int]
+    L.ggks_status_string.argtypes = [ctypes.c_int]
+    L.ggks_status_string.restype = ctypes.c_char_p
+    for f in (L.ggks_context_create, L.ggks_context_destroy, L.ggks_context_get_stats,
+              L.ggks_context_reset_stats, L.ggks_context_set_profiling, L.ggks_version):
+        f.restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def status_string(st):
+    try:
+        return lib().ggks_status_string(int(st)).decode()
+    except ImportError:
+        return "?"
+
+
+def _check(st, what):
+    if st != OK:
+        raise GgksError(st, what)
+
+
+class Context:
+    """An owned ggks_context (device, stream, workspace)."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        _check(lib().ggks_context_create(int(device), ctypes.byref(h)), "context_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().ggks_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def stats(self):
+        return get_stats(self)
+
+    def reset_stats(self):
+        reset_stats(self)
+
+    def set_profiling(self, on=True):
+        set_profiling(self, on)
+
+
+def _h(ctx):
+    return ctx.handle if isinstance(ctx, Context) else ctx
+
+
+def _opts(ctx=None, stream=None, flags=0):
+    o = Opts()
+    o.ctx = _h(ctx)
+    o.stream = stream
+    o.flags = flags
+    return o
+
+
+def get_stats(ctx=None):
+    s = Stats()
+    _check(lib().ggks_context_get_stats(_h(ctx), ctypes.byref(s)), "get_stats")
+    return s.as_dict()
+
+
+def reset_stats(ctx=None):
+    _check(lib().ggks_context_reset_stats(_h(ctx)), "reset_stats")
+
+
+def set_profiling(ctx=None, on=True):
+    _check(lib().ggks_context_set_profiling(_h(ctx), 1 if on else 0), "set_profiling")
+
+
+# ---------------------------------------------------------------------------
+# raw entry points (pointers)
+# ---------------------------------------------------------------------------
+
+
+def multiselect_ptr(d_ptr, n, dtype, k, ctx=None, stream=None, out=None, out_device_ptr=None):
+    """Multiselect of a device vector at d_ptr (n elements of dtype).
+    Returns a host array of len(k) values, or writes to out_device_ptr."""
+    dtype = np.dtype(dtype)
+    k = np.ascontiguousarray(k, dtype=np.uint32)
+    flags = 0
+    if out_device_ptr is not None:
+        flags |= FLAG_OUT_DEVICE
+        optr = out_device_ptr
+    else:
+        if out is None:
+            out = np.empty(k.size, dtype=dtype)
+        optr = out.ctypes.data
+    o = _opts(ctx, stream, flags)
+    st = getattr(lib(), "ggks_multiselect_" + _SFX[dtype])(
+        ctypes.c_void_p(d_ptr), int(n), k.ctypes.data, k.size, ctypes.c_void_p(optr),
+        ctypes.byref(o))
+    _check(st, "multiselect")
+    return out
+
+
+def topk_ptr(d_ptr, n, dtype, K, ctx=None, stream=None, out=None, out_device_ptr=None):
+    dtype = np.dtype(dtype)
+    flags = 0
+    if out_device_ptr is not None:
+        flags |= FLAG_OUT_DEVICE
+        optr = out_device_ptr
+    else:
+        if out is None:
+            out = np.empty(int(K), dtype=dtype)
+        optr = out.ctypes.data
+    o = _opts(ctx, stream, flags)
+    st = getattr(lib(), "ggks_topk_" + _SFX[dtype])(
+        ctypes.c_void_p(d_ptr), int(n), int(K), ctypes.c_void_p(optr), ctypes.byref(o))
+    _check(st, "topk")
+    return out
+
+
+def multiselect_host(h_vec, k, ctx=None, stream=None, out=None):
+    """Multiselect of a host vector (copied to the device inside the call)."""
+    h_vec = np.ascontiguousarray(h_vec)
+    k = np.ascontiguousarray(k, dtype=np.uint32)
+    if out is None:
+        out = np.empty(k.size, dtype=h_vec.dtype)
+    o = _opts(ctx, stream)
+    st = getattr(lib(), "ggks_multiselect_host_" + _SFX[h_vec.dtype])(
+        h_vec.ctypes.data, h_vec.size, k.ctypes.data, k.size, out.ctypes.data, ctypes.byref(o))
+    _check(st, "multiselect_host")
+    return out
+
+
+def topk_host(h_vec, K, ctx=None, stream=None, out=None):
+    h_vec = np.ascontiguousarray(h_vec)
+    if out is None:
+        out = np.empty(int(K), dtype=h_vec.dtype)
+    o = _opts(ctx, stream)
+    st = getattr(lib(), "ggks_topk_host_" + _SFX[h_vec.dtype])(
+        h_vec.ctypes.data, h_vec.size, int(K), out.ctypes.data, ctypes.byref(o))
+    _check(st, "topk_host")
+    return out
+
+
+# ---------------------------------------------------------------------------
+# torch-tensor conveniences (device memory is plumbing; torch is optional)
+# ---------------------------------------------------------------------------
+_TORCH_NP = {"torch.float32": np.float32, "torch.float64": np.float64, "torch.uint32": np.uint32,
+             "torch.int32": np.uint32}
+
+
+def _tensor_dtype(t):
+    return np.dtype(_TORCH_NP[str(t.dtype)])
+
+
+def multiselect(t, k, ctx=None, stream=None):
+    """Multiselect of a contiguous CUDA tensor (float32 / float64 / uint32;
+    an int32 tensor is read as uint32 bits)."""
+    assert t.is_cuda and t.is_contiguous()
+    return multiselect_ptr(t.data_ptr(), t.numel(), _tensor_dtype(t), k, ctx=ctx, stream=stream)
+
+
+def topk(t, K, ctx=None, stream=None):
+    assert t.is_cuda and t.is_contiguous()
+    return topk_ptr(t.data_ptr(), t.numel(), _tensor_dtype(t), K, ctx=ctx, stream=stream)
+
+
+# ---------------------------------------------------------------------------
+# mirrors of the reference's host interface
+# ---------------------------------------------------------------------------
+
+
+def bucketMultiselectWrapper(d_vector, length, kVals, numKs, outputs, blocks=0, threads=0,
+                             dtype=None):
+    """BucketMultiselect::bucketMultiselectWrapper (bucketMultiselect.cu:837-871).
+    d_vector: a CUDA tensor or a device pointer (then dtype is required);
+    kVals: host k's (k-th largest); outputs: a host numpy array of numKs values,
+    filled in k order.  blocks/threads are accepted and ignored.  Returns 1
+    like the reference; errors raise GgksError instead of being silent."""
+    if hasattr(d_vector, "data_ptr"):
+        ptr, dtype = d_vector.data_ptr(), _tensor_dtype(d_vector)
+    else:
+        ptr = int(d_vector)
+    k = np.ascontiguousarray(np.asarray(kVals)[:numKs], dtype=np.uint32)
+    multiselect_ptr(ptr, length, dtype, k, out=outputs)
+    return 1
+
+
+class Results:
+    """results_t<T> (multiselectTimingFunctions.cu:11-14): time (ms), vals."""
+
+    def __init__(self, time_ms, vals):
+        self.time = time_ms
+        self.vals = vals
+
+
+def timeBucketMultiselect(h_vec, kVals, kCount=None, ctx=None):
+    """timeBucketMultiselect (multiselectTimingFunctions.cu:100-122): the
+    vector is copied to the device before the timer starts; the wrapper call is
+    timed."""
+    import torch
+    kVals = np.asarray(kVals, dtype=np.uint32)[: (kCount or len(kVals))]
+    d = torch.from_numpy(np.ascontiguousarray(h_vec)).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    vals = multiselect_ptr(d.data_ptr(), d.numel(), h_vec.dtype, kVals, ctx=ctx)
+    t1 = time.perf_counter()
+    del d
+    return Results((t1 - t0) * 1e3, vals)
+
+
+def timeBucketTopkselect(h_vec, kCount, ctx=None):
+    """timeBucketTopkselect (multiselectTimingFunctions.cu:205-231): the K
+    largest, descending."""
+    import torch
+    d = torch.from_numpy(np.ascontiguousarray(h_vec)).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    vals = topk_ptr(d.data_ptr(), d.numel(), h_vec.dtype, kCount, ctx=ctx)
+    t1 = time.perf_counter()
+    del d
+    return Results((t1 - t0) * 1e3, vals)

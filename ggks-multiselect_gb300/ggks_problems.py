@@ -1,0 +1,236 @@
+"""Seeded host-side problem generators for GGKS multiselect / top-k.
+
+These restate the distribution recipes of the reference's generators
+(generateProblems.cu) with numpy's PCG64 in place of curand, so every input is
+reproducible from (distribution, n, seed) on any machine.  The k-list
+generators follow generateProblems.cu:489-584.
+
+k convention everywhere: k-th LARGEST, 1-based (bucketMultiselect.cu:842-846).
+"""
+import numpy as np
+
+# ---------------------------------------------------------------------------
+# value distributions
+# ---------------------------------------------------------------------------
+
+
+def _rng(seed):
+    return np.random.Generator(np.random.PCG64(seed))
+
+
+def uniform_f32(n, seed):
+    """generateUniformFloats (generateProblems.cu:62-68): uniform [0,1)."""
+    return _rng(seed).random(n, dtype=np.float32)
+
+
+def normal_f32(n, seed, sigma=1.0):
+    """generateNormalFloats (:70-76) and generateNormalFloats100 (:301-307)."""
+    x = _rng(seed).standard_normal(n, dtype=np.float32)
+    if sigma != 1.0:
+        x *= np.float32(sigma)
+    return x
+
+
+def half_normal_f32(n, seed):
+    """generateHalfNormalFloats (:322-341): |N(0,1)|."""
+    return np.abs(normal_f32(n, seed))
+
+
+def cauchy_f32(n, seed):
+    """generateCauchyFloats (:212-247): tan(pi (u - 1/2)) with u == 1 -> 0.9999
+    and u == 0 -> 0.0001 (:218-221)."""
+    u = uniform_f32(n, seed)
+    u[u == np.float32(1.0)] = np.float32(0.9999)
+    u[u == np.float32(0.0)] = np.float32(0.0001)
+    return np.tan(np.float32(np.pi) * (u - np.float32(0.5))).astype(np.float32)
+
+
+def huge_uniform_f32(n, seed):
+    """generateHugeUniformFloats (:287-298): uniform [0,1) times 1e6."""
+    return uniform_f32(n, seed) * np.float32(1000000)
+
+
+def all_ones_f32(n, seed=0):
+    """generateAllOnesFloats (:180-197)."""
+    return np.ones(n, dtype=np.float32)
+
+
+def ones_twos_f32(n, seed):
+    """generateOnesTwosFloats (:154-177): (n*50)/100 twos, the rest ones,
+    shuffled."""
+    n2 = (n * 50) // 100
+    x = np.ones(n, dtype=np.float32)
+    x[:n2] = 2.0
+    _rng(seed).shuffle(x)
+    return x
+
+
+def noisy_f32(n, seed):
+    """generateNoisyVector (:249-277): N(0, 0.01) plus 1.0 on 20% of the
+    entries."""
+    r = _rng(seed)
+    x = (r.standard_normal(n, dtype=np.float32) * np.float32(0.01)).astype(np.float32)
+    ones = np.zeros(n, dtype=np.float32)
+    ones[: (n * 20) // 100] = 1.0
+    r.shuffle(ones)
+    return (x + ones).astype(np.float32)
+
+
+def killer_f32(n, seed):
+    """generateBucketKillerFloats (:353-367): uniform bits masked with
+    0x80EFFFFF, sorted, with 2^i (i = -126..126) written over the head."""
+    b = _rng(seed).random(n, dtype=np.float32).view(np.uint32) & np.uint32(0x80EFFFFF)
+    x = np.sort(b).view(np.float32).copy()
+    m = min(n, 253)
+    x[:m] = np.exp2(np.arange(-126, -126 + m, dtype=np.float64)).astype(np.float32)
+    return x
+
+
+def uint_valued_f32(n, seed):
+    """Integer-valued floats in [0,256) (heavy duplicates)."""
+    return _rng(seed).integers(0, 256, n, dtype=np.int32).astype(np.float32)
+
+
+def uniform_f64(n, seed, lo=0.0, hi=1.0):
+    """generateUniformDoubles (:385-391); lo/hi rescale it (the large f64
+    workload is uniform [-1e6, 1e6))."""
+    x = _rng(seed).random(n, dtype=np.float64)
+    if lo != 0.0 or hi != 1.0:
+        x = lo + (hi - lo) * x
+    return x
+
+
+def normal_f64(n, seed):
+    """generateNormalDoubles (:393-399)."""
+    return _rng(seed).standard_normal(n, dtype=np.float64)
+
+
+def cauchy_f64(n, seed):
+    u = _rng(seed).random(n, dtype=np.float64)
+    u[u == 0.0] = 0.0001
+    return np.tan(np.pi * (u - 0.5))
+
+
+def killer_f64(n, seed):
+    """generateBucketKillerDoubles (:409-423): masked with 0x800FFFFFFFFFFFFF,
+    sorted, 2^i (i = -1022..1022) over the head."""
+    b = _rng(seed).random(n, dtype=np.float64).view(np.uint64) & np.uint64(0x800FFFFFFFFFFFFF)
+    x = np.sort(b).view(np.float64).copy()
+    m = min(n, 2045)
+    x[:m] = np.exp2(np.arange(-1022, -1022 + m, dtype=np.float64))
+    return x
+
+
+def uint_valued_f64(n, seed):
+    return _rng(seed).integers(0, 256, n, dtype=np.int32).astype(np.float64)
+
+
+def uniform_u32(n, seed, hi=1 << 32):
+    """generateUniformUnsignedIntegers (:25-31); hi < 2^32 gives the
+    heavy-duplicate top-k input (uniform over [0, 2^16))."""
+    return _rng(seed).integers(0, hi, n, dtype=np.uint64).astype(np.uint32)
+
+
+def sorted_u32(n, seed):
+    """generateSortedArrayUints (:34-44)."""
+    return np.sort(uniform_u32(n, seed))
+
+
+def zero_to_four_u32(n, seed=0):
+    """generateUniformZeroToFourUints (:46-51): i % 4."""
+    return (np.arange(n, dtype=np.uint64) % 4).astype(np.uint32)
+
+
+GENERATORS = {
+    "f32": {
+        "uniform": uniform_f32, "normal": normal_f32, "half_normal": half_normal_f32,
+        "cauchy": cauchy_f32, "huge_uniform": huge_uniform_f32, "all_ones": all_ones_f32,
+        "ones_twos": ones_twos_f32, "noisy": noisy_f32, "killer": killer_f32,
+        "normal100": lambda n, s: normal_f32(n, s, 100.0), "uint_valued": uint_valued_f32,
+    },
+    "f64": {
+        "uniform": uniform_f64, "normal": normal_f64, "killer": killer_f64,
+        "cauchy": cauchy_f64, "uint_valued": uint_valued_f64,
+        "uniform_pm1e6": lambda n, s: uniform_f64(n, s, -1e6, 1e6),
+    },
+    "u32": {
+        "uniform": uniform_u32, "sorted": sorted_u32, "zero_to_four": zero_to_four_u32,
+        "uniform16": lambda n, s: uniform_u32(n, s, 1 << 16),
+    },
+}
+
+DTYPES = {"f32": np.float32, "f64": np.float64, "u32": np.uint32}
+
+
+def generate(dtype, dist, n, seed):
+    return np.ascontiguousarray(GENERATORS[dtype][dist](int(n), int(seed)))
+
+
+# ---------------------------------------------------------------------------
+# k lists (k-th largest, 1-based)
+# ---------------------------------------------------------------------------
+
+
+def k_pgrid(n, count=101):
+    """k = floor(p (n-1)) + 1 for p = 0, 1/(count-1), ..., 1."""
+    p = np.arange(count, dtype=np.float64) / (count - 1)
+    return (np.floor(p * (n - 1)) + 1).astype(np.uint32)
+
+
+def k_uniform(n, count):
+    """generateKUniform (generateProblems.cu:506-513), float32 arithmetic as
+    written there."""
+    k = np.empty(count, dtype=np.uint32)
+    i = np.arange(count, dtype=np.float32)
+    k[:] = ((i / np.float32(count)) * np.float32(n)).astype(np.uint32)
+    k[0] = 1
+    k[count - 1] = n
+    return k
+
+
+def k_uniform_random(n, count, seed):
+    """generateKUniformRandom (:489-504) with the k = 0 case mapped to 1."""
+    u = _rng(seed).random(count, dtype=np.float64)
+    return np.clip((u * n).astype(np.uint64) + 1, 1, n).astype(np.uint32)
+
+
+def k_distinct(n, count, seed):
+    """count distinct k's uniform over [1, n]."""
+    count = min(count, n)
+    r = _rng(seed)
+    ks = set()
+    while len(ks) < count:
+        ks.update((r.integers(1, n + 1, count - len(ks))).tolist())
+    out = np.array(sorted(ks), dtype=np.uint32)
+    r.shuffle(out)
+    return out
+
+
+def k_normal(n, count, seed):
+    """generateKNormal (:515-530): (|N| + 7) n / 14."""
+    z = np.abs(_rng(seed).standard_normal(count))
+    return np.clip(((z + 7) * (n / 14.0)).astype(np.uint64), 1, n).astype(np.uint32)
+
+
+def k_cluster(n, count, seed):
+    """generateKCluster (:533-557): clusters of 9 consecutive k's."""
+    k = np.ones(count, dtype=np.uint32)
+    u = _rng(seed).random(max(count // 9, 1))
+    fi = 0
+    for i in range(4, count, 9):
+        c = int(u[fi] * (n - 10) + 5)
+        fi += 1
+        k[i] = c
+        for j in range(1, 5):
+            k[i - j] = c - j
+            if i + j < count:
+                k[i + j] = c + j
+    return np.clip(k, 1, n).astype(np.uint32)
+
+
+def k_sectioned(n, count, seed):
+    """generateKSectioned (:559-576): count consecutive k's from a random
+    start."""
+    u = _rng(seed).random()
+    start = max(1, int(u * (n - count)))
+    return (start + np.arange(count, dtype=np.uint64)).clip(1, n).astype(np.uint32)

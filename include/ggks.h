@@ -1,0 +1,155 @@
+/*
+ * ggks.h -- C ABI of the GB300 (sm_103a) GGKS bucket multiselect / top-k.
+ *
+ * Plain C types only (pointers, sizes, status codes): any FFI can bind it.
+ * Paths in the citations are relative to the reference project
+ * (uysalere/ggks-multiSelect).
+ *
+ * Conventions shared by every entry point
+ *   - k is the k-th LARGEST element, 1-based, exactly as the reference wrapper
+ *     takes it (bucketMultiselect.cu:842-846): out[i] = ascending[n - k[i]].
+ *   - Results are bit-exact order statistics under the order-preserving key
+ *     order (keyConversion.cu:9-23): -0.0 < +0.0, NaNs beyond the infinities
+ *     by sign.  For every other input this is the numeric order.
+ *   - The input vector is never modified.  The k array is read, not written.
+ *   - Outputs are written in the caller's k order (bucketMultiselect.cu:816-818)
+ *     or, for top-k, in descending order (multiselectTimingFunctions.cu:156-177).
+ *   - Every call returns a ggks_status; nothing is reported through the
+ *     return value of a selection (the reference returns 1 for both success
+ *     and failure, bucketMultiselect.cu:30-32, :832).
+ *   - Calls are synchronous with respect to the host outputs: when a call
+ *     returns GGKS_OK, host outputs are filled.  Work is issued on the
+ *     context's stream (or opts->stream).
+ *   - n must satisfy 1 <= n <= GGKS_MAX_N; device vectors must be aligned to
+ *     their element size.
+ */
+#ifndef GGKS_H_
+#define GGKS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GGKS_VERSION 10000 /* 1.0.0 */
+#define GGKS_MAX_N 4294967295ull
+
+typedef enum ggks_status {
+  GGKS_OK = 0,
+  GGKS_INVALID_ARG = 1,   /* null pointer, n or num_k out of range, k not in [1, n] */
+  GGKS_OOM = 2,           /* device or pinned host allocation failed */
+  GGKS_CUDA_ERROR = 3,    /* a CUDA runtime call or kernel launch failed */
+  GGKS_TIMEOUT = 4,       /* a bounded device-side wait gave up */
+  GGKS_INTERNAL = 5,      /* a device-side consistency check failed */
+  GGKS_NO_DEVICE = 6,     /* no usable CUDA device */
+  GGKS_UNSUPPORTED = 7
+} ggks_status;
+
+typedef struct ggks_context ggks_context;
+
+/* Options shared by the selection entry points.  Pass NULL for defaults. */
+typedef struct ggks_opts {
+  ggks_context *ctx; /* NULL: the calling thread's current device's default context */
+  void *stream;      /* cudaStream_t; NULL: the context's own stream */
+  uint32_t flags;    /* GGKS_FLAG_* */
+  uint32_t reserved;
+} ggks_opts;
+
+/* opts->flags: the output pointer is device memory (no device-to-host copy). */
+#define GGKS_FLAG_OUT_DEVICE 1u
+
+/* ------------------------------------------------------------------------ */
+/* Multiselect                                                               */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces BucketMultiselect::bucketMultiselectWrapper<T>
+ * (bucketMultiselect.cu:837-871): d_vec is a device vector of n elements,
+ * h_k a host array of num_k k's (k-th largest), h_out a host array of num_k
+ * results in the caller's k order.  The reference's blocks/threads launch
+ * arguments have no counterpart: launch shapes are chosen per problem. */
+int ggks_multiselect_f32(const float *d_vec, uint64_t n, const uint32_t *h_k, uint32_t num_k,
+                         float *h_out, const ggks_opts *opts);
+int ggks_multiselect_f64(const double *d_vec, uint64_t n, const uint32_t *h_k, uint32_t num_k,
+                         double *h_out, const ggks_opts *opts);
+int ggks_multiselect_u32(const uint32_t *d_vec, uint64_t n, const uint32_t *h_k,
+                         uint32_t num_k, uint32_t *h_out, const ggks_opts *opts);
+
+/* Replaces the timing adapter's host-vector form timeBucketMultiselect<T>
+ * (multiselectTimingFunctions.cu:100-122): the vector is in host memory and is
+ * copied to the device inside the call (overlapped with the first pass). */
+int ggks_multiselect_host_f32(const float *h_vec, uint64_t n, const uint32_t *h_k,
+                              uint32_t num_k, float *h_out, const ggks_opts *opts);
+int ggks_multiselect_host_f64(const double *h_vec, uint64_t n, const uint32_t *h_k,
+                              uint32_t num_k, double *h_out, const ggks_opts *opts);
+int ggks_multiselect_host_u32(const uint32_t *h_vec, uint64_t n, const uint32_t *h_k,
+                              uint32_t num_k, uint32_t *h_out, const ggks_opts *opts);
+
+/* ------------------------------------------------------------------------ */
+/* Top-k                                                                     */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces timeBucketTopkselect<T> (multiselectTimingFunctions.cu:205-231),
+ * which runs the bucket multiselect with k = 1..K, and the top-k wrapper
+ * signature randomizedTopkSelectWrapper<T> (randomizedTopkSelect.cu:210-213):
+ * h_out receives the K largest values of d_vec in descending order. */
+int ggks_topk_f32(const float *d_vec, uint64_t n, uint32_t K, float *h_out,
+                  const ggks_opts *opts);
+int ggks_topk_f64(const double *d_vec, uint64_t n, uint32_t K, double *h_out,
+                  const ggks_opts *opts);
+int ggks_topk_u32(const uint32_t *d_vec, uint64_t n, uint32_t K, uint32_t *h_out,
+                  const ggks_opts *opts);
+
+/* Host-vector form of the above (multiselectTimingFunctions.cu:205-231 takes
+ * h_vec). */
+int ggks_topk_host_f32(const float *h_vec, uint64_t n, uint32_t K, float *h_out,
+                       const ggks_opts *opts);
+int ggks_topk_host_f64(const double *h_vec, uint64_t n, uint32_t K, double *h_out,
+                       const ggks_opts *opts);
+int ggks_topk_host_u32(const uint32_t *h_vec, uint64_t n, uint32_t K, uint32_t *h_out,
+                       const ggks_opts *opts);
+
+/* ------------------------------------------------------------------------ */
+/* Contexts, statistics, utilities                                           */
+/* ------------------------------------------------------------------------ */
+
+/* A context owns a device, a stream, a device workspace and pinned staging.
+ * Calls on one context are serialised by the context; use one context per
+ * host thread for concurrency.  (The reference keeps its timer in namespace
+ * globals, bucketMultiselect.cu:49-50, and is not thread-safe.) */
+int ggks_context_create(int device, ggks_context **out);
+int ggks_context_destroy(ggks_context *ctx);
+
+/* Per-pass statistics of a context, accumulated since the last reset. */
+#define GGKS_NUM_PASSES 6
+typedef struct ggks_stats {
+  uint64_t calls;                     /* selection calls completed */
+  uint64_t launches;                  /* kernels launched by this library */
+  uint64_t pass_launches[GGKS_NUM_PASSES];
+  double pass_ms[GGKS_NUM_PASSES];    /* device time per pass (profiling on) */
+  uint64_t bytes_in;                  /* algorithmic input bytes (n * sizeof(T)) */
+  uint64_t survivors;                 /* elements compacted into active buckets */
+  uint64_t retries;                   /* survivor-buffer regrowth re-runs */
+  uint64_t recursions;                /* oversized segments re-selected */
+} ggks_stats;
+
+/* pass indices of ggks_stats.pass_* */
+#define GGKS_PASS_SAMPLE 0   /* sample + splitter table build */
+#define GGKS_PASS_HIST 1     /* bucket histogram over the input */
+#define GGKS_PASS_SCAN 2     /* bucket-count reduce + decoupled-lookback scan */
+#define GGKS_PASS_PLAN 3     /* k -> bucket marker, slot and request layout */
+#define GGKS_PASS_COMPACT 4  /* compaction of active-bucket elements */
+#define GGKS_PASS_FINISH 5   /* per-segment in-shared-memory selection */
+
+int ggks_context_get_stats(ggks_context *ctx, ggks_stats *out);
+int ggks_context_reset_stats(ggks_context *ctx);
+/* on != 0: time every pass with CUDA events on the context's stream */
+int ggks_context_set_profiling(ggks_context *ctx, int on);
+const char *ggks_status_string(int status);
+int ggks_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GGKS_H_ */

@@ -1,0 +1,113 @@
+"""CPU tests of the C ABI: the library builds for sm_103a, loads, exports
+every symbol include/ggks.h declares, and rejects invalid arguments before
+touching the device (no compute call runs without a GPU)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "ggks.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import ggks_build
+    ggks_build.build()
+    import ggks
+    return ggks.lib()
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(ggks_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for t in ("f32", "f64", "u32"):
+        for stem in ("ggks_multiselect_", "ggks_multiselect_host_", "ggks_topk_", "ggks_topk_host_"):
+            assert stem + t in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    import ggks
+    names = declared_functions()
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(names) <= set(ggks.EXPORTS) | set(names)
+    assert lib.ggks_version() == 10000
+
+
+def test_binary_is_sm103a(lib):
+    import ggks
+    # the fat binary carries sm_103a code (checked through nvcc's own listing
+    # tool would need a GPU-free dump; the build flags are asserted instead)
+    import ggks_build
+    assert "arch=compute_103a,code=sm_103a" in ggks_build.ARCH
+    assert os.path.getsize(ggks.LIB_PATH) > 100_000
+
+
+def test_status_strings(lib):
+    import ggks
+    assert ggks.status_string(0) == "ok"
+    assert ggks.status_string(1) == "invalid argument"
+
+
+@pytest.mark.parametrize("sfx,dt", [("f32", np.float32), ("f64", np.float64), ("u32", np.uint32)])
+def test_invalid_arguments_rejected_without_device(lib, sfx, dt):
+    import ggks
+    f = getattr(lib, "ggks_multiselect_" + sfx)
+    out = np.empty(4, dtype=dt)
+    k = np.array([1, 2, 3, 4], dtype=np.uint32)
+    fake = ctypes.c_void_p(1 << 20)  # never dereferenced: validation fails first
+    o = ggks.Opts()
+    # null vector, zero n, zero num_k, null k, null out
+    assert f(None, 10, k.ctypes.data, 4, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+    assert f(fake, 0, k.ctypes.data, 4, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+    assert f(fake, 10, k.ctypes.data, 0, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+    assert f(fake, 10, None, 4, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+    assert f(fake, 10, k.ctypes.data, 4, None, ctypes.byref(o)) == ggks.INVALID_ARG
+    # k outside [1, n] (generateKUniformRandom can emit k = 0)
+    bad = np.array([0, 1, 2, 3], dtype=np.uint32)
+    assert f(fake, 10, bad.ctypes.data, 4, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+    bad = np.array([1, 2, 3, 11], dtype=np.uint32)
+    assert f(fake, 10, bad.ctypes.data, 4, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+    # n beyond 2^32 - 1
+    assert f(fake, 1 << 32, k.ctypes.data, 4, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+    # misaligned device pointer
+    if dt().itemsize > 1:
+        mis = ctypes.c_void_p((1 << 20) + 1)
+        assert f(mis, 10, k.ctypes.data, 4, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+    g = getattr(lib, "ggks_topk_" + sfx)
+    assert g(fake, 10, 11, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+    assert g(fake, 10, 0, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+    assert g(None, 10, 3, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+
+
+def test_cpp_reference_mirror_header_compiles(lib, tmp_path):
+    """The C++ mirror of the reference interface compiles against the C ABI
+    (link only: nothing runs)."""
+    import subprocess
+    src = tmp_path / "mirror.cpp"
+    src.write_text(
+        '#include "ggks_bucket_multiselect.hpp"\n'
+        "int main(int argc, char** argv) {\n"
+        "  if (argc < 100) return 0;\n"
+        "  float* d = nullptr; unsigned k[2] = {1, 2}; float out[2];\n"
+        "  BucketMultiselect::bucketMultiselectWrapper(d, 10, k, 2, out, 152, 1024);\n"
+        "  results_t<float>* r = timeBucketMultiselect(out, 2u, k, 2u);\n"
+        "  results_t<float>* t = timeBucketTopkselect(out, 2u, 1u);\n"
+        "  float* tk = randomizedTopkSelectWrapper(d, 10, 2);\n"
+        "  free(tk); freeResults(r); freeResults(t);\n"
+        "  return 0;\n}\n")
+    import ggks
+    exe = tmp_path / "mirror"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", str(src), "-I", os.path.join(ROOT, "include"),
+                        ggks.LIB_PATH, "-o", str(exe), "-Wl,-rpath," + os.path.dirname(ggks.LIB_PATH)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
