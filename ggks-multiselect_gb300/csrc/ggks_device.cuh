@@ -251,17 +251,19 @@ __device__ __forceinline__ uint32_t hash32(uint32_t a) {
 // j cut into 2^b sub-buckets starting at bucket B_j: rs = shift - b and
 // C = B_j - (j << b).  Merged empty slices use b = 0; the top entry (keys
 // above the sampled span) uses rs = key width, i.e. a constant bucket.
+// Bucket 0 holds the keys below `base` (the sampled minimum); the table's
+// buckets start at 1, so the first of them starts exactly at `base`.
 template <class K>
 __device__ __forceinline__ uint32_t bucket_of(K key, K base, uint32_t shift, const uint2 *lut) {
-  K d = key > base ? key - base : K(0);
-  K idx = d >> shift;
-  uint32_t j = idx < (K)kLutIdx ? (uint32_t)idx : kLutIdx;
-  uint2 e = lut[j];
-  return e.x + shr_clamp(d, e.y);
+  const K d = key - base;  // wraps for key < base; that result is discarded
+  const K idx = d >> shift;
+  const uint32_t j = idx < (K)kLutIdx ? (uint32_t)idx : kLutIdx;
+  const uint2 e = lut[j];
+  const uint32_t b = e.x + shr_clamp(d, e.y);
+  return key < base ? 0u : b;
 }
 
-// smallest key that maps to bucket b (b < nb); keys below `base` map to the
-// first bucket, so its smallest key is 0.
+// smallest key that maps to bucket b (b < nb); bucket 0 starts at key 0.
 template <class K>
 __device__ __forceinline__ K bucket_lo(uint32_t b, K base, uint32_t shift, const uint2 *lut) {
   if (b == 0) return K(0);
@@ -420,10 +422,12 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
     }
     return prev_nonempty[q] ? 1u : 0u;
   };
+  // buckets in use for threshold t: the low-edge bucket 0, the slices, and
+  // the top entry when it starts a run of its own
   auto total_for = [&](int t) -> uint32_t {
     uint32_t s = contrib(0, t) + contrib(1, t) + contrib(2, t) + contrib(3, t);
     s = block_reduce(s, [](uint32_t a, uint32_t b) { return a + b; }, red32);
-    return s + (top_run_start ? 1u : 0u);
+    return 1u + s + (top_run_start ? 1u : 0u);
   };
   // smallest t with total(t) <= nb_max (total is non-increasing in t)
   int tlo = -kMaxSubBits - 1, thi = 33;
@@ -444,7 +448,7 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
   }
   uint32_t total;
   uint32_t incl = block_incl_scan(mysum, &total, red32);
-  uint32_t run = incl - mysum;
+  uint32_t run = incl - mysum + 1u;  // bucket 0 is the low edge
   uint32_t max_per_bucket = 0;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
@@ -468,9 +472,9 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
   max_per_bucket = block_reduce(max_per_bucket, [](uint32_t a, uint32_t b) { return a > b ? a : b; },
                                 red32);
   if (tid == 0) {
-    const uint32_t nb = total + (top_run_start ? 1u : 0u);
+    const uint32_t nb = 1u + total + (top_run_start ? 1u : 0u);
     uint2 e;
-    e.x = top_run_start ? total : total - 1u;
+    e.x = top_run_start ? total + 1u : total;
     e.y = (uint32_t)KeyMax<K>::bits;
     lut[kLutIdx] = e;
     LutHeader<K> h;
