@@ -353,14 +353,9 @@ int ggks_context_get_stats(ggks_context *ctx, ggks_stats *out) {
   if (!c) return st;
   std::lock_guard<std::mutex> lk(c->mu);
   *out = c->stats;
-  // recursive levels count toward their parent
-  for (Context *ch = c->child.get(); ch; ch = ch->child.get()) {
-    out->launches += ch->stats.launches;
-    for (int i = 0; i < GGKS_NUM_PASSES; ++i) {
-      out->pass_launches[i] += ch->stats.pass_launches[i];
-      out->pass_ms[i] += ch->stats.pass_ms[i];
-    }
-  }
+  // kernels of recursive levels count toward the total; the per-pass figures
+  // describe the top level only
+  for (Context *ch = c->child.get(); ch; ch = ch->child.get()) out->launches += ch->stats.launches;
   return GGKS_OK;
 }
 

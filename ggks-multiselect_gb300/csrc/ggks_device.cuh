@@ -911,8 +911,36 @@ __global__ void __launch_bounds__(1024, 1)
 }
 
 // ---------------------------------------------------------------------------
-// (g) per-segment finish: shared-memory bitonic sort + gather
+// (g) per-segment finish: shared-memory MSD radix select
 // ---------------------------------------------------------------------------
+// One CTA per segment (persistent over segments).  The segment's keys are
+// read from the survivor buffer (L2-resident) three times: min/max, a
+// 2048-bin histogram of the top 11 bits of (key - min), and a gather of only
+// the bins that hold requested ranks into shared memory.  Each gathered bin is
+// sorted (a warp bitonic network for bins of <= 32 keys, a CTA bitonic sort for
+// larger ones) and every request reads its rank.  Segments whose needed bins
+// exceed the shared-memory buffer are listed for a recursive re-selection.
+constexpr int kFinBins = 2048;
+constexpr int kFinBinBits = 11;
+constexpr int kFinThreads = 512;
+
+template <class K>
+__device__ __forceinline__ K warp_bitonic32(K v) {
+  const uint32_t lane = threadIdx.x & 31;
+#pragma unroll
+  for (uint32_t k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      const K o = __shfl_xor_sync(0xffffffffu, v, j);
+      const bool up = (lane & k) == 0;
+      const bool lower = (lane & j) == 0;
+      const K mn = v < o ? v : o, mx = v < o ? o : v;
+      v = (lower == up) ? mn : mx;
+    }
+  }
+  return v;
+}
+
 template <class K>
 __device__ __forceinline__ void bitonic_sort_smem(K *s, uint32_t P) {
   for (uint32_t k = 2; k <= P; k <<= 1) {
@@ -932,36 +960,154 @@ __device__ __forceinline__ void bitonic_sort_smem(K *s, uint32_t P) {
   }
 }
 
+// last bin with start[bin] <= r (start is an exclusive scan, start[0] = 0)
+__device__ __forceinline__ uint32_t bin_of_rank(const uint32_t *start, uint32_t r) {
+  uint32_t lo = 0, hi = kFinBins;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (start[mid] <= r)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
 template <class K, class OutT>
-__global__ void __launch_bounds__(1024)
+__global__ void __launch_bounds__(kFinThreads)
     k_finish(const K *__restrict__ surv, Ctrl *ctrl, const uint64_t *__restrict__ seg_off,
              const uint32_t *__restrict__ seg_size, const uint32_t *__restrict__ kstart,
              const uint32_t *__restrict__ kcnt, const Req *__restrict__ klist,
-             uint32_t *__restrict__ deferred, uint32_t cap_keys, OutT *__restrict__ out) {
+             uint32_t *__restrict__ deferred, uint32_t bcap, OutT *__restrict__ out) {
   extern __shared__ uint4 smem_raw[];
-  K *s = reinterpret_cast<K *>(smem_raw);
+  uint32_t *hist = reinterpret_cast<uint32_t *>(smem_raw);
+  uint32_t *start = hist + kFinBins;
+  uint32_t *gofs = start + kFinBins;  // gather offset of a needed bin, else kNoSlot
+  uint32_t *cur = gofs + kFinBins;
+  K *B = reinterpret_cast<K *>(cur + kFinBins);  // gathered keys of the needed bins
+  K *T = B + bcap;                               // scratch for sorting a large bin
+  __shared__ K redk[33];
+  __shared__ uint32_t red32[33];
+  constexpr uint32_t PER = kFinBins / kFinThreads;  // bins per thread
+
   if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
   const uint32_t num_slots = ctrl->num_slots;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t nwarps = blockDim.x >> 5;
   for (uint32_t slot = blockIdx.x; slot < num_slots; slot += gridDim.x) {
     const uint32_t size = seg_size[slot];
-    if (size > cap_keys) {
-      if (threadIdx.x == 0) {
+    const K *src = surv + seg_off[slot];
+    const Req *rq = klist + kstart[slot];
+    const uint32_t m = kcnt[slot];
+
+    // ---- min / max
+    K mn = KeyMax<K>::v, mx = 0;
+    for (uint32_t i = tid; i < size; i += blockDim.x) {
+      const K k = src[i];
+      mn = k < mn ? k : mn;
+      mx = k > mx ? k : mx;
+    }
+    mn = block_reduce(mn, [](K a, K b) { return a < b ? a : b; }, redk);
+    mx = block_reduce(mx, [](K a, K b) { return a > b ? a : b; }, redk);
+    if (mn == mx) {  // one distinct key: every rank is that key
+      for (uint32_t j = tid; j < m; j += blockDim.x) out[rq[j].out] = Traits<OutT>::value(mn);
+      continue;  // block_reduce ends with a barrier: shared state is free
+    }
+    const int bl = bitlen<K>(mx - mn);
+    const uint32_t sh = bl > kFinBinBits ? (uint32_t)(bl - kFinBinBits) : 0u;
+
+    // ---- histogram
+    for (uint32_t i = tid; i < kFinBins; i += blockDim.x) {
+      hist[i] = 0;
+      cur[i] = 0;
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < size; i += blockDim.x)
+      atomicAdd(&hist[(uint32_t)((src[i] - mn) >> sh)], 1u);
+    __syncthreads();
+    {
+      uint32_t c[PER], sum = 0;
+#pragma unroll
+      for (uint32_t q = 0; q < PER; ++q) {
+        c[q] = hist[tid * PER + q];
+        sum += c[q];
+      }
+      uint32_t tot;
+      uint32_t run = block_incl_scan(sum, &tot, red32) - sum;
+#pragma unroll
+      for (uint32_t q = 0; q < PER; ++q) {
+        start[tid * PER + q] = run;
+        gofs[tid * PER + q] = 0;  // "needed" flag until the next scan
+        run += c[q];
+      }
+    }
+    __syncthreads();
+    for (uint32_t j = tid; j < m; j += blockDim.x) gofs[bin_of_rank(start, rq[j].rank)] = 1u;
+    __syncthreads();
+    uint32_t V;
+    {
+      uint32_t c[PER], sum = 0;
+#pragma unroll
+      for (uint32_t q = 0; q < PER; ++q) {
+        const uint32_t b = tid * PER + q;
+        c[q] = gofs[b] ? hist[b] : 0u;
+        sum += c[q];
+      }
+      uint32_t run = block_incl_scan(sum, &V, red32) - sum;
+#pragma unroll
+      for (uint32_t q = 0; q < PER; ++q) {
+        const uint32_t b = tid * PER + q;
+        const bool need = gofs[b] != 0u;
+        gofs[b] = need ? run : kNoSlot;
+        run += c[q];
+      }
+    }
+    __syncthreads();
+    if (V > bcap) {  // the needed bins do not fit: re-select on the host side
+      if (tid == 0) {
         const uint32_t d = atomicAdd(&ctrl->deferred_count, 1u);
         deferred[d] = slot;
         atomicOr(&ctrl->status, ST_DEFERRED);
       }
+      __syncthreads();
       continue;
     }
-    uint32_t P = 1;
-    while (P < size) P <<= 1;
-    const K *src = surv + seg_off[slot];
-    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s[i] = i < size ? src[i] : KeyMax<K>::v;
+
+    // ---- gather the needed bins
+    for (uint32_t i = tid; i < size; i += blockDim.x) {
+      const K k = src[i];
+      const uint32_t b = (uint32_t)((k - mn) >> sh);
+      const uint32_t g = gofs[b];
+      if (g != kNoSlot) B[g + atomicAdd(&cur[b], 1u)] = k;
+    }
     __syncthreads();
-    bitonic_sort_smem(s, P);
-    const uint32_t k0 = kstart[slot], kc = kcnt[slot];
-    for (uint32_t j = threadIdx.x; j < kc; j += blockDim.x) {
-      const Req e = klist[k0 + j];
-      out[e.out] = Traits<OutT>::value(s[e.rank]);
+
+    // ---- sort each needed bin: warps take the small ones
+    for (uint32_t b = warp; b < kFinBins; b += nwarps) {
+      const uint32_t g = gofs[b], c = hist[b];
+      if (g == kNoSlot || c < 2 || c > 32) continue;
+      K v = lane < c ? B[g + lane] : KeyMax<K>::v;
+      v = warp_bitonic32(v);
+      if (lane < c) B[g + lane] = v;
+    }
+    __syncthreads();
+    for (uint32_t b = 0; b < kFinBins; ++b) {  // large bins: the whole CTA
+      const uint32_t g = gofs[b], c = hist[b];
+      if (g == kNoSlot || c <= 32) continue;
+      uint32_t P = 64;
+      while (P < c) P <<= 1;
+      for (uint32_t i = tid; i < P; i += blockDim.x) T[i] = i < c ? B[g + i] : KeyMax<K>::v;
+      __syncthreads();
+      bitonic_sort_smem(T, P);
+      for (uint32_t i = tid; i < c; i += blockDim.x) B[g + i] = T[i];
+      __syncthreads();
+    }
+
+    // ---- answer
+    for (uint32_t j = tid; j < m; j += blockDim.x) {
+      const Req e = rq[j];
+      const uint32_t b = bin_of_rank(start, e.rank);
+      out[e.out] = Traits<OutT>::value(B[gofs[b] + (e.rank - start[b])]);
     }
     __syncthreads();
   }

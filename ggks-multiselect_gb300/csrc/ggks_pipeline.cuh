@@ -10,9 +10,16 @@
 
 namespace ggks {
 
+// keys of needed bins that one finishing CTA holds in shared memory (plus an
+// equal scratch area for sorting a large bin)
 template <class T>
 static inline uint32_t cap_keys_for() {
-  return sizeof(typename Traits<T>::K) == 4 ? 16384u : 8192u;
+  return sizeof(typename Traits<T>::K) == 4 ? 8192u : 4096u;
+}
+template <class T>
+static inline int finish_smem_bytes() {
+  using K = typename Traits<T>::K;
+  return (int)(4 * kFinBins * sizeof(uint32_t) + 2 * (size_t)cap_keys_for<T>() * sizeof(K));
 }
 
 static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -235,11 +242,12 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       ran[GGKS_PASS_COMPACT] = true;
     }
     {
-      const int smem = (int)((size_t)p.cap_keys * sizeof(K));
+      const int smem = finish_smem_bytes<InT>();
       set_smem_max<k_finish<K, OutT>>(smem);
       PassTimer t(ctx, s, GGKS_PASS_FINISH);
-      k_finish<K, OutT><<<p.fin_grid, 1024, smem, s>>>(surv, ctrl, seg_off, seg_size, kstart, kcnt,
-                                                       klist, deferred, p.cap_keys, d_out);
+      k_finish<K, OutT><<<p.fin_grid, kFinThreads, smem, s>>>(surv, ctrl, seg_off, seg_size, kstart,
+                                                              kcnt, klist, deferred, p.cap_keys,
+                                                              d_out);
       ran[GGKS_PASS_FINISH] = true;
     }
   };
