@@ -21,8 +21,9 @@
 //                 sample shows heavy duplicates); one row of counts per CTA.
 //                 Replaces assignSmartBucket (bucketMultiselect.cu:129-205)
 //                 without its 4n-byte element-to-bucket array.
-//   (d) scan      k_scan: sums the per-CTA rows per bucket and computes the
-//                 global exclusive prefix with a single-pass decoupled
+//   (d) scan      k_scan: sums the per-CTA rows per bucket (rewriting each
+//                 column as its exclusive prefix over the CTAs) and computes
+//                 the global exclusive prefix with a single-pass decoupled
 //                 look-back scan (bounded spin).  Replaces sumCounts
 //                 (:214-221) and the host walk of findKBuckets (:87-111).
 //   (e) plan      k_plan: one CTA maps every requested rank to its bucket and
@@ -30,9 +31,13 @@
 //                 directly, assigns compact slots to the active buckets and
 //                 groups the requests by slot.  Replaces the host reindex loop
 //                 and reindexCounts (:714-756).
-//   (f) compact   k_compact: second pass over the input; elements of active
-//                 buckets are appended to their slot's segment of the
-//                 survivor buffer (keys).  Replaces copyElements (:249-308).
+//   (f) compact   k_compact: second pass over the input with the same
+//                 CTA-to-tile assignment as (c); every CTA starts a private
+//                 shared-memory cursor per active bucket at its prefix from
+//                 (d), so elements of active buckets land in their segment of
+//                 the survivor buffer with shared-memory atomics only.
+//                 Replaces copyElements (:249-308) and reindexCounts
+//                 (:229-241).
 //   (g) finish    k_finish: per segment, an in-shared-memory sort of the
 //                 survivors and a gather of the requested ranks.  Replaces
 //                 thrust::sort of all survivors + copyValuesInChunk
@@ -80,6 +85,8 @@ struct Ctrl {
   uint32_t scan_ticket;  // dynamic tile ids of k_scan (reset by k_plan)
   uint32_t nb;           // buckets in use
   uint64_t cap_needed;
+  uint64_t kmin_inv;     // ~(smallest sampled key), by atomicMax
+  uint64_t kmax;         // largest sampled key, by atomicMax
 };
 
 template <class K>
@@ -347,7 +354,14 @@ __device__ __forceinline__ V block_reduce(V v, Op op, V *sh /* >= 32 */) {
 // (b) sample + splitter table
 // ---------------------------------------------------------------------------
 // Grid: ceil(S / 1024) CTAs of 1024 threads.  Every thread gathers one key;
-// the last CTA to finish builds the table.
+// each CTA folds its min / max into Ctrl with one atomic each; the last CTA to
+// finish counts the samples per slice and builds the table.
+//
+// Allocation: a slice with c samples gets 2^b sub-buckets,
+// b = clamp(ceil(log2 c) - t, 0, min(shift, 20)), and empty slices merge into
+// one bucket per run.  The smallest threshold t whose bucket total fits nb_max
+// is found from a histogram of ceil(log2 c) over the slices, so each candidate
+// t costs a 33-term sum on one thread.
 template <class T>
 __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, uint64_t n,
                                                      uint32_t S, uint32_t seed,
@@ -356,20 +370,32 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
                                                      LutHeader<typename Traits<T>::K> *hdr,
                                                      uint2 *lut, uint32_t nb_max) {
   using K = typename Traits<T>::K;
-  __shared__ uint32_t cnt[kLutEntries + 3];
+  __shared__ uint32_t cnt[kLutIdx];
+  __shared__ uint32_t lch[36];  // [0, 33): slices by ceil(log2 c); [34]: empty-run starts
   __shared__ K redk[33];
   __shared__ uint32_t red32[33];
   __shared__ uint32_t s_last;
+  __shared__ int s_t;
 
   const uint32_t tid = threadIdx.x;
   const uint32_t i = blockIdx.x * blockDim.x + tid;
+  K mine_lo = KeyMax<K>::v, mine_hi = 0;
   if (i < S) {
     uint64_t pos;
     if ((uint64_t)S >= n)
       pos = i;
     else
       pos = ((uint64_t)hash32(i * 0x9E3779B9u + seed) * n) >> 32;
-    samples[i] = Traits<T>::key(x[pos]);
+    const K k = Traits<T>::key(x[pos]);
+    samples[i] = k;
+    mine_lo = k;
+    mine_hi = k;
+  }
+  mine_lo = block_reduce(mine_lo, [](K p, K q) { return p < q ? p : q; }, redk);
+  mine_hi = block_reduce(mine_hi, [](K p, K q) { return p > q ? p : q; }, redk);
+  if (tid == 0) {
+    atomicMax((unsigned long long *)&ctrl->kmin_inv, (unsigned long long)~(uint64_t)mine_lo);
+    atomicMax((unsigned long long *)&ctrl->kmax, (unsigned long long)mine_hi);
   }
   __threadfence();
   __syncthreads();
@@ -378,98 +404,92 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
   if (!s_last) return;
   __threadfence();
 
-  // --- span of the sample
-  K kmin = KeyMax<K>::v, kmax = 0;
-  for (uint32_t s = tid; s < S; s += blockDim.x) {
-    K k = __ldcg(samples + s);
-    kmin = k < kmin ? k : kmin;
-    kmax = k > kmax ? k : kmax;
-  }
-  kmin = block_reduce(kmin, [](K a, K b) { return a < b ? a : b; }, redk);
-  kmax = block_reduce(kmax, [](K a, K b) { return a > b ? a : b; }, redk);
+  const K kmin = (K)~__ldcg((const unsigned long long *)&ctrl->kmin_inv);
+  const K kmax = (K)__ldcg((const unsigned long long *)&ctrl->kmax);
   const int bl = bitlen<K>(kmax - kmin);
   const uint32_t shift = bl > kLutIdxBits ? (uint32_t)(bl - kLutIdxBits) : 0u;
   const int bcap = (int)(shift < (uint32_t)kMaxSubBits ? shift : (uint32_t)kMaxSubBits);
 
   // --- sample counts per slice
-  for (uint32_t j = tid; j < kLutEntries + 3; j += blockDim.x) cnt[j] = 0;
+  for (uint32_t j = tid; j < kLutIdx; j += blockDim.x) cnt[j] = 0;
+  if (tid < 36) lch[tid] = 0;
   __syncthreads();
+#pragma unroll 8
   for (uint32_t s = tid; s < S; s += blockDim.x) {
-    K k = __ldcg(samples + s);
+    const K k = __ldcg(samples + s);
     atomicAdd(&cnt[(uint32_t)((k - kmin) >> shift)], 1u);
   }
   __syncthreads();
 
-  // Each thread owns 4 consecutive slices [4 tid, 4 tid + 4); thread 0 also
-  // owns the top entry kLutIdx (appended after the scan).
+  // Each thread owns 4 consecutive slices [4 tid, 4 tid + 4); the top entry
+  // (keys above the sampled span) is written by thread 0 after the scan.
   int lc[4];
   uint32_t c[4];
   bool prev_nonempty[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    uint32_t j = 4 * tid + q;
+    const uint32_t j = 4 * tid + q;
     c[q] = cnt[j];
     lc[q] = c[q] ? (c[q] == 1 ? 0 : 32 - __clz(c[q] - 1)) : -1;  // ceil(log2 c)
     prev_nonempty[q] = (j == 0) ? true : (cnt[j - 1] != 0);
+    if (c[q])
+      atomicAdd(&lch[lc[q]], 1u);
+    else if (prev_nonempty[q])
+      atomicAdd(&lch[34], 1u);
   }
   const bool top_run_start = cnt[kLutIdx - 1] != 0;
-
-  auto contrib = [&](int q, int t) -> uint32_t {
-    if (c[q]) {
-      int b = lc[q] - t;
-      b = b < 0 ? 0 : (b > bcap ? bcap : b);
-      return 1u << b;
+  __syncthreads();
+  if (tid == 0) {
+    // smallest t with total(t) <= nb_max; total is non-increasing in t and
+    // total(33) <= 1 + 4096 + 1 <= nb_max
+    int t = -kMaxSubBits - 1;
+    for (; t < 33; ++t) {
+      uint64_t tot = 1u + lch[34] + (top_run_start ? 1u : 0u);
+      for (int l = 0; l < 33; ++l) {
+        int b = l - t;
+        b = b < 0 ? 0 : (b > bcap ? bcap : b);
+        tot += (uint64_t)lch[l] << b;
+      }
+      if (tot <= nb_max) break;
     }
-    return prev_nonempty[q] ? 1u : 0u;
-  };
-  // buckets in use for threshold t: the low-edge bucket 0, the slices, and
-  // the top entry when it starts a run of its own
-  auto total_for = [&](int t) -> uint32_t {
-    uint32_t s = contrib(0, t) + contrib(1, t) + contrib(2, t) + contrib(3, t);
-    s = block_reduce(s, [](uint32_t a, uint32_t b) { return a + b; }, red32);
-    return 1u + s + (top_run_start ? 1u : 0u);
-  };
-  // smallest t with total(t) <= nb_max (total is non-increasing in t)
-  int tlo = -kMaxSubBits - 1, thi = 33;
-  while (tlo < thi) {
-    int mid = (tlo + thi) >> 1;  // arithmetic shift: floor for negatives
-    if (total_for(mid) <= nb_max)
-      thi = mid;
-    else
-      tlo = mid + 1;
+    s_t = t;
   }
-  const int t = tlo;
+  __syncthreads();
+  const int t = s_t;
 
+  auto bits_of = [&](int q) -> int {
+    int b = lc[q] - t;
+    return b < 0 ? 0 : (b > bcap ? bcap : b);
+  };
   uint32_t my[4], mysum = 0;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    my[q] = contrib(q, t);
+    my[q] = c[q] ? (1u << bits_of(q)) : (prev_nonempty[q] ? 1u : 0u);
     mysum += my[q];
   }
   uint32_t total;
-  uint32_t incl = block_incl_scan(mysum, &total, red32);
+  const uint32_t incl = block_incl_scan(mysum, &total, red32);
   uint32_t run = incl - mysum + 1u;  // bucket 0 is the low edge
   uint32_t max_per_bucket = 0;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    uint32_t j = 4 * tid + q;
+    const uint32_t j = 4 * tid + q;
     uint2 e;
     if (c[q]) {
-      int b = lc[q] - t;
-      b = b < 0 ? 0 : (b > bcap ? bcap : b);
+      const int b = bits_of(q);
       e.x = run - (j << b);
       e.y = shift - (uint32_t)b;
-      uint32_t per = c[q] >> b;
+      const uint32_t per = c[q] >> b;
       max_per_bucket = per > max_per_bucket ? per : max_per_bucket;
     } else {
-      uint32_t B = prev_nonempty[q] ? run : run - 1u;
+      const uint32_t B = prev_nonempty[q] ? run : run - 1u;
       e.x = B - j;  // (d >> shift) == j on this slice
       e.y = shift;
     }
     lut[j] = e;
     run += my[q];
   }
-  max_per_bucket = block_reduce(max_per_bucket, [](uint32_t a, uint32_t b) { return a > b ? a : b; },
+  max_per_bucket = block_reduce(max_per_bucket, [](uint32_t p, uint32_t q) { return p > q ? p : q; },
                                 red32);
   if (tid == 0) {
     const uint32_t nb = 1u + total + (top_run_start ? 1u : 0u);
@@ -598,7 +618,7 @@ constexpr uint64_t kValMask = (1ull << 62) - 1;
 
 template <class K>
 __global__ void __launch_bounds__(kScanTile)
-    k_scan(const uint32_t *__restrict__ partials, uint32_t rows, uint32_t nb_max,
+    k_scan(uint32_t *__restrict__ partials, uint32_t rows, uint32_t nb_max,
            const LutHeader<K> *hdr, uint32_t *__restrict__ counts, uint32_t *__restrict__ excl,
            uint64_t *tile_state, Ctrl *ctrl) {
   __shared__ uint32_t s_tile;
@@ -613,16 +633,25 @@ __global__ void __launch_bounds__(kScanTile)
   const uint32_t b = tile * kScanTile + threadIdx.x;
   uint32_t c = 0;
   if (b < nb) {
-    const uint32_t *p = partials + b;
+    // column b of the per-CTA rows becomes its exclusive prefix over the rows:
+    // the compaction pass starts CTA r's cursor for bucket b there
+    uint32_t *p = partials + b;
     uint32_t r = 0;
-    uint32_t acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (; r + 8 <= rows; r += 8) {
+      uint32_t v[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) acc[q] += __ldcg(p + (uint64_t)(r + q) * nb_max);
+      for (int q = 0; q < 8; ++q) v[q] = __ldcg(p + (uint64_t)(r + q) * nb_max);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        p[(uint64_t)(r + q) * nb_max] = c;
+        c += v[q];
+      }
     }
-    for (; r < rows; ++r) acc[0] += __ldcg(p + (uint64_t)r * nb_max);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) c += acc[q];
+    for (; r < rows; ++r) {
+      const uint32_t v = __ldcg(p + (uint64_t)r * nb_max);
+      p[(uint64_t)r * nb_max] = c;
+      c += v;
+    }
   }
   uint32_t agg;
   const uint32_t incl = block_incl_scan(c, &agg, red);
@@ -687,9 +716,9 @@ __global__ void __launch_bounds__(1024, 1)
            uint64_t *tile_state, uint32_t scan_tiles, uint32_t *__restrict__ slot_of,
            uint64_t *__restrict__ seg_off, uint32_t *__restrict__ seg_size,
            uint32_t *__restrict__ kstart, uint32_t *__restrict__ kcnt,
-           uint32_t *__restrict__ kcur, uint32_t *__restrict__ seg_cursor,
-           uint32_t *__restrict__ req_bucket, Req *__restrict__ klist, uint64_t surv_cap,
-           OutT *__restrict__ out) {
+           uint32_t *__restrict__ kcur, typename Traits<InT>::K *__restrict__ seg_lo,
+           typename Traits<InT>::K *__restrict__ seg_hi, uint32_t *__restrict__ req_bucket,
+           Req *__restrict__ klist, uint64_t surv_cap, OutT *__restrict__ out) {
   using K = typename Traits<InT>::K;
   extern __shared__ uint4 smem_raw[];
   uint2 *lut = reinterpret_cast<uint2 *>(smem_raw);
@@ -766,7 +795,11 @@ __global__ void __launch_bounds__(1024, 1)
       seg_size[slot] = cb;
       kcnt[slot] = 0;
       kcur[slot] = 0;
-      seg_cursor[slot] = 0;
+      // key range of the bucket (its keys lie in [lo, hi])
+      const K klo = bucket_lo<K>(b, h.base, h.shift, lut);
+      const K knext = (b + 1 < nb) ? bucket_lo<K>(b + 1, h.base, h.shift, lut) : K(0);
+      seg_lo[slot] = klo;
+      seg_hi[slot] = knext > klo ? knext - K(1) : KeyMax<K>::v;
       slot++;
       off += cb;
     } else {
@@ -819,95 +852,133 @@ __global__ void __launch_bounds__(1024, 1)
 // ---------------------------------------------------------------------------
 // (f) compaction pass
 // ---------------------------------------------------------------------------
-template <class T>
+// cursor[b] (shared) = next survivor position of this CTA in bucket b, or
+// kNoSlot for inactive buckets.  In heavy mode lanes of a warp that hit the
+// same bucket take consecutive positions from one shared atomic.
+template <class T, bool HEAVY>
 __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Traits<T>::K base,
-                                            uint32_t shift, const uint2 *lut,
-                                            const uint32_t *active,
-                                            const uint32_t *__restrict__ slot_of,
-                                            const uint64_t *__restrict__ seg_off,
-                                            const uint32_t *__restrict__ seg_size,
-                                            uint32_t *seg_cursor,
+                                            uint32_t shift, const uint2 *lut, uint32_t *cursor,
                                             typename Traits<T>::K *__restrict__ surv,
-                                            Ctrl *ctrl) {
+                                            uint64_t surv_cap, bool *overrun) {
   const uint32_t b = bucket_of(k, base, shift, lut);
-  if ((active[b >> 5] >> (b & 31)) & 1u) {
-    const uint32_t s = __ldg(slot_of + b);
-    const uint32_t c = atomicAdd(seg_cursor + s, 1u);
-    // pass 2 recomputes pass 1's buckets, so c < seg_size[s]; an input changed
-    // between the passes is reported instead of writing past the segment
-    if (c < __ldg(seg_size + s))
-      surv[__ldg(seg_off + s) + c] = k;
+  const bool act = cursor[b] != kNoSlot;
+  if (HEAVY) {
+    const uint32_t act_mask = __ballot_sync(0xffffffffu, act);
+    if (!act_mask) return;
+    const uint32_t peers = __match_any_sync(0xffffffffu, act ? b : kNoSlot);
+    if (!act) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    uint32_t base_pos = 0;
+    if (lane == leader) base_pos = atomicAdd(&cursor[b], (uint32_t)__popc(peers));
+    base_pos = __shfl_sync(peers, base_pos, leader);
+    const uint32_t pos = base_pos + __popc(peers & ((1u << lane) - 1u));
+    if (pos < surv_cap)
+      surv[pos] = k;
     else
-      atomicOr(&ctrl->status, ST_INTERNAL);
+      *overrun = true;
+  } else if (act) {
+    const uint32_t pos = atomicAdd(&cursor[b], 1u);
+    if (pos < surv_cap)
+      surv[pos] = k;
+    else
+      *overrun = true;
   }
 }
 
-template <class T, int UNROLL>
-__global__ void __launch_bounds__(1024, 1)
-    k_compact(const T *__restrict__ x, uint64_t n, const LutHeader<typename Traits<T>::K> *hdr,
-              const uint2 *__restrict__ lut_g, const uint32_t *__restrict__ slot_of,
-              const uint64_t *__restrict__ seg_off, const uint32_t *__restrict__ seg_size,
-              uint32_t *seg_cursor, typename Traits<T>::K *__restrict__ surv, uint32_t nb_max,
-              Ctrl *ctrl) {
+template <class T, int UNROLL, bool HEAVY>
+__device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n, uint32_t *cursor,
+                                             const uint2 *lut, typename Traits<T>::K base,
+                                             uint32_t shift, typename Traits<T>::K *__restrict__ surv,
+                                             uint64_t surv_cap, bool *overrun) {
   using K = typename Traits<T>::K;
   using V = typename Traits<T>::Vec;
   constexpr int PV = Traits<T>::kPerVec;
-  extern __shared__ uint4 smem_raw[];
-  uint2 *lut = reinterpret_cast<uint2 *>(smem_raw);
-  uint32_t *active = reinterpret_cast<uint32_t *>(lut + kLutEntries + 1);
-  if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
-  const LutHeader<K> h = *hdr;
-  const uint32_t nwords = (h.nb + 31) >> 5;
-  for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
-  // one ballot per 32 buckets (blockDim.x is a multiple of 32)
-  for (uint32_t base_b = 0; base_b < nwords * 32; base_b += blockDim.x) {
-    const uint32_t b = base_b + threadIdx.x;
-    const bool on = b < h.nb && slot_of[b] != kNoSlot;
-    const uint32_t bits = __ballot_sync(0xffffffffu, on);
-    if ((threadIdx.x & 31) == 0 && (b >> 5) < nwords) active[b >> 5] = bits;
-  }
-  __syncthreads();
-
   const Span<T> sp = split_span(x, n);
   const V *xv = reinterpret_cast<const V *>(x + sp.head);
   const uint64_t tile_v = (uint64_t)blockDim.x * UNROLL;
   const uint64_t ntiles = sp.nvec / tile_v;
-  // walk the tiles from the end: the tail of the input read by the histogram
-  // pass is the part most likely to still be in L2
-  for (uint64_t q = blockIdx.x; q < ntiles; q += gridDim.x) {
-    const uint64_t tile = ntiles - 1 - q;
+  // The same tiles as the histogram pass (tile = blockIdx.x + q * gridDim.x),
+  // visited last-to-first: the tail of the input is the part most likely to
+  // still be in L2.
+  const uint64_t mine = ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  for (uint64_t q = mine; q-- > 0;) {
+    const uint64_t tile = blockIdx.x + q * gridDim.x;
     const V *p = xv + tile * tile_v + threadIdx.x;
     V v[UNROLL];
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) v[u] = ldg_stream(p + (uint64_t)u * blockDim.x);
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
-      K k[PV];
-      vec_keys<T>(v[u], k);
+      K kk[PV];
+      vec_keys<T>(v[u], kk);
 #pragma unroll
       for (int e = 0; e < PV; ++e)
-        compact_one<T>(k[e], h.base, h.shift, lut, active, slot_of, seg_off, seg_size, seg_cursor,
-                       surv, ctrl);
+        compact_one<T, HEAVY>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun);
     }
   }
   const uint32_t owner = (uint32_t)(ntiles % gridDim.x);
   if (blockIdx.x == owner) {
     for (uint64_t vi = ntiles * tile_v + threadIdx.x; vi < sp.nvec; vi += blockDim.x) {
       V vv = ldg_stream(xv + vi);
-      K k[PV];
-      vec_keys<T>(vv, k);
+      K kk[PV];
+      vec_keys<T>(vv, kk);
 #pragma unroll
       for (int e = 0; e < PV; ++e)
-        compact_one<T>(k[e], h.base, h.shift, lut, active, slot_of, seg_off, seg_size, seg_cursor,
-                       surv, ctrl);
+        compact_one<T, false>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun);
     }
     for (uint64_t e = threadIdx.x; e < sp.head; e += blockDim.x)
-      compact_one<T>(Traits<T>::key(x[e]), h.base, h.shift, lut, active, slot_of, seg_off,
-                     seg_size, seg_cursor, surv, ctrl);
+      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun);
     for (uint64_t e = sp.tail0 + threadIdx.x; e < n; e += blockDim.x)
-      compact_one<T>(Traits<T>::key(x[e]), h.base, h.shift, lut, active, slot_of, seg_off,
-                     seg_size, seg_cursor, surv, ctrl);
+      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun);
   }
+}
+
+// Grid and tile assignment must equal k_hist's (same G, same owner of the
+// leftovers), so that CTA c meets exactly the elements it counted.
+template <class T, int UNROLL>
+__global__ void __launch_bounds__(1024, 1)
+    k_compact(const T *__restrict__ x, uint64_t n, const LutHeader<typename Traits<T>::K> *hdr,
+              const uint2 *__restrict__ lut_g, const uint32_t *__restrict__ slot_of,
+              const uint64_t *__restrict__ seg_off, const uint32_t *__restrict__ prefix,
+              const uint32_t *__restrict__ counts, uint32_t nb_max,
+              typename Traits<T>::K *__restrict__ surv, uint64_t surv_cap, Ctrl *ctrl) {
+  using K = typename Traits<T>::K;
+  extern __shared__ uint4 smem_raw[];
+  uint2 *lut = reinterpret_cast<uint2 *>(smem_raw);
+  uint32_t *cursor = reinterpret_cast<uint32_t *>(lut + kLutEntries + 1);
+  __shared__ bool s_bad;
+  if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
+  const LutHeader<K> h = *hdr;
+  const uint32_t c = blockIdx.x;
+  for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
+  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) {
+    const uint32_t s = slot_of[b];
+    cursor[b] = s == kNoSlot ? kNoSlot
+                             : (uint32_t)(seg_off[s] + prefix[(uint64_t)c * nb_max + b]);
+  }
+  if (threadIdx.x == 0) s_bad = false;
+  __syncthreads();
+  bool overrun = false;
+  if (h.heavy)
+    compact_body<T, UNROLL, true>(x, n, cursor, lut, h.base, h.shift, surv, surv_cap, &overrun);
+  else
+    compact_body<T, UNROLL, false>(x, n, cursor, lut, h.base, h.shift, surv, surv_cap, &overrun);
+  if (overrun) s_bad = true;
+  __syncthreads();
+  // every cursor must have reached the start of the next CTA's range (the
+  // bucket's end for the last CTA); anything else means the input changed
+  // between the two passes
+  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) {
+    const uint32_t s = slot_of[b];
+    if (s == kNoSlot) continue;
+    const uint32_t end = (uint32_t)(seg_off[s] + (c + 1 < gridDim.x
+                                                       ? prefix[(uint64_t)(c + 1) * nb_max + b]
+                                                       : counts[b]));
+    if (cursor[b] != end) s_bad = true;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_bad) atomicOr(&ctrl->status, ST_INTERNAL);
 }
 
 // ---------------------------------------------------------------------------
@@ -976,7 +1047,8 @@ __device__ __forceinline__ uint32_t bin_of_rank(const uint32_t *start, uint32_t 
 template <class K, class OutT>
 __global__ void __launch_bounds__(kFinThreads)
     k_finish(const K *__restrict__ surv, Ctrl *ctrl, const uint64_t *__restrict__ seg_off,
-             const uint32_t *__restrict__ seg_size, const uint32_t *__restrict__ kstart,
+             const uint32_t *__restrict__ seg_size, const K *__restrict__ seg_lo,
+             const K *__restrict__ seg_hi, const uint32_t *__restrict__ kstart,
              const uint32_t *__restrict__ kcnt, const Req *__restrict__ klist,
              uint32_t *__restrict__ deferred, uint32_t bcap, OutT *__restrict__ out) {
   extern __shared__ uint4 smem_raw[];
@@ -986,8 +1058,11 @@ __global__ void __launch_bounds__(kFinThreads)
   uint32_t *cur = gofs + kFinBins;
   K *B = reinterpret_cast<K *>(cur + kFinBins);  // gathered keys of the needed bins
   K *T = B + bcap;                               // scratch for sorting a large bin
+  constexpr int kMaxBig = 64;
   __shared__ K redk[33];
   __shared__ uint32_t red32[33];
+  __shared__ uint32_t big[kMaxBig];
+  __shared__ uint32_t s_nbig;
   constexpr uint32_t PER = kFinBins / kFinThreads;  // bins per thread
 
   if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
@@ -1000,70 +1075,91 @@ __global__ void __launch_bounds__(kFinThreads)
     const Req *rq = klist + kstart[slot];
     const uint32_t m = kcnt[slot];
 
-    // ---- min / max
-    K mn = KeyMax<K>::v, mx = 0;
-    for (uint32_t i = tid; i < size; i += blockDim.x) {
-      const K k = src[i];
-      mn = k < mn ? k : mn;
-      mx = k > mx ? k : mx;
+    // digits of (key - mn): first over the bucket's key range; if the needed
+    // bins then hold too many keys, over the segment's actual min / max
+    K mn = seg_lo[slot], mx = seg_hi[slot];
+    uint32_t V = 0, sh = 0;
+    bool flat = false, fits = false;
+    for (int attempt = 0; attempt < 2 && !fits && !flat; ++attempt) {
+      if (attempt == 1) {
+        K a = KeyMax<K>::v, z = 0;
+        for (uint32_t i = tid; i < size; i += blockDim.x) {
+          const K k = src[i];
+          a = k < a ? k : a;
+          z = k > z ? k : z;
+        }
+        a = block_reduce(a, [](K p, K q) { return p < q ? p : q; }, redk);
+        z = block_reduce(z, [](K p, K q) { return p > q ? p : q; }, redk);
+        if (a == z) {
+          flat = true;
+          mn = a;
+          break;
+        }
+        mn = a;
+        mx = z;
+      }
+      const int bl = bitlen<K>(mx - mn);
+      sh = bl > kFinBinBits ? (uint32_t)(bl - kFinBinBits) : 0u;
+      for (uint32_t i = tid; i < kFinBins; i += blockDim.x) {
+        hist[i] = 0;
+        cur[i] = 0;
+      }
+      __syncthreads();
+      // keys lie in [mn, mx], so the digit is < kFinBins; the clamp keeps a
+      // shared-memory index in range whatever the data
+      for (uint32_t i = tid; i < size; i += blockDim.x)
+        atomicAdd(&hist[min((uint32_t)((src[i] - mn) >> sh), (uint32_t)kFinBins - 1u)], 1u);
+      __syncthreads();
+      {
+        uint32_t cc[PER], sum = 0;
+#pragma unroll
+        for (uint32_t q = 0; q < PER; ++q) {
+          cc[q] = hist[tid * PER + q];
+          sum += cc[q];
+        }
+        uint32_t tot;
+        uint32_t run = block_incl_scan(sum, &tot, red32) - sum;
+#pragma unroll
+        for (uint32_t q = 0; q < PER; ++q) {
+          start[tid * PER + q] = run;
+          gofs[tid * PER + q] = 0;  // "needed" flag until the next scan
+          run += cc[q];
+        }
+      }
+      __syncthreads();
+      for (uint32_t j = tid; j < m; j += blockDim.x) gofs[bin_of_rank(start, rq[j].rank)] = 1u;
+      if (tid == 0) s_nbig = 0;
+      __syncthreads();
+      {
+        uint32_t cc[PER], sum = 0;
+#pragma unroll
+        for (uint32_t q = 0; q < PER; ++q) {
+          const uint32_t b = tid * PER + q;
+          cc[q] = gofs[b] ? hist[b] : 0u;
+          sum += cc[q];
+        }
+        uint32_t run = block_incl_scan(sum, &V, red32) - sum;
+#pragma unroll
+        for (uint32_t q = 0; q < PER; ++q) {
+          const uint32_t b = tid * PER + q;
+          const bool need = gofs[b] != 0u;
+          gofs[b] = need ? run : kNoSlot;
+          if (need && cc[q] > 32) {
+            const uint32_t at = atomicAdd(&s_nbig, 1u);
+            if (at < kMaxBig) big[at] = b;
+          }
+          run += cc[q];
+        }
+      }
+      __syncthreads();
+      fits = V <= bcap;
     }
-    mn = block_reduce(mn, [](K a, K b) { return a < b ? a : b; }, redk);
-    mx = block_reduce(mx, [](K a, K b) { return a > b ? a : b; }, redk);
-    if (mn == mx) {  // one distinct key: every rank is that key
+    if (flat) {  // one distinct key: every rank is that key
       for (uint32_t j = tid; j < m; j += blockDim.x) out[rq[j].out] = Traits<OutT>::value(mn);
-      continue;  // block_reduce ends with a barrier: shared state is free
+      __syncthreads();
+      continue;
     }
-    const int bl = bitlen<K>(mx - mn);
-    const uint32_t sh = bl > kFinBinBits ? (uint32_t)(bl - kFinBinBits) : 0u;
-
-    // ---- histogram
-    for (uint32_t i = tid; i < kFinBins; i += blockDim.x) {
-      hist[i] = 0;
-      cur[i] = 0;
-    }
-    __syncthreads();
-    for (uint32_t i = tid; i < size; i += blockDim.x)
-      atomicAdd(&hist[(uint32_t)((src[i] - mn) >> sh)], 1u);
-    __syncthreads();
-    {
-      uint32_t c[PER], sum = 0;
-#pragma unroll
-      for (uint32_t q = 0; q < PER; ++q) {
-        c[q] = hist[tid * PER + q];
-        sum += c[q];
-      }
-      uint32_t tot;
-      uint32_t run = block_incl_scan(sum, &tot, red32) - sum;
-#pragma unroll
-      for (uint32_t q = 0; q < PER; ++q) {
-        start[tid * PER + q] = run;
-        gofs[tid * PER + q] = 0;  // "needed" flag until the next scan
-        run += c[q];
-      }
-    }
-    __syncthreads();
-    for (uint32_t j = tid; j < m; j += blockDim.x) gofs[bin_of_rank(start, rq[j].rank)] = 1u;
-    __syncthreads();
-    uint32_t V;
-    {
-      uint32_t c[PER], sum = 0;
-#pragma unroll
-      for (uint32_t q = 0; q < PER; ++q) {
-        const uint32_t b = tid * PER + q;
-        c[q] = gofs[b] ? hist[b] : 0u;
-        sum += c[q];
-      }
-      uint32_t run = block_incl_scan(sum, &V, red32) - sum;
-#pragma unroll
-      for (uint32_t q = 0; q < PER; ++q) {
-        const uint32_t b = tid * PER + q;
-        const bool need = gofs[b] != 0u;
-        gofs[b] = need ? run : kNoSlot;
-        run += c[q];
-      }
-    }
-    __syncthreads();
-    if (V > bcap) {  // the needed bins do not fit: re-select on the host side
+    if (!fits) {  // the needed bins do not fit: re-select on the host side
       if (tid == 0) {
         const uint32_t d = atomicAdd(&ctrl->deferred_count, 1u);
         deferred[d] = slot;
@@ -1076,13 +1172,13 @@ __global__ void __launch_bounds__(kFinThreads)
     // ---- gather the needed bins
     for (uint32_t i = tid; i < size; i += blockDim.x) {
       const K k = src[i];
-      const uint32_t b = (uint32_t)((k - mn) >> sh);
+      const uint32_t b = min((uint32_t)((k - mn) >> sh), (uint32_t)kFinBins - 1u);
       const uint32_t g = gofs[b];
       if (g != kNoSlot) B[g + atomicAdd(&cur[b], 1u)] = k;
     }
     __syncthreads();
 
-    // ---- sort each needed bin: warps take the small ones
+    // ---- sort each needed bin: warps take bins of <= 32 keys
     for (uint32_t b = warp; b < kFinBins; b += nwarps) {
       const uint32_t g = gofs[b], c = hist[b];
       if (g == kNoSlot || c < 2 || c > 32) continue;
@@ -1090,18 +1186,22 @@ __global__ void __launch_bounds__(kFinThreads)
       v = warp_bitonic32(v);
       if (lane < c) B[g + lane] = v;
     }
-    __syncthreads();
-    for (uint32_t b = 0; b < kFinBins; ++b) {  // large bins: the whole CTA
+    // larger bins: the whole CTA, one at a time
+    const uint32_t nbig = s_nbig;
+    for (uint32_t q = 0; q < (nbig < kMaxBig ? nbig : kFinBins); ++q) {
+      uint32_t b = q;
+      if (nbig < kMaxBig) b = big[q];
       const uint32_t g = gofs[b], c = hist[b];
       if (g == kNoSlot || c <= 32) continue;
       uint32_t P = 64;
       while (P < c) P <<= 1;
+      __syncthreads();
       for (uint32_t i = tid; i < P; i += blockDim.x) T[i] = i < c ? B[g + i] : KeyMax<K>::v;
       __syncthreads();
       bitonic_sort_smem(T, P);
       for (uint32_t i = tid; i < c; i += blockDim.x) B[g + i] = T[i];
-      __syncthreads();
     }
+    __syncthreads();
 
     // ---- answer
     for (uint32_t j = tid; j < m; j += blockDim.x) {

@@ -37,7 +37,7 @@ struct Plan {
   // arena offsets
   size_t out = 0, ctrl = 0, reqs = 0, hdr = 0, lut = 0, samples = 0, partials = 0,
          counts = 0, excl = 0, slot_of = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0,
-         kcur = 0, seg_cursor = 0, deferred = 0, req_bucket = 0, klist = 0, total = 0;
+         kcur = 0, seg_lo = 0, seg_hi = 0, deferred = 0, req_bucket = 0, klist = 0, total = 0;
 };
 
 template <class InT, class OutT>
@@ -91,7 +91,8 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   arr(p.kstart, p.nb_max, 4);
   arr(p.kcnt, p.nb_max, 4);
   arr(p.kcur, p.nb_max, 4);
-  arr(p.seg_cursor, p.nb_max, 4);
+  arr(p.seg_lo, p.nb_max, sizeof(K));
+  arr(p.seg_hi, p.nb_max, sizeof(K));
   arr(p.deferred, p.nb_max, 4);
   arr(p.req_bucket, num_req, 4);
   arr(p.klist, num_req, sizeof(Req));
@@ -162,7 +163,8 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   uint32_t *kstart = reinterpret_cast<uint32_t *>(A + p.kstart);
   uint32_t *kcnt = reinterpret_cast<uint32_t *>(A + p.kcnt);
   uint32_t *kcur = reinterpret_cast<uint32_t *>(A + p.kcur);
-  uint32_t *seg_cursor = reinterpret_cast<uint32_t *>(A + p.seg_cursor);
+  K *seg_lo = reinterpret_cast<K *>(A + p.seg_lo);
+  K *seg_hi = reinterpret_cast<K *>(A + p.seg_hi);
   uint32_t *deferred = reinterpret_cast<uint32_t *>(A + p.deferred);
   uint32_t *req_bucket = reinterpret_cast<uint32_t *>(A + p.req_bucket);
   Req *klist = reinterpret_cast<Req *>(A + p.klist);
@@ -228,26 +230,27 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     PassTimer t(ctx, s, GGKS_PASS_PLAN);
     k_plan<InT, OutT><<<1, 1024, smem, s>>>(hdr, lut, counts, excl, n, rq, num_req, p.nb_max, ctrl,
                                              tile_state, p.scan_tiles, slot_of, seg_off, seg_size,
-                                             kstart, kcnt, kcur, seg_cursor, req_bucket, klist,
+                                             kstart, kcnt, kcur, seg_lo, seg_hi, req_bucket, klist,
                                              p.surv_cap, d_out);
     ran[GGKS_PASS_PLAN] = true;
   }
+  uint64_t surv_cap = p.surv_cap;
   auto launch_tail = [&]() {
     {
-      const int smem = (int)((kLutEntries + 1) * sizeof(uint2) + (size_t)(p.nb_max / 32 + 1) * 4);
-      set_smem_max<k_compact<InT, UNROLL>>((int)((kLutEntries + 1) * sizeof(uint2) + (size_t)(kMaxNb / 32 + 1) * 4));
+      const int smem = (int)((kLutEntries + 1) * sizeof(uint2) + (size_t)p.nb_max * 4);
+      set_smem_max<k_compact<InT, UNROLL>>((int)((kLutEntries + 1) * sizeof(uint2) + (size_t)kMaxNb * 4));
       PassTimer t(ctx, s, GGKS_PASS_COMPACT);
-      k_compact<InT, UNROLL><<<p.G, 1024, smem, s>>>(d_in, n, hdr, lut, slot_of, seg_off,
-                                                     seg_size, seg_cursor, surv, p.nb_max, ctrl);
+      k_compact<InT, UNROLL><<<p.G, 1024, smem, s>>>(d_in, n, hdr, lut, slot_of, seg_off, partials,
+                                                     counts, p.nb_max, surv, surv_cap, ctrl);
       ran[GGKS_PASS_COMPACT] = true;
     }
     {
       const int smem = finish_smem_bytes<InT>();
       set_smem_max<k_finish<K, OutT>>(smem);
       PassTimer t(ctx, s, GGKS_PASS_FINISH);
-      k_finish<K, OutT><<<p.fin_grid, kFinThreads, smem, s>>>(surv, ctrl, seg_off, seg_size, kstart,
-                                                              kcnt, klist, deferred, p.cap_keys,
-                                                              d_out);
+      k_finish<K, OutT><<<p.fin_grid, kFinThreads, smem, s>>>(surv, ctrl, seg_off, seg_size, seg_lo,
+                                                              seg_hi, kstart, kcnt, klist, deferred,
+                                                              p.cap_keys, d_out);
       ran[GGKS_PASS_FINISH] = true;
     }
   };
@@ -285,6 +288,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       e = ensure_surv(ctx, (size_t)need * sizeof(K));
       if (e != cudaSuccess) return from_cuda(e);
       surv = reinterpret_cast<K *>(ctx.surv);
+      surv_cap = need;
       ctx.stats.retries++;
       e = cudaMemsetAsync(&ctrl->status, 0, sizeof(uint32_t), s);
       if (e != cudaSuccess) return from_cuda(e);
