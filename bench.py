@@ -222,10 +222,12 @@ def cpu_baseline(x, k):
                       f"single-threaded sort-and-choose ({dt:.2f} s)"}
 
 
-def timed_steps(fn, steps, warmup, stream, torch):
+def timed_steps(fn, steps, warmup, stream, torch, after_warmup=None):
     for _ in range(warmup):
         fn()
     torch.cuda.synchronize()
+    if after_warmup:
+        after_warmup()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     with torch.cuda.stream(stream):
@@ -267,17 +269,15 @@ def run_ggks(args):
     # against the sort of a 2^26 slice is too weak; the full-size check lives in
     # the gpu tests.  Here: ranks of the answers by counting on the device.
     ctx.set_profiling(True)
-    ctx.reset_stats()
     if ws > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    launches0 = ctx.stats()["launches"]
-    ms, t0, t1 = timed_steps(step, args.steps, args.warmup, stream, torch)
+    # statistics (launch counts, per-pass CUDA-event times) cover the timed
+    # steps only
+    ms, t0, t1 = timed_steps(step, args.steps, args.warmup, stream, torch,
+                             after_warmup=ctx.reset_stats)
     st = ctx.stats()
-    launches = st["launches"] - launches0
-    # launches include the warm-up steps: report the timed ones
-    per_step_launches = launches / (args.steps + args.warmup)
-    gpu_launches = int(round(per_step_launches * args.steps))
+    gpu_launches = int(st["launches"])
     clocks = sampler.summary(t0, t1)
     tmax = torch.tensor([ms], dtype=torch.float64, device=dev)
     if ws > 1:
@@ -287,7 +287,6 @@ def run_ggks(args):
     value = ws * n * 4 / (ms_max * 1e-3) / 1e9
 
     # per-pass device times (CUDA events on the library's stream)
-    calls = args.steps + args.warmup
     pass_ms = {p: st["pass_ms"][p] / max(1, st["pass_launches"][p]) for p in ggks.PASS_NAMES}
     dom = max(("hist", "compact"), key=lambda p: pass_ms[p])
     peak, peak_kind = measured_peak()

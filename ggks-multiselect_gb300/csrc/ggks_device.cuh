@@ -56,6 +56,7 @@ namespace ggks {
 constexpr int kLutIdxBits = 12;
 constexpr uint32_t kLutIdx = 1u << kLutIdxBits;  // slices over the sample span
 constexpr uint32_t kLutEntries = kLutIdx + 1;    // + one for keys above the span
+constexpr uint32_t kLutPadded = (kLutEntries + 3) & ~3u;  // 16-byte multiple
 constexpr int kMaxSubBits = 20;                  // at most 2^20 buckets per slice
 constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
 constexpr int kSpinLimit = 1 << 22;              // bounded device-side waits
@@ -254,51 +255,48 @@ __device__ __forceinline__ uint32_t hash32(uint32_t a) {
 // ---------------------------------------------------------------------------
 // bucket function: slice lookup + sub-bucket by the next bits of the key
 // ---------------------------------------------------------------------------
-// lut[j] = {C, rs}: bucket = C + ((key - base) >> rs) (mod 2^32).  For a slice
-// j cut into 2^b sub-buckets starting at bucket B_j: rs = shift - b and
-// C = B_j - (j << b).  Merged empty slices use b = 0; the top entry (keys
-// above the sampled span) uses rs = key width, i.e. a constant bucket.
-// Bucket 0 holds the keys below `base` (the sampled minimum); the table's
-// buckets start at 1, so the first of them starts exactly at `base`.
+// lut[j] = (B_j << 6) | b_j: slice j's first bucket and its number of
+// sub-bucket bits.  bucket = B_j + ((d >> (shift - b_j)) & (2^b_j - 1)) with
+// d = key - base.  Empty slices (b = 0) of one run share a bucket; the top
+// entry (keys above the sampled span) is one bucket.  Bucket 0 holds the
+// keys below `base` (the sampled minimum), so the first slice's buckets start
+// at 1 and its first bucket starts exactly at `base`.  One 4-byte entry per
+// slice keeps the shared-memory lookup to a single wavefront for runs of
+// neighbouring slices.
 template <class K>
-__device__ __forceinline__ uint32_t bucket_of(K key, K base, uint32_t shift, const uint2 *lut) {
+__device__ __forceinline__ uint32_t bucket_of(K key, K base, uint32_t shift, const uint32_t *lut) {
   const K d = key - base;  // wraps for key < base; that result is discarded
   const K idx = d >> shift;
   const uint32_t j = idx < (K)kLutIdx ? (uint32_t)idx : kLutIdx;
-  const uint2 e = lut[j];
-  const uint32_t b = e.x + shr_clamp(d, e.y);
+  const uint32_t e = lut[j];
+  const uint32_t bb = e & 63u;
+  const uint32_t sub = (uint32_t)(d >> (shift - bb)) & ((1u << bb) - 1u);
+  const uint32_t b = (e >> 6) + sub;
   return key < base ? 0u : b;
+}
+
+__device__ __forceinline__ uint32_t lut_last_bucket(uint32_t e) {
+  return (e >> 6) + (1u << (e & 63u)) - 1u;
 }
 
 // smallest key that maps to bucket b (b < nb); bucket 0 starts at key 0.
 template <class K>
-__device__ __forceinline__ K bucket_lo(uint32_t b, K base, uint32_t shift, const uint2 *lut) {
+__device__ __forceinline__ K bucket_lo(uint32_t b, K base, uint32_t shift, const uint32_t *lut) {
   if (b == 0) return K(0);
-  // first entry whose last bucket >= b: entries' bucket ranges are
-  // non-decreasing in j.  last_bucket(j) = C_j + (((j+1) << shift) - 1) >> rs_j
-  uint32_t lo = 0, hi = kLutIdx;  // search over [0, kLutIdx]
+  // first entry whose last bucket >= b (bucket ranges are non-decreasing in j)
+  uint32_t lo = 0, hi = kLutIdx;
   while (lo < hi) {
-    uint32_t mid = (lo + hi) >> 1;
-    uint2 e = lut[mid];
-    uint32_t last;
-    if (mid == kLutIdx) {
-      last = e.x;
-    } else {
-      K dmax = (((K)(mid + 1)) << shift) - 1;
-      last = e.x + shr_clamp(dmax, e.y);
-    }
-    if (last >= b)
+    const uint32_t mid = (lo + hi) >> 1;
+    if (lut_last_bucket(lut[mid]) >= b)
       hi = mid;
     else
       lo = mid + 1;
   }
-  uint2 e = lut[lo];
-  if (lo == kLutIdx) return base + (((K)kLutIdx) << shift);
-  K dstart = ((K)lo) << shift;
-  uint32_t first = e.x + shr_clamp(dstart, e.y);
+  const uint32_t e = lut[lo];
+  const K dstart = ((K)lo) << shift;  // for lo == kLutIdx this may wrap: see the caller
+  const uint32_t first = e >> 6;
   if (first >= b) return base + dstart;
-  // within slice lo: sub-bucket (b - first) starts at dstart + ((b - first) << rs)
-  return base + dstart + (((K)(b - first)) << e.y);
+  return base + dstart + (((K)(b - first)) << (shift - (e & 63u)));
 }
 
 // ---------------------------------------------------------------------------
@@ -368,7 +366,7 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
                                                      typename Traits<T>::K *samples,
                                                      Ctrl *ctrl,
                                                      LutHeader<typename Traits<T>::K> *hdr,
-                                                     uint2 *lut, uint32_t nb_max) {
+                                                     uint32_t *lut, uint32_t nb_max) {
   using K = typename Traits<T>::K;
   __shared__ uint32_t cnt[kLutIdx];
   __shared__ uint32_t lch[36];  // [0, 33): slices by ceil(log2 c); [34]: empty-run starts
@@ -438,21 +436,18 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
       atomicAdd(&lch[34], 1u);
   }
   const bool top_run_start = cnt[kLutIdx - 1] != 0;
+  if (tid == 0) s_t = 33;  // total(33) <= 1 + 4096 + 1 <= nb_max: always feasible
   __syncthreads();
-  if (tid == 0) {
-    // smallest t with total(t) <= nb_max; total is non-increasing in t and
-    // total(33) <= 1 + 4096 + 1 <= nb_max
-    int t = -kMaxSubBits - 1;
-    for (; t < 33; ++t) {
-      uint64_t tot = 1u + lch[34] + (top_run_start ? 1u : 0u);
-      for (int l = 0; l < 33; ++l) {
-        int b = l - t;
-        b = b < 0 ? 0 : (b > bcap ? bcap : b);
-        tot += (uint64_t)lch[l] << b;
-      }
-      if (tot <= nb_max) break;
+  if (tid < 54) {
+    // smallest t with total(t) <= nb_max; one candidate t per thread
+    const int t = -kMaxSubBits - 1 + (int)tid;
+    uint64_t tot = 1u + lch[34] + (top_run_start ? 1u : 0u);
+    for (int l = 0; l < 33; ++l) {
+      int b = l - t;
+      b = b < 0 ? 0 : (b > bcap ? bcap : b);
+      tot += (uint64_t)lch[l] << b;
     }
-    s_t = t;
+    if (tot <= nb_max) atomicMin(&s_t, t);
   }
   __syncthreads();
   const int t = s_t;
@@ -474,29 +469,21 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const uint32_t j = 4 * tid + q;
-    uint2 e;
     if (c[q]) {
       const int b = bits_of(q);
-      e.x = run - (j << b);
-      e.y = shift - (uint32_t)b;
+      lut[j] = (run << 6) | (uint32_t)b;
       const uint32_t per = c[q] >> b;
       max_per_bucket = per > max_per_bucket ? per : max_per_bucket;
     } else {
-      const uint32_t B = prev_nonempty[q] ? run : run - 1u;
-      e.x = B - j;  // (d >> shift) == j on this slice
-      e.y = shift;
+      lut[j] = (prev_nonempty[q] ? run : run - 1u) << 6;  // one bucket per empty run
     }
-    lut[j] = e;
     run += my[q];
   }
   max_per_bucket = block_reduce(max_per_bucket, [](uint32_t p, uint32_t q) { return p > q ? p : q; },
                                 red32);
   if (tid == 0) {
     const uint32_t nb = 1u + total + (top_run_start ? 1u : 0u);
-    uint2 e;
-    e.x = top_run_start ? total + 1u : total;
-    e.y = (uint32_t)KeyMax<K>::bits;
-    lut[kLutIdx] = e;
+    lut[kLutIdx] = (top_run_start ? total + 1u : total) << 6;
     LutHeader<K> h;
     h.base = kmin;
     h.shift = shift;
@@ -547,7 +534,7 @@ __device__ __forceinline__ void hist_add(uint32_t *hist, uint32_t b) {
 
 template <class T, int UNROLL, bool HEAVY>
 __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, uint32_t *hist,
-                                          const uint2 *lut, typename Traits<T>::K base,
+                                          const uint32_t *lut, typename Traits<T>::K base,
                                           uint32_t shift) {
   using K = typename Traits<T>::K;
   using V = typename Traits<T>::Vec;
@@ -589,12 +576,12 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
 template <class T, int UNROLL>
 __global__ void __launch_bounds__(1024, 1)
     k_hist(const T *__restrict__ x, uint64_t n, const LutHeader<typename Traits<T>::K> *hdr,
-           const uint2 *__restrict__ lut_g, uint32_t *__restrict__ partials, uint32_t nb_max,
+           const uint32_t *__restrict__ lut_g, uint32_t *__restrict__ partials, uint32_t nb_max,
            const Ctrl *ctrl) {
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
-  uint2 *lut = reinterpret_cast<uint2 *>(smem_raw);
-  uint32_t *hist = reinterpret_cast<uint32_t *>(lut + kLutEntries + 1);
+  uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
+  uint32_t *hist = (lut + kLutPadded);
   if (ctrl->status & ST_FATAL) return;
   const LutHeader<K> h = *hdr;
   for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
@@ -612,17 +599,24 @@ __global__ void __launch_bounds__(1024, 1)
 // ---------------------------------------------------------------------------
 // (d) reduce the per-CTA rows and scan (decoupled look-back, one pass)
 // ---------------------------------------------------------------------------
-constexpr int kScanTile = 256;
+constexpr int kScanThreads = 256;
+constexpr int kScanGroups = 4;                            // row groups per bucket
+constexpr int kScanTile = kScanThreads / kScanGroups;     // buckets per CTA
 constexpr uint64_t kFlagAgg = 1ull << 62, kFlagIncl = 2ull << 62;
 constexpr uint64_t kValMask = (1ull << 62) - 1;
 
+// Thread t handles bucket tile * kScanTile + (t % kScanTile) over row group
+// t / kScanTile, so a warp reads 32 neighbouring buckets of one row (128
+// bytes).  The rows are read twice from L2: once to sum, once to rewrite them
+// as their exclusive prefix.
 template <class K>
-__global__ void __launch_bounds__(kScanTile)
+__global__ void __launch_bounds__(kScanThreads)
     k_scan(uint32_t *__restrict__ partials, uint32_t rows, uint32_t nb_max,
            const LutHeader<K> *hdr, uint32_t *__restrict__ counts, uint32_t *__restrict__ excl,
            uint64_t *tile_state, Ctrl *ctrl) {
   __shared__ uint32_t s_tile;
   __shared__ uint32_t red[33];
+  __shared__ uint32_t gsum[kScanGroups][kScanTile];
   __shared__ uint64_t s_prefix;
   if (ctrl->status & ST_FATAL) return;
   const uint32_t nb = hdr->nb;
@@ -630,31 +624,56 @@ __global__ void __launch_bounds__(kScanTile)
   __syncthreads();
   const uint32_t tile = s_tile;
   if ((uint64_t)tile * kScanTile >= nb) return;
-  const uint32_t b = tile * kScanTile + threadIdx.x;
-  uint32_t c = 0;
+  const uint32_t col = threadIdx.x % kScanTile, grp = threadIdx.x / kScanTile;
+  const uint32_t b = tile * kScanTile + col;
+  const uint32_t per = (rows + kScanGroups - 1) / kScanGroups;
+  const uint32_t r0 = grp * per, r1 = min(rows, r0 + per);
+  uint32_t *p = partials + b;
+  uint32_t gs = 0;
   if (b < nb) {
-    // column b of the per-CTA rows becomes its exclusive prefix over the rows:
-    // the compaction pass starts CTA r's cursor for bucket b there
-    uint32_t *p = partials + b;
-    uint32_t r = 0;
-    for (; r + 8 <= rows; r += 8) {
+    uint32_t r = r0;
+    for (; r + 8 <= r1; r += 8) {
+      uint32_t v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) v[q] = __ldcg(p + (uint64_t)(r + q) * nb_max);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) gs += v[q];
+    }
+    for (; r < r1; ++r) gs += __ldcg(p + (uint64_t)r * nb_max);
+  }
+  gsum[grp][col] = gs;
+  __syncthreads();
+  uint32_t c = 0, before = 0;  // bucket total; rows of the groups before mine
+#pragma unroll
+  for (int g = 0; g < kScanGroups; ++g) {
+    const uint32_t v = gsum[g][col];
+    before += (g < (int)grp) ? v : 0u;
+    c += v;
+  }
+  if (b < nb) {
+    // column b becomes its exclusive prefix over the rows: the compaction
+    // pass starts CTA r's cursor for bucket b there
+    uint32_t run = before;
+    uint32_t r = r0;
+    for (; r + 8 <= r1; r += 8) {
       uint32_t v[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) v[q] = __ldcg(p + (uint64_t)(r + q) * nb_max);
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        p[(uint64_t)(r + q) * nb_max] = c;
-        c += v[q];
+        p[(uint64_t)(r + q) * nb_max] = run;
+        run += v[q];
       }
     }
-    for (; r < rows; ++r) {
+    for (; r < r1; ++r) {
       const uint32_t v = __ldcg(p + (uint64_t)r * nb_max);
-      p[(uint64_t)r * nb_max] = c;
-      c += v;
+      p[(uint64_t)r * nb_max] = run;
+      run += v;
     }
   }
+  // scan of the tile's bucket totals (group 0's threads hold one bucket each)
   uint32_t agg;
-  const uint32_t incl = block_incl_scan(c, &agg, red);
+  const uint32_t incl = block_incl_scan(grp == 0 ? c : 0u, &agg, red);
 
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
@@ -666,11 +685,11 @@ __global__ void __launch_bounds__(kScanTile)
       int64_t pred = (int64_t)tile - 1;
       bool timed_out = false;
       while (true) {
-        const int64_t p = pred - lane;
+        const int64_t pp = pred - lane;
         uint64_t st = 0;
         int iters = 0;
         while (true) {
-          st = p >= 0 ? ld_acquire_u64(&tile_state[p]) : kFlagIncl;
+          st = pp >= 0 ? ld_acquire_u64(&tile_state[pp]) : kFlagIncl;
           if (__all_sync(0xffffffffu, (st >> 62) != 0)) break;
           if (++iters > kSpinLimit) {
             timed_out = true;
@@ -697,7 +716,7 @@ __global__ void __launch_bounds__(kScanTile)
     if (lane == 0) s_prefix = prefix;
   }
   __syncthreads();
-  if (b < nb) {
+  if (grp == 0 && b < nb) {
     counts[b] = c;
     excl[b] = (uint32_t)(s_prefix + incl - c);
   }
@@ -706,11 +725,17 @@ __global__ void __launch_bounds__(kScanTile)
 // ---------------------------------------------------------------------------
 // (e) plan: requests -> buckets -> slots; request lists per slot
 // ---------------------------------------------------------------------------
-// One CTA of 1024 threads.  Dynamic shared memory: excl[nb_max] (u32),
-// lut[kLutEntries + 1] (uint2), active flags[nb_max] (u8).
+// One CTA of 1024 threads.  Dynamic shared memory: lut[kLutEntries + 1] (u32,
+// padded to 16 bytes), excl[nb_max] (u32), flags[nb_max] (u8).
+//
+// Every bucket that holds a requested rank gets a slot, in bucket order.  A
+// bucket whose key range is a single key is a "flat" slot: seg_size 0, no
+// survivors (compaction skips it), and the finisher answers its requests with
+// that key.  Other slots own a segment of the survivor buffer of exactly the
+// bucket's count.
 template <class InT, class OutT>
 __global__ void __launch_bounds__(1024, 1)
-    k_plan(const LutHeader<typename Traits<InT>::K> *hdr, const uint2 *__restrict__ lut_g,
+    k_plan(const LutHeader<typename Traits<InT>::K> *hdr, const uint32_t *__restrict__ lut_g,
            const uint32_t *__restrict__ counts, const uint32_t *__restrict__ excl_g, uint64_t n,
            const Req *__restrict__ reqs, uint32_t num_req, uint32_t nb_max, Ctrl *ctrl,
            uint64_t *tile_state, uint32_t scan_tiles, uint32_t *__restrict__ slot_of,
@@ -721,21 +746,27 @@ __global__ void __launch_bounds__(1024, 1)
            Req *__restrict__ klist, uint64_t surv_cap, OutT *__restrict__ out) {
   using K = typename Traits<InT>::K;
   extern __shared__ uint4 smem_raw[];
-  uint2 *lut = reinterpret_cast<uint2 *>(smem_raw);
-  uint32_t *excl = reinterpret_cast<uint32_t *>(lut + kLutEntries + 1);
+  uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
+  uint32_t *excl = lut + kLutPadded;  // 16-byte aligned
   uint8_t *flag = reinterpret_cast<uint8_t *>(excl + nb_max);
   __shared__ uint32_t red32[33];
   __shared__ uint64_t red64[33];
   const uint32_t tid = threadIdx.x, nt = blockDim.x;
+  (void)out;
 
   if (ctrl->status & ST_FATAL) return;
   const LutHeader<K> h = *hdr;
   const uint32_t nb = h.nb;
-  for (uint32_t j = tid; j < kLutEntries; j += nt) lut[j] = lut_g[j];
-  for (uint32_t b = tid; b < nb; b += nt) {
-    excl[b] = excl_g[b];
-    flag[b] = 0;
+  // 16-byte loads: the buffers are 16-byte aligned and hold nb_max (a
+  // multiple of 4) entries
+  const uint32_t nb4 = (nb + 3) >> 2;
+#pragma unroll 4
+  for (uint32_t v = tid; v < nb4; v += nt) {
+    reinterpret_cast<uint4 *>(excl)[v] = __ldcg(reinterpret_cast<const uint4 *>(excl_g) + v);
+    reinterpret_cast<uint32_t *>(flag)[v] = 0u;
   }
+#pragma unroll 4
+  for (uint32_t j = tid; j < kLutEntries; j += nt) lut[j] = __ldcg(lut_g + j);
   // re-arm the scan's state for the next call on this workspace
   for (uint32_t t = tid; t < scan_tiles; t += nt) tile_state[t] = 0;
   if (tid == 0) {
@@ -745,66 +776,64 @@ __global__ void __launch_bounds__(1024, 1)
   }
   __syncthreads();
 
-  // requests -> bucket; single-key buckets are answered here
+  // requests -> bucket (the last b with excl[b] <= rank is never empty)
   for (uint32_t i = tid; i < num_req; i += nt) {
-    const Req r = reqs[i];
-    uint32_t lo = 0, hi = nb;  // last b with excl[b] <= rank
+    const uint32_t rank = reqs[i].rank;
+    uint32_t lo = 0, hi = nb;
     while (hi - lo > 1) {
-      uint32_t mid = (lo + hi) >> 1;
-      if (excl[mid] <= r.rank)
+      const uint32_t mid = (lo + hi) >> 1;
+      if (excl[mid] <= rank)
         lo = mid;
       else
         hi = mid;
     }
-    const uint32_t b = lo;
-    // bucket b holds a single key iff the next bucket starts one key later.
-    // The start of the top entry's bucket can wrap past the key width; then
-    // no key reaches it and bucket b runs up to the largest key.
-    const K klo = bucket_lo<K>(b, h.base, h.shift, lut);
-    const K knext = (b + 1 < nb) ? bucket_lo<K>(b + 1, h.base, h.shift, lut) : K(0);
-    const bool single = (knext > klo) ? (knext - klo == K(1)) : (klo == KeyMax<K>::v);
-    if (single) {
-      out[r.out] = Traits<OutT>::value(klo);
-      req_bucket[i] = kNoSlot;
-    } else {
-      flag[b] = 1;
-      req_bucket[i] = b;
-    }
+    flag[lo] = 1;
+    req_bucket[i] = lo;
   }
   __syncthreads();
 
-  // slots: exclusive scan of active flags and of active counts over buckets
+  // slots in bucket order (contiguous bucket range per thread); survivor
+  // offsets over the non-flat slots
   const uint32_t per = (nb + nt - 1) / nt;
-  const uint32_t b0 = tid * per, b1 = min(nb, b0 + per);
+  const uint32_t b0 = min(nb, tid * per), b1 = min(nb, b0 + per);
   uint32_t my_slots = 0;
   uint64_t my_surv = 0;
-  for (uint32_t b = b0; b < b1; ++b)
-    if (flag[b]) {
-      my_slots++;
-      my_surv += counts[b];
-    }
+  for (uint32_t b = b0; b < b1; ++b) {
+    if (!flag[b]) continue;
+    my_slots++;
+    const K klo = bucket_lo<K>(b, h.base, h.shift, lut);
+    const K knext = (b + 1 < nb) ? bucket_lo<K>(b + 1, h.base, h.shift, lut) : K(0);
+    // single key iff the next bucket starts one key later; the start of the
+    // top entry's bucket can wrap past the key width, and then bucket b runs
+    // up to the largest key
+    const bool single = (knext > klo) ? (knext - klo == K(1)) : (klo == KeyMax<K>::v);
+    if (single)
+      flag[b] = 2;
+    else
+      my_surv += __ldg(counts + b);
+  }
   uint32_t tot_slots;
   uint64_t tot_surv;
   uint32_t slot = block_incl_scan(my_slots, &tot_slots, red32) - my_slots;
   uint64_t off = block_incl_scan(my_surv, &tot_surv, red64) - my_surv;
   for (uint32_t b = b0; b < b1; ++b) {
-    if (flag[b]) {
-      const uint32_t cb = counts[b];
-      slot_of[b] = slot;
-      seg_off[slot] = off;
-      seg_size[slot] = cb;
-      kcnt[slot] = 0;
-      kcur[slot] = 0;
-      // key range of the bucket (its keys lie in [lo, hi])
-      const K klo = bucket_lo<K>(b, h.base, h.shift, lut);
-      const K knext = (b + 1 < nb) ? bucket_lo<K>(b + 1, h.base, h.shift, lut) : K(0);
-      seg_lo[slot] = klo;
-      seg_hi[slot] = knext > klo ? knext - K(1) : KeyMax<K>::v;
-      slot++;
-      off += cb;
-    } else {
+    const uint8_t f = flag[b];
+    if (!f) {
       slot_of[b] = kNoSlot;
+      continue;
     }
+    const uint32_t cb = f == 2 ? 0u : __ldg(counts + b);
+    const K klo = bucket_lo<K>(b, h.base, h.shift, lut);
+    const K knext = (b + 1 < nb) ? bucket_lo<K>(b + 1, h.base, h.shift, lut) : K(0);
+    slot_of[b] = slot;
+    seg_off[slot] = off;
+    seg_size[slot] = cb;
+    seg_lo[slot] = klo;
+    seg_hi[slot] = f == 2 ? klo : (knext > klo ? knext - K(1) : KeyMax<K>::v);
+    kcnt[slot] = 0;
+    kcur[slot] = 0;
+    slot++;
+    off += cb;
   }
   if (tid == 0) {
     ctrl->num_slots = tot_slots;
@@ -816,36 +845,31 @@ __global__ void __launch_bounds__(1024, 1)
   }
   __syncthreads();
 
-  // requests per slot
-  for (uint32_t i = tid; i < num_req; i += nt) {
-    const uint32_t b = req_bucket[i];
-    if (b != kNoSlot) atomicAdd(&kcnt[slot_of[b]], 1u);
-  }
+  // requests per slot, then the request lists (local ranks)
+  for (uint32_t i = tid; i < num_req; i += nt) atomicAdd(&kcnt[slot_of[req_bucket[i]]], 1u);
   __syncthreads();
   {
     const uint32_t sper = (tot_slots + nt - 1) / nt;
-    const uint32_t s0 = tid * sper, s1 = min(tot_slots, s0 + sper);
+    const uint32_t s0 = min(tot_slots, tid * sper), s1 = min(tot_slots, s0 + sper);
     uint32_t mine = 0;
-    for (uint32_t s = s0; s < s1; ++s) mine += kcnt[s];
+    for (uint32_t q = s0; q < s1; ++q) mine += kcnt[q];
     uint32_t tot;
     uint32_t run = block_incl_scan(mine, &tot, red32) - mine;
-    for (uint32_t s = s0; s < s1; ++s) {
-      kstart[s] = run;
-      run += kcnt[s];
+    for (uint32_t q = s0; q < s1; ++q) {
+      kstart[q] = run;
+      run += kcnt[q];
     }
   }
   __syncthreads();
   for (uint32_t i = tid; i < num_req; i += nt) {
     const uint32_t b = req_bucket[i];
-    if (b != kNoSlot) {
-      const uint32_t s = slot_of[b];
-      const uint32_t pos = kstart[s] + atomicAdd(&kcur[s], 1u);
-      const Req r = reqs[i];
-      Req e;
-      e.rank = r.rank - excl[b];
-      e.out = r.out;
-      klist[pos] = e;
-    }
+    const uint32_t q = slot_of[b];
+    const uint32_t pos = kstart[q] + atomicAdd(&kcur[q], 1u);
+    const Req r = reqs[i];
+    Req e;
+    e.rank = r.rank - excl[b];
+    e.out = r.out;
+    klist[pos] = e;
   }
 }
 
@@ -857,7 +881,7 @@ __global__ void __launch_bounds__(1024, 1)
 // same bucket take consecutive positions from one shared atomic.
 template <class T, bool HEAVY>
 __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Traits<T>::K base,
-                                            uint32_t shift, const uint2 *lut, uint32_t *cursor,
+                                            uint32_t shift, const uint32_t *lut, uint32_t *cursor,
                                             typename Traits<T>::K *__restrict__ surv,
                                             uint64_t surv_cap, bool *overrun) {
   const uint32_t b = bucket_of(k, base, shift, lut);
@@ -888,7 +912,7 @@ __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Tr
 
 template <class T, int UNROLL, bool HEAVY>
 __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n, uint32_t *cursor,
-                                             const uint2 *lut, typename Traits<T>::K base,
+                                             const uint32_t *lut, typename Traits<T>::K base,
                                              uint32_t shift, typename Traits<T>::K *__restrict__ surv,
                                              uint64_t surv_cap, bool *overrun) {
   using K = typename Traits<T>::K;
@@ -939,23 +963,26 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
 template <class T, int UNROLL>
 __global__ void __launch_bounds__(1024, 1)
     k_compact(const T *__restrict__ x, uint64_t n, const LutHeader<typename Traits<T>::K> *hdr,
-              const uint2 *__restrict__ lut_g, const uint32_t *__restrict__ slot_of,
-              const uint64_t *__restrict__ seg_off, const uint32_t *__restrict__ prefix,
-              const uint32_t *__restrict__ counts, uint32_t nb_max,
+              const uint32_t *__restrict__ lut_g, const uint32_t *__restrict__ slot_of,
+              const uint64_t *__restrict__ seg_off, const uint32_t *__restrict__ seg_size,
+              const uint32_t *__restrict__ prefix, const uint32_t *__restrict__ counts,
+              uint32_t nb_max,
               typename Traits<T>::K *__restrict__ surv, uint64_t surv_cap, Ctrl *ctrl) {
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
-  uint2 *lut = reinterpret_cast<uint2 *>(smem_raw);
-  uint32_t *cursor = reinterpret_cast<uint32_t *>(lut + kLutEntries + 1);
+  uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
+  uint32_t *cursor = (lut + kLutPadded);
   __shared__ bool s_bad;
   if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
   const LutHeader<K> h = *hdr;
   const uint32_t c = blockIdx.x;
   for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
+  // flat slots (seg_size 0: a single-key bucket) are answered without survivors
   for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) {
     const uint32_t s = slot_of[b];
-    cursor[b] = s == kNoSlot ? kNoSlot
-                             : (uint32_t)(seg_off[s] + prefix[(uint64_t)c * nb_max + b]);
+    cursor[b] = (s == kNoSlot || seg_size[s] == 0)
+                    ? kNoSlot
+                    : (uint32_t)(seg_off[s] + prefix[(uint64_t)c * nb_max + b]);
   }
   if (threadIdx.x == 0) s_bad = false;
   __syncthreads();
@@ -971,7 +998,7 @@ __global__ void __launch_bounds__(1024, 1)
   // between the two passes
   for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) {
     const uint32_t s = slot_of[b];
-    if (s == kNoSlot) continue;
+    if (s == kNoSlot || seg_size[s] == 0) continue;
     const uint32_t end = (uint32_t)(seg_off[s] + (c + 1 < gridDim.x
                                                        ? prefix[(uint64_t)(c + 1) * nb_max + b]
                                                        : counts[b]));
@@ -1074,6 +1101,11 @@ __global__ void __launch_bounds__(kFinThreads)
     const K *src = surv + seg_off[slot];
     const Req *rq = klist + kstart[slot];
     const uint32_t m = kcnt[slot];
+    if (size == 0) {  // flat slot: every rank in the bucket is its single key
+      const K key = seg_lo[slot];
+      for (uint32_t j = tid; j < m; j += blockDim.x) out[rq[j].out] = Traits<OutT>::value(key);
+      continue;
+    }
 
     // digits of (key - mn): first over the bucket's key range; if the needed
     // bins then hold too many keys, over the segment's actual min / max
@@ -1107,8 +1139,19 @@ __global__ void __launch_bounds__(kFinThreads)
       __syncthreads();
       // keys lie in [mn, mx], so the digit is < kFinBins; the clamp keeps a
       // shared-memory index in range whatever the data
-      for (uint32_t i = tid; i < size; i += blockDim.x)
-        atomicAdd(&hist[min((uint32_t)((src[i] - mn) >> sh), (uint32_t)kFinBins - 1u)], 1u);
+      {
+        uint32_t i = tid;
+        for (; i + 3 * blockDim.x < size; i += 4 * blockDim.x) {
+          K kk[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) kk[q] = src[i + q * blockDim.x];
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            atomicAdd(&hist[min((uint32_t)((kk[q] - mn) >> sh), (uint32_t)kFinBins - 1u)], 1u);
+        }
+        for (; i < size; i += blockDim.x)
+          atomicAdd(&hist[min((uint32_t)((src[i] - mn) >> sh), (uint32_t)kFinBins - 1u)], 1u);
+      }
       __syncthreads();
       {
         uint32_t cc[PER], sum = 0;
@@ -1170,11 +1213,21 @@ __global__ void __launch_bounds__(kFinThreads)
     }
 
     // ---- gather the needed bins
-    for (uint32_t i = tid; i < size; i += blockDim.x) {
-      const K k = src[i];
-      const uint32_t b = min((uint32_t)((k - mn) >> sh), (uint32_t)kFinBins - 1u);
-      const uint32_t g = gofs[b];
-      if (g != kNoSlot) B[g + atomicAdd(&cur[b], 1u)] = k;
+    {
+      auto put = [&](K k) {
+        const uint32_t b = min((uint32_t)((k - mn) >> sh), (uint32_t)kFinBins - 1u);
+        const uint32_t g = gofs[b];
+        if (g != kNoSlot) B[g + atomicAdd(&cur[b], 1u)] = k;
+      };
+      uint32_t i = tid;
+      for (; i + 3 * blockDim.x < size; i += 4 * blockDim.x) {
+        K kk[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) kk[q] = src[i + q * blockDim.x];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) put(kk[q]);
+      }
+      for (; i < size; i += blockDim.x) put(src[i]);
     }
     __syncthreads();
 

@@ -74,7 +74,7 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   p.hdr = o;
   o = align_up(o + sizeof(LutHeader<K>), A);
   p.lut = o;
-  o = align_up(o + (kLutEntries + 1) * sizeof(uint2), A);
+  o = align_up(o + kLutPadded * sizeof(uint32_t), A);
   p.samples = o;
   o = align_up(o + (size_t)p.S * sizeof(K), A);
   p.partials = o;
@@ -151,7 +151,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   Ctrl *ctrl = reinterpret_cast<Ctrl *>(A + p.ctrl);
   Req *reqs = reinterpret_cast<Req *>(A + p.reqs);
   LutHeader<K> *hdr = reinterpret_cast<LutHeader<K> *>(A + p.hdr);
-  uint2 *lut = reinterpret_cast<uint2 *>(A + p.lut);
+  uint32_t *lut = reinterpret_cast<uint32_t *>(A + p.lut);
   K *samples = reinterpret_cast<K *>(A + p.samples);
   uint32_t *partials = reinterpret_cast<uint32_t *>(A + p.partials);
   uint32_t *counts = reinterpret_cast<uint32_t *>(A + p.counts);
@@ -209,8 +209,8 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   }
   // ---- (c) histogram
   {
-    const int smem = (int)((kLutEntries + 1) * sizeof(uint2) + (size_t)p.nb_max * 4);
-    set_smem_max<k_hist<InT, UNROLL>>((int)((kLutEntries + 1) * sizeof(uint2) + (size_t)kMaxNb * 4));
+    const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 4);
+    set_smem_max<k_hist<InT, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
     PassTimer t(ctx, s, GGKS_PASS_HIST);
     k_hist<InT, UNROLL><<<p.G, 1024, smem, s>>>(d_in, n, hdr, lut, partials, p.nb_max, ctrl);
     ran[GGKS_PASS_HIST] = true;
@@ -218,15 +218,15 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   // ---- (d) reduce + decoupled look-back scan
   {
     PassTimer t(ctx, s, GGKS_PASS_SCAN);
-    k_scan<K><<<p.scan_tiles, kScanTile, 0, s>>>(partials, p.G, p.nb_max, hdr, counts, excl,
+    k_scan<K><<<p.scan_tiles, kScanThreads, 0, s>>>(partials, p.G, p.nb_max, hdr, counts, excl,
                                                   tile_state, ctrl);
     ran[GGKS_PASS_SCAN] = true;
   }
   // ---- (e) plan
   {
     const int smem =
-        (int)((kLutEntries + 1) * sizeof(uint2) + (size_t)p.nb_max * 4 + (size_t)p.nb_max);
-    set_smem_max<k_plan<InT, OutT>>((int)((kLutEntries + 1) * sizeof(uint2) + (size_t)kMaxNb * 5));
+        (int)(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 4 + (size_t)p.nb_max);
+    set_smem_max<k_plan<InT, OutT>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 5));
     PassTimer t(ctx, s, GGKS_PASS_PLAN);
     k_plan<InT, OutT><<<1, 1024, smem, s>>>(hdr, lut, counts, excl, n, rq, num_req, p.nb_max, ctrl,
                                              tile_state, p.scan_tiles, slot_of, seg_off, seg_size,
@@ -237,11 +237,12 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   uint64_t surv_cap = p.surv_cap;
   auto launch_tail = [&]() {
     {
-      const int smem = (int)((kLutEntries + 1) * sizeof(uint2) + (size_t)p.nb_max * 4);
-      set_smem_max<k_compact<InT, UNROLL>>((int)((kLutEntries + 1) * sizeof(uint2) + (size_t)kMaxNb * 4));
+      const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 4);
+      set_smem_max<k_compact<InT, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
       PassTimer t(ctx, s, GGKS_PASS_COMPACT);
-      k_compact<InT, UNROLL><<<p.G, 1024, smem, s>>>(d_in, n, hdr, lut, slot_of, seg_off, partials,
-                                                     counts, p.nb_max, surv, surv_cap, ctrl);
+      k_compact<InT, UNROLL><<<p.G, 1024, smem, s>>>(d_in, n, hdr, lut, slot_of, seg_off, seg_size,
+                                                     partials, counts, p.nb_max, surv, surv_cap,
+                                                     ctrl);
       ran[GGKS_PASS_COMPACT] = true;
     }
     {
