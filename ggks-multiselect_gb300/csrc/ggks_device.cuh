@@ -738,21 +738,20 @@ __global__ void __launch_bounds__(1024, 1)
     k_plan(const LutHeader<typename Traits<InT>::K> *hdr, const uint32_t *__restrict__ lut_g,
            const uint32_t *__restrict__ counts, const uint32_t *__restrict__ excl_g, uint64_t n,
            const Req *__restrict__ reqs, uint32_t num_req, uint32_t nb_max, Ctrl *ctrl,
-           uint64_t *tile_state, uint32_t scan_tiles, uint32_t *__restrict__ slot_of,
+           uint64_t *tile_state, uint32_t scan_tiles, uint32_t *__restrict__ seg_bucket,
            uint64_t *__restrict__ seg_off, uint32_t *__restrict__ seg_size,
            uint32_t *__restrict__ kstart, uint32_t *__restrict__ kcnt,
            uint32_t *__restrict__ kcur, typename Traits<InT>::K *__restrict__ seg_lo,
            typename Traits<InT>::K *__restrict__ seg_hi, uint32_t *__restrict__ req_bucket,
-           Req *__restrict__ klist, uint64_t surv_cap, OutT *__restrict__ out) {
+           uint32_t *__restrict__ req_local, Req *__restrict__ klist, uint64_t surv_cap) {
   using K = typename Traits<InT>::K;
   extern __shared__ uint4 smem_raw[];
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
-  uint32_t *excl = lut + kLutPadded;  // 16-byte aligned
+  uint32_t *excl = lut + kLutPadded;  // 16-byte aligned; later: slot of each bucket
   uint8_t *flag = reinterpret_cast<uint8_t *>(excl + nb_max);
   __shared__ uint32_t red32[33];
   __shared__ uint64_t red64[33];
   const uint32_t tid = threadIdx.x, nt = blockDim.x;
-  (void)out;
 
   if (ctrl->status & ST_FATAL) return;
   const LutHeader<K> h = *hdr;
@@ -776,7 +775,8 @@ __global__ void __launch_bounds__(1024, 1)
   }
   __syncthreads();
 
-  // requests -> bucket (the last b with excl[b] <= rank is never empty)
+  // requests -> bucket (the last b with excl[b] <= rank is never empty) and
+  // the rank inside it
   for (uint32_t i = tid; i < num_req; i += nt) {
     const uint32_t rank = reqs[i].rank;
     uint32_t lo = 0, hi = nb;
@@ -789,11 +789,13 @@ __global__ void __launch_bounds__(1024, 1)
     }
     flag[lo] = 1;
     req_bucket[i] = lo;
+    req_local[i] = rank - excl[lo];
   }
   __syncthreads();
 
   // slots in bucket order (contiguous bucket range per thread); survivor
-  // offsets over the non-flat slots
+  // offsets over the non-flat slots.  excl[] is dead from here on and holds
+  // the slot of each flagged bucket.
   const uint32_t per = (nb + nt - 1) / nt;
   const uint32_t b0 = min(nb, tid * per), b1 = min(nb, b0 + per);
   uint32_t my_slots = 0;
@@ -818,14 +820,12 @@ __global__ void __launch_bounds__(1024, 1)
   uint64_t off = block_incl_scan(my_surv, &tot_surv, red64) - my_surv;
   for (uint32_t b = b0; b < b1; ++b) {
     const uint8_t f = flag[b];
-    if (!f) {
-      slot_of[b] = kNoSlot;
-      continue;
-    }
+    if (!f) continue;
     const uint32_t cb = f == 2 ? 0u : __ldg(counts + b);
     const K klo = bucket_lo<K>(b, h.base, h.shift, lut);
     const K knext = (b + 1 < nb) ? bucket_lo<K>(b + 1, h.base, h.shift, lut) : K(0);
-    slot_of[b] = slot;
+    excl[b] = slot;
+    seg_bucket[slot] = b;
     seg_off[slot] = off;
     seg_size[slot] = cb;
     seg_lo[slot] = klo;
@@ -846,7 +846,7 @@ __global__ void __launch_bounds__(1024, 1)
   __syncthreads();
 
   // requests per slot, then the request lists (local ranks)
-  for (uint32_t i = tid; i < num_req; i += nt) atomicAdd(&kcnt[slot_of[req_bucket[i]]], 1u);
+  for (uint32_t i = tid; i < num_req; i += nt) atomicAdd(&kcnt[excl[req_bucket[i]]], 1u);
   __syncthreads();
   {
     const uint32_t sper = (tot_slots + nt - 1) / nt;
@@ -862,13 +862,11 @@ __global__ void __launch_bounds__(1024, 1)
   }
   __syncthreads();
   for (uint32_t i = tid; i < num_req; i += nt) {
-    const uint32_t b = req_bucket[i];
-    const uint32_t q = slot_of[b];
+    const uint32_t q = excl[req_bucket[i]];
     const uint32_t pos = kstart[q] + atomicAdd(&kcur[q], 1u);
-    const Req r = reqs[i];
     Req e;
-    e.rank = r.rank - excl[b];
-    e.out = r.out;
+    e.rank = req_local[i];
+    e.out = reqs[i].out;
     klist[pos] = e;
   }
 }
@@ -963,7 +961,7 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
 template <class T, int UNROLL>
 __global__ void __launch_bounds__(1024, 1)
     k_compact(const T *__restrict__ x, uint64_t n, const LutHeader<typename Traits<T>::K> *hdr,
-              const uint32_t *__restrict__ lut_g, const uint32_t *__restrict__ slot_of,
+              const uint32_t *__restrict__ lut_g, const uint32_t *__restrict__ seg_bucket,
               const uint64_t *__restrict__ seg_off, const uint32_t *__restrict__ seg_size,
               const uint32_t *__restrict__ prefix, const uint32_t *__restrict__ counts,
               uint32_t nb_max,
@@ -977,14 +975,17 @@ __global__ void __launch_bounds__(1024, 1)
   const LutHeader<K> h = *hdr;
   const uint32_t c = blockIdx.x;
   for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
-  // flat slots (seg_size 0: a single-key bucket) are answered without survivors
-  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) {
-    const uint32_t s = slot_of[b];
-    cursor[b] = (s == kNoSlot || seg_size[s] == 0)
-                    ? kNoSlot
-                    : (uint32_t)(seg_off[s] + prefix[(uint64_t)c * nb_max + b]);
-  }
+  const uint32_t num_slots = ctrl->num_slots;
+  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) cursor[b] = kNoSlot;
   if (threadIdx.x == 0) s_bad = false;
+  __syncthreads();
+  // flat slots (seg_size 0: a single-key bucket) are answered without survivors
+  for (uint32_t s = threadIdx.x; s < num_slots; s += blockDim.x) {
+    const uint32_t sz = seg_size[s];
+    if (sz == 0) continue;
+    const uint32_t b = seg_bucket[s];
+    cursor[b] = (uint32_t)(seg_off[s] + prefix[(uint64_t)c * nb_max + b]);
+  }
   __syncthreads();
   bool overrun = false;
   if (h.heavy)
@@ -996,9 +997,9 @@ __global__ void __launch_bounds__(1024, 1)
   // every cursor must have reached the start of the next CTA's range (the
   // bucket's end for the last CTA); anything else means the input changed
   // between the two passes
-  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) {
-    const uint32_t s = slot_of[b];
-    if (s == kNoSlot || seg_size[s] == 0) continue;
+  for (uint32_t s = threadIdx.x; s < num_slots; s += blockDim.x) {
+    if (seg_size[s] == 0) continue;
+    const uint32_t b = seg_bucket[s];
     const uint32_t end = (uint32_t)(seg_off[s] + (c + 1 < gridDim.x
                                                        ? prefix[(uint64_t)(c + 1) * nb_max + b]
                                                        : counts[b]));

@@ -36,8 +36,9 @@ struct Plan {
   uint64_t surv_cap = 0;
   // arena offsets
   size_t out = 0, ctrl = 0, reqs = 0, hdr = 0, lut = 0, samples = 0, partials = 0,
-         counts = 0, excl = 0, slot_of = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0,
-         kcur = 0, seg_lo = 0, seg_hi = 0, deferred = 0, req_bucket = 0, klist = 0, total = 0;
+         counts = 0, excl = 0, seg_bucket = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0,
+         kcur = 0, seg_lo = 0, seg_hi = 0, deferred = 0, req_bucket = 0, req_local = 0, klist = 0,
+         total = 0;
 };
 
 template <class InT, class OutT>
@@ -85,7 +86,7 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   };
   arr(p.counts, p.nb_max, 4);
   arr(p.excl, p.nb_max, 4);
-  arr(p.slot_of, p.nb_max, 4);
+  arr(p.seg_bucket, p.nb_max, 4);
   arr(p.seg_off, p.nb_max, 8);
   arr(p.seg_size, p.nb_max, 4);
   arr(p.kstart, p.nb_max, 4);
@@ -95,6 +96,7 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   arr(p.seg_hi, p.nb_max, sizeof(K));
   arr(p.deferred, p.nb_max, 4);
   arr(p.req_bucket, num_req, 4);
+  arr(p.req_local, num_req, 4);
   arr(p.klist, num_req, sizeof(Req));
   p.total = o;
   return p;
@@ -157,7 +159,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   uint32_t *counts = reinterpret_cast<uint32_t *>(A + p.counts);
   uint32_t *excl = reinterpret_cast<uint32_t *>(A + p.excl);
   uint64_t *tile_state = reinterpret_cast<uint64_t *>(A);
-  uint32_t *slot_of = reinterpret_cast<uint32_t *>(A + p.slot_of);
+  uint32_t *seg_bucket = reinterpret_cast<uint32_t *>(A + p.seg_bucket);
   uint64_t *seg_off = reinterpret_cast<uint64_t *>(A + p.seg_off);
   uint32_t *seg_size = reinterpret_cast<uint32_t *>(A + p.seg_size);
   uint32_t *kstart = reinterpret_cast<uint32_t *>(A + p.kstart);
@@ -167,6 +169,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   K *seg_hi = reinterpret_cast<K *>(A + p.seg_hi);
   uint32_t *deferred = reinterpret_cast<uint32_t *>(A + p.deferred);
   uint32_t *req_bucket = reinterpret_cast<uint32_t *>(A + p.req_bucket);
+  uint32_t *req_local = reinterpret_cast<uint32_t *>(A + p.req_local);
   Req *klist = reinterpret_cast<Req *>(A + p.klist);
   K *surv = reinterpret_cast<K *>(ctx.surv);
   OutT *d_out = d_out_user ? d_out_user : reinterpret_cast<OutT *>(A + p.out);
@@ -229,9 +232,9 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     set_smem_max<k_plan<InT, OutT>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 5));
     PassTimer t(ctx, s, GGKS_PASS_PLAN);
     k_plan<InT, OutT><<<1, 1024, smem, s>>>(hdr, lut, counts, excl, n, rq, num_req, p.nb_max, ctrl,
-                                             tile_state, p.scan_tiles, slot_of, seg_off, seg_size,
-                                             kstart, kcnt, kcur, seg_lo, seg_hi, req_bucket, klist,
-                                             p.surv_cap, d_out);
+                                             tile_state, p.scan_tiles, seg_bucket, seg_off,
+                                             seg_size, kstart, kcnt, kcur, seg_lo, seg_hi,
+                                             req_bucket, req_local, klist, p.surv_cap);
     ran[GGKS_PASS_PLAN] = true;
   }
   uint64_t surv_cap = p.surv_cap;
@@ -240,7 +243,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 4);
       set_smem_max<k_compact<InT, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
       PassTimer t(ctx, s, GGKS_PASS_COMPACT);
-      k_compact<InT, UNROLL><<<p.G, 1024, smem, s>>>(d_in, n, hdr, lut, slot_of, seg_off, seg_size,
+      k_compact<InT, UNROLL><<<p.G, 1024, smem, s>>>(d_in, n, hdr, lut, seg_bucket, seg_off, seg_size,
                                                      partials, counts, p.nb_max, surv, surv_cap,
                                                      ctrl);
       ran[GGKS_PASS_COMPACT] = true;
