@@ -57,7 +57,7 @@ constexpr int kLutIdxBits = 12;
 constexpr uint32_t kLutIdx = 1u << kLutIdxBits;  // slices over the sample span
 constexpr uint32_t kLutEntries = kLutIdx + 1;    // + one for keys above the span
 constexpr uint32_t kLutPadded = (kLutEntries + 3) & ~3u;  // 16-byte multiple
-constexpr int kMaxSubBits = 20;                  // at most 2^20 buckets per slice
+constexpr int kMaxSubBits = 12;                  // at most 2^12 buckets per slice
 constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
 constexpr int kSpinLimit = 1 << 22;              // bounded device-side waits
 
@@ -255,28 +255,42 @@ __device__ __forceinline__ uint32_t hash32(uint32_t a) {
 // ---------------------------------------------------------------------------
 // bucket function: slice lookup + sub-bucket by the next bits of the key
 // ---------------------------------------------------------------------------
-// lut[j] = (B_j << 6) | b_j: slice j's first bucket and its number of
-// sub-bucket bits.  bucket = B_j + ((d >> (shift - b_j)) & (2^b_j - 1)) with
-// d = key - base.  Empty slices (b = 0) of one run share a bucket; the top
-// entry (keys above the sampled span) is one bucket.  Bucket 0 holds the
-// keys below `base` (the sampled minimum), so the first slice's buckets start
-// at 1 and its first bucket starts exactly at `base`.  One 4-byte entry per
-// slice keeps the shared-memory lookup to a single wavefront for runs of
-// neighbouring slices.
+// lut[j] = (C_j << 7) | rs_j.  For slice j with first bucket B_j cut into 2^b_j
+// sub-buckets: rs_j = shift - b_j and C_j = B_j - (j << b_j), a signed 25-bit
+// value (|j << b_j| < 2^24 because j < 2^12 and b_j <= 12).  Then
+//   bucket = C_j + ((key - base) >> rs_j),
+// since (key - base) >> rs_j = (j << b_j) + sub-bucket on slice j.  Empty
+// slices of one run share a bucket (b = 0); the top entry (keys above the
+// sampled span) has rs = key width, i.e. the constant bucket C.  Bucket 0
+// holds the keys below `base` (the sampled minimum), so the first slice's
+// buckets start at 1 and its first bucket starts exactly at `base`.  One 4-byte
+// entry per slice keeps the shared-memory lookup to a single wavefront for
+// runs of neighbouring slices; the bucket costs two ALU operations.
 template <class K>
 __device__ __forceinline__ uint32_t bucket_of(K key, K base, uint32_t shift, const uint32_t *lut) {
   const K d = key - base;  // wraps for key < base; that result is discarded
   const K idx = d >> shift;
   const uint32_t j = idx < (K)kLutIdx ? (uint32_t)idx : kLutIdx;
   const uint32_t e = lut[j];
-  const uint32_t bb = e & 63u;
-  const uint32_t sub = (uint32_t)(d >> (shift - bb)) & ((1u << bb) - 1u);
-  const uint32_t b = (e >> 6) + sub;
+  const uint32_t b = (uint32_t)((int32_t)e >> 7) + shr_clamp(d, e & 127u);
   return key < base ? 0u : b;
 }
 
-__device__ __forceinline__ uint32_t lut_last_bucket(uint32_t e) {
-  return (e >> 6) + (1u << (e & 63u)) - 1u;
+__device__ __forceinline__ uint32_t lut_pack(int32_t C, uint32_t rs) {
+  return ((uint32_t)C << 7) | rs;
+}
+
+// first bucket and sub-bucket bits of entry j
+__device__ __forceinline__ void lut_entry(uint32_t e, uint32_t j, uint32_t shift, uint32_t *B,
+                                          uint32_t *bb) {
+  const int32_t C = (int32_t)e >> 7;
+  if (j == kLutIdx) {
+    *B = (uint32_t)C;
+    *bb = 0;
+  } else {
+    *bb = shift - (e & 127u);
+    *B = (uint32_t)(C + (int32_t)(j << *bb));
+  }
 }
 
 // smallest key that maps to bucket b (b < nb); bucket 0 starts at key 0.
@@ -287,16 +301,18 @@ __device__ __forceinline__ K bucket_lo(uint32_t b, K base, uint32_t shift, const
   uint32_t lo = 0, hi = kLutIdx;
   while (lo < hi) {
     const uint32_t mid = (lo + hi) >> 1;
-    if (lut_last_bucket(lut[mid]) >= b)
+    uint32_t B, bb;
+    lut_entry(lut[mid], mid, shift, &B, &bb);
+    if (B + (1u << bb) - 1u >= b)
       hi = mid;
     else
       lo = mid + 1;
   }
-  const uint32_t e = lut[lo];
+  uint32_t B, bb;
+  lut_entry(lut[lo], lo, shift, &B, &bb);
   const K dstart = ((K)lo) << shift;  // for lo == kLutIdx this may wrap: see the caller
-  const uint32_t first = e >> 6;
-  if (first >= b) return base + dstart;
-  return base + dstart + (((K)(b - first)) << (shift - (e & 63u)));
+  if (B >= b) return base + dstart;
+  return base + dstart + (((K)(b - B)) << (shift - bb));
 }
 
 // ---------------------------------------------------------------------------
@@ -391,16 +407,17 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
   }
   mine_lo = block_reduce(mine_lo, [](K p, K q) { return p < q ? p : q; }, redk);
   mine_hi = block_reduce(mine_hi, [](K p, K q) { return p > q ? p : q; }, redk);
+  // block_reduce ended with a barrier: the CTA's sample stores happen before
+  // thread 0's fence, which orders them (cumulatively) before the ticket
   if (tid == 0) {
     atomicMax((unsigned long long *)&ctrl->kmin_inv, (unsigned long long)~(uint64_t)mine_lo);
     atomicMax((unsigned long long *)&ctrl->kmax, (unsigned long long)mine_hi);
+    __threadfence();
+    s_last = (atomicAdd(&ctrl->sample_done, 1u) == gridDim.x - 1) ? 1u : 0u;
+    if (s_last) __threadfence();
   }
-  __threadfence();
-  __syncthreads();
-  if (tid == 0) s_last = (atomicAdd(&ctrl->sample_done, 1u) == gridDim.x - 1) ? 1u : 0u;
   __syncthreads();
   if (!s_last) return;
-  __threadfence();
 
   const K kmin = (K)~__ldcg((const unsigned long long *)&ctrl->kmin_inv);
   const K kmax = (K)__ldcg((const unsigned long long *)&ctrl->kmax);
@@ -412,7 +429,7 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
   for (uint32_t j = tid; j < kLutIdx; j += blockDim.x) cnt[j] = 0;
   if (tid < 36) lch[tid] = 0;
   __syncthreads();
-#pragma unroll 8
+#pragma unroll 16
   for (uint32_t s = tid; s < S; s += blockDim.x) {
     const K k = __ldcg(samples + s);
     atomicAdd(&cnt[(uint32_t)((k - kmin) >> shift)], 1u);
@@ -471,11 +488,12 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
     const uint32_t j = 4 * tid + q;
     if (c[q]) {
       const int b = bits_of(q);
-      lut[j] = (run << 6) | (uint32_t)b;
+      lut[j] = lut_pack((int32_t)run - (int32_t)(j << b), shift - (uint32_t)b);
       const uint32_t per = c[q] >> b;
       max_per_bucket = per > max_per_bucket ? per : max_per_bucket;
     } else {
-      lut[j] = (prev_nonempty[q] ? run : run - 1u) << 6;  // one bucket per empty run
+      // one bucket per run of empty slices
+      lut[j] = lut_pack((int32_t)(prev_nonempty[q] ? run : run - 1u) - (int32_t)j, shift);
     }
     run += my[q];
   }
@@ -483,7 +501,7 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
                                 red32);
   if (tid == 0) {
     const uint32_t nb = 1u + total + (top_run_start ? 1u : 0u);
-    lut[kLutIdx] = (top_run_start ? total + 1u : total) << 6;
+    lut[kLutIdx] = lut_pack((int32_t)(top_run_start ? total + 1u : total), (uint32_t)KeyMax<K>::bits);
     LutHeader<K> h;
     h.base = kmin;
     h.shift = shift;
@@ -793,47 +811,53 @@ __global__ void __launch_bounds__(1024, 1)
   }
   __syncthreads();
 
-  // slots in bucket order (contiguous bucket range per thread); survivor
-  // offsets over the non-flat slots.  excl[] is dead from here on and holds
-  // the slot of each flagged bucket.
+  // Slots in bucket order.  A block scan over the flags (contiguous bucket
+  // range per thread) numbers the flagged buckets; excl[] is dead from here on
+  // and maps each flagged bucket to its slot, seg_bucket[] lists the slots'
+  // buckets.
   const uint32_t per = (nb + nt - 1) / nt;
   const uint32_t b0 = min(nb, tid * per), b1 = min(nb, b0 + per);
   uint32_t my_slots = 0;
+  for (uint32_t b = b0; b < b1; ++b) my_slots += flag[b] ? 1u : 0u;
+  uint32_t tot_slots;
+  {
+    uint32_t slot = block_incl_scan(my_slots, &tot_slots, red32) - my_slots;
+    for (uint32_t b = b0; b < b1; ++b)
+      if (flag[b]) {
+        excl[b] = slot;
+        seg_bucket[slot] = b;
+        slot++;
+      }
+  }
+  __syncthreads();
+  // one thread per slot (contiguous slot range per thread for the offsets):
+  // key range, flat test, survivor count
+  const uint32_t sper = (tot_slots + nt - 1) / nt;
+  const uint32_t s0 = min(tot_slots, tid * sper), s1 = min(tot_slots, s0 + sper);
   uint64_t my_surv = 0;
-  for (uint32_t b = b0; b < b1; ++b) {
-    if (!flag[b]) continue;
-    my_slots++;
+  for (uint32_t q = s0; q < s1; ++q) {
+    const uint32_t b = __ldcg(seg_bucket + q);
     const K klo = bucket_lo<K>(b, h.base, h.shift, lut);
     const K knext = (b + 1 < nb) ? bucket_lo<K>(b + 1, h.base, h.shift, lut) : K(0);
     // single key iff the next bucket starts one key later; the start of the
     // top entry's bucket can wrap past the key width, and then bucket b runs
     // up to the largest key
     const bool single = (knext > klo) ? (knext - klo == K(1)) : (klo == KeyMax<K>::v);
-    if (single)
-      flag[b] = 2;
-    else
-      my_surv += __ldg(counts + b);
+    const uint32_t cb = single ? 0u : __ldg(counts + b);
+    seg_size[q] = cb;  // 0 marks a flat slot
+    seg_lo[q] = klo;
+    seg_hi[q] = single ? klo : (knext > klo ? knext - K(1) : KeyMax<K>::v);
+    kcnt[q] = 0;
+    kcur[q] = 0;
+    my_surv += cb;
   }
-  uint32_t tot_slots;
   uint64_t tot_surv;
-  uint32_t slot = block_incl_scan(my_slots, &tot_slots, red32) - my_slots;
-  uint64_t off = block_incl_scan(my_surv, &tot_surv, red64) - my_surv;
-  for (uint32_t b = b0; b < b1; ++b) {
-    const uint8_t f = flag[b];
-    if (!f) continue;
-    const uint32_t cb = f == 2 ? 0u : __ldg(counts + b);
-    const K klo = bucket_lo<K>(b, h.base, h.shift, lut);
-    const K knext = (b + 1 < nb) ? bucket_lo<K>(b + 1, h.base, h.shift, lut) : K(0);
-    excl[b] = slot;
-    seg_bucket[slot] = b;
-    seg_off[slot] = off;
-    seg_size[slot] = cb;
-    seg_lo[slot] = klo;
-    seg_hi[slot] = f == 2 ? klo : (knext > klo ? knext - K(1) : KeyMax<K>::v);
-    kcnt[slot] = 0;
-    kcur[slot] = 0;
-    slot++;
-    off += cb;
+  {
+    uint64_t off = block_incl_scan(my_surv, &tot_surv, red64) - my_surv;
+    for (uint32_t q = s0; q < s1; ++q) {
+      seg_off[q] = off;
+      off += __ldcg(seg_size + q);
+    }
   }
   if (tid == 0) {
     ctrl->num_slots = tot_slots;
@@ -849,8 +873,6 @@ __global__ void __launch_bounds__(1024, 1)
   for (uint32_t i = tid; i < num_req; i += nt) atomicAdd(&kcnt[excl[req_bucket[i]]], 1u);
   __syncthreads();
   {
-    const uint32_t sper = (tot_slots + nt - 1) / nt;
-    const uint32_t s0 = min(tot_slots, tid * sper), s1 = min(tot_slots, s0 + sper);
     uint32_t mine = 0;
     for (uint32_t q = s0; q < s1; ++q) mine += kcnt[q];
     uint32_t tot;
@@ -1060,8 +1082,8 @@ __device__ __forceinline__ void bitonic_sort_smem(K *s, uint32_t P) {
 }
 
 // last bin with start[bin] <= r (start is an exclusive scan, start[0] = 0)
-__device__ __forceinline__ uint32_t bin_of_rank(const uint32_t *start, uint32_t r) {
-  uint32_t lo = 0, hi = kFinBins;
+__device__ __forceinline__ uint32_t bin_of_rank(const uint32_t *start, uint32_t nbins, uint32_t r) {
+  uint32_t lo = 0, hi = nbins;
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
     if (start[mid] <= r)
@@ -1084,14 +1106,15 @@ __global__ void __launch_bounds__(kFinThreads)
   uint32_t *start = hist + kFinBins;
   uint32_t *gofs = start + kFinBins;  // gather offset of a needed bin, else kNoSlot
   uint32_t *cur = gofs + kFinBins;
-  K *B = reinterpret_cast<K *>(cur + kFinBins);  // gathered keys of the needed bins
-  K *T = B + bcap;                               // scratch for sorting a large bin
+  uint32_t *small = cur + kFinBins;   // needed bins of 2..32 keys
+  K *B = reinterpret_cast<K *>(small + kFinBins);  // gathered keys of the needed bins
+  K *T = B + bcap;                                 // scratch for sorting a large bin
   constexpr int kMaxBig = 64;
   __shared__ K redk[33];
   __shared__ uint32_t red32[33];
   __shared__ uint32_t big[kMaxBig];
-  __shared__ uint32_t s_nbig;
-  constexpr uint32_t PER = kFinBins / kFinThreads;  // bins per thread
+  __shared__ uint32_t s_nbig, s_nsmall;
+  constexpr uint32_t PER = kFinBins / kFinThreads;  // bins per thread (at most)
 
   if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
   const uint32_t num_slots = ctrl->num_slots;
@@ -1107,6 +1130,10 @@ __global__ void __launch_bounds__(kFinThreads)
       for (uint32_t j = tid; j < m; j += blockDim.x) out[rq[j].out] = Traits<OutT>::value(key);
       continue;
     }
+    // about four keys per bin
+    uint32_t nbits = 8;
+    while (nbits < (uint32_t)kFinBinBits && (4u << nbits) < size) ++nbits;
+    const uint32_t nbins = 1u << nbits;
 
     // digits of (key - mn): first over the bucket's key range; if the needed
     // bins then hold too many keys, over the segment's actual min / max
@@ -1132,13 +1159,17 @@ __global__ void __launch_bounds__(kFinThreads)
         mx = z;
       }
       const int bl = bitlen<K>(mx - mn);
-      sh = bl > kFinBinBits ? (uint32_t)(bl - kFinBinBits) : 0u;
-      for (uint32_t i = tid; i < kFinBins; i += blockDim.x) {
+      sh = bl > (int)nbits ? (uint32_t)(bl - (int)nbits) : 0u;
+      for (uint32_t i = tid; i < nbins; i += blockDim.x) {
         hist[i] = 0;
         cur[i] = 0;
       }
+      if (tid == 0) {
+        s_nbig = 0;
+        s_nsmall = 0;
+      }
       __syncthreads();
-      // keys lie in [mn, mx], so the digit is < kFinBins; the clamp keeps a
+      // keys lie in [mn, mx], so the digit is < nbins; the clamp keeps a
       // shared-memory index in range whatever the data
       {
         uint32_t i = tid;
@@ -1148,49 +1179,57 @@ __global__ void __launch_bounds__(kFinThreads)
           for (int q = 0; q < 4; ++q) kk[q] = src[i + q * blockDim.x];
 #pragma unroll
           for (int q = 0; q < 4; ++q)
-            atomicAdd(&hist[min((uint32_t)((kk[q] - mn) >> sh), (uint32_t)kFinBins - 1u)], 1u);
+            atomicAdd(&hist[min((uint32_t)((kk[q] - mn) >> sh), nbins - 1u)], 1u);
         }
         for (; i < size; i += blockDim.x)
-          atomicAdd(&hist[min((uint32_t)((src[i] - mn) >> sh), (uint32_t)kFinBins - 1u)], 1u);
+          atomicAdd(&hist[min((uint32_t)((src[i] - mn) >> sh), nbins - 1u)], 1u);
       }
       __syncthreads();
       {
         uint32_t cc[PER], sum = 0;
 #pragma unroll
         for (uint32_t q = 0; q < PER; ++q) {
-          cc[q] = hist[tid * PER + q];
+          const uint32_t bb = tid * PER + q;
+          cc[q] = bb < nbins ? hist[bb] : 0u;
           sum += cc[q];
         }
         uint32_t tot;
         uint32_t run = block_incl_scan(sum, &tot, red32) - sum;
 #pragma unroll
         for (uint32_t q = 0; q < PER; ++q) {
-          start[tid * PER + q] = run;
-          gofs[tid * PER + q] = 0;  // "needed" flag until the next scan
+          const uint32_t bb = tid * PER + q;
+          if (bb < nbins) {
+            start[bb] = run;
+            gofs[bb] = 0;  // "needed" flag until the next scan
+          }
           run += cc[q];
         }
       }
       __syncthreads();
-      for (uint32_t j = tid; j < m; j += blockDim.x) gofs[bin_of_rank(start, rq[j].rank)] = 1u;
-      if (tid == 0) s_nbig = 0;
+      for (uint32_t j = tid; j < m; j += blockDim.x)
+        gofs[bin_of_rank(start, nbins, rq[j].rank)] = 1u;
       __syncthreads();
       {
         uint32_t cc[PER], sum = 0;
 #pragma unroll
         for (uint32_t q = 0; q < PER; ++q) {
-          const uint32_t b = tid * PER + q;
-          cc[q] = gofs[b] ? hist[b] : 0u;
+          const uint32_t bb = tid * PER + q;
+          cc[q] = (bb < nbins && gofs[bb]) ? hist[bb] : 0u;
           sum += cc[q];
         }
         uint32_t run = block_incl_scan(sum, &V, red32) - sum;
 #pragma unroll
         for (uint32_t q = 0; q < PER; ++q) {
-          const uint32_t b = tid * PER + q;
-          const bool need = gofs[b] != 0u;
-          gofs[b] = need ? run : kNoSlot;
-          if (need && cc[q] > 32) {
-            const uint32_t at = atomicAdd(&s_nbig, 1u);
-            if (at < kMaxBig) big[at] = b;
+          const uint32_t bb = tid * PER + q;
+          if (bb < nbins) {
+            const bool need = gofs[bb] != 0u;
+            gofs[bb] = need ? run : kNoSlot;
+            if (need && cc[q] > 32) {
+              const uint32_t at = atomicAdd(&s_nbig, 1u);
+              if (at < kMaxBig) big[at] = bb;
+            } else if (need && cc[q] > 1) {
+              small[atomicAdd(&s_nsmall, 1u)] = bb;
+            }
           }
           run += cc[q];
         }
@@ -1216,9 +1255,9 @@ __global__ void __launch_bounds__(kFinThreads)
     // ---- gather the needed bins
     {
       auto put = [&](K k) {
-        const uint32_t b = min((uint32_t)((k - mn) >> sh), (uint32_t)kFinBins - 1u);
-        const uint32_t g = gofs[b];
-        if (g != kNoSlot) B[g + atomicAdd(&cur[b], 1u)] = k;
+        const uint32_t bb = min((uint32_t)((k - mn) >> sh), nbins - 1u);
+        const uint32_t g = gofs[bb];
+        if (g != kNoSlot) B[g + atomicAdd(&cur[bb], 1u)] = k;
       };
       uint32_t i = tid;
       for (; i + 3 * blockDim.x < size; i += 4 * blockDim.x) {
@@ -1232,20 +1271,20 @@ __global__ void __launch_bounds__(kFinThreads)
     }
     __syncthreads();
 
-    // ---- sort each needed bin: warps take bins of <= 32 keys
-    for (uint32_t b = warp; b < kFinBins; b += nwarps) {
-      const uint32_t g = gofs[b], c = hist[b];
-      if (g == kNoSlot || c < 2 || c > 32) continue;
+    // ---- sort each needed bin: a warp per bin of 2..32 keys
+    const uint32_t nsmall = s_nsmall;
+    for (uint32_t q = warp; q < nsmall; q += nwarps) {
+      const uint32_t bb = small[q];
+      const uint32_t g = gofs[bb], c = hist[bb];
       K v = lane < c ? B[g + lane] : KeyMax<K>::v;
       v = warp_bitonic32(v);
       if (lane < c) B[g + lane] = v;
     }
     // larger bins: the whole CTA, one at a time
     const uint32_t nbig = s_nbig;
-    for (uint32_t q = 0; q < (nbig < kMaxBig ? nbig : kFinBins); ++q) {
-      uint32_t b = q;
-      if (nbig < kMaxBig) b = big[q];
-      const uint32_t g = gofs[b], c = hist[b];
+    for (uint32_t q = 0; q < (nbig <= (uint32_t)kMaxBig ? nbig : nbins); ++q) {
+      const uint32_t bb = nbig <= (uint32_t)kMaxBig ? big[q] : q;
+      const uint32_t g = gofs[bb], c = hist[bb];
       if (g == kNoSlot || c <= 32) continue;
       uint32_t P = 64;
       while (P < c) P <<= 1;
@@ -1260,8 +1299,8 @@ __global__ void __launch_bounds__(kFinThreads)
     // ---- answer
     for (uint32_t j = tid; j < m; j += blockDim.x) {
       const Req e = rq[j];
-      const uint32_t b = bin_of_rank(start, e.rank);
-      out[e.out] = Traits<OutT>::value(B[gofs[b] + (e.rank - start[b])]);
+      const uint32_t bb = bin_of_rank(start, nbins, e.rank);
+      out[e.out] = Traits<OutT>::value(B[gofs[bb] + (e.rank - start[bb])]);
     }
     __syncthreads();
   }

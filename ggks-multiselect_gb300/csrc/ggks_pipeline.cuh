@@ -19,7 +19,7 @@ static inline uint32_t cap_keys_for() {
 template <class T>
 static inline int finish_smem_bytes() {
   using K = typename Traits<T>::K;
-  return (int)(4 * kFinBins * sizeof(uint32_t) + 2 * (size_t)cap_keys_for<T>() * sizeof(K));
+  return (int)(5 * kFinBins * sizeof(uint32_t) + 2 * (size_t)cap_keys_for<T>() * sizeof(K));
 }
 
 static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
