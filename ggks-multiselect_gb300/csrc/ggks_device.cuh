@@ -59,6 +59,7 @@ constexpr uint32_t kLutEntries = kLutIdx + 1;    // + one for keys above the spa
 constexpr uint32_t kLutPadded = (kLutEntries + 3) & ~3u;  // 16-byte multiple
 constexpr int kMaxSubBits = 12;                  // at most 2^12 buckets per slice
 constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
+constexpr uint32_t kInactive = 0x80000000u;  // compaction cursor of an inactive bucket
 constexpr int kSpinLimit = 1 << 22;              // bounded device-side waits
 
 // status bits in Ctrl::status
@@ -866,6 +867,8 @@ __global__ void __launch_bounds__(1024, 1)
       atomicOr(&ctrl->status, ST_OVERFLOW);
       ctrl->cap_needed = tot_surv;
     }
+    // compaction cursors carry the survivor position in 31 bits
+    if (tot_surv >= (uint64_t)kInactive) atomicOr(&ctrl->status, ST_INTERNAL);
   }
   __syncthreads();
 
@@ -896,33 +899,31 @@ __global__ void __launch_bounds__(1024, 1)
 // ---------------------------------------------------------------------------
 // (f) compaction pass
 // ---------------------------------------------------------------------------
-// cursor[b] (shared) = next survivor position of this CTA in bucket b, or
-// kNoSlot for inactive buckets.  In heavy mode lanes of a warp that hit the
-// same bucket take consecutive positions from one shared atomic.
+// cursor[b] (shared) = next survivor position of this CTA in bucket b for an
+// active bucket (< 2^31), or kInactive + (elements seen so far) for an inactive
+// one.  Every element takes one shared atomic on its bucket's cursor and the
+// returned value decides whether it is stored: no divergent branch per
+// survivor.  In heavy mode lanes of a warp that hit the same bucket share one
+// atomic (match.any) and take consecutive positions.
 template <class T, bool HEAVY>
 __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Traits<T>::K base,
                                             uint32_t shift, const uint32_t *lut, uint32_t *cursor,
                                             typename Traits<T>::K *__restrict__ surv,
                                             uint64_t surv_cap, bool *overrun) {
   const uint32_t b = bucket_of(k, base, shift, lut);
-  const bool act = cursor[b] != kNoSlot;
+  uint32_t pos;
   if (HEAVY) {
-    const uint32_t act_mask = __ballot_sync(0xffffffffu, act);
-    if (!act_mask) return;
-    const uint32_t peers = __match_any_sync(0xffffffffu, act ? b : kNoSlot);
-    if (!act) return;
+    const uint32_t peers = __match_any_sync(0xffffffffu, b);
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(peers) - 1;
-    uint32_t base_pos = 0;
-    if (lane == leader) base_pos = atomicAdd(&cursor[b], (uint32_t)__popc(peers));
-    base_pos = __shfl_sync(peers, base_pos, leader);
-    const uint32_t pos = base_pos + __popc(peers & ((1u << lane) - 1u));
-    if (pos < surv_cap)
-      surv[pos] = k;
-    else
-      *overrun = true;
-  } else if (act) {
-    const uint32_t pos = atomicAdd(&cursor[b], 1u);
+    uint32_t p0 = 0;
+    if (lane == leader) p0 = atomicAdd(&cursor[b], (uint32_t)__popc(peers));
+    p0 = __shfl_sync(peers, p0, leader);
+    pos = p0 + __popc(peers & ((1u << lane) - 1u));
+  } else {
+    pos = atomicAdd(&cursor[b], 1u);
+  }
+  if (!(pos & kInactive)) {
     if (pos < surv_cap)
       surv[pos] = k;
     else
@@ -998,7 +999,7 @@ __global__ void __launch_bounds__(1024, 1)
   const uint32_t c = blockIdx.x;
   for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
   const uint32_t num_slots = ctrl->num_slots;
-  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) cursor[b] = kNoSlot;
+  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) cursor[b] = kInactive;
   if (threadIdx.x == 0) s_bad = false;
   __syncthreads();
   // flat slots (seg_size 0: a single-key bucket) are answered without survivors
