@@ -195,6 +195,38 @@ static Context *resolve(const ggks_opts *opts, int *status) {
 }
 
 // ---------------------------------------------------------------------------
+// host vectors
+// ---------------------------------------------------------------------------
+// A pinned (page-locked, mapped) host vector is read by the kernels directly
+// over the CPU-GPU link: the histogram pass ingests it and writes the device
+// copy in the same pass, so the copy overlaps the first pass.  Any other host
+// memory is copied to the device first.  The device copy keeps the host
+// vector's alignment modulo 16 bytes, so both are split into the same
+// 16-byte vectors.
+template <class T>
+static int stage_host_vector(Context &ctx, const T *vec, uint64_t n, cudaStream_t s,
+                             const T **d_in, const T **ingest) {
+  cudaError_t e = ensure_dvec(ctx, n * sizeof(T) + 16);
+  if (e != cudaSuccess) return from_cuda(e);
+  const uintptr_t mis = (uintptr_t)vec & 15u;
+  T *dst = reinterpret_cast<T *>(static_cast<char *>(ctx.dvec) + mis);
+  cudaPointerAttributes attr{};
+  const bool mapped = cudaPointerGetAttributes(&attr, vec) == cudaSuccess &&
+                      attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr &&
+                      ((uintptr_t)attr.devicePointer & 15u) == mis;
+  cudaGetLastError();  // a plain host pointer is not an error
+  if (mapped) {
+    *ingest = static_cast<const T *>(attr.devicePointer);
+  } else {
+    e = cudaMemcpyAsync(dst, vec, n * sizeof(T), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return from_cuda(e);
+    *ingest = nullptr;
+  }
+  *d_in = dst;
+  return GGKS_OK;
+}
+
+// ---------------------------------------------------------------------------
 // API bodies
 // ---------------------------------------------------------------------------
 template <class T>
@@ -211,17 +243,17 @@ static int api_multiselect(const T *vec, uint64_t n, const uint32_t *h_k, uint32
   DeviceGuard dg(ctx->device);
   cudaStream_t s = (opts && opts->stream) ? static_cast<cudaStream_t>(opts->stream) : ctx->stream;
   const T *d_in = vec;
+  const T *ingest = nullptr;
   if (host_input) {
-    cudaError_t e = ensure_dvec(*ctx, n * sizeof(T));
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->dvec, vec, n * sizeof(T), cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return from_cuda(e);
-    d_in = static_cast<const T *>(ctx->dvec);
+    int st2 = stage_host_vector(*ctx, vec, n, s, &d_in, &ingest);
+    if (st2 != GGKS_OK) return st2;
   }
   const bool out_dev = opts && (opts->flags & GGKS_FLAG_OUT_DEVICE);
   ReqSource src;
   src.h_k = h_k;
   const T *hres = nullptr;
-  st = select<T, T>(*ctx, d_in, n, src, num_k, out_dev ? out : nullptr, out_dev ? nullptr : &hres, s);
+  st = select<T, T>(*ctx, d_in, n, src, num_k, out_dev ? out : nullptr, out_dev ? nullptr : &hres, s,
+                   ingest);
   if (st == GGKS_OK) {
     if (!out_dev) std::memcpy(out, hres, (size_t)num_k * sizeof(T));
     ctx->stats.calls++;
@@ -242,17 +274,17 @@ static int api_topk(const T *vec, uint64_t n, uint32_t K, T *out, const ggks_opt
   DeviceGuard dg(ctx->device);
   cudaStream_t s = (opts && opts->stream) ? static_cast<cudaStream_t>(opts->stream) : ctx->stream;
   const T *d_in = vec;
+  const T *ingest = nullptr;
   if (host_input) {
-    cudaError_t e = ensure_dvec(*ctx, n * sizeof(T));
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->dvec, vec, n * sizeof(T), cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return from_cuda(e);
-    d_in = static_cast<const T *>(ctx->dvec);
+    int st2 = stage_host_vector(*ctx, vec, n, s, &d_in, &ingest);
+    if (st2 != GGKS_OK) return st2;
   }
   const bool out_dev = opts && (opts->flags & GGKS_FLAG_OUT_DEVICE);
   ReqSource src;
   src.topk = true;
   const T *hres = nullptr;
-  st = select<T, T>(*ctx, d_in, n, src, K, out_dev ? out : nullptr, out_dev ? nullptr : &hres, s);
+  st = select<T, T>(*ctx, d_in, n, src, K, out_dev ? out : nullptr, out_dev ? nullptr : &hres, s,
+                   ingest);
   if (st == GGKS_OK) {
     if (!out_dev) std::memcpy(out, hres, (size_t)K * sizeof(T));
     ctx->stats.calls++;

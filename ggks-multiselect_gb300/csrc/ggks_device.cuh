@@ -224,6 +224,45 @@ __device__ __forceinline__ ulonglong2 ldg_stream<ulonglong2>(const ulonglong2 *p
   return v;
 }
 
+// L2 cache policies (createpolicy) and loads / stores that carry them: the
+// streamed input is evict-first except for the tail that the compaction pass
+// re-reads first; survivors are evict-last so that they stay in L2 for the
+// finishing pass.
+__device__ __forceinline__ uint64_t l2_policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+template <class V>
+__device__ __forceinline__ V ldg_hint(const V *p, uint64_t pol);
+template <>
+__device__ __forceinline__ uint4 ldg_hint<uint4>(const uint4 *p, uint64_t pol) {
+  uint4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p), "l"(pol));
+  return v;
+}
+template <>
+__device__ __forceinline__ ulonglong2 ldg_hint<ulonglong2>(const ulonglong2 *p, uint64_t pol) {
+  ulonglong2 v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u64 {%0,%1}, [%2], %3;"
+               : "=l"(v.x), "=l"(v.y)
+               : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st_hint(uint32_t *p, uint32_t v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_hint(uint64_t *p, uint64_t v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.b64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
+}
+
 // right shift that yields 0 for shift >= width
 __device__ __forceinline__ uint32_t shr_clamp(uint32_t d, uint32_t s) {
   return __funnelshift_r(d, 0u, s);  // shf.r.clamp: shift clamped to 32
@@ -551,52 +590,95 @@ __device__ __forceinline__ void hist_add(uint32_t *hist, uint32_t b) {
   }
 }
 
-template <class T, int UNROLL, bool HEAVY>
+// plain 128-bit store with an L2 policy (the device copy written while
+// ingesting a host vector)
+__device__ __forceinline__ void st_vec_hint(uint4 *p, const uint4 &v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1,%2,%3,%4}, %5;" ::"l"(p), "r"(v.x),
+               "r"(v.y), "r"(v.z), "r"(v.w), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void st_vec_hint(ulonglong2 *p, const ulonglong2 &v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.u64 [%0], {%1,%2}, %3;" ::"l"(p), "l"(v.x), "l"(v.y),
+               "l"(pol)
+               : "memory");
+}
+
+// INGEST: x is a host vector mapped into the device address space (pinned
+// memory read over NVLink-C2C); every tile is also written to copy_to, the
+// device copy that the later passes read.  copy_to has the same alignment
+// modulo 16 bytes as x.
+template <class T, int UNROLL, bool HEAVY, bool INGEST>
 __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, uint32_t *hist,
                                           const uint32_t *lut, typename Traits<T>::K base,
-                                          uint32_t shift) {
+                                          uint32_t shift, uint32_t keep_layers,
+                                          T *__restrict__ copy_to) {
   using K = typename Traits<T>::K;
   using V = typename Traits<T>::Vec;
   constexpr int PV = Traits<T>::kPerVec;
   const Span<T> sp = split_span(x, n);
   const V *xv = reinterpret_cast<const V *>(x + sp.head);
+  V *cv = reinterpret_cast<V *>(copy_to + sp.head);
   const uint64_t tile_v = (uint64_t)blockDim.x * UNROLL;
   const uint64_t ntiles = sp.nvec / tile_v;
-  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const V *p = xv + tile * tile_v + threadIdx.x;
+  // the last keep_layers tiles of every CTA stay in L2 for the compaction pass,
+  // which visits them first
+  const uint64_t pol_first = l2_policy_evict_first(), pol_last = l2_policy_evict_last();
+  const uint64_t mine = ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  for (uint64_t q = 0; q < mine; ++q) {
+    const uint64_t tile = blockIdx.x + q * gridDim.x;
+    const uint64_t pol = (q + keep_layers >= mine) ? pol_last : pol_first;
+    const uint64_t off = tile * tile_v + threadIdx.x;
     V v[UNROLL];
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) v[u] = ldg_stream(p + (uint64_t)u * blockDim.x);
+    for (int u = 0; u < UNROLL; ++u) {
+      if (INGEST)
+        v[u] = xv[off + (uint64_t)u * blockDim.x];
+      else
+        v[u] = ldg_hint(xv + off + (uint64_t)u * blockDim.x, pol);
+    }
+    if (INGEST) {
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) st_vec_hint(cv + off + (uint64_t)u * blockDim.x, v[u], pol);
+    }
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
       K k[PV];
       vec_keys<T>(v[u], k);
 #pragma unroll
-      for (int q = 0; q < PV; ++q) hist_add<HEAVY>(hist, bucket_of<K>(k[q], base, shift, lut));
+      for (int e = 0; e < PV; ++e) hist_add<HEAVY>(hist, bucket_of<K>(k[e], base, shift, lut));
     }
   }
   // leftover vectors (fewer than one tile) and the scalar head / tail
   const uint32_t owner = (uint32_t)(ntiles % gridDim.x);
   if (blockIdx.x == owner) {
     for (uint64_t vi = ntiles * tile_v + threadIdx.x; vi < sp.nvec; vi += blockDim.x) {
-      V vv = ldg_stream(xv + vi);
+      V vv = INGEST ? xv[vi] : ldg_stream(xv + vi);
+      if (INGEST) cv[vi] = vv;
       K k[PV];
       vec_keys<T>(vv, k);
 #pragma unroll
-      for (int q = 0; q < PV; ++q) atomicAdd(&hist[bucket_of<K>(k[q], base, shift, lut)], 1u);
+      for (int e = 0; e < PV; ++e) atomicAdd(&hist[bucket_of<K>(k[e], base, shift, lut)], 1u);
     }
-    for (uint64_t e = threadIdx.x; e < sp.head; e += blockDim.x)
-      atomicAdd(&hist[bucket_of<K>(Traits<T>::key(x[e]), base, shift, lut)], 1u);
-    for (uint64_t e = sp.tail0 + threadIdx.x; e < n; e += blockDim.x)
-      atomicAdd(&hist[bucket_of<K>(Traits<T>::key(x[e]), base, shift, lut)], 1u);
+    for (uint64_t e = threadIdx.x; e < sp.head; e += blockDim.x) {
+      const T v = x[e];
+      if (INGEST) copy_to[e] = v;
+      atomicAdd(&hist[bucket_of<K>(Traits<T>::key(v), base, shift, lut)], 1u);
+    }
+    for (uint64_t e = sp.tail0 + threadIdx.x; e < n; e += blockDim.x) {
+      const T v = x[e];
+      if (INGEST) copy_to[e] = v;
+      atomicAdd(&hist[bucket_of<K>(Traits<T>::key(v), base, shift, lut)], 1u);
+    }
   }
 }
 
+// copy_to == nullptr: x is the device vector.  Otherwise x is a mapped host
+// vector and this pass also writes the device copy (see hist_body).
 template <class T, int UNROLL>
 __global__ void __launch_bounds__(1024, 1)
     k_hist(const T *__restrict__ x, uint64_t n, const LutHeader<typename Traits<T>::K> *hdr,
            const uint32_t *__restrict__ lut_g, uint32_t *__restrict__ partials, uint32_t nb_max,
-           const Ctrl *ctrl) {
+           uint32_t keep_layers, const Ctrl *ctrl, T *__restrict__ copy_to) {
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
@@ -606,10 +688,17 @@ __global__ void __launch_bounds__(1024, 1)
   for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
   for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) hist[b] = 0;
   __syncthreads();
-  if (h.heavy)
-    hist_body<T, UNROLL, true>(x, n, hist, lut, h.base, h.shift);
-  else
-    hist_body<T, UNROLL, false>(x, n, hist, lut, h.base, h.shift);
+  if (copy_to) {
+    if (h.heavy)
+      hist_body<T, UNROLL, true, true>(x, n, hist, lut, h.base, h.shift, keep_layers, copy_to);
+    else
+      hist_body<T, UNROLL, false, true>(x, n, hist, lut, h.base, h.shift, keep_layers, copy_to);
+  } else {
+    if (h.heavy)
+      hist_body<T, UNROLL, true, false>(x, n, hist, lut, h.base, h.shift, keep_layers, nullptr);
+    else
+      hist_body<T, UNROLL, false, false>(x, n, hist, lut, h.base, h.shift, keep_layers, nullptr);
+  }
   __syncthreads();
   uint32_t *row = partials + (uint64_t)blockIdx.x * nb_max;
   for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) row[b] = hist[b];
@@ -909,7 +998,7 @@ template <class T, bool HEAVY>
 __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Traits<T>::K base,
                                             uint32_t shift, const uint32_t *lut, uint32_t *cursor,
                                             typename Traits<T>::K *__restrict__ surv,
-                                            uint64_t surv_cap, bool *overrun) {
+                                            uint64_t surv_cap, bool *overrun, uint64_t pol_keep) {
   const uint32_t b = bucket_of(k, base, shift, lut);
   uint32_t pos;
   if (HEAVY) {
@@ -925,7 +1014,7 @@ __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Tr
   }
   if (!(pos & kInactive)) {
     if (pos < surv_cap)
-      surv[pos] = k;
+      st_hint(surv + pos, k, pol_keep);
     else
       *overrun = true;
   }
@@ -947,19 +1036,20 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
   // visited last-to-first: the tail of the input is the part most likely to
   // still be in L2.
   const uint64_t mine = ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const uint64_t pol_first = l2_policy_evict_first(), pol_keep = l2_policy_evict_last();
   for (uint64_t q = mine; q-- > 0;) {
     const uint64_t tile = blockIdx.x + q * gridDim.x;
     const V *p = xv + tile * tile_v + threadIdx.x;
     V v[UNROLL];
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) v[u] = ldg_stream(p + (uint64_t)u * blockDim.x);
+    for (int u = 0; u < UNROLL; ++u) v[u] = ldg_hint(p + (uint64_t)u * blockDim.x, pol_first);
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
       K kk[PV];
       vec_keys<T>(v[u], kk);
 #pragma unroll
       for (int e = 0; e < PV; ++e)
-        compact_one<T, HEAVY>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun);
+        compact_one<T, HEAVY>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun, pol_keep);
     }
   }
   const uint32_t owner = (uint32_t)(ntiles % gridDim.x);
@@ -970,12 +1060,14 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
       vec_keys<T>(vv, kk);
 #pragma unroll
       for (int e = 0; e < PV; ++e)
-        compact_one<T, false>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun);
+        compact_one<T, false>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun, pol_keep);
     }
     for (uint64_t e = threadIdx.x; e < sp.head; e += blockDim.x)
-      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun);
+      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun,
+                            pol_keep);
     for (uint64_t e = sp.tail0 + threadIdx.x; e < n; e += blockDim.x)
-      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun);
+      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun,
+                            pol_keep);
   }
 }
 

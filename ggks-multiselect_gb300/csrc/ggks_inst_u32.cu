@@ -4,5 +4,5 @@
 
 namespace ggks {
 template int select<uint32_t, uint32_t>(Context &, const uint32_t *, uint64_t, const ReqSource &, uint32_t,
-                        uint32_t *, const uint32_t **, cudaStream_t);
+                            uint32_t *, const uint32_t **, cudaStream_t, const uint32_t *);
 }  // namespace ggks

@@ -72,8 +72,11 @@ struct ReqSource {
 // null, in the context's arena.  If host_results is not null the results are
 // also copied to pinned host memory and *host_results points there (valid
 // until the next call on the context).  The stream is synchronised.
+// ingest: when not null, a host vector mapped into the device address space;
+// the first passes read it and the histogram pass writes it to d_in (a device
+// buffer with the same alignment modulo 16 bytes).
 template <class InT, class OutT>
 int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint32_t num_req,
-           OutT *d_out_user, const OutT **host_results, cudaStream_t s);
+           OutT *d_out_user, const OutT **host_results, cudaStream_t s, const InT *ingest);
 
 }  // namespace ggks

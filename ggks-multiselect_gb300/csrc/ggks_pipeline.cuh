@@ -24,6 +24,9 @@ static inline int finish_smem_bytes() {
 
 static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// input bytes the histogram pass leaves in L2 (evict-last) for compaction
+constexpr uint64_t kL2KeepBytes = 32ull << 20;
+
 struct Plan {
   uint64_t n = 0;
   uint32_t num_req = 0;
@@ -140,7 +143,7 @@ __global__ void k_make_topk_reqs(Req *reqs, uint64_t n, uint32_t K);
 
 template <class InT, class OutT>
 int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint32_t num_req,
-           OutT *d_out_user, const OutT **host_results, cudaStream_t s) {
+           OutT *d_out_user, const OutT **host_results, cudaStream_t s, const InT *ingest) {
   using K = typename Traits<InT>::K;
   constexpr int UNROLL = 4;
   if (ctx.depth > 12) return GGKS_INTERNAL;
@@ -206,8 +209,8 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   // ---- (b) sample + splitter table
   {
     PassTimer t(ctx, s, GGKS_PASS_SAMPLE);
-    k_sample_lut<InT><<<p.sample_grid, 1024, 0, s>>>(d_in, n, p.S, 0x5EEDu, samples, ctrl, hdr,
-                                                      lut, p.nb_max);
+    k_sample_lut<InT><<<p.sample_grid, 1024, 0, s>>>(ingest ? ingest : d_in, n, p.S, 0x5EEDu,
+                                                      samples, ctrl, hdr, lut, p.nb_max);
     ran[GGKS_PASS_SAMPLE] = true;
   }
   // ---- (c) histogram
@@ -215,7 +218,13 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 4);
     set_smem_max<k_hist<InT, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
     PassTimer t(ctx, s, GGKS_PASS_HIST);
-    k_hist<InT, UNROLL><<<p.G, 1024, smem, s>>>(d_in, n, hdr, lut, partials, p.nb_max, ctrl);
+    // tile layers (one tile per CTA) whose input stays in L2 for compaction
+    const uint64_t layer_bytes = (uint64_t)p.G * 1024 * UNROLL * 16;
+    const uint32_t keep_layers = (uint32_t)((kL2KeepBytes + layer_bytes - 1) / layer_bytes);
+    // with a mapped host vector, this pass also writes the device copy d_in
+    k_hist<InT, UNROLL><<<p.G, 1024, smem, s>>>(ingest ? ingest : d_in, n, hdr, lut, partials,
+                                                p.nb_max, keep_layers, ctrl,
+                                                ingest ? const_cast<InT *>(d_in) : nullptr);
     ran[GGKS_PASS_HIST] = true;
   }
   // ---- (d) reduce + decoupled look-back scan
@@ -323,7 +332,8 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
         ReqSource cs;
         cs.d_reqs = klist + ks[slot];
         ctx.stats.recursions++;
-        st = select<K, OutT>(*ch, surv + so[slot], sz[slot], cs, kc[slot], d_out, nullptr, s);
+        st = select<K, OutT>(*ch, surv + so[slot], sz[slot], cs, kc[slot], d_out, nullptr, s,
+                             nullptr);
         if (st != GGKS_OK) return st;
       }
       if (want_host) {

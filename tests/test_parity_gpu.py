@@ -265,3 +265,23 @@ def test_reference_bucket_algorithm_agrees(g, orc):
         d = DeviceArray(x)
         assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks), orc.bucket_multiselect(x, ks, 9),
                     f"{dtype}/{dist}")
+
+
+@pytest.mark.parametrize("offset", [0, 1, 3])
+def test_pinned_host_vector_ingest(g, orc, offset):
+    """A pinned host vector is read over the CPU-GPU link by the histogram
+    pass, which also writes the device copy; views off a 16-byte boundary
+    keep their alignment in the copy."""
+    import torch
+
+    import ggks_problems as gp
+    for dtype, dist, tdt in (("f32", "normal", torch.float32), ("f64", "cauchy", torch.float64),
+                             ("u32", "uniform", torch.int32)):
+        n = (1 << 20) + 7
+        x = gp.generate(dtype, dist, n, seed=offset + 1)
+        pin = torch.empty(n + offset, dtype=tdt, pin_memory=True)
+        view = pin.numpy().view(x.dtype)[offset:]
+        view[:] = x
+        ks = gp.k_distinct(n, 333, offset)
+        assert_same(g.multiselect_host(view, ks), orc.multiselect(x, ks), f"pinned {dtype}")
+        assert_same(g.topk_host(view, 2048), orc.topk(x, 2048), f"pinned topk {dtype}")
