@@ -217,10 +217,12 @@ static int stage_host_vector(Context &ctx, const T *vec, uint64_t n, cudaStream_
   cudaGetLastError();  // a plain host pointer is not an error
   if (mapped) {
     *ingest = static_cast<const T *>(attr.devicePointer);
+    ctx.stats.host_ingested++;
   } else {
     e = cudaMemcpyAsync(dst, vec, n * sizeof(T), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return from_cuda(e);
     *ingest = nullptr;
+    ctx.stats.host_staged++;
   }
   *d_in = dst;
   return GGKS_OK;

@@ -45,14 +45,16 @@ class Stats(ctypes.Structure):
                 ("pass_launches", ctypes.c_uint64 * NUM_PASSES),
                 ("pass_ms", ctypes.c_double * NUM_PASSES),
                 ("bytes_in", ctypes.c_uint64), ("survivors", ctypes.c_uint64),
-                ("retries", ctypes.c_uint64), ("recursions", ctypes.c_uint64)]
+                ("retries", ctypes.c_uint64), ("recursions", ctypes.c_uint64),
+                ("host_ingested", ctypes.c_uint64), ("host_staged", ctypes.c_uint64)]
 
     def as_dict(self):
         return {"calls": self.calls, "launches": self.launches,
                 "pass_launches": dict(zip(PASS_NAMES, list(self.pass_launches))),
                 "pass_ms": dict(zip(PASS_NAMES, list(self.pass_ms))),
                 "bytes_in": self.bytes_in, "survivors": self.survivors,
-                "retries": self.retries, "recursions": self.recursions}
+                "retries": self.retries, "recursions": self.recursions,
+                "host_ingested": self.host_ingested, "host_staged": self.host_staged}
 
 
 # every symbol declared in include/ggks.h

@@ -132,6 +132,8 @@ typedef struct ggks_stats {
   uint64_t survivors;                 /* elements compacted into active buckets */
   uint64_t retries;                   /* survivor-buffer regrowth re-runs */
   uint64_t recursions;                /* oversized segments re-selected */
+  uint64_t host_ingested;             /* host vectors read in place by the first pass */
+  uint64_t host_staged;               /* host vectors copied to the device first */
 } ggks_stats;
 
 /* pass indices of ggks_stats.pass_* */
