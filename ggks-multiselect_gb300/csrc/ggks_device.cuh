@@ -224,45 +224,6 @@ __device__ __forceinline__ ulonglong2 ldg_stream<ulonglong2>(const ulonglong2 *p
   return v;
 }
 
-// L2 cache policies (createpolicy) and loads / stores that carry them: the
-// streamed input is evict-first except for the tail that the compaction pass
-// re-reads first; survivors are evict-last so that they stay in L2 for the
-// finishing pass.
-__device__ __forceinline__ uint64_t l2_policy_evict_first() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ uint64_t l2_policy_evict_last() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-template <class V>
-__device__ __forceinline__ V ldg_hint(const V *p, uint64_t pol);
-template <>
-__device__ __forceinline__ uint4 ldg_hint<uint4>(const uint4 *p, uint64_t pol) {
-  uint4 v;
-  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
-               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-               : "l"(p), "l"(pol));
-  return v;
-}
-template <>
-__device__ __forceinline__ ulonglong2 ldg_hint<ulonglong2>(const ulonglong2 *p, uint64_t pol) {
-  ulonglong2 v;
-  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u64 {%0,%1}, [%2], %3;"
-               : "=l"(v.x), "=l"(v.y)
-               : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ void st_hint(uint32_t *p, uint32_t v, uint64_t pol) {
-  asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
-}
-__device__ __forceinline__ void st_hint(uint64_t *p, uint64_t v, uint64_t pol) {
-  asm volatile("st.global.L2::cache_hint.b64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
-}
-
 // right shift that yields 0 for shift >= width
 __device__ __forceinline__ uint32_t shr_clamp(uint32_t d, uint32_t s) {
   return __funnelshift_r(d, 0u, s);  // shf.r.clamp: shift clamped to 32
@@ -429,7 +390,9 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
   __shared__ K redk[33];
   __shared__ uint32_t red32[33];
   __shared__ uint32_t s_last;
-  __shared__ int s_t;
+  __shared__ int s_t, s_r0;
+  __shared__ uint32_t s_tot[54];
+  __shared__ uint32_t s_cost[34];
 
   const uint32_t tid = threadIdx.x;
   const uint32_t i = blockIdx.x * blockDim.x + tid;
@@ -494,6 +457,7 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
   }
   const bool top_run_start = cnt[kLutIdx - 1] != 0;
   if (tid == 0) s_t = 33;  // total(33) <= 1 + 4096 + 1 <= nb_max: always feasible
+  if (tid < 34) s_cost[tid] = 0;
   __syncthreads();
   if (tid < 54) {
     // smallest t with total(t) <= nb_max; one candidate t per thread
@@ -504,15 +468,49 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
       b = b < 0 ? 0 : (b > bcap ? bcap : b);
       tot += (uint64_t)lch[l] << b;
     }
+    s_tot[tid] = (uint32_t)(tot < 0xFFFFFFFFull ? tot : 0xFFFFFFFFull);
     if (tot <= nb_max) atomicMin(&s_t, t);
   }
   __syncthreads();
   const int t = s_t;
+  const uint32_t spare = nb_max - s_tot[t + kMaxSubBits + 1];
 
-  auto bits_of = [&](int q) -> int {
+  // Power-of-two rounding leaves part of the budget unused.  Spend it on the
+  // slices whose buckets are expected to be the fullest: r = 32 * (samples per
+  // bucket) / 2^t in [0, 32]; doubling slice j's buckets costs 2^b_j.  The
+  // largest r first, as long as the whole bin of r fits.
+  int bq[4];
+  uint32_t rq[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
     int b = lc[q] - t;
-    return b < 0 ? 0 : (b > bcap ? bcap : b);
-  };
+    bq[q] = b < 0 ? 0 : (b > bcap ? bcap : b);
+    rq[q] = 0xFFFFFFFFu;  // not a candidate
+    if (c[q] && bq[q] < bcap) {
+      const int e = bq[q] + t - 5;  // r = c * 32 / 2^(b + t)
+      uint32_t r = e >= 0 ? (e >= 32 ? 0u : c[q] >> e) : (-e >= 32 ? 32u : c[q] << (-e));
+      rq[q] = r > 32u ? 32u : r;
+      atomicAdd(&s_cost[rq[q]], 1u << bq[q]);
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    uint32_t acc = 0;
+    int r0 = 33;
+    for (int r = 32; r >= 0; --r) {
+      if (acc + s_cost[r] > spare) break;
+      acc += s_cost[r];
+      r0 = r;
+    }
+    s_r0 = r0;
+  }
+  __syncthreads();
+  const uint32_t r0 = (uint32_t)s_r0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (rq[q] != 0xFFFFFFFFu && rq[q] >= r0) bq[q] += 1;
+
+  auto bits_of = [&](int q) -> int { return bq[q]; };
   uint32_t my[4], mysum = 0;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
@@ -590,19 +588,6 @@ __device__ __forceinline__ void hist_add(uint32_t *hist, uint32_t b) {
   }
 }
 
-// plain 128-bit store with an L2 policy (the device copy written while
-// ingesting a host vector)
-__device__ __forceinline__ void st_vec_hint(uint4 *p, const uint4 &v, uint64_t pol) {
-  asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1,%2,%3,%4}, %5;" ::"l"(p), "r"(v.x),
-               "r"(v.y), "r"(v.z), "r"(v.w), "l"(pol)
-               : "memory");
-}
-__device__ __forceinline__ void st_vec_hint(ulonglong2 *p, const ulonglong2 &v, uint64_t pol) {
-  asm volatile("st.global.L2::cache_hint.v2.u64 [%0], {%1,%2}, %3;" ::"l"(p), "l"(v.x), "l"(v.y),
-               "l"(pol)
-               : "memory");
-}
-
 // INGEST: x is a host vector mapped into the device address space (pinned
 // memory read over NVLink-C2C); every tile is also written to copy_to, the
 // device copy that the later passes read.  copy_to has the same alignment
@@ -610,8 +595,7 @@ __device__ __forceinline__ void st_vec_hint(ulonglong2 *p, const ulonglong2 &v, 
 template <class T, int UNROLL, bool HEAVY, bool INGEST>
 __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, uint32_t *hist,
                                           const uint32_t *lut, typename Traits<T>::K base,
-                                          uint32_t shift, uint32_t keep_layers,
-                                          T *__restrict__ copy_to) {
+                                          uint32_t shift, T *__restrict__ copy_to) {
   using K = typename Traits<T>::K;
   using V = typename Traits<T>::Vec;
   constexpr int PV = Traits<T>::kPerVec;
@@ -620,13 +604,7 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
   V *cv = reinterpret_cast<V *>(copy_to + sp.head);
   const uint64_t tile_v = (uint64_t)blockDim.x * UNROLL;
   const uint64_t ntiles = sp.nvec / tile_v;
-  // the last keep_layers tiles of every CTA stay in L2 for the compaction pass,
-  // which visits them first
-  const uint64_t pol_first = l2_policy_evict_first(), pol_last = l2_policy_evict_last();
-  const uint64_t mine = ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  for (uint64_t q = 0; q < mine; ++q) {
-    const uint64_t tile = blockIdx.x + q * gridDim.x;
-    const uint64_t pol = (q + keep_layers >= mine) ? pol_last : pol_first;
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const uint64_t off = tile * tile_v + threadIdx.x;
     V v[UNROLL];
 #pragma unroll
@@ -634,11 +612,11 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
       if (INGEST)
         v[u] = xv[off + (uint64_t)u * blockDim.x];
       else
-        v[u] = ldg_hint(xv + off + (uint64_t)u * blockDim.x, pol);
+        v[u] = ldg_stream(xv + off + (uint64_t)u * blockDim.x);
     }
     if (INGEST) {
 #pragma unroll
-      for (int u = 0; u < UNROLL; ++u) st_vec_hint(cv + off + (uint64_t)u * blockDim.x, v[u], pol);
+      for (int u = 0; u < UNROLL; ++u) cv[off + (uint64_t)u * blockDim.x] = v[u];
     }
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
@@ -678,7 +656,7 @@ template <class T, int UNROLL>
 __global__ void __launch_bounds__(1024, 1)
     k_hist(const T *__restrict__ x, uint64_t n, const LutHeader<typename Traits<T>::K> *hdr,
            const uint32_t *__restrict__ lut_g, uint32_t *__restrict__ partials, uint32_t nb_max,
-           uint32_t keep_layers, const Ctrl *ctrl, T *__restrict__ copy_to) {
+           const Ctrl *ctrl, T *__restrict__ copy_to) {
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
@@ -690,14 +668,14 @@ __global__ void __launch_bounds__(1024, 1)
   __syncthreads();
   if (copy_to) {
     if (h.heavy)
-      hist_body<T, UNROLL, true, true>(x, n, hist, lut, h.base, h.shift, keep_layers, copy_to);
+      hist_body<T, UNROLL, true, true>(x, n, hist, lut, h.base, h.shift, copy_to);
     else
-      hist_body<T, UNROLL, false, true>(x, n, hist, lut, h.base, h.shift, keep_layers, copy_to);
+      hist_body<T, UNROLL, false, true>(x, n, hist, lut, h.base, h.shift, copy_to);
   } else {
     if (h.heavy)
-      hist_body<T, UNROLL, true, false>(x, n, hist, lut, h.base, h.shift, keep_layers, nullptr);
+      hist_body<T, UNROLL, true, false>(x, n, hist, lut, h.base, h.shift, nullptr);
     else
-      hist_body<T, UNROLL, false, false>(x, n, hist, lut, h.base, h.shift, keep_layers, nullptr);
+      hist_body<T, UNROLL, false, false>(x, n, hist, lut, h.base, h.shift, nullptr);
   }
   __syncthreads();
   uint32_t *row = partials + (uint64_t)blockIdx.x * nb_max;
@@ -994,14 +972,20 @@ __global__ void __launch_bounds__(1024, 1)
 // returned value decides whether it is stored: no divergent branch per
 // survivor.  In heavy mode lanes of a warp that hit the same bucket share one
 // atomic (match.any) and take consecutive positions.
+// In the non-heavy path the CTA's copy of the splitter table marks the slices
+// that hold no active bucket (shift field kSkipSlice): their elements take no
+// atomic at all.  Keys below `base` belong to bucket 0 (low_active).
+constexpr uint32_t kSkipSlice = 127u;
+
 template <class T, bool HEAVY>
 __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Traits<T>::K base,
                                             uint32_t shift, const uint32_t *lut, uint32_t *cursor,
                                             typename Traits<T>::K *__restrict__ surv,
-                                            uint64_t surv_cap, bool *overrun, uint64_t pol_keep) {
-  const uint32_t b = bucket_of(k, base, shift, lut);
+                                            uint64_t surv_cap, bool *overrun, bool low_active) {
+  using K = typename Traits<T>::K;
   uint32_t pos;
   if (HEAVY) {
+    const uint32_t b = bucket_of(k, base, shift, lut);
     const uint32_t peers = __match_any_sync(0xffffffffu, b);
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(peers) - 1;
@@ -1010,11 +994,18 @@ __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Tr
     p0 = __shfl_sync(peers, p0, leader);
     pos = p0 + __popc(peers & ((1u << lane) - 1u));
   } else {
+    const K d = k - base;
+    const K idx = d >> shift;
+    const uint32_t e = lut[idx < (K)kLutIdx ? (uint32_t)idx : kLutIdx];
+    const bool low = k < base;
+    const uint32_t rs = e & 127u;
+    if (!(low ? low_active : rs != kSkipSlice)) return;
+    const uint32_t b = low ? 0u : (uint32_t)((int32_t)e >> 7) + shr_clamp(d, rs);
     pos = atomicAdd(&cursor[b], 1u);
   }
   if (!(pos & kInactive)) {
     if (pos < surv_cap)
-      st_hint(surv + pos, k, pol_keep);
+      surv[pos] = k;
     else
       *overrun = true;
   }
@@ -1024,7 +1015,7 @@ template <class T, int UNROLL, bool HEAVY>
 __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n, uint32_t *cursor,
                                              const uint32_t *lut, typename Traits<T>::K base,
                                              uint32_t shift, typename Traits<T>::K *__restrict__ surv,
-                                             uint64_t surv_cap, bool *overrun) {
+                                             uint64_t surv_cap, bool *overrun, bool low_active) {
   using K = typename Traits<T>::K;
   using V = typename Traits<T>::Vec;
   constexpr int PV = Traits<T>::kPerVec;
@@ -1033,23 +1024,22 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
   const uint64_t tile_v = (uint64_t)blockDim.x * UNROLL;
   const uint64_t ntiles = sp.nvec / tile_v;
   // The same tiles as the histogram pass (tile = blockIdx.x + q * gridDim.x),
-  // visited last-to-first: the tail of the input is the part most likely to
-  // still be in L2.
+  // visited last-to-first: the tail of the input read by that pass is the part
+  // most likely to still be in L2.
   const uint64_t mine = ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  const uint64_t pol_first = l2_policy_evict_first(), pol_keep = l2_policy_evict_last();
   for (uint64_t q = mine; q-- > 0;) {
     const uint64_t tile = blockIdx.x + q * gridDim.x;
     const V *p = xv + tile * tile_v + threadIdx.x;
     V v[UNROLL];
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) v[u] = ldg_hint(p + (uint64_t)u * blockDim.x, pol_first);
+    for (int u = 0; u < UNROLL; ++u) v[u] = ldg_stream(p + (uint64_t)u * blockDim.x);
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
       K kk[PV];
       vec_keys<T>(v[u], kk);
 #pragma unroll
       for (int e = 0; e < PV; ++e)
-        compact_one<T, HEAVY>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun, pol_keep);
+        compact_one<T, HEAVY>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun, low_active);
     }
   }
   const uint32_t owner = (uint32_t)(ntiles % gridDim.x);
@@ -1060,14 +1050,14 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
       vec_keys<T>(vv, kk);
 #pragma unroll
       for (int e = 0; e < PV; ++e)
-        compact_one<T, false>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun, pol_keep);
+        compact_one<T, false>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun, low_active);
     }
     for (uint64_t e = threadIdx.x; e < sp.head; e += blockDim.x)
       compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun,
-                            pol_keep);
+                            low_active);
     for (uint64_t e = sp.tail0 + threadIdx.x; e < n; e += blockDim.x)
       compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun,
-                            pol_keep);
+                            low_active);
   }
 }
 
@@ -1079,20 +1069,27 @@ __global__ void __launch_bounds__(1024, 1)
               const uint32_t *__restrict__ lut_g, const uint32_t *__restrict__ seg_bucket,
               const uint64_t *__restrict__ seg_off, const uint32_t *__restrict__ seg_size,
               const uint32_t *__restrict__ prefix, const uint32_t *__restrict__ counts,
-              uint32_t nb_max,
+              const typename Traits<T>::K *__restrict__ seg_lo,
+              const typename Traits<T>::K *__restrict__ seg_hi, uint32_t nb_max,
               typename Traits<T>::K *__restrict__ surv, uint64_t surv_cap, Ctrl *ctrl) {
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
   uint32_t *cursor = (lut + kLutPadded);
-  __shared__ bool s_bad;
+  __shared__ bool s_bad, s_low;
   if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
   const LutHeader<K> h = *hdr;
   const uint32_t c = blockIdx.x;
-  for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
+  // non-heavy: every slice starts marked "skip"; slices of active buckets get
+  // their real entry back below
+  const uint32_t skip_mark = h.heavy ? 0u : kSkipSlice;
+  for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j] | skip_mark;
   const uint32_t num_slots = ctrl->num_slots;
   for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) cursor[b] = kInactive;
-  if (threadIdx.x == 0) s_bad = false;
+  if (threadIdx.x == 0) {
+    s_bad = false;
+    s_low = false;
+  }
   __syncthreads();
   // flat slots (seg_size 0: a single-key bucket) are answered without survivors
   for (uint32_t s = threadIdx.x; s < num_slots; s += blockDim.x) {
@@ -1100,13 +1097,27 @@ __global__ void __launch_bounds__(1024, 1)
     if (sz == 0) continue;
     const uint32_t b = seg_bucket[s];
     cursor[b] = (uint32_t)(seg_off[s] + prefix[(uint64_t)c * nb_max + b]);
+    if (b == 0) {
+      s_low = true;
+    } else if (skip_mark) {
+      // slices the bucket's keys [lo, hi] cover (more than one only for a run
+      // of empty slices sharing one bucket)
+      const K lo = seg_lo[s], hi = seg_hi[s];
+      const K j0 = (lo - h.base) >> h.shift, j1 = (hi - h.base) >> h.shift;
+      const uint32_t a = j0 < (K)kLutIdx ? (uint32_t)j0 : kLutIdx;
+      const uint32_t z = j1 < (K)kLutIdx ? (uint32_t)j1 : kLutIdx;
+      for (uint32_t j = a; j <= z; ++j) lut[j] = lut_g[j];
+    }
   }
   __syncthreads();
   bool overrun = false;
+  const bool low_active = s_low;
   if (h.heavy)
-    compact_body<T, UNROLL, true>(x, n, cursor, lut, h.base, h.shift, surv, surv_cap, &overrun);
+    compact_body<T, UNROLL, true>(x, n, cursor, lut, h.base, h.shift, surv, surv_cap, &overrun,
+                                  low_active);
   else
-    compact_body<T, UNROLL, false>(x, n, cursor, lut, h.base, h.shift, surv, surv_cap, &overrun);
+    compact_body<T, UNROLL, false>(x, n, cursor, lut, h.base, h.shift, surv, surv_cap, &overrun,
+                                   low_active);
   if (overrun) s_bad = true;
   __syncthreads();
   // every cursor must have reached the start of the next CTA's range (the
@@ -1266,12 +1277,12 @@ __global__ void __launch_bounds__(kFinThreads)
       // shared-memory index in range whatever the data
       {
         uint32_t i = tid;
-        for (; i + 3 * blockDim.x < size; i += 4 * blockDim.x) {
-          K kk[4];
+        for (; i + 7 * blockDim.x < size; i += 8 * blockDim.x) {
+          K kk[8];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) kk[q] = src[i + q * blockDim.x];
+          for (int q = 0; q < 8; ++q) kk[q] = src[i + q * blockDim.x];
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
+          for (int q = 0; q < 8; ++q)
             atomicAdd(&hist[min((uint32_t)((kk[q] - mn) >> sh), nbins - 1u)], 1u);
         }
         for (; i < size; i += blockDim.x)
@@ -1353,12 +1364,12 @@ __global__ void __launch_bounds__(kFinThreads)
         if (g != kNoSlot) B[g + atomicAdd(&cur[bb], 1u)] = k;
       };
       uint32_t i = tid;
-      for (; i + 3 * blockDim.x < size; i += 4 * blockDim.x) {
-        K kk[4];
+      for (; i + 7 * blockDim.x < size; i += 8 * blockDim.x) {
+        K kk[8];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) kk[q] = src[i + q * blockDim.x];
+        for (int q = 0; q < 8; ++q) kk[q] = src[i + q * blockDim.x];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) put(kk[q]);
+        for (int q = 0; q < 8; ++q) put(kk[q]);
       }
       for (; i < size; i += blockDim.x) put(src[i]);
     }

@@ -24,9 +24,6 @@ static inline int finish_smem_bytes() {
 
 static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-// input bytes the histogram pass leaves in L2 (evict-last) for compaction
-constexpr uint64_t kL2KeepBytes = 32ull << 20;
-
 struct Plan {
   uint64_t n = 0;
   uint32_t num_req = 0;
@@ -218,12 +215,9 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 4);
     set_smem_max<k_hist<InT, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
     PassTimer t(ctx, s, GGKS_PASS_HIST);
-    // tile layers (one tile per CTA) whose input stays in L2 for compaction
-    const uint64_t layer_bytes = (uint64_t)p.G * 1024 * UNROLL * 16;
-    const uint32_t keep_layers = (uint32_t)((kL2KeepBytes + layer_bytes - 1) / layer_bytes);
     // with a mapped host vector, this pass also writes the device copy d_in
     k_hist<InT, UNROLL><<<p.G, 1024, smem, s>>>(ingest ? ingest : d_in, n, hdr, lut, partials,
-                                                p.nb_max, keep_layers, ctrl,
+                                                p.nb_max, ctrl,
                                                 ingest ? const_cast<InT *>(d_in) : nullptr);
     ran[GGKS_PASS_HIST] = true;
   }
@@ -253,8 +247,8 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       set_smem_max<k_compact<InT, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
       PassTimer t(ctx, s, GGKS_PASS_COMPACT);
       k_compact<InT, UNROLL><<<p.G, 1024, smem, s>>>(d_in, n, hdr, lut, seg_bucket, seg_off, seg_size,
-                                                     partials, counts, p.nb_max, surv, surv_cap,
-                                                     ctrl);
+                                                     partials, counts, seg_lo, seg_hi, p.nb_max,
+                                                     surv, surv_cap, ctrl);
       ran[GGKS_PASS_COMPACT] = true;
     }
     {
