@@ -972,20 +972,14 @@ __global__ void __launch_bounds__(1024, 1)
 // returned value decides whether it is stored: no divergent branch per
 // survivor.  In heavy mode lanes of a warp that hit the same bucket share one
 // atomic (match.any) and take consecutive positions.
-// In the non-heavy path the CTA's copy of the splitter table marks the slices
-// that hold no active bucket (shift field kSkipSlice): their elements take no
-// atomic at all.  Keys below `base` belong to bucket 0 (low_active).
-constexpr uint32_t kSkipSlice = 127u;
-
 template <class T, bool HEAVY>
 __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Traits<T>::K base,
                                             uint32_t shift, const uint32_t *lut, uint32_t *cursor,
                                             typename Traits<T>::K *__restrict__ surv,
-                                            uint64_t surv_cap, bool *overrun, bool low_active) {
-  using K = typename Traits<T>::K;
+                                            uint64_t surv_cap, bool *overrun) {
+  const uint32_t b = bucket_of(k, base, shift, lut);
   uint32_t pos;
   if (HEAVY) {
-    const uint32_t b = bucket_of(k, base, shift, lut);
     const uint32_t peers = __match_any_sync(0xffffffffu, b);
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(peers) - 1;
@@ -994,13 +988,6 @@ __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Tr
     p0 = __shfl_sync(peers, p0, leader);
     pos = p0 + __popc(peers & ((1u << lane) - 1u));
   } else {
-    const K d = k - base;
-    const K idx = d >> shift;
-    const uint32_t e = lut[idx < (K)kLutIdx ? (uint32_t)idx : kLutIdx];
-    const bool low = k < base;
-    const uint32_t rs = e & 127u;
-    if (!(low ? low_active : rs != kSkipSlice)) return;
-    const uint32_t b = low ? 0u : (uint32_t)((int32_t)e >> 7) + shr_clamp(d, rs);
     pos = atomicAdd(&cursor[b], 1u);
   }
   if (!(pos & kInactive)) {
@@ -1015,7 +1002,7 @@ template <class T, int UNROLL, bool HEAVY>
 __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n, uint32_t *cursor,
                                              const uint32_t *lut, typename Traits<T>::K base,
                                              uint32_t shift, typename Traits<T>::K *__restrict__ surv,
-                                             uint64_t surv_cap, bool *overrun, bool low_active) {
+                                             uint64_t surv_cap, bool *overrun) {
   using K = typename Traits<T>::K;
   using V = typename Traits<T>::Vec;
   constexpr int PV = Traits<T>::kPerVec;
@@ -1039,7 +1026,7 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
       vec_keys<T>(v[u], kk);
 #pragma unroll
       for (int e = 0; e < PV; ++e)
-        compact_one<T, HEAVY>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun, low_active);
+        compact_one<T, HEAVY>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun);
     }
   }
   const uint32_t owner = (uint32_t)(ntiles % gridDim.x);
@@ -1050,14 +1037,12 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
       vec_keys<T>(vv, kk);
 #pragma unroll
       for (int e = 0; e < PV; ++e)
-        compact_one<T, false>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun, low_active);
+        compact_one<T, false>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun);
     }
     for (uint64_t e = threadIdx.x; e < sp.head; e += blockDim.x)
-      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun,
-                            low_active);
+      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun);
     for (uint64_t e = sp.tail0 + threadIdx.x; e < n; e += blockDim.x)
-      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun,
-                            low_active);
+      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun);
   }
 }
 
@@ -1069,27 +1054,20 @@ __global__ void __launch_bounds__(1024, 1)
               const uint32_t *__restrict__ lut_g, const uint32_t *__restrict__ seg_bucket,
               const uint64_t *__restrict__ seg_off, const uint32_t *__restrict__ seg_size,
               const uint32_t *__restrict__ prefix, const uint32_t *__restrict__ counts,
-              const typename Traits<T>::K *__restrict__ seg_lo,
-              const typename Traits<T>::K *__restrict__ seg_hi, uint32_t nb_max,
+              uint32_t nb_max,
               typename Traits<T>::K *__restrict__ surv, uint64_t surv_cap, Ctrl *ctrl) {
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
   uint32_t *cursor = (lut + kLutPadded);
-  __shared__ bool s_bad, s_low;
+  __shared__ bool s_bad;
   if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
   const LutHeader<K> h = *hdr;
   const uint32_t c = blockIdx.x;
-  // non-heavy: every slice starts marked "skip"; slices of active buckets get
-  // their real entry back below
-  const uint32_t skip_mark = h.heavy ? 0u : kSkipSlice;
-  for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j] | skip_mark;
+  for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
   const uint32_t num_slots = ctrl->num_slots;
   for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) cursor[b] = kInactive;
-  if (threadIdx.x == 0) {
-    s_bad = false;
-    s_low = false;
-  }
+  if (threadIdx.x == 0) s_bad = false;
   __syncthreads();
   // flat slots (seg_size 0: a single-key bucket) are answered without survivors
   for (uint32_t s = threadIdx.x; s < num_slots; s += blockDim.x) {
@@ -1097,27 +1075,13 @@ __global__ void __launch_bounds__(1024, 1)
     if (sz == 0) continue;
     const uint32_t b = seg_bucket[s];
     cursor[b] = (uint32_t)(seg_off[s] + prefix[(uint64_t)c * nb_max + b]);
-    if (b == 0) {
-      s_low = true;
-    } else if (skip_mark) {
-      // slices the bucket's keys [lo, hi] cover (more than one only for a run
-      // of empty slices sharing one bucket)
-      const K lo = seg_lo[s], hi = seg_hi[s];
-      const K j0 = (lo - h.base) >> h.shift, j1 = (hi - h.base) >> h.shift;
-      const uint32_t a = j0 < (K)kLutIdx ? (uint32_t)j0 : kLutIdx;
-      const uint32_t z = j1 < (K)kLutIdx ? (uint32_t)j1 : kLutIdx;
-      for (uint32_t j = a; j <= z; ++j) lut[j] = lut_g[j];
-    }
   }
   __syncthreads();
   bool overrun = false;
-  const bool low_active = s_low;
   if (h.heavy)
-    compact_body<T, UNROLL, true>(x, n, cursor, lut, h.base, h.shift, surv, surv_cap, &overrun,
-                                  low_active);
+    compact_body<T, UNROLL, true>(x, n, cursor, lut, h.base, h.shift, surv, surv_cap, &overrun);
   else
-    compact_body<T, UNROLL, false>(x, n, cursor, lut, h.base, h.shift, surv, surv_cap, &overrun,
-                                   low_active);
+    compact_body<T, UNROLL, false>(x, n, cursor, lut, h.base, h.shift, surv, surv_cap, &overrun);
   if (overrun) s_bad = true;
   __syncthreads();
   // every cursor must have reached the start of the next CTA's range (the

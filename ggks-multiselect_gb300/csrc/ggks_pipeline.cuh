@@ -247,8 +247,8 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       set_smem_max<k_compact<InT, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
       PassTimer t(ctx, s, GGKS_PASS_COMPACT);
       k_compact<InT, UNROLL><<<p.G, 1024, smem, s>>>(d_in, n, hdr, lut, seg_bucket, seg_off, seg_size,
-                                                     partials, counts, seg_lo, seg_hi, p.nb_max,
-                                                     surv, surv_cap, ctrl);
+                                                     partials, counts, p.nb_max, surv, surv_cap,
+                                                     ctrl);
       ran[GGKS_PASS_COMPACT] = true;
     }
     {
