@@ -224,6 +224,20 @@ __device__ __forceinline__ ulonglong2 ldg_stream<ulonglong2>(const ulonglong2 *p
   return v;
 }
 
+// predicated global stores (no branch around them)
+__device__ __forceinline__ void st_global_if(uint32_t *p, uint32_t v, bool pred) {
+  asm volatile(
+      "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %2, 0;\n\t@q st.global.b32 [%0], %1;\n\t}" ::"l"(p),
+      "r"(v), "r"((uint32_t)pred)
+      : "memory");
+}
+__device__ __forceinline__ void st_global_if(uint64_t *p, uint64_t v, bool pred) {
+  asm volatile(
+      "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %2, 0;\n\t@q st.global.b64 [%0], %1;\n\t}" ::"l"(p),
+      "l"(v), "r"((uint32_t)pred)
+      : "memory");
+}
+
 // right shift that yields 0 for shift >= width
 __device__ __forceinline__ uint32_t shr_clamp(uint32_t d, uint32_t s) {
   return __funnelshift_r(d, 0u, s);  // shf.r.clamp: shift clamped to 32
@@ -990,12 +1004,11 @@ __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Tr
   } else {
     pos = atomicAdd(&cursor[b], 1u);
   }
-  if (!(pos & kInactive)) {
-    if (pos < surv_cap)
-      surv[pos] = k;
-    else
-      *overrun = true;
-  }
+  // store without a branch: a predicated st.global
+  const bool active = !(pos & kInactive);
+  const bool fits = pos < surv_cap;
+  st_global_if(surv + pos, k, active && fits);
+  *overrun |= active && !fits;
 }
 
 template <class T, int UNROLL, bool HEAVY>
@@ -1104,14 +1117,14 @@ __global__ void __launch_bounds__(1024, 1)
 // ---------------------------------------------------------------------------
 // One CTA per segment (persistent over segments).  The segment's keys are
 // read from the survivor buffer (L2-resident) three times: min/max, a
-// 2048-bin histogram of the top 11 bits of (key - min), and a gather of only
+// histogram of up to 1024 bins over the top bits of (key - min), and a gather of only
 // the bins that hold requested ranks into shared memory.  Each gathered bin is
 // sorted (a warp bitonic network for bins of <= 32 keys, a CTA bitonic sort for
 // larger ones) and every request reads its rank.  Segments whose needed bins
 // exceed the shared-memory buffer are listed for a recursive re-selection.
-constexpr int kFinBins = 2048;
-constexpr int kFinBinBits = 11;
-constexpr int kFinThreads = 512;
+constexpr int kFinBins = 1024;
+constexpr int kFinBinBits = 10;
+constexpr int kFinThreads = 256;
 
 template <class K>
 __device__ __forceinline__ K warp_bitonic32(K v) {
@@ -1176,13 +1189,14 @@ __global__ void __launch_bounds__(kFinThreads)
   uint32_t *cur = gofs + kFinBins;
   uint32_t *small = cur + kFinBins;   // needed bins of 2..32 keys
   K *B = reinterpret_cast<K *>(small + kFinBins);  // gathered keys of the needed bins
-  K *T = B + bcap;                                 // scratch for sorting a large bin
+  K *T = B + bcap;                                 // scratch for sorting a large bin (tcap keys)
   constexpr int kMaxBig = 64;
   __shared__ K redk[33];
   __shared__ uint32_t red32[33];
   __shared__ uint32_t big[kMaxBig];
-  __shared__ uint32_t s_nbig, s_nsmall;
+  __shared__ uint32_t s_nbig, s_nsmall, s_maxneed;
   constexpr uint32_t PER = kFinBins / kFinThreads;  // bins per thread (at most)
+  const uint32_t tcap = bcap / 2;                   // scratch T holds one bin of <= tcap keys
 
   if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
   const uint32_t num_slots = ctrl->num_slots;
@@ -1235,6 +1249,7 @@ __global__ void __launch_bounds__(kFinThreads)
       if (tid == 0) {
         s_nbig = 0;
         s_nsmall = 0;
+        s_maxneed = 0;
       }
       __syncthreads();
       // keys lie in [mn, mx], so the digit is < nbins; the clamp keeps a
@@ -1292,6 +1307,7 @@ __global__ void __launch_bounds__(kFinThreads)
           if (bb < nbins) {
             const bool need = gofs[bb] != 0u;
             gofs[bb] = need ? run : kNoSlot;
+            if (need) atomicMax(&s_maxneed, cc[q]);
             if (need && cc[q] > 32) {
               const uint32_t at = atomicAdd(&s_nbig, 1u);
               if (at < kMaxBig) big[at] = bb;
@@ -1303,7 +1319,7 @@ __global__ void __launch_bounds__(kFinThreads)
         }
       }
       __syncthreads();
-      fits = V <= bcap;
+      fits = V <= bcap && s_maxneed <= tcap;
     }
     if (flat) {  // one distinct key: every rank is that key
       for (uint32_t j = tid; j < m; j += blockDim.x) out[rq[j].out] = Traits<OutT>::value(mn);

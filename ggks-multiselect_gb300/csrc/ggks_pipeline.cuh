@@ -14,12 +14,14 @@ namespace ggks {
 // equal scratch area for sorting a large bin)
 template <class T>
 static inline uint32_t cap_keys_for() {
-  return sizeof(typename Traits<T>::K) == 4 ? 8192u : 4096u;
+  return sizeof(typename Traits<T>::K) == 4 ? 4096u : 2048u;
 }
+// bins (5 arrays), the gather buffer, and a scratch half its size for sorting
+// one large bin: about 44 KB, so that several finishing CTAs share an SM
 template <class T>
 static inline int finish_smem_bytes() {
   using K = typename Traits<T>::K;
-  return (int)(5 * kFinBins * sizeof(uint32_t) + 2 * (size_t)cap_keys_for<T>() * sizeof(K));
+  return (int)(5 * kFinBins * sizeof(uint32_t) + (size_t)cap_keys_for<T>() * sizeof(K) * 3 / 2);
 }
 
 static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -58,7 +60,7 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   p.scan_tiles = (p.nb_max + kScanTile - 1) / kScanTile;
   p.cap_keys = cap_keys_for<InT>();
   uint32_t slots_bound = num_req < p.nb_max ? num_req : p.nb_max;
-  uint32_t fg = 2u * (uint32_t)ctx.sm_count;
+  uint32_t fg = 5u * (uint32_t)ctx.sm_count;
   p.fin_grid = slots_bound < fg ? (slots_bound ? slots_bound : 1) : fg;
   uint64_t cap = n / 8;
   p.surv_cap = cap < (1u << 20) ? (1u << 20) : cap;
