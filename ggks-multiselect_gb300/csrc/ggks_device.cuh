@@ -68,6 +68,7 @@ enum : uint32_t {
   ST_DEFERRED = 2u,  // some segments exceed shared memory: host re-selects them
   ST_TIMEOUT = 4u,   // a bounded wait gave up
   ST_INTERNAL = 8u,  // a consistency check failed (counts do not add up to n)
+  ST_BAD_K = 16u,    // a k outside [1, n] (device-side k lists)
 };
 constexpr uint32_t ST_FATAL = ST_TIMEOUT | ST_INTERNAL;
 
@@ -1390,7 +1391,5 @@ __global__ void __launch_bounds__(kFinThreads)
   }
 }
 
-// top-k request builder: rank n-1-i goes to output i (descending)
-__global__ void k_topk_reqs(Req *reqs, uint64_t n, uint32_t K);
 
 }  // namespace ggks

@@ -65,7 +65,7 @@ EXPORTS = [
     "ggks_topk_host_f32", "ggks_topk_host_f64", "ggks_topk_host_u32",
     "ggks_context_create", "ggks_context_destroy", "ggks_context_get_stats",
     "ggks_context_reset_stats", "ggks_context_set_profiling", "ggks_status_string",
-    "ggks_version",
+    "ggks_version", "ggks_multiselect_noalloc_f32",
 ]
 
 _lib = None
@@ -88,6 +88,8 @@ def lib():
             f = getattr(L, nm + sfx)
             f.argtypes = [P, U64, U32, P, ctypes.POINTER(Opts)]
             f.restype = ctypes.c_int
+    L.ggks_multiselect_noalloc_f32.argtypes = [P, U64, P, U32, P, P]
+    L.ggks_multiselect_noalloc_f32.restype = ctypes.c_int
     L.ggks_context_create.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
     L.ggks_context_destroy.argtypes = [P]
     L.ggks_context_get_stats.argtypes = [P, ctypes.POINTER(Stats)]
@@ -210,6 +212,14 @@ def topk_ptr(d_ptr, n, dtype, K, ctx=None, stream=None, out=None, out_device_ptr
         ctypes.c_void_p(d_ptr), int(n), int(K), ctypes.c_void_p(optr), ctypes.byref(o))
     _check(st, "topk")
     return out
+
+
+def multiselect_noalloc_f32(d_ptr, n, d_k_ptr, num_k, d_out_ptr, stream=None):
+    """ggks_multiselect_noalloc_f32: every pointer is device memory; returns
+    the ggks status (no exception), like the C call."""
+    return lib().ggks_multiselect_noalloc_f32(ctypes.c_void_p(d_ptr), int(n),
+                                              ctypes.c_void_p(d_k_ptr), int(num_k),
+                                              ctypes.c_void_p(d_out_ptr), stream)
 
 
 def multiselect_host(h_vec, k, ctx=None, stream=None, out=None):

@@ -111,6 +111,32 @@ int ggks_topk_host_u32(const uint32_t *h_vec, uint64_t n, uint32_t K, uint32_t *
                        const ggks_opts *opts);
 
 /* ------------------------------------------------------------------------ */
+/* Multiselect without allocation                                            */
+/* ------------------------------------------------------------------------ */
+
+/* No counterpart in the reference.  A float32 multiselect for callers that
+ * cannot allocate memory when they call it: code running while a CUDA graph is
+ * captured, engines whose device memory belongs to another allocator, and
+ * latency-critical paths that may not block on an allocator.  It calls no
+ * cudaMalloc, cudaFree, cudaHostAlloc or other allocating routine; its scratch
+ * is one fixed device array (about 11 MB) that every GPU loading this library
+ * holds until the process exits.
+ *   d_vec: device vector of n floats; d_k: device array of num_k k's (k-th
+ *   largest, 1-based); d_out: device array of num_k results in k order;
+ *   stream: a cudaStream_t (NULL: the legacy default stream).  The call
+ *   returns when the results are in d_out.
+ * Limits: 1 <= n <= GGKS_NOALLOC_MAX_N and 1 <= num_k <= GGKS_NOALLOC_MAX_K,
+ * else GGKS_INVALID_ARG (also for a k outside [1, n]); an input whose buckets
+ * would need a recursive re-selection (heavy, nearly equal duplicates) returns
+ * GGKS_UNSUPPORTED.  The first call on a device looks up the scratch's device
+ * address; make it before capturing a stream.  All calls share the scratch:
+ * calls that overlap on the GPU race and must be serialised by the caller. */
+#define GGKS_NOALLOC_MAX_N (1ull << 21)
+#define GGKS_NOALLOC_MAX_K 2048u
+int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, const uint32_t *d_k,
+                                 uint32_t num_k, float *d_out, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Contexts, statistics, utilities                                           */
 /* ------------------------------------------------------------------------ */
 
