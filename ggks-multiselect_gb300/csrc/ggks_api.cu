@@ -1,8 +1,10 @@
 // ggks_api.cu -- contexts, workspace management and the extern "C" entry
 // points declared in include/ggks.h.
+#include <chrono>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "ggks_internal.h"
 
@@ -43,6 +45,10 @@ Context::~Context() {
   if (surv) cudaFree(surv);
   if (dvec) cudaFree(dvec);
   if (pin) cudaFreeHost(pin);
+  if (barena) cudaFree(barena);
+  if (bpin) cudaFreeHost(bpin);
+  if (bev0) cudaEventDestroy(bev0);
+  if (bev1) cudaEventDestroy(bev1);
   if (events_ready) {
     for (int i = 0; i < GGKS_NUM_PASSES; ++i) {
       cudaEventDestroy(ev0[i]);
@@ -96,6 +102,33 @@ cudaError_t ensure_arena(Context &ctx, size_t bytes) {
   e = grow(&p, &ctx.arena_bytes, bytes, true);
   ctx.arena = static_cast<char *>(p);
   return e;
+}
+
+cudaError_t ensure_buffer(Context &ctx, char **p, size_t *have, size_t bytes) {
+  if (bytes <= *have && *p) return cudaSuccess;
+  cudaError_t e = cudaStreamSynchronize(ctx.stream);
+  if (e != cudaSuccess) return e;
+  void *v = *p;
+  e = grow(&v, have, bytes, false);
+  *p = static_cast<char *>(v);
+  return e;
+}
+
+cudaError_t ensure_pinned(Context &ctx, char **p, size_t *have, size_t bytes) {
+  (void)ctx;
+  if (bytes <= *have && *p) return cudaSuccess;
+  if (*p) {
+    cudaFreeHost(*p);
+    *p = nullptr;
+    *have = 0;
+  }
+  size_t want = bytes + bytes / 4 + 4096;
+  void *v = nullptr;
+  cudaError_t e = cudaHostAlloc(&v, want, cudaHostAllocDefault);
+  if (e != cudaSuccess) return e;
+  *p = static_cast<char *>(v);
+  *have = want;
+  return cudaSuccess;
 }
 
 cudaError_t ensure_surv(Context &ctx, size_t bytes) {
@@ -295,6 +328,107 @@ static int api_topk(const T *vec, uint64_t n, uint32_t K, T *out, const ggks_opt
   return st;
 }
 
+// ---------------------------------------------------------------------------
+// batched selection
+// ---------------------------------------------------------------------------
+// Autotuner candidates: bucket divisor (elements per bucket, roughly) x tile
+// size (elements per work item).  Results do not depend on the choice.
+static const BatchTune kTuneCandidates[] = {
+    {256, 1u << 16},  {256, 1u << 18},  {256, 1u << 20},  {1024, 1u << 16}, {1024, 1u << 18},
+    {1024, 1u << 20}, {4096, 1u << 16}, {4096, 1u << 18}, {4096, 1u << 20},
+};
+
+static inline uint32_t log2_round(uint64_t v) {
+  uint32_t r = 0;
+  while (r < 63 && (1ull << (r + 1)) <= v + (v >> 1)) ++r;
+  return r;
+}
+
+template <class T>
+static int api_batch(const T *const *vecs, const uint64_t *n, uint32_t P, const uint32_t *k_off,
+                     const uint32_t *h_k, const uint32_t *K, T *out, const ggks_opts *opts) {
+  if (!vecs || !n || P == 0 || !out) return GGKS_INVALID_ARG;
+  std::vector<uint32_t> off_topk;
+  if (K) {
+    // top-k: output offsets are the prefix sums of K
+    off_topk.resize((size_t)P + 1);
+    uint64_t run = 0;
+    for (uint32_t p = 0; p < P; ++p) {
+      off_topk[p] = (uint32_t)run;
+      run += K[p];
+      if (run > 0xFFFFFFFFull) return GGKS_INVALID_ARG;
+    }
+    off_topk[P] = (uint32_t)run;
+    k_off = off_topk.data();
+  } else if (!k_off || k_off[0] != 0) {
+    return GGKS_INVALID_ARG;
+  }
+  const uint32_t R = k_off[P];
+  if (R > 0 && !K && !h_k) return GGKS_INVALID_ARG;
+  uint64_t bytes = 0, elems = 0;
+  uint32_t active = 0;
+  for (uint32_t p = 0; p < P; ++p) {
+    if (k_off[p + 1] < k_off[p]) return GGKS_INVALID_ARG;
+    const uint32_t nr = k_off[p + 1] - k_off[p];
+    if (nr == 0) continue;
+    if (!vecs[p] || n[p] == 0 || n[p] > GGKS_MAX_N) return GGKS_INVALID_ARG;
+    if ((uintptr_t)vecs[p] % sizeof(T) != 0) return GGKS_INVALID_ARG;
+    if (K) {
+      if ((uint64_t)K[p] > n[p]) return GGKS_INVALID_ARG;
+    } else {
+      for (uint32_t j = k_off[p]; j < k_off[p + 1]; ++j)
+        if (h_k[j] < 1 || (uint64_t)h_k[j] > n[p]) return GGKS_INVALID_ARG;
+    }
+    bytes += n[p] * sizeof(T);
+    elems += n[p];
+    active++;
+  }
+  if (R == 0) return GGKS_OK;
+  int st = GGKS_OK;
+  Context *ctx = resolve(opts, &st);
+  if (!ctx) return st;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  DeviceGuard dg(ctx->device);
+  cudaStream_t s = (opts && opts->stream) ? static_cast<cudaStream_t>(opts->stream) : ctx->stream;
+  const bool out_dev = opts && (opts->flags & GGKS_FLAG_OUT_DEVICE);
+  BatchInput in;
+  in.vecs = reinterpret_cast<const void *const *>(vecs);
+  in.n = n;
+  in.num_problems = P;
+  in.k_off = k_off;
+  in.k = K ? nullptr : h_k;
+  // batch shape: element size, total elements, problems, outputs per problem
+  const uint64_t key = ((uint64_t)sizeof(T) << 24) | ((uint64_t)log2_round(elems) << 16) |
+                       ((uint64_t)log2_round(active) << 8) | log2_round(R / active);
+  auto it = ctx->tuned.find(key);
+  BatchTune tune = it != ctx->tuned.end() ? it->second : BatchTune{};
+  if (ctx->pinned_tune.div != 0) {
+    tune = ctx->pinned_tune;
+  } else if (it == ctx->tuned.end() && opts && (opts->flags & GGKS_FLAG_AUTOTUNE)) {
+    // whole calls are timed: planning, launches, re-runs and recursion
+    double best = -1.0;
+    for (const BatchTune &c : kTuneCandidates) {
+      const auto t0 = std::chrono::steady_clock::now();
+      st = select_batch<T>(*ctx, in, out_dev ? out : nullptr, nullptr, s, c, nullptr);
+      const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      if (st != GGKS_OK) return st;
+      if (best < 0.0 || dt < best) {
+        best = dt;
+        tune = c;
+      }
+    }
+    ctx->tuned[key] = tune;
+  }
+  float ms = 0.f;
+  st = select_batch<T>(*ctx, in, out_dev ? out : nullptr, out_dev ? nullptr : out, s, tune, &ms);
+  if (st == GGKS_OK) {
+    ctx->last_tune = tune;
+    ctx->stats.calls++;
+    ctx->stats.bytes_in += bytes;
+  }
+  return st;
+}
+
 }  // namespace ggks
 
 using namespace ggks;
@@ -347,6 +481,61 @@ int ggks_topk_host_f64(const double *h_vec, uint64_t n, uint32_t K, double *h_ou
 int ggks_topk_host_u32(const uint32_t *h_vec, uint64_t n, uint32_t K, uint32_t *h_out,
                        const ggks_opts *opts) {
   return api_topk<uint32_t>(h_vec, n, K, h_out, opts, true);
+}
+
+int ggks_multiselect_batch_f32(const float *const *d_vecs, const uint64_t *n, uint32_t num_problems,
+                               const uint32_t *k_offsets, const uint32_t *h_k, float *out,
+                               const ggks_opts *opts) {
+  return api_batch<float>(d_vecs, n, num_problems, k_offsets, h_k, nullptr, out, opts);
+}
+int ggks_multiselect_batch_f64(const double *const *d_vecs, const uint64_t *n,
+                               uint32_t num_problems, const uint32_t *k_offsets,
+                               const uint32_t *h_k, double *out, const ggks_opts *opts) {
+  return api_batch<double>(d_vecs, n, num_problems, k_offsets, h_k, nullptr, out, opts);
+}
+int ggks_multiselect_batch_u32(const uint32_t *const *d_vecs, const uint64_t *n,
+                               uint32_t num_problems, const uint32_t *k_offsets,
+                               const uint32_t *h_k, uint32_t *out, const ggks_opts *opts) {
+  return api_batch<uint32_t>(d_vecs, n, num_problems, k_offsets, h_k, nullptr, out, opts);
+}
+int ggks_topk_batch_f32(const float *const *d_vecs, const uint64_t *n, uint32_t num_problems,
+                        const uint32_t *K, float *out, const ggks_opts *opts) {
+  if (!K) return GGKS_INVALID_ARG;
+  return api_batch<float>(d_vecs, n, num_problems, nullptr, nullptr, K, out, opts);
+}
+int ggks_topk_batch_f64(const double *const *d_vecs, const uint64_t *n, uint32_t num_problems,
+                        const uint32_t *K, double *out, const ggks_opts *opts) {
+  if (!K) return GGKS_INVALID_ARG;
+  return api_batch<double>(d_vecs, n, num_problems, nullptr, nullptr, K, out, opts);
+}
+int ggks_topk_batch_u32(const uint32_t *const *d_vecs, const uint64_t *n, uint32_t num_problems,
+                        const uint32_t *K, uint32_t *out, const ggks_opts *opts) {
+  if (!K) return GGKS_INVALID_ARG;
+  return api_batch<uint32_t>(d_vecs, n, num_problems, nullptr, nullptr, K, out, opts);
+}
+
+static Context *ctx_or_default(ggks_context *ctx, int *st);
+
+int ggks_batch_set_tuning(ggks_context *ctx, uint32_t div, uint32_t tile) {
+  if (div != 0 && (div < 16 || div > (1u << 24) || tile < 64)) return GGKS_INVALID_ARG;
+  int st = GGKS_OK;
+  Context *c = ctx_or_default(ctx, &st);
+  if (!c) return st;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->pinned_tune.div = div;
+  c->pinned_tune.tile = tile;
+  return GGKS_OK;
+}
+
+int ggks_batch_last_tuning(ggks_context *ctx, uint32_t *div, uint32_t *tile) {
+  if (!div || !tile) return GGKS_INVALID_ARG;
+  int st = GGKS_OK;
+  Context *c = ctx_or_default(ctx, &st);
+  if (!c) return st;
+  std::lock_guard<std::mutex> lk(c->mu);
+  *div = c->last_tune.div;
+  *tile = c->last_tune.tile;
+  return GGKS_OK;
 }
 
 int ggks_context_create(int device, ggks_context **out) {

@@ -1,0 +1,631 @@
+// ggks_batch.cuh -- batched multiselect: thousands of independent vectors of
+// uneven lengths, each with its own k list, selected in one persistent
+// cooperative launch driven by work queues.
+//
+// The reference selects one vector per call (bucketMultiselectWrapper,
+// bucketMultiselect.cu:837-871) and picks its algorithm per size offline
+// (analyzeMultiselect.cu:209-274); here every problem of a batch runs the same
+// bucket pipeline as the single-vector path, phase by phase across the whole
+// batch, inside one kernel:
+//
+//   1 table    queue over problems: up to kBMaxS keys sampled into shared
+//              memory, the problem's splitter table built by build_lut_cta
+//              (the single-vector builder) with 2^nsl_bits slices.
+//   2 hist     queue over (problem, tile) items: a tile is a contiguous range
+//              of one problem; its shared-memory histogram becomes one row of
+//              counts (rows of a problem's tiles are consecutive).
+//   3 plan     queue over problems: the problem's rows become their exclusive
+//              prefix over its tiles (column sums = bucket counts), a block
+//              scan gives the bucket prefix, requested ranks map to buckets
+//              and slots, the slots' survivors get a range of the shared
+//              survivor buffer from a bump allocator, request lists per slot.
+//   4 compact  queue over the same (problem, tile) items: cursors start at the
+//              tile's prefix row, one shared atomic per element.
+//   5 finish   queue over the large slots: finish_slot (the single-vector
+//              finisher), a whole CTA each; then a queue over the small slots
+//              (at most warp_cap keys, the common case), one warp each.
+//
+// A grid-wide barrier with a bounded wait separates the phases; the grid is
+// launched cooperatively (all CTAs co-resident).  No CTA leaves early: a CTA
+// that sees an error status skips the remaining work but still passes every
+// barrier.  Data written by other CTAs in an earlier phase is read with
+// ld.global.cg (L2), never through a possibly stale L1 line.
+#pragma once
+
+#include "ggks_device.cuh"
+
+namespace ggks {
+
+constexpr int kBThreads = 512;
+constexpr int kBSpt = (int)kLutIdx / kBThreads;  // slices per thread in the table build
+constexpr uint32_t kBMaxNb = 8192;               // bucket budget of one problem
+constexpr uint32_t kBMaxS = 8192;                // samples of one problem (shared memory)
+constexpr int kBPhases = 5;
+constexpr uint32_t kBWarpBytes = 2048;  // shared memory of one warp-finisher buffer
+
+// segments of at most this many keys are finished by one warp
+template <class K>
+__host__ __device__ constexpr uint32_t warp_cap() {
+  return kBWarpBytes / (uint32_t)sizeof(K);
+}
+
+// one problem (host-written, read-only on the device)
+struct BProb {
+  const void *x;
+  uint64_t n;
+  uint64_t lut_off;  // u32 index of the splitter table (nsl + 1 entries, 16-byte aligned)
+  uint64_t cnt_off;  // u32 index of the bucket counts (nb_max entries)
+  uint64_t row0;     // u32 index of the first tile's row (tile r: row0 + r * nb_max)
+  uint32_t req_off, num_req;  // requests [req_off, req_off + num_req); slots use the same range
+  uint32_t nb_max, nsl_bits;
+  uint32_t S, ntiles;
+};
+
+// splitter-table header and plan results of one problem (device-written)
+struct BHdr {
+  uint64_t base;
+  uint64_t surv_off;
+  uint32_t shift, nb, heavy, num_slots;
+};
+
+// one (problem, tile) work item (host-written)
+struct BTile {
+  uint64_t begin, end;  // elements [begin, end) of problem prob
+  uint32_t prob, rank;  // rank of the tile among its problem's tiles
+};
+
+struct BCtrl {
+  uint32_t status;
+  uint32_t queue[kBPhases];  // work queue counters of the phases
+  uint32_t bar_count, bar_gen;
+  uint32_t deferred_count;
+  uint32_t n_big, n_small;  // slots finished by a whole CTA / by one warp
+  uint32_t small_pop;       // warp queue of the small slots
+  uint32_t pad;
+  uint64_t surv_top;    // survivor bump allocator
+  uint64_t cap_needed;  // survivors wanted when they did not fit
+  uint64_t t_ns[kBPhases + 1];  // %globaltimer at the start and after each phase (CTA 0)
+};
+
+struct BArgs {
+  const BProb *probs;
+  BHdr *hdrs;
+  const BTile *tiles;
+  uint32_t num_probs, num_tiles;
+  uint32_t num_req;  // requests of all problems (= slot index space)
+  uint32_t bcap;     // finisher gather capacity (keys)
+  uint64_t surv_cap;
+  uint32_t *luts;
+  uint32_t *rows;
+  uint32_t *counts;
+  const Req *reqs;  // rank within the problem, output position in out[]
+  uint32_t *req_bucket, *req_local;
+  uint32_t *seg_bucket, *seg_size, *kstart, *kcnt, *kcur;
+  uint64_t *seg_off;
+  void *seg_lo, *seg_hi;  // key arrays
+  Req *klist;
+  uint32_t *big_list, *small_list;  // slot indices by finisher kind
+  void *surv;             // key array
+  uint32_t *deferred;
+  void *out;              // output values
+  BCtrl *ctrl;
+};
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier of a co-resident grid (generation counter).  A wait that
+// runs out sets ST_TIMEOUT and goes on, so every wait ends.  Returns the
+// status seen after the barrier (same value in every thread of the CTA).
+__device__ __forceinline__ uint32_t grid_barrier(BCtrl *c, uint32_t *s_status, int phase) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t g0 = ld_acquire_u32(&c->bar_gen);
+    __threadfence();
+    if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1) {
+      atomicExch(&c->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&c->bar_gen, 1u);
+    } else {
+      int iters = 0;
+      while (ld_acquire_u32(&c->bar_gen) == g0) {
+        if (++iters > kSpinLimit) {
+          atomicOr(&c->status, ST_TIMEOUT);
+          break;
+        }
+        __nanosleep(100);
+      }
+    }
+    __threadfence();
+    if (blockIdx.x == 0) c->t_ns[phase] = global_ns();
+    *s_status = ld_acquire_u32(&c->status);
+  }
+  __syncthreads();
+  return *s_status;
+}
+
+// next item of a work queue, shared with the whole CTA
+__device__ __forceinline__ uint32_t queue_pop(uint32_t *q, uint32_t *s_item) {
+  __syncthreads();
+  if (threadIdx.x == 0) *s_item = atomicAdd(q, 1u);
+  __syncthreads();
+  return *s_item;
+}
+
+__device__ __forceinline__ uint32_t ldcg_u(const uint32_t *p) { return __ldcg(p); }
+__device__ __forceinline__ uint64_t ldcg_u(const uint64_t *p) {
+  return __ldcg(reinterpret_cast<const unsigned long long *>(p));
+}
+
+__device__ __forceinline__ BHdr load_hdr(const BHdr *h) {
+  BHdr r;
+  r.base = ldcg_u(&h->base);
+  r.surv_off = ldcg_u(&h->surv_off);
+  const uint4 w = __ldcg(reinterpret_cast<const uint4 *>(&h->shift));
+  r.shift = w.x;
+  r.nb = w.y;
+  r.heavy = w.z;
+  r.num_slots = w.w;
+  return r;
+}
+
+// One warp finishes a segment of at most warp_cap<K>() keys: the keys are
+// sorted in the warp's shared-memory buffer (32-key runs in registers, then
+// bitonic merges whose first step compares mirrored positions, so every run
+// stays ascending) and each request reads its rank.  size 0: a flat slot
+// whose single key is lo.
+template <class K, class OutT>
+__device__ __forceinline__ void finish_warp(const K *__restrict__ src, uint32_t size, K lo,
+                                            const Req *__restrict__ rq, uint32_t m, K *buf,
+                                            OutT *__restrict__ out) {
+  const uint32_t lane = threadIdx.x & 31;
+  if (size == 0) {
+    for (uint32_t j = lane; j < m; j += 32) out[rq[j].out] = Traits<OutT>::value(lo);
+    return;
+  }
+  uint32_t P = 32;
+  while (P < size) P <<= 1;
+  for (uint32_t c = 0; c < P; c += 32) {
+    const K v = c + lane < size ? src[c + lane] : KeyMax<K>::v;
+    buf[c + lane] = warp_bitonic32(v);
+  }
+  __syncwarp();
+  for (uint32_t k = 64; k <= P; k <<= 1) {
+    const uint32_t half = k >> 1;
+    for (uint32_t t = lane; t < (P >> 1); t += 32) {
+      const uint32_t a = ((t & ~(half - 1)) << 1) | (t & (half - 1));
+      const uint32_t b = a ^ (k - 1);
+      const K x = buf[a], y = buf[b];
+      if (x > y) {
+        buf[a] = y;
+        buf[b] = x;
+      }
+    }
+    __syncwarp();
+    for (uint32_t j = k >> 2; j > 0; j >>= 1) {
+      for (uint32_t t = lane; t < (P >> 1); t += 32) {
+        const uint32_t a = ((t & ~(j - 1)) << 1) | (t & (j - 1)), b = a + j;
+        const K x = buf[a], y = buf[b];
+        if (x > y) {
+          buf[a] = y;
+          buf[b] = x;
+        }
+      }
+      __syncwarp();
+    }
+  }
+  for (uint32_t j = lane; j < m; j += 32) {
+    const Req e = rq[j];
+    out[e.out] = Traits<OutT>::value(buf[e.rank]);
+  }
+  __syncwarp();
+}
+
+// Elements [a, b) of x (any alignment): scalar head up to a 16-byte boundary,
+// a 128-bit body with four vectors in flight per thread, a scalar tail.
+// f(key, full) is called once per element; full: all 32 lanes of the warp
+// make the same call (the unrolled body), so warp-collective operations are
+// allowed.
+template <class T, class F>
+__device__ __forceinline__ void for_range(const T *__restrict__ x, uint64_t a, uint64_t b, F &&f) {
+  using K = typename Traits<T>::K;
+  using V = typename Traits<T>::Vec;
+  constexpr int PV = Traits<T>::kPerVec;
+  uint64_t va = a + (uint64_t)((16u - ((uint32_t)(uintptr_t)(x + a) & 15u)) & 15u) / sizeof(T);
+  if (va > b) va = b;
+  const uint64_t nvec = (b - va) / PV;
+  const uint64_t vb = va + nvec * PV;
+  for (uint64_t e = a + threadIdx.x; e < va; e += blockDim.x) f(Traits<T>::key(x[e]), false);
+  for (uint64_t e = vb + threadIdx.x; e < b; e += blockDim.x) f(Traits<T>::key(x[e]), false);
+  const V *xv = reinterpret_cast<const V *>(x + va);
+  const uint64_t step = 4ull * blockDim.x;
+  uint64_t v0 = 0;
+  for (; v0 + step <= nvec; v0 += step) {
+    V vv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) vv[u] = ldg_stream(xv + v0 + (uint64_t)u * blockDim.x + threadIdx.x);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      K k[PV];
+      vec_keys<T>(vv[u], k);
+#pragma unroll
+      for (int e = 0; e < PV; ++e) f(k[e], true);
+    }
+  }
+  for (uint64_t vi = v0 + threadIdx.x; vi < nvec; vi += blockDim.x) {
+    K k[PV];
+    vec_keys<T>(ldg_stream(xv + vi), k);
+#pragma unroll
+    for (int e = 0; e < PV; ++e) f(k[e], false);
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
+  using K = typename Traits<T>::K;
+  using OutT = T;
+  extern __shared__ uint4 smem_raw[];
+  uint32_t *sm = reinterpret_cast<uint32_t *>(smem_raw);
+  __shared__ uint32_t s_item, s_status, s_cur;
+  __shared__ K redk[33];
+  __shared__ uint32_t red32[33];
+  __shared__ uint64_t red64[33];
+  __shared__ uint64_t s_base;
+  __shared__ uint32_t s_lb[2];
+  __shared__ LutHeader<K> s_hdr;
+  __shared__ bool s_bad;
+  BCtrl *ctrl = A.ctrl;
+  const uint32_t tid = threadIdx.x, nt = blockDim.x;
+  K *surv = reinterpret_cast<K *>(A.surv);
+  K *seg_lo = reinterpret_cast<K *>(A.seg_lo);
+  K *seg_hi = reinterpret_cast<K *>(A.seg_hi);
+  OutT *out = reinterpret_cast<OutT *>(A.out);
+  if (blockIdx.x == 0 && tid == 0) ctrl->t_ns[0] = global_ns();
+
+  // ---------------- phase 1: splitter tables
+  for (uint32_t p = queue_pop(&ctrl->queue[0], &s_item); p < A.num_probs;
+       p = queue_pop(&ctrl->queue[0], &s_item)) {
+    const BProb P = A.probs[p];
+    const T *x = reinterpret_cast<const T *>(P.x);
+    K *samples = reinterpret_cast<K *>(sm);
+    K lo = KeyMax<K>::v, hi = 0;
+    for (uint32_t i = tid; i < P.S; i += nt) {
+      const uint64_t pos =
+          (uint64_t)P.S >= P.n ? i : ((uint64_t)hash32(i * 0x9E3779B9u + 0x5EEDu) * P.n) >> 32;
+      const K k = Traits<T>::key(x[pos]);
+      samples[i] = k;
+      lo = k < lo ? k : lo;
+      hi = k > hi ? k : hi;
+    }
+    lo = block_reduce(lo, [](K u, K v) { return u < v ? u : v; }, redk);
+    hi = block_reduce(hi, [](K u, K v) { return u > v ? u : v; }, redk);
+    build_lut_cta<K, kBSpt, true>(samples, P.S, lo, hi, P.nb_max, A.luts + P.lut_off, &s_hdr,
+                                  (int)P.nsl_bits);
+    __syncthreads();
+    if (tid == 0) {
+      BHdr h;
+      h.base = s_hdr.base;
+      h.surv_off = 0;
+      h.shift = s_hdr.shift;
+      h.nb = s_hdr.nb;
+      h.heavy = s_hdr.heavy;
+      h.num_slots = 0;
+      A.hdrs[p] = h;
+    }
+  }
+  uint32_t st = grid_barrier(ctrl, &s_status, 1);
+
+  // ---------------- phase 2: one histogram row per tile
+  if (tid == 0) s_cur = 0xFFFFFFFFu;  // problem whose table is in shared memory
+  uint32_t *lut = sm;
+  uint32_t *hist = sm + kLutPadded;
+  if (!(st & ST_FATAL)) {
+    for (uint32_t t = queue_pop(&ctrl->queue[1], &s_item); t < A.num_tiles;
+         t = queue_pop(&ctrl->queue[1], &s_item)) {
+      const BTile tl = A.tiles[t];
+      const BProb P = A.probs[tl.prob];
+      const BHdr H = load_hdr(A.hdrs + tl.prob);
+      const uint32_t nsl = 1u << P.nsl_bits;
+      if (s_cur != tl.prob)
+        for (uint32_t j = tid; j <= nsl; j += nt) lut[j] = __ldcg(A.luts + P.lut_off + j);
+      for (uint32_t b = tid; b < H.nb; b += nt) hist[b] = 0;
+      __syncthreads();
+      if (tid == 0) s_cur = tl.prob;
+      const K base = (K)H.base;
+      const uint32_t shift = H.shift;
+      if (H.heavy) {
+        for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool full) {
+          const uint32_t b = bucket_of<K>(k, base, shift, lut, nsl);
+          if (full)
+            hist_add<true>(hist, b);
+          else
+            atomicAdd(&hist[b], 1u);
+        });
+      } else {
+        for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
+          atomicAdd(&hist[bucket_of<K>(k, base, shift, lut, nsl)], 1u);
+        });
+      }
+      __syncthreads();
+      uint32_t *row = A.rows + P.row0 + (uint64_t)tl.rank * P.nb_max;
+      for (uint32_t b = tid; b < H.nb; b += nt) row[b] = hist[b];
+    }
+  }
+  st = grid_barrier(ctrl, &s_status, 2);
+
+  // ---------------- phase 3: per-problem scan and plan
+  if (!(st & ST_FATAL)) {
+    for (uint32_t p = queue_pop(&ctrl->queue[2], &s_item); p < A.num_probs;
+         p = queue_pop(&ctrl->queue[2], &s_item)) {
+      const BProb P = A.probs[p];
+      const BHdr H = load_hdr(A.hdrs + p);
+      const uint32_t nb = H.nb, nsl = 1u << P.nsl_bits, nr = P.ntiles;
+      uint32_t *excl = sm + kLutPadded;  // bucket prefix; later: slot of each flagged bucket
+      uint8_t *flag = reinterpret_cast<uint8_t *>(excl + kBMaxNb);
+      uint32_t *cnt = A.counts + P.cnt_off;
+      for (uint32_t j = tid; j <= nsl; j += nt) lut[j] = __ldcg(A.luts + P.lut_off + j);
+      // each column of the rows becomes its exclusive prefix over the tiles;
+      // a warp covers 32 neighbouring buckets of a row
+      for (uint32_t b = tid; b < nb; b += nt) {
+        uint32_t *col = A.rows + P.row0 + b;
+        uint32_t run = 0, r = 0;
+        for (; r + 8 <= nr; r += 8) {
+          uint32_t v[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) v[q] = __ldcg(col + (uint64_t)(r + q) * P.nb_max);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            col[(uint64_t)(r + q) * P.nb_max] = run;
+            run += v[q];
+          }
+        }
+        for (; r < nr; ++r) {
+          const uint32_t v = __ldcg(col + (uint64_t)r * P.nb_max);
+          col[(uint64_t)r * P.nb_max] = run;
+          run += v;
+        }
+        cnt[b] = run;
+        excl[b] = run;  // the count, until the scan below
+        flag[b] = 0;
+      }
+      __syncthreads();
+      // bucket prefix: contiguous bucket range per thread
+      const uint32_t per = (nb + nt - 1) / nt;
+      const uint32_t b0 = min(nb, tid * per), b1 = min(nb, b0 + per);
+      uint32_t mysum = 0;
+      for (uint32_t b = b0; b < b1; ++b) mysum += excl[b];
+      uint32_t tot;
+      uint32_t run = block_incl_scan(mysum, &tot, red32) - mysum;
+      for (uint32_t b = b0; b < b1; ++b) {
+        const uint32_t c = excl[b];
+        excl[b] = run;
+        run += c;
+      }
+      if (tid == 0 && (uint64_t)tot != P.n) atomicOr(&ctrl->status, ST_INTERNAL);
+      __syncthreads();
+      // requests -> bucket (the last b with excl[b] <= rank) and local rank
+      const Req *rq = A.reqs + P.req_off;
+      for (uint32_t i = tid; i < P.num_req; i += nt) {
+        const uint32_t rank = rq[i].rank;
+        uint32_t lo = 0, hi = nb;
+        while (hi - lo > 1) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (excl[mid] <= rank)
+            lo = mid;
+          else
+            hi = mid;
+        }
+        flag[lo] = 1;
+        A.req_bucket[P.req_off + i] = lo;
+        A.req_local[P.req_off + i] = rank - excl[lo];
+      }
+      __syncthreads();
+      // flagged buckets -> slots in bucket order; excl[] now maps bucket -> slot
+      uint32_t my_slots = 0;
+      for (uint32_t b = b0; b < b1; ++b) my_slots += flag[b] ? 1u : 0u;
+      uint32_t tot_slots;
+      {
+        uint32_t slot = block_incl_scan(my_slots, &tot_slots, red32) - my_slots;
+        for (uint32_t b = b0; b < b1; ++b)
+          if (flag[b]) {
+            excl[b] = slot;
+            A.seg_bucket[P.req_off + slot] = b;
+            slot++;
+          }
+      }
+      __syncthreads();
+      // key range, flat test and survivor count of each slot
+      const uint32_t sper = (tot_slots + nt - 1) / nt;
+      const uint32_t s0 = min(tot_slots, tid * sper), s1 = min(tot_slots, s0 + sper);
+      uint64_t my_surv = 0;
+      for (uint32_t q = s0; q < s1; ++q) {
+        const uint32_t g = P.req_off + q;
+        const uint32_t b = __ldcg(A.seg_bucket + g);
+        const K klo = bucket_lo<K>(b, (K)H.base, H.shift, lut, nsl);
+        const K knext = (b + 1 < nb) ? bucket_lo<K>(b + 1, (K)H.base, H.shift, lut, nsl) : K(0);
+        // single key iff the next bucket starts one key later (see k_plan)
+        const bool single = (knext > klo) ? (knext - klo == K(1)) : (klo == KeyMax<K>::v);
+        const uint32_t cb = single ? 0u : __ldcg(cnt + b);
+        A.seg_size[g] = cb;
+        seg_lo[g] = klo;
+        seg_hi[g] = single ? klo : (knext > klo ? knext - K(1) : KeyMax<K>::v);
+        A.kcnt[g] = 0;
+        A.kcur[g] = 0;
+        my_surv += cb;
+      }
+      uint64_t tot_surv;
+      uint64_t off = block_incl_scan(my_surv, &tot_surv, red64) - my_surv;
+      if (tid == 0) {
+        const uint64_t base = atomicAdd((unsigned long long *)&ctrl->surv_top,
+                                        (unsigned long long)tot_surv);
+        if (base + tot_surv > A.surv_cap) {
+          atomicOr(&ctrl->status, ST_OVERFLOW);
+          atomicMax((unsigned long long *)&ctrl->cap_needed,
+                    (unsigned long long)(base + tot_surv));
+        }
+        // compaction cursors carry the position inside the problem in 31 bits
+        if (tot_surv >= (uint64_t)kInactive) atomicOr(&ctrl->status, ST_INTERNAL);
+        s_base = base;
+        A.hdrs[p].surv_off = base;
+        A.hdrs[p].num_slots = tot_slots;
+      }
+      __syncthreads();
+      off += s_base;
+      for (uint32_t q = s0; q < s1; ++q) {
+        const uint32_t g = P.req_off + q;
+        A.seg_off[g] = off;
+        off += __ldcg(A.seg_size + g);
+      }
+      // finisher lists: small segments go to one warp each, the others to a
+      // whole CTA each
+      {
+        uint32_t my_small = 0;
+        for (uint32_t q = s0; q < s1; ++q)
+          my_small += __ldcg(A.seg_size + P.req_off + q) <= warp_cap<K>() ? 1u : 0u;
+        const uint32_t my_big = (s1 - s0) - my_small;
+        uint32_t tot_small, tot_big;
+        uint32_t rs = block_incl_scan(my_small, &tot_small, red32) - my_small;
+        uint32_t rb = block_incl_scan(my_big, &tot_big, red32) - my_big;
+        if (tid == 0) {
+          s_lb[0] = atomicAdd(&ctrl->n_small, tot_small);
+          s_lb[1] = atomicAdd(&ctrl->n_big, tot_big);
+        }
+        __syncthreads();
+        rs += s_lb[0];
+        rb += s_lb[1];
+        for (uint32_t q = s0; q < s1; ++q) {
+          const uint32_t g = P.req_off + q;
+          if (__ldcg(A.seg_size + g) <= warp_cap<K>())
+            A.small_list[rs++] = g;
+          else
+            A.big_list[rb++] = g;
+        }
+      }
+      __syncthreads();
+      for (uint32_t i = tid; i < P.num_req; i += nt)
+        atomicAdd(&A.kcnt[P.req_off + excl[__ldcg(A.req_bucket + P.req_off + i)]], 1u);
+      __syncthreads();
+      {
+        uint32_t mine = 0;
+        for (uint32_t q = s0; q < s1; ++q) mine += __ldcg(A.kcnt + P.req_off + q);
+        uint32_t t2;
+        uint32_t r2 = block_incl_scan(mine, &t2, red32) - mine + P.req_off;
+        for (uint32_t q = s0; q < s1; ++q) {
+          A.kstart[P.req_off + q] = r2;
+          r2 += __ldcg(A.kcnt + P.req_off + q);
+        }
+      }
+      __syncthreads();
+      for (uint32_t i = tid; i < P.num_req; i += nt) {
+        const uint32_t g = P.req_off + excl[__ldcg(A.req_bucket + P.req_off + i)];
+        const uint32_t pos = __ldcg(A.kstart + g) + atomicAdd(&A.kcur[g], 1u);
+        Req e;
+        e.rank = __ldcg(A.req_local + P.req_off + i);
+        e.out = rq[i].out;
+        A.klist[pos] = e;
+      }
+    }
+  }
+  st = grid_barrier(ctrl, &s_status, 3);
+
+  // ---------------- phase 4: compaction, the same (problem, tile) items
+  if (!(st & (ST_FATAL | ST_OVERFLOW))) {
+    if (tid == 0) {
+      s_cur = 0xFFFFFFFFu;
+      s_bad = false;
+    }
+    uint32_t *cursor = sm + kLutPadded;
+    for (uint32_t t = queue_pop(&ctrl->queue[3], &s_item); t < A.num_tiles;
+         t = queue_pop(&ctrl->queue[3], &s_item)) {
+      const BTile tl = A.tiles[t];
+      const BProb P = A.probs[tl.prob];
+      const BHdr H = load_hdr(A.hdrs + tl.prob);
+      const uint32_t nsl = 1u << P.nsl_bits;
+      if (s_cur != tl.prob)
+        for (uint32_t j = tid; j <= nsl; j += nt) lut[j] = __ldcg(A.luts + P.lut_off + j);
+      for (uint32_t b = tid; b < H.nb; b += nt) cursor[b] = kInactive;
+      __syncthreads();
+      if (tid == 0) s_cur = tl.prob;
+      const uint32_t *row = A.rows + P.row0 + (uint64_t)tl.rank * P.nb_max;
+      // positions relative to the problem's survivor range (flat slots have none)
+      for (uint32_t s = tid; s < H.num_slots; s += nt) {
+        const uint32_t g = P.req_off + s;
+        if (__ldcg(A.seg_size + g) == 0) continue;
+        const uint32_t b = __ldcg(A.seg_bucket + g);
+        cursor[b] = (uint32_t)(ldcg_u(A.seg_off + g) - H.surv_off + __ldcg(row + b));
+      }
+      __syncthreads();
+      K *sp = surv + H.surv_off;
+      const uint64_t cap = A.surv_cap - H.surv_off;
+      const K base = (K)H.base;
+      const uint32_t shift = H.shift;
+      bool overrun = false;
+      for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
+        const uint32_t pos = atomicAdd(&cursor[bucket_of<K>(k, base, shift, lut, nsl)], 1u);
+        const bool active = !(pos & kInactive);
+        const bool fits = pos < cap;
+        st_global_if(sp + pos, k, active && fits);
+        overrun |= active && !fits;
+      });
+      if (overrun) s_bad = true;
+      __syncthreads();
+      // each cursor must end where the next tile's range of the bucket starts
+      for (uint32_t s = tid; s < H.num_slots; s += nt) {
+        const uint32_t g = P.req_off + s;
+        if (__ldcg(A.seg_size + g) == 0) continue;
+        const uint32_t b = __ldcg(A.seg_bucket + g);
+        const uint32_t nxt = tl.rank + 1 < P.ntiles ? __ldcg(row + P.nb_max + b)
+                                                     : __ldcg(A.counts + P.cnt_off + b);
+        const uint32_t end = (uint32_t)(ldcg_u(A.seg_off + g) - H.surv_off + nxt);
+        if (cursor[b] != end) s_bad = true;
+      }
+    }
+    __syncthreads();
+    if (tid == 0 && s_bad) atomicOr(&ctrl->status, ST_INTERNAL);
+  }
+  st = grid_barrier(ctrl, &s_status, 4);
+
+  // ---------------- phase 5: finish every slot
+  if (!(st & (ST_FATAL | ST_OVERFLOW))) {
+    const uint32_t n_big = __ldcg(&ctrl->n_big), n_small = __ldcg(&ctrl->n_small);
+    // large segments first, a whole CTA each
+    for (uint32_t i = queue_pop(&ctrl->queue[4], &s_item); i < n_big;
+         i = queue_pop(&ctrl->queue[4], &s_item)) {
+      const uint32_t g = __ldcg(A.big_list + i);
+      const bool done = finish_slot<K, OutT>(
+          surv + ldcg_u(A.seg_off + g), __ldcg(A.seg_size + g), ldcg_u(seg_lo + g), ldcg_u(seg_hi + g),
+          A.klist + __ldcg(A.kstart + g), __ldcg(A.kcnt + g), A.bcap, sm, out);
+      if (!done && tid == 0) {
+        const uint32_t d = atomicAdd(&ctrl->deferred_count, 1u);
+        A.deferred[d] = g;
+        atomicOr(&ctrl->status, ST_DEFERRED);
+      }
+    }
+    // then the small ones, one warp each (the queue pop above ended with a
+    // barrier, so no thread of this CTA still uses the shared memory)
+    const uint32_t lane = tid & 31;
+    K *wbuf = reinterpret_cast<K *>(sm) + (size_t)(tid >> 5) * warp_cap<K>();
+    while (true) {
+      uint32_t i = 0;
+      if (lane == 0) i = atomicAdd(&ctrl->small_pop, 1u);
+      i = __shfl_sync(0xffffffffu, i, 0);
+      if (i >= n_small) break;
+      const uint32_t g = __ldcg(A.small_list + i);
+      finish_warp<K, OutT>(surv + ldcg_u(A.seg_off + g), __ldcg(A.seg_size + g), ldcg_u(seg_lo + g),
+                           A.klist + __ldcg(A.kstart + g), __ldcg(A.kcnt + g), wbuf, out);
+    }
+  }
+  __syncthreads();
+  if (blockIdx.x == 0 && tid == 0) ctrl->t_ns[kBPhases] = global_ns();
+}
+
+}  // namespace ggks

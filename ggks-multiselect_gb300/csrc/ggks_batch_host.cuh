@@ -1,0 +1,285 @@
+// ggks_batch_host.cuh -- host driver of the batched multiselect (one
+// cooperative launch of k_batch per batch).  Included by the per-type units.
+#pragma once
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "ggks_batch.cuh"
+#include "ggks_internal.h"
+
+namespace ggks {
+
+static inline size_t balign(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+static inline uint32_t pow2_ceil_u32(uint64_t v) {
+  uint32_t r = 1;
+  while (r < v && r < 0x80000000u) r <<= 1;
+  return r;
+}
+
+// the batch's shared-memory need: the largest of the phases' layouts
+template <class T>
+static inline int batch_smem_bytes() {
+  using K = typename Traits<T>::K;
+  const size_t table = (size_t)kBMaxS * sizeof(K);
+  const size_t plan = kLutPadded * 4 + (size_t)kBMaxNb * 5;
+  const size_t fin = 5 * kFinBins * 4 + (size_t)(sizeof(K) == 4 ? 4096 : 2048) * sizeof(K) * 3 / 2;
+  return (int)std::max(table, std::max(plan, fin));
+}
+
+template <class T>
+int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cudaStream_t s,
+                 const BatchTune &tune, float *kernel_ms) {
+  using K = typename Traits<T>::K;
+  const uint32_t bcap = sizeof(K) == 4 ? 4096u : 2048u;
+  const uint32_t R = in.k_off[in.num_problems];
+
+  // ---- plan: problems with requests, their bucket budgets and tiles
+  std::vector<BProb> probs;
+  std::vector<uint32_t> orig;  // problem index in the caller's arrays
+  probs.reserve(in.num_problems);
+  uint64_t lut_words = 0, cnt_words = 0, row_words = 0, surv_est = 0;
+  uint32_t num_tiles = 0;
+  const uint64_t tile = std::max<uint64_t>(64, tune.tile & ~63ull);
+  for (uint32_t p = 0; p < in.num_problems; ++p) {
+    const uint32_t nr = in.k_off[p + 1] - in.k_off[p];
+    if (nr == 0) continue;
+    BProb b{};
+    b.x = in.vecs[p];
+    b.n = in.n[p];
+    // buckets: about n / div elements each, a power of two in [4, kBMaxNb];
+    // half as many slices (the table needs nb_max >= slices + 2)
+    uint32_t nbm = pow2_ceil_u32((b.n + tune.div - 1) / tune.div);
+    nbm = std::min(kBMaxNb, std::max(4u, nbm));
+    uint32_t nsl_bits = 0;
+    while ((2u << nsl_bits) < nbm && nsl_bits < (uint32_t)kLutIdxBits) ++nsl_bits;
+    b.nb_max = nbm;
+    b.nsl_bits = nsl_bits;
+    b.S = (uint32_t)std::min<uint64_t>(b.n, kBMaxS);
+    b.ntiles = (uint32_t)((b.n + tile - 1) / tile);
+    b.req_off = in.k_off[p];
+    b.num_req = nr;
+    b.lut_off = lut_words;
+    lut_words += ((1u << nsl_bits) + 1 + 3) & ~3u;
+    b.cnt_off = cnt_words;
+    cnt_words += nbm;
+    b.row0 = row_words;
+    row_words += (uint64_t)b.ntiles * nbm;
+    num_tiles += b.ntiles;
+    surv_est += std::min<uint64_t>(b.n, (uint64_t)nr * 4 * ((b.n + nbm - 1) / nbm) + 64);
+    probs.push_back(b);
+    orig.push_back(p);
+  }
+  const uint32_t P = (uint32_t)probs.size();
+  if (P == 0) return GGKS_OK;
+  // tiles, largest first, so that the end of each tile phase has the small ones
+  std::vector<BTile> tiles;
+  tiles.reserve(num_tiles);
+  for (uint32_t q = 0; q < P; ++q)
+    for (uint32_t r = 0; r < probs[q].ntiles; ++r) {
+      BTile t{};
+      t.begin = (uint64_t)r * tile;
+      t.end = std::min<uint64_t>(probs[q].n, t.begin + tile);
+      t.prob = q;
+      t.rank = r;
+      tiles.push_back(t);
+    }
+  std::stable_sort(tiles.begin(), tiles.end(), [](const BTile &a, const BTile &b) {
+    return (a.end - a.begin) > (b.end - b.begin);
+  });
+
+  // ---- workspace: [ctrl | probs | tiles | reqs] is uploaded in one copy
+  const size_t A = 256;
+  size_t o = 0;
+  auto arr = [&](size_t elems, size_t esz) {
+    const size_t at = o;
+    o = balign(o + elems * esz, A);
+    return at;
+  };
+  const size_t o_ctrl = arr(1, A);
+  const size_t o_probs = arr(P, sizeof(BProb));
+  const size_t o_tiles = arr(num_tiles, sizeof(BTile));
+  const size_t o_reqs = arr(R, sizeof(Req));
+  const size_t up_bytes = o;
+  const size_t o_hdrs = arr(P, sizeof(BHdr));
+  const size_t o_luts = arr(lut_words, 4);
+  const size_t o_rows = arr(row_words, 4);
+  const size_t o_counts = arr(cnt_words, 4);
+  const size_t o_req_bucket = arr(R, 4), o_req_local = arr(R, 4);
+  const size_t o_seg_bucket = arr(R, 4), o_seg_size = arr(R, 4), o_kstart = arr(R, 4),
+               o_kcnt = arr(R, 4), o_kcur = arr(R, 4);
+  const size_t o_seg_off = arr(R, 8), o_seg_lo = arr(R, sizeof(K)), o_seg_hi = arr(R, sizeof(K));
+  const size_t o_klist = arr(R, sizeof(Req)), o_deferred = arr(R, 4);
+  const size_t o_big = arr(R, 4), o_small = arr(R, 4);
+  const size_t o_out = arr(R, sizeof(T));
+  const size_t total = o;
+
+  cudaError_t e = ensure_buffer(ctx, &ctx.barena, &ctx.barena_bytes, total);
+  if (e != cudaSuccess) return from_cuda(e);
+  const size_t out_bytes = (size_t)R * sizeof(T);
+  e = ensure_pinned(ctx, &ctx.bpin, &ctx.bpin_bytes, up_bytes + A + out_bytes);
+  if (e != cudaSuccess) return from_cuda(e);
+  uint64_t surv_cap = std::max<uint64_t>(surv_est, 1u << 20);
+  if (ctx.surv_bytes / sizeof(K) > surv_cap) surv_cap = ctx.surv_bytes / sizeof(K);
+  e = ensure_surv(ctx, (size_t)surv_cap * sizeof(K));
+  if (e != cudaSuccess) return from_cuda(e);
+
+  char *hp = ctx.bpin;
+  std::memset(hp, 0, A);
+  std::memcpy(hp + o_probs, probs.data(), (size_t)P * sizeof(BProb));
+  std::memcpy(hp + o_tiles, tiles.data(), (size_t)num_tiles * sizeof(BTile));
+  Req *hr = reinterpret_cast<Req *>(hp + o_reqs);
+  for (uint32_t q = 0; q < P; ++q) {
+    const uint32_t p = orig[q];
+    const uint64_t n = probs[q].n;
+    const uint32_t off = in.k_off[p], nr = probs[q].num_req;
+    for (uint32_t i = 0; i < nr; ++i) {
+      // k-th largest (1-based) is ascending rank n - k; top-k output i is
+      // the (i + 1)-th largest
+      const uint64_t k = in.k ? in.k[off + i] : (uint64_t)i + 1;
+      hr[off + i].rank = (uint32_t)(n - k);
+      hr[off + i].out = off + i;
+    }
+  }
+  char *D = ctx.barena;
+  BCtrl *ctrl = reinterpret_cast<BCtrl *>(D + o_ctrl);
+  char *h_ctrl = hp + up_bytes;
+  T *h_res = reinterpret_cast<T *>(hp + up_bytes + A);
+  e = cudaMemcpyAsync(D, hp, up_bytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return from_cuda(e);
+
+  T *d_out = d_out_user ? d_out_user : reinterpret_cast<T *>(D + o_out);
+  BArgs a{};
+  a.probs = reinterpret_cast<const BProb *>(D + o_probs);
+  a.hdrs = reinterpret_cast<BHdr *>(D + o_hdrs);
+  a.tiles = reinterpret_cast<const BTile *>(D + o_tiles);
+  a.num_probs = P;
+  a.num_tiles = num_tiles;
+  a.num_req = R;
+  a.bcap = bcap;
+  a.luts = reinterpret_cast<uint32_t *>(D + o_luts);
+  a.rows = reinterpret_cast<uint32_t *>(D + o_rows);
+  a.counts = reinterpret_cast<uint32_t *>(D + o_counts);
+  a.reqs = reinterpret_cast<const Req *>(D + o_reqs);
+  a.req_bucket = reinterpret_cast<uint32_t *>(D + o_req_bucket);
+  a.req_local = reinterpret_cast<uint32_t *>(D + o_req_local);
+  a.seg_bucket = reinterpret_cast<uint32_t *>(D + o_seg_bucket);
+  a.seg_size = reinterpret_cast<uint32_t *>(D + o_seg_size);
+  a.kstart = reinterpret_cast<uint32_t *>(D + o_kstart);
+  a.kcnt = reinterpret_cast<uint32_t *>(D + o_kcnt);
+  a.kcur = reinterpret_cast<uint32_t *>(D + o_kcur);
+  a.seg_off = reinterpret_cast<uint64_t *>(D + o_seg_off);
+  a.seg_lo = D + o_seg_lo;
+  a.seg_hi = D + o_seg_hi;
+  a.klist = reinterpret_cast<Req *>(D + o_klist);
+  a.big_list = reinterpret_cast<uint32_t *>(D + o_big);
+  a.small_list = reinterpret_cast<uint32_t *>(D + o_small);
+  a.deferred = reinterpret_cast<uint32_t *>(D + o_deferred);
+  a.out = d_out;
+  a.ctrl = ctrl;
+
+  // co-resident grid: every CTA the SMs hold at once
+  const int smem = batch_smem_bytes<T>();
+  static int blocks_per_sm = -1;  // per instantiation; one GPU model per process
+  if (blocks_per_sm < 0) {
+    cudaFuncSetAttribute((const void *)k_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int b = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<T>, kBThreads, smem);
+    if (e != cudaSuccess) return from_cuda(e);
+    blocks_per_sm = b;
+  }
+  if (blocks_per_sm < 1) return GGKS_UNSUPPORTED;
+  const uint32_t grid = (uint32_t)blocks_per_sm * (uint32_t)ctx.sm_count;
+
+  float ms_total = 0.f;
+  auto launch = [&]() -> cudaError_t {
+    a.surv = ctx.surv;
+    a.surv_cap = surv_cap;
+    void *args[] = {&a};
+    if (ctx.bev0 == nullptr) {
+      cudaError_t r = cudaEventCreate(&ctx.bev0);
+      if (r == cudaSuccess) r = cudaEventCreate(&ctx.bev1);
+      if (r != cudaSuccess) return r;
+    }
+    cudaEventRecord(ctx.bev0, s);
+    cudaError_t r = cudaLaunchCooperativeKernel((const void *)k_batch<T>, dim3(grid), dim3(kBThreads),
+                                                args, (size_t)smem, s);
+    cudaEventRecord(ctx.bev1, s);
+    ctx.stats.launches++;
+    if (r != cudaSuccess) return r;
+    r = cudaMemcpyAsync(h_ctrl, ctrl, sizeof(BCtrl), cudaMemcpyDeviceToHost, s);
+    if (r != cudaSuccess) return r;
+    r = cudaStreamSynchronize(s);
+    float ms = 0.f;
+    if (r == cudaSuccess && cudaEventElapsedTime(&ms, ctx.bev0, ctx.bev1) == cudaSuccess)
+      ms_total += ms;
+    return r;
+  };
+  e = launch();
+  if (e != cudaSuccess) return from_cuda(e);
+
+  for (int round = 0;; ++round) {
+    BCtrl c;
+    std::memcpy(&c, h_ctrl, sizeof(BCtrl));
+    if (c.status & ST_FATAL) return (c.status & ST_TIMEOUT) ? GGKS_TIMEOUT : GGKS_INTERNAL;
+    if (c.status & ST_OVERFLOW) {
+      if (round >= 3) return GGKS_INTERNAL;
+      // survivors did not fit: grow the buffer and run the batch again
+      surv_cap = c.cap_needed + (c.cap_needed >> 3);
+      e = ensure_surv(ctx, (size_t)surv_cap * sizeof(K));
+      if (e != cudaSuccess) return from_cuda(e);
+      ctx.stats.retries++;
+      e = cudaMemsetAsync(ctrl, 0, sizeof(BCtrl), s);
+      if (e == cudaSuccess) e = launch();
+      if (e != cudaSuccess) return from_cuda(e);
+      continue;
+    }
+    for (int ph = 0; ph < kBPhases; ++ph)
+      if (c.t_ns[ph + 1] >= c.t_ns[ph]) ctx.stats.batch_phase_ms[ph] += (c.t_ns[ph + 1] - c.t_ns[ph]) * 1e-6;
+    ctx.stats.survivors += c.surv_top;
+    if (c.status & ST_DEFERRED) {
+      // slots whose needed bins exceed shared memory: select each again on
+      // its survivor keys (recursively, single-vector path)
+      const uint32_t Dn = c.deferred_count;
+      std::vector<uint32_t> dl(Dn);
+      e = cudaMemcpyAsync(dl.data(), a.deferred, (size_t)Dn * 4, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) return from_cuda(e);
+      int st = GGKS_OK;
+      Context *ch = child_of(ctx, &st);
+      if (!ch) return st;
+      for (uint32_t d = 0; d < Dn; ++d) {
+        const uint32_t g = dl[d];
+        uint64_t so = 0;
+        uint32_t sz = 0, ks = 0, kc = 0;
+        e = cudaMemcpyAsync(&so, a.seg_off + g, 8, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&sz, a.seg_size + g, 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&ks, a.kstart + g, 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&kc, a.kcnt + g, 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return from_cuda(e);
+        ReqSource cs;
+        cs.d_reqs = a.klist + ks;
+        ctx.stats.recursions++;
+        st = select<K, T>(*ch, reinterpret_cast<const K *>(ctx.surv) + so, sz, cs, kc, d_out,
+                          nullptr, s, nullptr);
+        if (st != GGKS_OK) return st;
+      }
+    }
+    break;
+  }
+  if (h_out) {
+    e = cudaMemcpyAsync(h_res, d_out, out_bytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return from_cuda(e);
+    std::memcpy(h_out, h_res, out_bytes);
+  }
+  if (kernel_ms) *kernel_ms = ms_total;
+  ctx.stats.batch_calls++;
+  ctx.stats.batch_problems += P;
+  return GGKS_OK;
+}
+
+}  // namespace ggks

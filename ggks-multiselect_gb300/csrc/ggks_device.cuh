@@ -282,11 +282,16 @@ __device__ __forceinline__ uint32_t hash32(uint32_t a) {
 // buckets start at 1 and its first bucket starts exactly at `base`.  One 4-byte
 // entry per slice keeps the shared-memory lookup to a single wavefront for
 // runs of neighbouring slices; the bucket costs two ALU operations.
+//
+// nsl (a power of two <= kLutIdx) is the number of slices; the top entry sits
+// at lut[nsl].  The single-vector path always uses kLutIdx slices; small
+// problems of a batch use fewer.
 template <class K>
-__device__ __forceinline__ uint32_t bucket_of(K key, K base, uint32_t shift, const uint32_t *lut) {
+__device__ __forceinline__ uint32_t bucket_of(K key, K base, uint32_t shift, const uint32_t *lut,
+                                              uint32_t nsl = kLutIdx) {
   const K d = key - base;  // wraps for key < base; that result is discarded
   const K idx = d >> shift;
-  const uint32_t j = idx < (K)kLutIdx ? (uint32_t)idx : kLutIdx;
+  const uint32_t j = idx < (K)nsl ? (uint32_t)idx : nsl;
   const uint32_t e = lut[j];
   const uint32_t b = (uint32_t)((int32_t)e >> 7) + shr_clamp(d, e & 127u);
   return key < base ? 0u : b;
@@ -298,9 +303,9 @@ __device__ __forceinline__ uint32_t lut_pack(int32_t C, uint32_t rs) {
 
 // first bucket and sub-bucket bits of entry j
 __device__ __forceinline__ void lut_entry(uint32_t e, uint32_t j, uint32_t shift, uint32_t *B,
-                                          uint32_t *bb) {
+                                          uint32_t *bb, uint32_t nsl = kLutIdx) {
   const int32_t C = (int32_t)e >> 7;
-  if (j == kLutIdx) {
+  if (j == nsl) {
     *B = (uint32_t)C;
     *bb = 0;
   } else {
@@ -311,22 +316,23 @@ __device__ __forceinline__ void lut_entry(uint32_t e, uint32_t j, uint32_t shift
 
 // smallest key that maps to bucket b (b < nb); bucket 0 starts at key 0.
 template <class K>
-__device__ __forceinline__ K bucket_lo(uint32_t b, K base, uint32_t shift, const uint32_t *lut) {
+__device__ __forceinline__ K bucket_lo(uint32_t b, K base, uint32_t shift, const uint32_t *lut,
+                                       uint32_t nsl = kLutIdx) {
   if (b == 0) return K(0);
   // first entry whose last bucket >= b (bucket ranges are non-decreasing in j)
-  uint32_t lo = 0, hi = kLutIdx;
+  uint32_t lo = 0, hi = nsl;
   while (lo < hi) {
     const uint32_t mid = (lo + hi) >> 1;
     uint32_t B, bb;
-    lut_entry(lut[mid], mid, shift, &B, &bb);
+    lut_entry(lut[mid], mid, shift, &B, &bb, nsl);
     if (B + (1u << bb) - 1u >= b)
       hi = mid;
     else
       lo = mid + 1;
   }
   uint32_t B, bb;
-  lut_entry(lut[lo], lo, shift, &B, &bb);
-  const K dstart = ((K)lo) << shift;  // for lo == kLutIdx this may wrap: see the caller
+  lut_entry(lut[lo], lo, shift, &B, &bb, nsl);
+  const K dstart = ((K)lo) << shift;  // for lo == nsl this may wrap: see the caller
   if (B >= b) return base + dstart;
   return base + dstart + (((K)(b - B)) << (shift - bb));
 }
@@ -392,6 +398,154 @@ __device__ __forceinline__ V block_reduce(V v, Op op, V *sh /* >= 32 */) {
 // one bucket per run.  The smallest threshold t whose bucket total fits nb_max
 // is found from a histogram of ceil(log2 c) over the slices, so each candidate
 // t costs a 33-term sum on one thread.
+// Builds the splitter table of one problem from its S sampled keys (kmin /
+// kmax: the sample's extremes) with one whole CTA of 4096 / SPT threads; the
+// table goes to lut[0 .. nsl] with nsl = 2^nsl_bits slices (nb_max >= nsl + 2
+// makes every threshold feasible), and thread 0 writes the header.  The
+// samples are in shared memory (SMEM) or in global memory written by other
+// CTAs (read past L1).
+template <class K, int SPT, bool SMEM>
+__device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint32_t nb_max,
+                              uint32_t *lut, LutHeader<K> *hdr, int nsl_bits = kLutIdxBits) {
+  __shared__ uint32_t cnt[kLutIdx];
+  __shared__ uint32_t lch[36];  // [0, 33): slices by ceil(log2 c); [34]: empty-run starts
+  __shared__ uint32_t red32[33];
+  __shared__ int s_t, s_r0;
+  __shared__ uint32_t s_tot[54];
+  __shared__ uint32_t s_cost[34];
+  const uint32_t tid = threadIdx.x;
+  const uint32_t nsl = 1u << nsl_bits;
+  const int bl = bitlen<K>(kmax - kmin);
+  const uint32_t shift = bl > nsl_bits ? (uint32_t)(bl - nsl_bits) : 0u;
+  const int bcap = (int)(shift < (uint32_t)kMaxSubBits ? shift : (uint32_t)kMaxSubBits);
+
+  // --- sample counts per slice
+  for (uint32_t j = tid; j < kLutIdx; j += blockDim.x) cnt[j] = 0;
+  if (tid < 36) lch[tid] = 0;
+  __syncthreads();
+#pragma unroll 16
+  for (uint32_t s = tid; s < S; s += blockDim.x) {
+    const K k = SMEM ? samples[s] : __ldcg(samples + s);
+    atomicAdd(&cnt[(uint32_t)((k - kmin) >> shift)], 1u);
+  }
+  __syncthreads();
+
+  // Each thread owns SPT consecutive slices [SPT tid, SPT tid + SPT) (those at
+  // or beyond nsl are unused); the top entry (keys above the sampled span) is
+  // written by thread 0 after the scan.
+  int lc[SPT];
+  uint32_t c[SPT];
+  bool prev_nonempty[SPT];
+#pragma unroll
+  for (int q = 0; q < SPT; ++q) {
+    const uint32_t j = SPT * tid + q;
+    const bool in = j < nsl;
+    c[q] = in ? cnt[j] : 0u;
+    lc[q] = c[q] ? (c[q] == 1 ? 0 : 32 - __clz(c[q] - 1)) : -1;  // ceil(log2 c)
+    prev_nonempty[q] = in && ((j == 0) ? true : (cnt[j - 1] != 0));
+    if (c[q])
+      atomicAdd(&lch[lc[q]], 1u);
+    else if (prev_nonempty[q])
+      atomicAdd(&lch[34], 1u);
+  }
+  const bool top_run_start = cnt[nsl - 1] != 0;
+  if (tid == 0) s_t = 33;  // total(33) <= 1 + nsl + 1 <= nb_max: always feasible
+  if (tid < 34) s_cost[tid] = 0;
+  __syncthreads();
+  if (tid < 54) {
+    // smallest t with total(t) <= nb_max; one candidate t per thread
+    const int t = -kMaxSubBits - 1 + (int)tid;
+    uint64_t tot = 1u + lch[34] + (top_run_start ? 1u : 0u);
+    for (int l = 0; l < 33; ++l) {
+      int b = l - t;
+      b = b < 0 ? 0 : (b > bcap ? bcap : b);
+      tot += (uint64_t)lch[l] << b;
+    }
+    s_tot[tid] = (uint32_t)(tot < 0xFFFFFFFFull ? tot : 0xFFFFFFFFull);
+    if (tot <= nb_max) atomicMin(&s_t, t);
+  }
+  __syncthreads();
+  const int t = s_t;
+  const uint32_t spare = nb_max - s_tot[t + kMaxSubBits + 1];
+
+  // Power-of-two rounding leaves part of the budget unused.  Spend it on the
+  // slices whose buckets are expected to be the fullest: r = 32 * (samples per
+  // bucket) / 2^t in [0, 32]; doubling slice j's buckets costs 2^b_j.  The
+  // largest r first, as long as the whole bin of r fits.
+  int bq[SPT];
+  uint32_t rq[SPT];
+#pragma unroll
+  for (int q = 0; q < SPT; ++q) {
+    int b = lc[q] - t;
+    bq[q] = b < 0 ? 0 : (b > bcap ? bcap : b);
+    rq[q] = 0xFFFFFFFFu;  // not a candidate
+    if (c[q] && bq[q] < bcap) {
+      const int e = bq[q] + t - 5;  // r = c * 32 / 2^(b + t)
+      uint32_t r = e >= 0 ? (e >= 32 ? 0u : c[q] >> e) : (-e >= 32 ? 32u : c[q] << (-e));
+      rq[q] = r > 32u ? 32u : r;
+      atomicAdd(&s_cost[rq[q]], 1u << bq[q]);
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    uint32_t acc = 0;
+    int r0 = 33;
+    for (int r = 32; r >= 0; --r) {
+      if (acc + s_cost[r] > spare) break;
+      acc += s_cost[r];
+      r0 = r;
+    }
+    s_r0 = r0;
+  }
+  __syncthreads();
+  const uint32_t r0 = (uint32_t)s_r0;
+#pragma unroll
+  for (int q = 0; q < SPT; ++q)
+    if (rq[q] != 0xFFFFFFFFu && rq[q] >= r0) bq[q] += 1;
+
+  auto bits_of = [&](int q) -> int { return bq[q]; };
+  uint32_t my[SPT], mysum = 0;
+#pragma unroll
+  for (int q = 0; q < SPT; ++q) {
+    my[q] = c[q] ? (1u << bits_of(q)) : (prev_nonempty[q] ? 1u : 0u);
+    mysum += my[q];
+  }
+  uint32_t total;
+  const uint32_t incl = block_incl_scan(mysum, &total, red32);
+  uint32_t run = incl - mysum + 1u;  // bucket 0 is the low edge
+  uint32_t max_per_bucket = 0;
+#pragma unroll
+  for (int q = 0; q < SPT; ++q) {
+    const uint32_t j = SPT * tid + q;
+    if (j >= nsl) {
+      // unused slice
+    } else if (c[q]) {
+      const int b = bits_of(q);
+      lut[j] = lut_pack((int32_t)run - (int32_t)(j << b), shift - (uint32_t)b);
+      const uint32_t per = c[q] >> b;
+      max_per_bucket = per > max_per_bucket ? per : max_per_bucket;
+    } else {
+      // one bucket per run of empty slices
+      lut[j] = lut_pack((int32_t)(prev_nonempty[q] ? run : run - 1u) - (int32_t)j, shift);
+    }
+    run += my[q];
+  }
+  max_per_bucket = block_reduce(max_per_bucket, [](uint32_t p, uint32_t q) { return p > q ? p : q; },
+                                red32);
+  if (tid == 0) {
+    const uint32_t nb = 1u + total + (top_run_start ? 1u : 0u);
+    lut[nsl] = lut_pack((int32_t)(top_run_start ? total + 1u : total), (uint32_t)KeyMax<K>::bits);
+    LutHeader<K> h;
+    h.base = kmin;
+    h.shift = shift;
+    h.nb = nb;
+    // a bucket expected to hold >= 16x the mean: warp-aggregate updates
+    h.heavy = ((uint64_t)max_per_bucket * nb >= 16ull * S && S >= 256) ? 1u : 0u;
+    h.pad = 0;
+    *hdr = h;
+  }
+}
+
 template <class T>
 __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, uint64_t n,
                                                      uint32_t S, uint32_t seed,
@@ -400,14 +554,8 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
                                                      LutHeader<typename Traits<T>::K> *hdr,
                                                      uint32_t *lut, uint32_t nb_max) {
   using K = typename Traits<T>::K;
-  __shared__ uint32_t cnt[kLutIdx];
-  __shared__ uint32_t lch[36];  // [0, 33): slices by ceil(log2 c); [34]: empty-run starts
   __shared__ K redk[33];
-  __shared__ uint32_t red32[33];
   __shared__ uint32_t s_last;
-  __shared__ int s_t, s_r0;
-  __shared__ uint32_t s_tot[54];
-  __shared__ uint32_t s_cost[34];
 
   const uint32_t tid = threadIdx.x;
   const uint32_t i = blockIdx.x * blockDim.x + tid;
@@ -439,131 +587,9 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
 
   const K kmin = (K)~__ldcg((const unsigned long long *)&ctrl->kmin_inv);
   const K kmax = (K)__ldcg((const unsigned long long *)&ctrl->kmax);
-  const int bl = bitlen<K>(kmax - kmin);
-  const uint32_t shift = bl > kLutIdxBits ? (uint32_t)(bl - kLutIdxBits) : 0u;
-  const int bcap = (int)(shift < (uint32_t)kMaxSubBits ? shift : (uint32_t)kMaxSubBits);
-
-  // --- sample counts per slice
-  for (uint32_t j = tid; j < kLutIdx; j += blockDim.x) cnt[j] = 0;
-  if (tid < 36) lch[tid] = 0;
-  __syncthreads();
-#pragma unroll 16
-  for (uint32_t s = tid; s < S; s += blockDim.x) {
-    const K k = __ldcg(samples + s);
-    atomicAdd(&cnt[(uint32_t)((k - kmin) >> shift)], 1u);
-  }
-  __syncthreads();
-
-  // Each thread owns 4 consecutive slices [4 tid, 4 tid + 4); the top entry
-  // (keys above the sampled span) is written by thread 0 after the scan.
-  int lc[4];
-  uint32_t c[4];
-  bool prev_nonempty[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const uint32_t j = 4 * tid + q;
-    c[q] = cnt[j];
-    lc[q] = c[q] ? (c[q] == 1 ? 0 : 32 - __clz(c[q] - 1)) : -1;  // ceil(log2 c)
-    prev_nonempty[q] = (j == 0) ? true : (cnt[j - 1] != 0);
-    if (c[q])
-      atomicAdd(&lch[lc[q]], 1u);
-    else if (prev_nonempty[q])
-      atomicAdd(&lch[34], 1u);
-  }
-  const bool top_run_start = cnt[kLutIdx - 1] != 0;
-  if (tid == 0) s_t = 33;  // total(33) <= 1 + 4096 + 1 <= nb_max: always feasible
-  if (tid < 34) s_cost[tid] = 0;
-  __syncthreads();
-  if (tid < 54) {
-    // smallest t with total(t) <= nb_max; one candidate t per thread
-    const int t = -kMaxSubBits - 1 + (int)tid;
-    uint64_t tot = 1u + lch[34] + (top_run_start ? 1u : 0u);
-    for (int l = 0; l < 33; ++l) {
-      int b = l - t;
-      b = b < 0 ? 0 : (b > bcap ? bcap : b);
-      tot += (uint64_t)lch[l] << b;
-    }
-    s_tot[tid] = (uint32_t)(tot < 0xFFFFFFFFull ? tot : 0xFFFFFFFFull);
-    if (tot <= nb_max) atomicMin(&s_t, t);
-  }
-  __syncthreads();
-  const int t = s_t;
-  const uint32_t spare = nb_max - s_tot[t + kMaxSubBits + 1];
-
-  // Power-of-two rounding leaves part of the budget unused.  Spend it on the
-  // slices whose buckets are expected to be the fullest: r = 32 * (samples per
-  // bucket) / 2^t in [0, 32]; doubling slice j's buckets costs 2^b_j.  The
-  // largest r first, as long as the whole bin of r fits.
-  int bq[4];
-  uint32_t rq[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    int b = lc[q] - t;
-    bq[q] = b < 0 ? 0 : (b > bcap ? bcap : b);
-    rq[q] = 0xFFFFFFFFu;  // not a candidate
-    if (c[q] && bq[q] < bcap) {
-      const int e = bq[q] + t - 5;  // r = c * 32 / 2^(b + t)
-      uint32_t r = e >= 0 ? (e >= 32 ? 0u : c[q] >> e) : (-e >= 32 ? 32u : c[q] << (-e));
-      rq[q] = r > 32u ? 32u : r;
-      atomicAdd(&s_cost[rq[q]], 1u << bq[q]);
-    }
-  }
-  __syncthreads();
+  build_lut_cta<K, 4, false>(samples, S, kmin, kmax, nb_max, lut, hdr);
   if (tid == 0) {
-    uint32_t acc = 0;
-    int r0 = 33;
-    for (int r = 32; r >= 0; --r) {
-      if (acc + s_cost[r] > spare) break;
-      acc += s_cost[r];
-      r0 = r;
-    }
-    s_r0 = r0;
-  }
-  __syncthreads();
-  const uint32_t r0 = (uint32_t)s_r0;
-#pragma unroll
-  for (int q = 0; q < 4; ++q)
-    if (rq[q] != 0xFFFFFFFFu && rq[q] >= r0) bq[q] += 1;
-
-  auto bits_of = [&](int q) -> int { return bq[q]; };
-  uint32_t my[4], mysum = 0;
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    my[q] = c[q] ? (1u << bits_of(q)) : (prev_nonempty[q] ? 1u : 0u);
-    mysum += my[q];
-  }
-  uint32_t total;
-  const uint32_t incl = block_incl_scan(mysum, &total, red32);
-  uint32_t run = incl - mysum + 1u;  // bucket 0 is the low edge
-  uint32_t max_per_bucket = 0;
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const uint32_t j = 4 * tid + q;
-    if (c[q]) {
-      const int b = bits_of(q);
-      lut[j] = lut_pack((int32_t)run - (int32_t)(j << b), shift - (uint32_t)b);
-      const uint32_t per = c[q] >> b;
-      max_per_bucket = per > max_per_bucket ? per : max_per_bucket;
-    } else {
-      // one bucket per run of empty slices
-      lut[j] = lut_pack((int32_t)(prev_nonempty[q] ? run : run - 1u) - (int32_t)j, shift);
-    }
-    run += my[q];
-  }
-  max_per_bucket = block_reduce(max_per_bucket, [](uint32_t p, uint32_t q) { return p > q ? p : q; },
-                                red32);
-  if (tid == 0) {
-    const uint32_t nb = 1u + total + (top_run_start ? 1u : 0u);
-    lut[kLutIdx] = lut_pack((int32_t)(top_run_start ? total + 1u : total), (uint32_t)KeyMax<K>::bits);
-    LutHeader<K> h;
-    h.base = kmin;
-    h.shift = shift;
-    h.nb = nb;
-    // a bucket expected to hold >= 16x the mean: warp-aggregate updates
-    h.heavy = ((uint64_t)max_per_bucket * nb >= 16ull * S && S >= 256) ? 1u : 0u;
-    h.pad = 0;
-    *hdr = h;
-    ctrl->nb = nb;
+    ctrl->nb = hdr->nb;
     ctrl->sample_done = 0;  // re-arm for the next call on this workspace
   }
 }
@@ -1176,15 +1202,17 @@ __device__ __forceinline__ uint32_t bin_of_rank(const uint32_t *start, uint32_t 
   return lo;
 }
 
+// Finishes one slot: its segment src[0 .. size) of survivor keys lies in the
+// key range [lo, hi] (size 0: a flat slot whose single key is lo); the m
+// requests rq[] hold local ranks and output positions.  Called by a whole CTA
+// of kFinThreads threads; smem holds 5 * kFinBins u32 followed by the gather
+// buffer (bcap keys) and the scratch (bcap / 2 keys).  Returns false when the
+// needed bins do not fit: the slot needs a recursive re-selection.
 template <class K, class OutT>
-__global__ void __launch_bounds__(kFinThreads)
-    k_finish(const K *__restrict__ surv, Ctrl *ctrl, const uint64_t *__restrict__ seg_off,
-             const uint32_t *__restrict__ seg_size, const K *__restrict__ seg_lo,
-             const K *__restrict__ seg_hi, const uint32_t *__restrict__ kstart,
-             const uint32_t *__restrict__ kcnt, const Req *__restrict__ klist,
-             uint32_t *__restrict__ deferred, uint32_t bcap, OutT *__restrict__ out) {
-  extern __shared__ uint4 smem_raw[];
-  uint32_t *hist = reinterpret_cast<uint32_t *>(smem_raw);
+__device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi,
+                            const Req *__restrict__ rq, uint32_t m, uint32_t bcap, uint32_t *smem,
+                            OutT *__restrict__ out) {
+  uint32_t *hist = smem;
   uint32_t *start = hist + kFinBins;
   uint32_t *gofs = start + kFinBins;  // gather offset of a needed bin, else kNoSlot
   uint32_t *cur = gofs + kFinBins;
@@ -1198,196 +1226,216 @@ __global__ void __launch_bounds__(kFinThreads)
   __shared__ uint32_t s_nbig, s_nsmall, s_maxneed;
   constexpr uint32_t PER = kFinBins / kFinThreads;  // bins per thread (at most)
   const uint32_t tcap = bcap / 2;                   // scratch T holds one bin of <= tcap keys
-
-  if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
-  const uint32_t num_slots = ctrl->num_slots;
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t nwarps = blockDim.x >> 5;
-  for (uint32_t slot = blockIdx.x; slot < num_slots; slot += gridDim.x) {
-    const uint32_t size = seg_size[slot];
-    const K *src = surv + seg_off[slot];
-    const Req *rq = klist + kstart[slot];
-    const uint32_t m = kcnt[slot];
-    if (size == 0) {  // flat slot: every rank in the bucket is its single key
-      const K key = seg_lo[slot];
-      for (uint32_t j = tid; j < m; j += blockDim.x) out[rq[j].out] = Traits<OutT>::value(key);
-      continue;
-    }
-    // about four keys per bin
-    uint32_t nbits = 8;
-    while (nbits < (uint32_t)kFinBinBits && (4u << nbits) < size) ++nbits;
-    const uint32_t nbins = 1u << nbits;
+  if (size == 0) {  // flat slot: every rank in the bucket is its single key
+    for (uint32_t j = tid; j < m; j += blockDim.x) out[rq[j].out] = Traits<OutT>::value(lo);
+    return true;
+  }
+  // about four keys per bin
+  uint32_t nbits = 8;
+  while (nbits < (uint32_t)kFinBinBits && (4u << nbits) < size) ++nbits;
+  const uint32_t nbins = 1u << nbits;
 
-    // digits of (key - mn): first over the bucket's key range; if the needed
-    // bins then hold too many keys, over the segment's actual min / max
-    K mn = seg_lo[slot], mx = seg_hi[slot];
-    uint32_t V = 0, sh = 0;
-    bool flat = false, fits = false;
-    for (int attempt = 0; attempt < 2 && !fits && !flat; ++attempt) {
-      if (attempt == 1) {
-        K a = KeyMax<K>::v, z = 0;
-        for (uint32_t i = tid; i < size; i += blockDim.x) {
-          const K k = src[i];
-          a = k < a ? k : a;
-          z = k > z ? k : z;
-        }
-        a = block_reduce(a, [](K p, K q) { return p < q ? p : q; }, redk);
-        z = block_reduce(z, [](K p, K q) { return p > q ? p : q; }, redk);
-        if (a == z) {
-          flat = true;
-          mn = a;
-          break;
-        }
+  // digits of (key - mn): first over the bucket's key range; if the needed
+  // bins then hold too many keys, over the segment's actual min / max
+  K mn = lo, mx = hi;
+  uint32_t V = 0, sh = 0;
+  bool flat = false, fits = false, direct = false;
+  for (int attempt = 0; attempt < 2 && !fits && !flat && !direct; ++attempt) {
+    if (attempt == 1) {
+      K a = KeyMax<K>::v, z = 0;
+      for (uint32_t i = tid; i < size; i += blockDim.x) {
+        const K k = src[i];
+        a = k < a ? k : a;
+        z = k > z ? k : z;
+      }
+      a = block_reduce(a, [](K p, K q) { return p < q ? p : q; }, redk);
+      z = block_reduce(z, [](K p, K q) { return p > q ? p : q; }, redk);
+      if (a == z) {
+        flat = true;
         mn = a;
-        mx = z;
+        break;
       }
-      const int bl = bitlen<K>(mx - mn);
-      sh = bl > (int)nbits ? (uint32_t)(bl - (int)nbits) : 0u;
-      for (uint32_t i = tid; i < nbins; i += blockDim.x) {
-        hist[i] = 0;
-        cur[i] = 0;
-      }
-      if (tid == 0) {
-        s_nbig = 0;
-        s_nsmall = 0;
-        s_maxneed = 0;
-      }
-      __syncthreads();
-      // keys lie in [mn, mx], so the digit is < nbins; the clamp keeps a
-      // shared-memory index in range whatever the data
-      {
-        uint32_t i = tid;
-        for (; i + 7 * blockDim.x < size; i += 8 * blockDim.x) {
-          K kk[8];
-#pragma unroll
-          for (int q = 0; q < 8; ++q) kk[q] = src[i + q * blockDim.x];
-#pragma unroll
-          for (int q = 0; q < 8; ++q)
-            atomicAdd(&hist[min((uint32_t)((kk[q] - mn) >> sh), nbins - 1u)], 1u);
-        }
-        for (; i < size; i += blockDim.x)
-          atomicAdd(&hist[min((uint32_t)((src[i] - mn) >> sh), nbins - 1u)], 1u);
-      }
-      __syncthreads();
-      {
-        uint32_t cc[PER], sum = 0;
-#pragma unroll
-        for (uint32_t q = 0; q < PER; ++q) {
-          const uint32_t bb = tid * PER + q;
-          cc[q] = bb < nbins ? hist[bb] : 0u;
-          sum += cc[q];
-        }
-        uint32_t tot;
-        uint32_t run = block_incl_scan(sum, &tot, red32) - sum;
-#pragma unroll
-        for (uint32_t q = 0; q < PER; ++q) {
-          const uint32_t bb = tid * PER + q;
-          if (bb < nbins) {
-            start[bb] = run;
-            gofs[bb] = 0;  // "needed" flag until the next scan
-          }
-          run += cc[q];
-        }
-      }
-      __syncthreads();
-      for (uint32_t j = tid; j < m; j += blockDim.x)
-        gofs[bin_of_rank(start, nbins, rq[j].rank)] = 1u;
-      __syncthreads();
-      {
-        uint32_t cc[PER], sum = 0;
-#pragma unroll
-        for (uint32_t q = 0; q < PER; ++q) {
-          const uint32_t bb = tid * PER + q;
-          cc[q] = (bb < nbins && gofs[bb]) ? hist[bb] : 0u;
-          sum += cc[q];
-        }
-        uint32_t run = block_incl_scan(sum, &V, red32) - sum;
-#pragma unroll
-        for (uint32_t q = 0; q < PER; ++q) {
-          const uint32_t bb = tid * PER + q;
-          if (bb < nbins) {
-            const bool need = gofs[bb] != 0u;
-            gofs[bb] = need ? run : kNoSlot;
-            if (need) atomicMax(&s_maxneed, cc[q]);
-            if (need && cc[q] > 32) {
-              const uint32_t at = atomicAdd(&s_nbig, 1u);
-              if (at < kMaxBig) big[at] = bb;
-            } else if (need && cc[q] > 1) {
-              small[atomicAdd(&s_nsmall, 1u)] = bb;
-            }
-          }
-          run += cc[q];
-        }
-      }
-      __syncthreads();
-      fits = V <= bcap && s_maxneed <= tcap;
+      mn = a;
+      mx = z;
     }
-    if (flat) {  // one distinct key: every rank is that key
-      for (uint32_t j = tid; j < m; j += blockDim.x) out[rq[j].out] = Traits<OutT>::value(mn);
-      __syncthreads();
-      continue;
+    const int bl = bitlen<K>(mx - mn);
+    sh = bl > (int)nbits ? (uint32_t)(bl - (int)nbits) : 0u;
+    for (uint32_t i = tid; i < nbins; i += blockDim.x) {
+      hist[i] = 0;
+      cur[i] = 0;
     }
-    if (!fits) {  // the needed bins do not fit: re-select on the host side
-      if (tid == 0) {
-        const uint32_t d = atomicAdd(&ctrl->deferred_count, 1u);
-        deferred[d] = slot;
-        atomicOr(&ctrl->status, ST_DEFERRED);
-      }
-      __syncthreads();
-      continue;
+    if (tid == 0) {
+      s_nbig = 0;
+      s_nsmall = 0;
+      s_maxneed = 0;
     }
-
-    // ---- gather the needed bins
+    __syncthreads();
+    // keys lie in [mn, mx], so the digit is < nbins; the clamp keeps a
+    // shared-memory index in range whatever the data
     {
-      auto put = [&](K k) {
-        const uint32_t bb = min((uint32_t)((k - mn) >> sh), nbins - 1u);
-        const uint32_t g = gofs[bb];
-        if (g != kNoSlot) B[g + atomicAdd(&cur[bb], 1u)] = k;
-      };
       uint32_t i = tid;
       for (; i + 7 * blockDim.x < size; i += 8 * blockDim.x) {
         K kk[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) kk[q] = src[i + q * blockDim.x];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) put(kk[q]);
+        for (int q = 0; q < 8; ++q)
+          atomicAdd(&hist[min((uint32_t)((kk[q] - mn) >> sh), nbins - 1u)], 1u);
       }
-      for (; i < size; i += blockDim.x) put(src[i]);
+      for (; i < size; i += blockDim.x)
+        atomicAdd(&hist[min((uint32_t)((src[i] - mn) >> sh), nbins - 1u)], 1u);
     }
     __syncthreads();
-
-    // ---- sort each needed bin: a warp per bin of 2..32 keys
-    const uint32_t nsmall = s_nsmall;
-    for (uint32_t q = warp; q < nsmall; q += nwarps) {
-      const uint32_t bb = small[q];
-      const uint32_t g = gofs[bb], c = hist[bb];
-      K v = lane < c ? B[g + lane] : KeyMax<K>::v;
-      v = warp_bitonic32(v);
-      if (lane < c) B[g + lane] = v;
-    }
-    // larger bins: the whole CTA, one at a time
-    const uint32_t nbig = s_nbig;
-    for (uint32_t q = 0; q < (nbig <= (uint32_t)kMaxBig ? nbig : nbins); ++q) {
-      const uint32_t bb = nbig <= (uint32_t)kMaxBig ? big[q] : q;
-      const uint32_t g = gofs[bb], c = hist[bb];
-      if (g == kNoSlot || c <= 32) continue;
-      uint32_t P = 64;
-      while (P < c) P <<= 1;
-      __syncthreads();
-      for (uint32_t i = tid; i < P; i += blockDim.x) T[i] = i < c ? B[g + i] : KeyMax<K>::v;
-      __syncthreads();
-      bitonic_sort_smem(T, P);
-      for (uint32_t i = tid; i < c; i += blockDim.x) B[g + i] = T[i];
+    {
+      uint32_t cc[PER], sum = 0;
+#pragma unroll
+      for (uint32_t q = 0; q < PER; ++q) {
+        const uint32_t bb = tid * PER + q;
+        cc[q] = bb < nbins ? hist[bb] : 0u;
+        sum += cc[q];
+      }
+      uint32_t tot;
+      uint32_t run = block_incl_scan(sum, &tot, red32) - sum;
+#pragma unroll
+      for (uint32_t q = 0; q < PER; ++q) {
+        const uint32_t bb = tid * PER + q;
+        if (bb < nbins) {
+          start[bb] = run;
+          gofs[bb] = 0;  // "needed" flag until the next scan
+        }
+        run += cc[q];
+      }
     }
     __syncthreads();
-
-    // ---- answer
+    if (sh == 0) {  // every bin is a single key: the ranks read their bins
+      direct = true;
+      break;
+    }
+    for (uint32_t j = tid; j < m; j += blockDim.x)
+      gofs[bin_of_rank(start, nbins, rq[j].rank)] = 1u;
+    __syncthreads();
+    {
+      uint32_t cc[PER], sum = 0;
+#pragma unroll
+      for (uint32_t q = 0; q < PER; ++q) {
+        const uint32_t bb = tid * PER + q;
+        cc[q] = (bb < nbins && gofs[bb]) ? hist[bb] : 0u;
+        sum += cc[q];
+      }
+      uint32_t run = block_incl_scan(sum, &V, red32) - sum;
+#pragma unroll
+      for (uint32_t q = 0; q < PER; ++q) {
+        const uint32_t bb = tid * PER + q;
+        if (bb < nbins) {
+          const bool need = gofs[bb] != 0u;
+          gofs[bb] = need ? run : kNoSlot;
+          if (need) atomicMax(&s_maxneed, cc[q]);
+          if (need && cc[q] > 32) {
+            const uint32_t at = atomicAdd(&s_nbig, 1u);
+            if (at < kMaxBig) big[at] = bb;
+          } else if (need && cc[q] > 1) {
+            small[atomicAdd(&s_nsmall, 1u)] = bb;
+          }
+        }
+        run += cc[q];
+      }
+    }
+    __syncthreads();
+    fits = V <= bcap && s_maxneed <= tcap;
+  }
+  if (flat) {  // one distinct key: every rank is that key
+    for (uint32_t j = tid; j < m; j += blockDim.x) out[rq[j].out] = Traits<OutT>::value(mn);
+    __syncthreads();
+    return true;
+  }
+  if (direct) {  // bins of one key each (few distinct keys, many copies)
     for (uint32_t j = tid; j < m; j += blockDim.x) {
       const Req e = rq[j];
-      const uint32_t bb = bin_of_rank(start, nbins, e.rank);
-      out[e.out] = Traits<OutT>::value(B[gofs[bb] + (e.rank - start[bb])]);
+      out[e.out] = Traits<OutT>::value(mn + (K)bin_of_rank(start, nbins, e.rank));
     }
     __syncthreads();
+    return true;
+  }
+  if (!fits) {  // the needed bins do not fit: the caller re-selects this slot
+    __syncthreads();
+    return false;
+  }
+
+  // ---- gather the needed bins
+  {
+    auto put = [&](K k) {
+      const uint32_t bb = min((uint32_t)((k - mn) >> sh), nbins - 1u);
+      const uint32_t g = gofs[bb];
+      if (g != kNoSlot) B[g + atomicAdd(&cur[bb], 1u)] = k;
+    };
+    uint32_t i = tid;
+    for (; i + 7 * blockDim.x < size; i += 8 * blockDim.x) {
+      K kk[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) kk[q] = src[i + q * blockDim.x];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) put(kk[q]);
+    }
+    for (; i < size; i += blockDim.x) put(src[i]);
+  }
+  __syncthreads();
+
+  // ---- sort each needed bin: a warp per bin of 2..32 keys
+  const uint32_t nsmall = s_nsmall;
+  for (uint32_t q = warp; q < nsmall; q += nwarps) {
+    const uint32_t bb = small[q];
+    const uint32_t g = gofs[bb], c = hist[bb];
+    K v = lane < c ? B[g + lane] : KeyMax<K>::v;
+    v = warp_bitonic32(v);
+    if (lane < c) B[g + lane] = v;
+  }
+  // larger bins: the whole CTA, one at a time
+  const uint32_t nbig = s_nbig;
+  for (uint32_t q = 0; q < (nbig <= (uint32_t)kMaxBig ? nbig : nbins); ++q) {
+    const uint32_t bb = nbig <= (uint32_t)kMaxBig ? big[q] : q;
+    const uint32_t g = gofs[bb], c = hist[bb];
+    if (g == kNoSlot || c <= 32) continue;
+    uint32_t P = 64;
+    while (P < c) P <<= 1;
+    __syncthreads();
+    for (uint32_t i = tid; i < P; i += blockDim.x) T[i] = i < c ? B[g + i] : KeyMax<K>::v;
+    __syncthreads();
+    bitonic_sort_smem(T, P);
+    for (uint32_t i = tid; i < c; i += blockDim.x) B[g + i] = T[i];
+  }
+  __syncthreads();
+
+  // ---- answer
+  for (uint32_t j = tid; j < m; j += blockDim.x) {
+    const Req e = rq[j];
+    const uint32_t bb = bin_of_rank(start, nbins, e.rank);
+    out[e.out] = Traits<OutT>::value(B[gofs[bb] + (e.rank - start[bb])]);
+  }
+  __syncthreads();
+  return true;
+}
+
+template <class K, class OutT>
+__global__ void __launch_bounds__(kFinThreads)
+    k_finish(const K *__restrict__ surv, Ctrl *ctrl, const uint64_t *__restrict__ seg_off,
+             const uint32_t *__restrict__ seg_size, const K *__restrict__ seg_lo,
+             const K *__restrict__ seg_hi, const uint32_t *__restrict__ kstart,
+             const uint32_t *__restrict__ kcnt, const Req *__restrict__ klist,
+             uint32_t *__restrict__ deferred, uint32_t bcap, OutT *__restrict__ out) {
+  extern __shared__ uint4 smem_raw[];
+  if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
+  const uint32_t num_slots = ctrl->num_slots;
+  for (uint32_t slot = blockIdx.x; slot < num_slots; slot += gridDim.x) {
+    const bool done = finish_slot<K, OutT>(surv + seg_off[slot], seg_size[slot], seg_lo[slot],
+                                           seg_hi[slot], klist + kstart[slot], kcnt[slot], bcap,
+                                           reinterpret_cast<uint32_t *>(smem_raw), out);
+    if (!done && threadIdx.x == 0) {
+      const uint32_t d = atomicAdd(&ctrl->deferred_count, 1u);
+      deferred[d] = slot;
+      atomicOr(&ctrl->status, ST_DEFERRED);
+    }
   }
 }
 

@@ -5,6 +5,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <map>
 #include <memory>
 #include <mutex>
 
@@ -12,6 +13,13 @@
 #include "ggks_device.cuh"
 
 namespace ggks {
+
+// Tunables of the batched path: bucket budget of a problem is about n / div
+// buckets; tiles of the (problem, tile) queue hold `tile` elements.
+struct BatchTune {
+  uint32_t div = 1024;
+  uint32_t tile = 1u << 18;
+};
 
 // A context owns one device, one stream, a device arena (per-call scratch), a
 // survivor buffer, a device staging buffer for host-vector inputs, pinned host
@@ -36,6 +44,17 @@ struct Context {
   std::unique_ptr<Context> child;
   int depth = 0;
 
+  // batched selection: device workspace, pinned staging, kernel events and
+  // the autotuner's choices per batch shape
+  char *barena = nullptr;
+  size_t barena_bytes = 0;
+  char *bpin = nullptr;
+  size_t bpin_bytes = 0;
+  cudaEvent_t bev0 = nullptr, bev1 = nullptr;
+  std::map<uint64_t, BatchTune> tuned;
+  BatchTune last_tune;
+  BatchTune pinned_tune{0, 0};  // div != 0: used for every batch (no autotuning)
+
   ggks_stats stats{};
   bool profiling = false;
   bool events_ready = false;
@@ -53,6 +72,8 @@ Context *default_context(int device, int *status);
 Context *child_of(Context &ctx, int *status);
 
 cudaError_t ensure_arena(Context &ctx, size_t bytes);
+cudaError_t ensure_buffer(Context &ctx, char **p, size_t *have, size_t bytes);
+cudaError_t ensure_pinned(Context &ctx, char **p, size_t *have, size_t bytes);
 cudaError_t ensure_surv(Context &ctx, size_t bytes);
 cudaError_t ensure_dvec(Context &ctx, size_t bytes);
 cudaError_t ensure_pin(Context &ctx, size_t bytes);
@@ -78,5 +99,26 @@ struct ReqSource {
 template <class InT, class OutT>
 int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint32_t num_req,
            OutT *d_out_user, const OutT **host_results, cudaStream_t s, const InT *ingest);
+
+// One batch: problem p is vecs[p] (device, n[p] elements) with outputs
+// [k_off[p], k_off[p + 1]); output j asks for the k[j]-th largest of its
+// problem, or, when k is null, output k_off[p] + i is the (i + 1)-th largest
+// (top-k).  k values are already checked to lie in [1, n[p]].
+struct BatchInput {
+  const void *const *vecs = nullptr;
+  const uint64_t *n = nullptr;
+  uint32_t num_problems = 0;
+  const uint32_t *k_off = nullptr;
+  const uint32_t *k = nullptr;
+};
+
+// Run one batch in one cooperative launch (plus re-runs on survivor overflow
+// and a recursive re-selection of oversized segments).  Results go to
+// d_out_user (device) when it is not null, else to the context's workspace;
+// h_out (host), when not null, receives them too.  *kernel_ms: device time of
+// the launches.  The stream is synchronised.
+template <class T>
+int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cudaStream_t s,
+                 const BatchTune &tune, float *kernel_ms);
 
 }  // namespace ggks

@@ -23,8 +23,11 @@ LIB_PATH = os.path.join(HERE, "libggks_gb300.so")
 
 OK, INVALID_ARG, OOM, CUDA_ERROR, TIMEOUT, INTERNAL, NO_DEVICE, UNSUPPORTED = range(8)
 FLAG_OUT_DEVICE = 1
+FLAG_AUTOTUNE = 2
 NUM_PASSES = 6
 PASS_NAMES = ("sample", "hist", "scan", "plan", "compact", "finish")
+NUM_BATCH_PHASES = 5
+BATCH_PHASE_NAMES = ("table", "hist", "plan", "compact", "finish")
 
 _SFX = {np.dtype(np.float32): "f32", np.dtype(np.float64): "f64", np.dtype(np.uint32): "u32"}
 
@@ -46,7 +49,9 @@ class Stats(ctypes.Structure):
                 ("pass_ms", ctypes.c_double * NUM_PASSES),
                 ("bytes_in", ctypes.c_uint64), ("survivors", ctypes.c_uint64),
                 ("retries", ctypes.c_uint64), ("recursions", ctypes.c_uint64),
-                ("host_ingested", ctypes.c_uint64), ("host_staged", ctypes.c_uint64)]
+                ("host_ingested", ctypes.c_uint64), ("host_staged", ctypes.c_uint64),
+                ("batch_calls", ctypes.c_uint64), ("batch_problems", ctypes.c_uint64),
+                ("batch_phase_ms", ctypes.c_double * NUM_BATCH_PHASES)]
 
     def as_dict(self):
         return {"calls": self.calls, "launches": self.launches,
@@ -54,7 +59,9 @@ class Stats(ctypes.Structure):
                 "pass_ms": dict(zip(PASS_NAMES, list(self.pass_ms))),
                 "bytes_in": self.bytes_in, "survivors": self.survivors,
                 "retries": self.retries, "recursions": self.recursions,
-                "host_ingested": self.host_ingested, "host_staged": self.host_staged}
+                "host_ingested": self.host_ingested, "host_staged": self.host_staged,
+                "batch_calls": self.batch_calls, "batch_problems": self.batch_problems,
+                "batch_phase_ms": dict(zip(BATCH_PHASE_NAMES, list(self.batch_phase_ms)))}
 
 
 # every symbol declared in include/ggks.h
@@ -66,6 +73,9 @@ EXPORTS = [
     "ggks_context_create", "ggks_context_destroy", "ggks_context_get_stats",
     "ggks_context_reset_stats", "ggks_context_set_profiling", "ggks_status_string",
     "ggks_version", "ggks_multiselect_noalloc_f32",
+    "ggks_multiselect_batch_f32", "ggks_multiselect_batch_f64", "ggks_multiselect_batch_u32",
+    "ggks_topk_batch_f32", "ggks_topk_batch_f64", "ggks_topk_batch_u32",
+    "ggks_batch_last_tuning", "ggks_batch_set_tuning",
 ]
 
 _lib = None
@@ -88,6 +98,18 @@ def lib():
             f = getattr(L, nm + sfx)
             f.argtypes = [P, U64, U32, P, ctypes.POINTER(Opts)]
             f.restype = ctypes.c_int
+    for sfx in ("f32", "f64", "u32"):
+        f = getattr(L, "ggks_multiselect_batch_" + sfx)
+        f.argtypes = [P, P, U32, P, P, P, ctypes.POINTER(Opts)]
+        f.restype = ctypes.c_int
+        f = getattr(L, "ggks_topk_batch_" + sfx)
+        f.argtypes = [P, P, U32, P, P, ctypes.POINTER(Opts)]
+        f.restype = ctypes.c_int
+    L.ggks_batch_last_tuning.argtypes = [P, ctypes.POINTER(ctypes.c_uint32),
+                                         ctypes.POINTER(ctypes.c_uint32)]
+    L.ggks_batch_last_tuning.restype = ctypes.c_int
+    L.ggks_batch_set_tuning.argtypes = [P, U32, U32]
+    L.ggks_batch_set_tuning.restype = ctypes.c_int
     L.ggks_multiselect_noalloc_f32.argtypes = [P, U64, P, U32, P, P]
     L.ggks_multiselect_noalloc_f32.restype = ctypes.c_int
     L.ggks_context_create.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
@@ -244,6 +266,75 @@ def topk_host(h_vec, K, ctx=None, stream=None, out=None):
         h_vec.ctypes.data, h_vec.size, int(K), out.ctypes.data, ctypes.byref(o))
     _check(st, "topk_host")
     return out
+
+
+def _batch_arrays(ptrs, ns):
+    ptrs = np.ascontiguousarray(np.asarray(ptrs, dtype=np.uint64))
+    ns = np.ascontiguousarray(np.asarray(ns, dtype=np.uint64))
+    assert ptrs.size == ns.size
+    return ptrs, ns
+
+
+def multiselect_batch_ptr(ptrs, ns, dtype, k_lists, ctx=None, stream=None, autotune=False,
+                          out_device_ptr=None):
+    """Batched multiselect: problem p is the device vector at ptrs[p] with
+    ns[p] elements of dtype and the k list k_lists[p] (k-th largest).  One
+    persistent launch selects every problem.  Returns a list of host arrays
+    (one per problem), or None when writing to out_device_ptr (outputs
+    concatenated in problem order)."""
+    dtype = np.dtype(dtype)
+    ptrs, ns = _batch_arrays(ptrs, ns)
+    sizes = np.array([len(k) for k in k_lists], dtype=np.int64)
+    off = np.zeros(len(k_lists) + 1, dtype=np.uint32)
+    np.cumsum(sizes, out=off[1:])
+    ks = (np.concatenate([np.asarray(k, dtype=np.uint32) for k in k_lists])
+          if len(k_lists) else np.zeros(0, np.uint32))
+    ks = np.ascontiguousarray(ks, dtype=np.uint32)
+    flags = FLAG_AUTOTUNE if autotune else 0
+    if out_device_ptr is not None:
+        flags |= FLAG_OUT_DEVICE
+        optr, out = out_device_ptr, None
+    else:
+        out = np.empty(int(off[-1]), dtype=dtype)
+        optr = out.ctypes.data
+    o = _opts(ctx, stream, flags)
+    st = getattr(lib(), "ggks_multiselect_batch_" + _SFX[dtype])(
+        ptrs.ctypes.data, ns.ctypes.data, ptrs.size, off.ctypes.data,
+        ks.ctypes.data if ks.size else None, ctypes.c_void_p(optr), ctypes.byref(o))
+    _check(st, "multiselect_batch")
+    if out is None:
+        return None
+    return [out[off[p]:off[p + 1]] for p in range(ptrs.size)]
+
+
+def topk_batch_ptr(ptrs, ns, dtype, Ks, ctx=None, stream=None, autotune=False):
+    """Batched top-k: the Ks[p] largest of each device vector, descending."""
+    dtype = np.dtype(dtype)
+    ptrs, ns = _batch_arrays(ptrs, ns)
+    Ks = np.ascontiguousarray(np.asarray(Ks, dtype=np.uint32))
+    off = np.zeros(Ks.size + 1, dtype=np.int64)
+    np.cumsum(Ks, out=off[1:])
+    out = np.empty(int(off[-1]), dtype=dtype)
+    o = _opts(ctx, stream, FLAG_AUTOTUNE if autotune else 0)
+    st = getattr(lib(), "ggks_topk_batch_" + _SFX[dtype])(
+        ptrs.ctypes.data, ns.ctypes.data, ptrs.size, Ks.ctypes.data, out.ctypes.data,
+        ctypes.byref(o))
+    _check(st, "topk_batch")
+    return [out[off[p]:off[p + 1]] for p in range(ptrs.size)]
+
+
+def batch_set_tuning(ctx=None, div=0, tile=0):
+    """Pin the batched path's bucket divisor and tile size on a context
+    (div = 0: back to the autotuner / default)."""
+    _check(lib().ggks_batch_set_tuning(_h(ctx), int(div), int(tile)), "batch_set_tuning")
+
+
+def batch_last_tuning(ctx=None):
+    """(div, tile) used by the context's last batched call."""
+    d, t = ctypes.c_uint32(), ctypes.c_uint32()
+    _check(lib().ggks_batch_last_tuning(_h(ctx), ctypes.byref(d), ctypes.byref(t)),
+           "batch_last_tuning")
+    return d.value, t.value
 
 
 # ---------------------------------------------------------------------------

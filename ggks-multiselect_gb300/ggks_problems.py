@@ -234,3 +234,35 @@ def k_sectioned(n, count, seed):
     u = _rng(seed).random()
     start = max(1, int(u * (n - count)))
     return (start + np.arange(count, dtype=np.uint64)).clip(1, n).astype(np.uint32)
+
+
+# ---------------------------------------------------------------------------
+# batched workload: many independent vectors of uneven lengths
+# ---------------------------------------------------------------------------
+BATCH_DISTS = ("uniform", "normal", "cauchy", "uint_valued")
+
+
+def batch_problems(count, seed, lo_log2=10.0, hi_log2=22.0, k_lo=1, k_hi=64):
+    """The problem list of a batched multiselect: lengths log-uniform in
+    [2^lo_log2, 2^hi_log2], each vector's distribution drawn uniformly from
+    BATCH_DISTS (float32: uniform [0,1), normal(0,1), standard Cauchy,
+    integer-valued floats in [0,256)), each with k_lo..k_hi k's drawn
+    uniformly from [1, length].  Returns a list of dicts with keys dist, n,
+    seed (the vector's data seed) and k (uint32 array)."""
+    r = _rng(seed)
+    lens = np.floor(2.0 ** r.uniform(lo_log2, hi_log2, count)).astype(np.int64)
+    lens = np.clip(lens, 1, None)
+    dists = r.integers(0, len(BATCH_DISTS), count)
+    nks = r.integers(k_lo, k_hi + 1, count)
+    out = []
+    for i in range(count):
+        n = int(lens[i])
+        ks = r.integers(1, n + 1, int(nks[i]), dtype=np.int64).astype(np.uint32)
+        out.append({"dist": BATCH_DISTS[int(dists[i])], "n": n, "seed": int(seed) * 100003 + i,
+                    "k": ks})
+    return out
+
+
+def batch_vector(prob):
+    """The float32 data of one batch problem (numpy, seeded)."""
+    return generate("f32", prob["dist"], prob["n"], prob["seed"])

@@ -137,6 +137,59 @@ int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, const uint32_t 
                                  uint32_t num_k, float *d_out, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Batched selection                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* No counterpart in the reference, which selects one vector per call
+ * (bucketMultiselectWrapper, bucketMultiselect.cu:837-871) and compares
+ * algorithms per size in an offline loop (analyzeMultiselect.cu:209-274).
+ * Selects many independent vectors of uneven lengths, each with its own k
+ * list, in one persistent kernel launch driven by a (problem, tile) work
+ * queue.  Results are bit-exact and equal, output for output, to separate
+ * ggks_multiselect_* calls.
+ *   d_vecs[p]: device vector of n[p] elements (p < num_problems), aligned to
+ *   the element size.  k_offsets: num_problems + 1 non-decreasing entries,
+ *   k_offsets[0] = 0; the outputs of problem p are
+ *   out[k_offsets[p] .. k_offsets[p + 1]) and out[j] is the h_k[j]-th largest
+ *   (1-based) of its problem's vector.  A problem without outputs is skipped
+ *   (its vector may be NULL, n 0).  out: host array of k_offsets[num_problems]
+ *   values, or device memory with GGKS_FLAG_OUT_DEVICE.
+ * opts->flags & GGKS_FLAG_AUTOTUNE: the first call for a batch shape (element
+ * type, total elements, problems, outputs per problem, each rounded to a power
+ * of two) times every candidate bucket budget / tile size and keeps the
+ * fastest for later calls of that shape on the context. */
+#define GGKS_FLAG_AUTOTUNE 2u
+int ggks_multiselect_batch_f32(const float *const *d_vecs, const uint64_t *n,
+                               uint32_t num_problems, const uint32_t *k_offsets,
+                               const uint32_t *h_k, float *out, const ggks_opts *opts);
+int ggks_multiselect_batch_f64(const double *const *d_vecs, const uint64_t *n,
+                               uint32_t num_problems, const uint32_t *k_offsets,
+                               const uint32_t *h_k, double *out, const ggks_opts *opts);
+int ggks_multiselect_batch_u32(const uint32_t *const *d_vecs, const uint64_t *n,
+                               uint32_t num_problems, const uint32_t *k_offsets,
+                               const uint32_t *h_k, uint32_t *out, const ggks_opts *opts);
+
+/* Batched top-k (no reference counterpart; per vector it matches
+ * ggks_topk_*): problem p's K[p] largest values, descending, go to
+ * out[off_p .. off_p + K[p]) with off_p = K[0] + ... + K[p - 1].  K[p] = 0
+ * skips the problem; K[p] <= n[p]. */
+int ggks_topk_batch_f32(const float *const *d_vecs, const uint64_t *n, uint32_t num_problems,
+                        const uint32_t *K, float *out, const ggks_opts *opts);
+int ggks_topk_batch_f64(const double *const *d_vecs, const uint64_t *n, uint32_t num_problems,
+                        const uint32_t *K, double *out, const ggks_opts *opts);
+int ggks_topk_batch_u32(const uint32_t *const *d_vecs, const uint64_t *n,
+                        uint32_t num_problems, const uint32_t *K, uint32_t *out,
+                        const ggks_opts *opts);
+
+/* The bucket divisor (about n / div buckets per problem) and tile size
+ * (elements per work item) used by the context's last batched call. */
+int ggks_batch_last_tuning(ggks_context *ctx, uint32_t *div, uint32_t *tile);
+/* Pin the divisor (16 <= div <= 2^24) and tile size (>= 64 elements, rounded
+ * down to a multiple of 64) for every later batched call on the context,
+ * instead of the autotuner's choice; div = 0 unpins. */
+int ggks_batch_set_tuning(ggks_context *ctx, uint32_t div, uint32_t tile);
+
+/* ------------------------------------------------------------------------ */
 /* Contexts, statistics, utilities                                           */
 /* ------------------------------------------------------------------------ */
 
@@ -149,6 +202,7 @@ int ggks_context_destroy(ggks_context *ctx);
 
 /* Per-pass statistics of a context, accumulated since the last reset. */
 #define GGKS_NUM_PASSES 6
+#define GGKS_NUM_BATCH_PHASES 5
 typedef struct ggks_stats {
   uint64_t calls;                     /* selection calls completed */
   uint64_t launches;                  /* kernels launched by this library */
@@ -160,7 +214,18 @@ typedef struct ggks_stats {
   uint64_t recursions;                /* oversized segments re-selected */
   uint64_t host_ingested;             /* host vectors read in place by the first pass */
   uint64_t host_staged;               /* host vectors copied to the device first */
+  uint64_t batch_calls;               /* batched calls completed */
+  uint64_t batch_problems;            /* problems selected by batched calls */
+  double batch_phase_ms[GGKS_NUM_BATCH_PHASES]; /* device time per batch phase */
 } ggks_stats;
+
+/* phase indices of ggks_stats.batch_phase_ms (one persistent launch; each
+ * phase is timed from the grid barrier before it to the one after it) */
+#define GGKS_BATCH_TABLE 0    /* samples + splitter table of every problem */
+#define GGKS_BATCH_HIST 1     /* histogram rows of every (problem, tile) */
+#define GGKS_BATCH_PLAN 2     /* per-problem scan, k -> bucket, slots */
+#define GGKS_BATCH_COMPACT 3  /* compaction of every (problem, tile) */
+#define GGKS_BATCH_FINISH 4   /* every slot's in-shared-memory selection */
 
 /* pass indices of ggks_stats.pass_* */
 #define GGKS_PASS_SAMPLE 0   /* sample + splitter table build */

@@ -111,3 +111,44 @@ def test_cpp_reference_mirror_header_compiles(lib, tmp_path):
                         ggks.LIB_PATH, "-o", str(exe), "-Wl,-rpath," + os.path.dirname(ggks.LIB_PATH)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("sfx,dt", [("f32", np.float32), ("f64", np.float64), ("u32", np.uint32)])
+def test_batch_invalid_arguments_rejected_without_device(lib, sfx, dt):
+    """The batched entry points validate every problem before touching a
+    device."""
+    import ggks
+    f = getattr(lib, "ggks_multiselect_batch_" + sfx)
+    t = getattr(lib, "ggks_topk_batch_" + sfx)
+    o = ggks.Opts()
+    fake = 4096  # never dereferenced: validation fails first
+    ptrs = np.array([fake, fake], dtype=np.uint64)
+    ns = np.array([10, 20], dtype=np.uint64)
+    off = np.array([0, 2, 3], dtype=np.uint32)
+    ks = np.array([1, 10, 20], dtype=np.uint32)
+    out = np.zeros(3, dtype=dt)
+
+    def call(p=ptrs, n=ns, o_=off, k=ks, num=2):
+        return f(p.ctypes.data if p is not None else None, n.ctypes.data, num,
+                 o_.ctypes.data if o_ is not None else None,
+                 k.ctypes.data if k is not None else None, out.ctypes.data, ctypes.byref(o))
+
+    assert call(num=0) == ggks.INVALID_ARG
+    assert call(p=None) == ggks.INVALID_ARG
+    assert call(o_=None) == ggks.INVALID_ARG
+    assert call(k=None) == ggks.INVALID_ARG
+    assert call(o_=np.array([1, 2, 3], dtype=np.uint32)) == ggks.INVALID_ARG   # k_offsets[0] != 0
+    assert call(o_=np.array([0, 3, 2], dtype=np.uint32)) == ggks.INVALID_ARG   # decreasing
+    assert call(k=np.array([0, 10, 20], dtype=np.uint32)) == ggks.INVALID_ARG  # k = 0
+    assert call(k=np.array([1, 11, 20], dtype=np.uint32)) == ggks.INVALID_ARG  # k > n
+    assert call(n=np.array([10, 0], dtype=np.uint64)) == ggks.INVALID_ARG      # n = 0 with k's
+    assert call(p=np.array([fake, 0], dtype=np.uint64)) == ggks.INVALID_ARG    # null vector
+    mis = np.array([fake + 1, fake], dtype=np.uint64)
+    assert call(p=mis) == ggks.INVALID_ARG                                     # misaligned
+    # no outputs at all: nothing to do
+    assert call(o_=np.array([0, 0, 0], dtype=np.uint32)) == ggks.OK
+    K = np.array([11, 3], dtype=np.uint32)                                    # K > n
+    assert t(ptrs.ctypes.data, ns.ctypes.data, 2, K.ctypes.data, out.ctypes.data,
+             ctypes.byref(o)) == ggks.INVALID_ARG
+    assert t(ptrs.ctypes.data, ns.ctypes.data, 2, None, out.ctypes.data,
+             ctypes.byref(o)) == ggks.INVALID_ARG
