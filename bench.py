@@ -13,6 +13,11 @@ Metric: input GB/s per multiselect = n * sizeof(T) / time of one wrapper call
 metric through the host-vector entry point with the 1 GiB vector in pinned host
 memory, so the host-to-device copy is inside every step.
 
+"batched": the batched workload -- 4096 resident float32 vectors of log-uniform
+lengths in [2^10, 2^22] with 1-64 k's each -- selected by one batched call (one
+persistent launch), against 4096 sequential ggks_multiselect_f32 calls on the
+same vectors (requests/s, bit-exact comparison).
+
 Under torchrun (N > 1) every rank runs an independent replica on its own GPU
 (the path does not shard: replicas only); value = all ranks' bytes / max time.
 
@@ -49,6 +54,8 @@ def parse():
     ap.add_argument("--impl", default="ggks", choices=["ggks", "reference"])
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--log2n", type=int, default=N_LOG2)
     return ap.parse_args()
 
@@ -320,6 +327,11 @@ def run_ggks(args):
     variants = {}
     if not args.no_variants and rank == 0:
         variants = run_variants(torch, ggks, gp, ctx, stream, sptr, dev, args.log2n)
+    batched = served = None
+    if not args.no_batched and rank == 0:
+        batched = run_batched(torch, ggks, gp, dev, sptr)
+    if not args.no_served and rank == 0:
+        served = run_served(torch, ggks, gp, dev, sptr)
 
     if rank == 0:
         line = {
@@ -343,6 +355,10 @@ def run_ggks(args):
         }
         if variants:
             line["variants"] = variants
+        if batched:
+            line["batched"] = batched
+        if served:
+            line["served"] = served
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(x, k)
         print(json.dumps(line), flush=True)
@@ -387,6 +403,192 @@ def run_variants(torch, ggks, gp, ctx, stream, sptr, dev, log2n):
     res["topk_f32_2^26_K65536"] = {"n": n, "ms": round(ms, 4),
                                    "GB/s": round(x.nbytes / (ms * 1e-3) / 1e9, 1)}
     return res
+
+
+def run_batched(torch, ggks, gp, dev, sptr, count=4096):
+    """The batched workload: `count` float32 vectors with log-uniform lengths
+    in [2^10, 2^22], four distributions, 1-64 k's each (seed 1), resident on
+    the device.  One batched call (one persistent launch) against `count`
+    sequential ggks_multiselect_f32 calls on the same vectors; outputs are
+    compared bit for bit."""
+    probs = gp.batch_problems(count, seed=1)
+    vecs = gp.batch_vectors_device(probs, seed=1, device=dev)
+    torch.cuda.synchronize()
+    ptrs = [v.data_ptr() for v in vecs]
+    ns = [v.numel() for v in vecs]
+    ks = [np.ascontiguousarray(p["k"], dtype=np.uint32) for p in probs]
+    total = int(sum(ns))
+    reqs = int(sum(k.size for k in ks))
+    ctx = ggks.Context(dev.index or 0)
+    b = ggks.PreparedBatch(ptrs, ns, np.float32, ks, ctx=ctx, stream=sptr, autotune=True)
+    t0 = time.perf_counter()
+    b()  # first call of this batch shape: the autotuner times every candidate
+    tune_s = time.perf_counter() - t0
+    batch_out = b().copy()
+    ctx.reset_stats()
+    wall = []
+    for _ in range(7):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b()
+        wall.append(time.perf_counter() - t0)
+    st = ctx.stats()
+    calls = max(1, st["batch_calls"])
+    phase_ms = {k: round(v / calls, 4) for k, v in st["batch_phase_ms"].items()}
+    t_batch = statistics.median(wall)
+
+    # sequential plain calls on the same resident vectors
+    L = ggks.lib()
+    f = L.ggks_multiselect_f32
+    o = ggks._opts(ctx, sptr)
+    outs = [np.empty(k.size, dtype=np.float32) for k in ks]
+    args_list = [(ctypes.c_void_p(p), int(n), k.ctypes.data, k.size, out.ctypes.data)
+                 for p, n, k, out in zip(ptrs, ns, ks, outs)]
+    for a in args_list[:32]:
+        f(*a, ctypes.byref(o))
+    torch.cuda.synchronize()
+    seq = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        for a in args_list:
+            st_ = f(*a, ctypes.byref(o))
+            if st_ != 0:
+                raise RuntimeError(f"plain call failed: {st_}")
+        seq.append(time.perf_counter() - t0)
+    t_seq = min(seq)
+    exact = all(np.array_equal(a.view(np.uint32), c.view(np.uint32))
+                for a, c in zip(b.split(batch_out), outs))
+    tune = ggks.batch_last_tuning(ctx)
+    ctx.close()
+    del vecs
+    torch.cuda.empty_cache()
+    return {
+        "workload": f"{count} float32 vectors, lengths log-uniform in [2^10, 2^22] (seed 1), "
+                    "distributions uniform[0,1) / normal(0,1) / Cauchy / integer-valued "
+                    "[0,256), 1-64 k's each uniform in [1, len]; resident in HBM",
+        "problems": count, "elements": total, "outputs": reqs,
+        "req_per_s": round(count / t_batch, 1), "ms_per_batch": round(t_batch * 1e3, 3),
+        "GB/s": round(total * 4 / t_batch / 1e9, 1),
+        "kernel_ms": round(sum(phase_ms.values()), 3), "phase_ms": phase_ms,
+        "launches_per_batch": round(st["launches"] / calls, 2),
+        "survivors_per_batch": int(st["survivors"] // calls),
+        "recursions_per_batch": round(st["recursions"] / calls, 2),
+        "tuning": {"div": tune[0], "tile": tune[1], "autotune_s": round(tune_s, 3)},
+        "sequential_plain": {"ms": round(t_seq * 1e3, 2), "req_per_s": round(count / t_seq, 1),
+                             "entry": "ggks_multiselect_f32, one call per vector"},
+        "speedup_req_per_s": round(t_seq / t_batch, 2),
+        "bit_exact_vs_plain": bool(exact),
+        "timing": "host wall clock per call (synchronous C-ABI call: planning, upload, launch, "
+                  "results); median of 7",
+    }
+
+
+SERVE_RATES = (1000, 5000, 20000, 50000)
+
+
+def run_served(torch, ggks, gp, dev, sptr, per_rate=1500):
+    """The served workload: Poisson arrivals at each rate of SERVE_RATES over
+    a resident pool of mixed vectors (float32 : uint32 : float64 = 6 : 3 : 1,
+    lengths log-uniform in [2^12, 2^26]); 70% multiselects with 8-1024 k's,
+    30% top-k with K in [16, 4096]; HBM admission cap 64 GB.  The served arm
+    submits every request at its arrival time to a ggks_server (continuous
+    batching); the sequential arm runs plain calls in arrival order, each
+    starting at its arrival time or when the previous one returns.  Latency =
+    completion - scheduled arrival."""
+    DT = {"f32": np.float32, "u32": np.uint32, "f64": np.float64}
+    pool = gp.serving_pool({"f32": 48, "u32": 24, "f64": 8}, seed=7, device=dev)
+    torch.cuda.synchronize()
+    sizes = {dt: [v.numel() for v in vs] for dt, vs in pool.items()}
+    ptrs = {dt: [v.data_ptr() for v in vs] for dt, vs in pool.items()}
+    L = ggks.lib()
+    ctx = ggks.Context(dev.index or 0)
+    o = ggks._opts(ctx, sptr)
+    fms = {dt: getattr(L, "ggks_multiselect_" + dt) for dt in DT}
+    ftk = {dt: getattr(L, "ggks_topk_" + dt) for dt in DT}
+
+    def pct(a, q):
+        return round(float(np.percentile(np.asarray(a) * 1e3, q)), 3)
+
+    out = {"workload": "Poisson arrivals; requests 70% multiselect (8-1024 k's) / 30% top-k "
+                       "(K in [16,4096]); float32:uint32:float64 = 6:3:1 over a resident pool "
+                       "of 80 vectors, lengths log-uniform in [2^12, 2^26], mixed distributions; "
+                       "HBM admission cap 64 GB",
+           "requests_per_rate": per_rate, "rates": {}}
+    all_exact = True
+    for rate in SERVE_RATES:
+        trace = gp.serving_trace(sizes, rate, per_rate, seed=rate)
+        bufs = []
+        for q in trace:
+            num = q["K"] if q["k"] is None else q["k"].size
+            bufs.append((np.empty(num, dtype=DT[q["dtype"]]), np.empty(num, dtype=DT[q["dtype"]])))
+        in_bytes = sum(sizes[q["dtype"]][q["vec"]] * np.dtype(DT[q["dtype"]]).itemsize for q in trace)
+
+        # ---- sequential plain calls
+        seq_lat = []
+        t0 = time.perf_counter() + 0.01
+        for q, (so, _) in zip(trace, bufs):
+            ta = t0 + q["t"]
+            while time.perf_counter() < ta:
+                pass
+            dt = q["dtype"]
+            p, n = ptrs[dt][q["vec"]], sizes[dt][q["vec"]]
+            if q["k"] is None:
+                st = ftk[dt](ctypes.c_void_p(p), n, q["K"], so.ctypes.data, ctypes.byref(o))
+            else:
+                st = fms[dt](ctypes.c_void_p(p), n, q["k"].ctypes.data, q["k"].size,
+                             so.ctypes.data, ctypes.byref(o))
+            if st != 0:
+                raise RuntimeError(f"plain call failed: {st}")
+            seq_lat.append(time.perf_counter() - ta)
+        seq_span = (t0 + trace[-1]["t"] + seq_lat[-1]) - t0
+
+        # ---- served: submit at arrival times, wait in order
+        srv = ggks.Server(dev.index or 0, hbm_cap_bytes=64 << 30)
+        tickets = [None] * len(trace)
+        sub_t = [0.0] * len(trace)
+
+        def submitter():
+            for i, q in enumerate(trace):
+                ta = t1 + q["t"]
+                while time.perf_counter() < ta:
+                    pass
+                dt = q["dtype"]
+                sub_t[i] = time.perf_counter() - ta
+                tickets[i] = srv.submit(ptrs[dt][q["vec"]], sizes[dt][q["vec"]], DT[dt],
+                                        k=q["k"], K=q["K"], out=bufs[i][1])
+
+        t1 = time.perf_counter() + 0.01
+        th = threading.Thread(target=submitter)
+        th.start()
+        srv_lat = [0.0] * len(trace)
+        for i in range(len(trace)):
+            while tickets[i] is None:
+                time.sleep(50e-6)
+            _, lat_ms = srv.wait(tickets[i])
+            srv_lat[i] = sub_t[i] + lat_ms * 1e-3
+        th.join()
+        sst = srv.stats()
+        srv.close()
+        srv_span = max(q["t"] + lat for q, lat in zip(trace, srv_lat))
+        exact = all(np.array_equal(a.view(np.uint8), b.view(np.uint8)) for a, b in bufs)
+        all_exact &= exact
+        out["rates"][str(rate)] = {
+            "offered_req_per_s": rate,
+            "served": {"req_per_s": round(len(trace) / srv_span, 1),
+                       "p50_ms": pct(srv_lat, 50), "p99_ms": pct(srv_lat, 99),
+                       "GB/s": round(in_bytes / srv_span / 1e9, 1),
+                       "batches": sst["batches"], "launches": sst["launches"],
+                       "mean_batch": round(sst["batched_requests"] / max(1, sst["batches"]), 2)},
+            "sequential_plain": {"req_per_s": round(len(trace) / seq_span, 1),
+                                 "p50_ms": pct(seq_lat, 50), "p99_ms": pct(seq_lat, 99)},
+            "req_per_s_ratio": round(seq_span / srv_span, 2),
+            "bit_exact_vs_plain": bool(exact),
+        }
+    out["bit_exact_vs_plain"] = bool(all_exact)
+    ctx.close()
+    del pool
+    torch.cuda.empty_cache()
+    return out
 
 
 def read_traffic(kernel):

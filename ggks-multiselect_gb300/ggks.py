@@ -64,6 +64,31 @@ class Stats(ctypes.Structure):
                 "batch_phase_ms": dict(zip(BATCH_PHASE_NAMES, list(self.batch_phase_ms)))}
 
 
+DTYPE_CODES = {np.dtype(np.float32): 0, np.dtype(np.float64): 1, np.dtype(np.uint32): 2}
+REQ_TOPK = 1
+REQ_HOST_VECTOR = 2
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("max_batch", ctypes.c_uint32),
+                ("hbm_cap_bytes", ctypes.c_uint64)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("dtype", ctypes.c_int32), ("flags", ctypes.c_uint32), ("vec", ctypes.c_void_p),
+                ("n", ctypes.c_uint64), ("k", ctypes.c_void_p), ("num_k", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in (
+        "submitted", "completed", "batches", "batched_requests", "max_batch_seen", "launches",
+        "uploads", "upload_bytes", "peak_bytes", "in_flight_bytes")]
+
+    def as_dict(self):
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
 # every symbol declared in include/ggks.h
 EXPORTS = [
     "ggks_multiselect_f32", "ggks_multiselect_f64", "ggks_multiselect_u32",
@@ -76,6 +101,8 @@ EXPORTS = [
     "ggks_multiselect_batch_f32", "ggks_multiselect_batch_f64", "ggks_multiselect_batch_u32",
     "ggks_topk_batch_f32", "ggks_topk_batch_f64", "ggks_topk_batch_u32",
     "ggks_batch_last_tuning", "ggks_batch_set_tuning",
+    "ggks_server_create", "ggks_server_destroy", "ggks_server_submit", "ggks_server_wait",
+    "ggks_server_get_stats", "ggks_server_set_tuning",
 ]
 
 _lib = None
@@ -110,6 +137,14 @@ def lib():
     L.ggks_batch_last_tuning.restype = ctypes.c_int
     L.ggks_batch_set_tuning.argtypes = [P, U32, U32]
     L.ggks_batch_set_tuning.restype = ctypes.c_int
+    L.ggks_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]
+    L.ggks_server_destroy.argtypes = [P]
+    L.ggks_server_submit.argtypes = [P, ctypes.POINTER(Request), P, ctypes.POINTER(U64)]
+    L.ggks_server_wait.argtypes = [P, U64, ctypes.POINTER(ctypes.c_double)]
+    L.ggks_server_get_stats.argtypes = [P, ctypes.POINTER(ServerStats)]
+    L.ggks_server_set_tuning.argtypes = [P, U32, U32]
+    for nm in ("create", "destroy", "submit", "wait", "get_stats", "set_tuning"):
+        getattr(L, "ggks_server_" + nm).restype = ctypes.c_int
     L.ggks_multiselect_noalloc_f32.argtypes = [P, U64, P, U32, P, P]
     L.ggks_multiselect_noalloc_f32.restype = ctypes.c_int
     L.ggks_context_create.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
@@ -321,6 +356,109 @@ def topk_batch_ptr(ptrs, ns, dtype, Ks, ctx=None, stream=None, autotune=False):
         ctypes.byref(o))
     _check(st, "topk_batch")
     return [out[off[p]:off[p + 1]] for p in range(ptrs.size)]
+
+
+class PreparedBatch:
+    """A batched multiselect (k_lists) or top-k (Ks) whose argument arrays are
+    built once, the way a C or C++ caller keeps them: each call runs one
+    ggks_multiselect_batch_* / ggks_topk_batch_* and returns the concatenated
+    outputs (problem order); split() cuts them per problem."""
+
+    def __init__(self, ptrs, ns, dtype, k_lists=None, Ks=None, ctx=None, stream=None,
+                 autotune=False):
+        self.dtype = np.dtype(dtype)
+        self.ptrs, self.ns = _batch_arrays(ptrs, ns)
+        if Ks is not None:
+            self.Ks = np.ascontiguousarray(np.asarray(Ks, dtype=np.uint32))
+            sizes = self.Ks.astype(np.int64)
+            self.fn = getattr(lib(), "ggks_topk_batch_" + _SFX[self.dtype])
+        else:
+            self.Ks = None
+            sizes = np.array([len(k) for k in k_lists], dtype=np.int64)
+            self.fn = getattr(lib(), "ggks_multiselect_batch_" + _SFX[self.dtype])
+            self.ks = np.ascontiguousarray(
+                np.concatenate([np.asarray(k, dtype=np.uint32) for k in k_lists])
+                if len(k_lists) else np.zeros(0, np.uint32), dtype=np.uint32)
+        self.off = np.zeros(self.ptrs.size + 1, dtype=np.uint32)
+        np.cumsum(sizes, out=self.off[1:])
+        self.out = np.empty(int(self.off[-1]), dtype=self.dtype)
+        self.opts = _opts(ctx, stream, FLAG_AUTOTUNE if autotune else 0)
+        self.num_outputs = int(self.off[-1])
+
+    def __call__(self):
+        if self.Ks is not None:
+            st = self.fn(self.ptrs.ctypes.data, self.ns.ctypes.data, self.ptrs.size,
+                         self.Ks.ctypes.data, self.out.ctypes.data, ctypes.byref(self.opts))
+        else:
+            st = self.fn(self.ptrs.ctypes.data, self.ns.ctypes.data, self.ptrs.size,
+                         self.off.ctypes.data, self.ks.ctypes.data if self.ks.size else None,
+                         self.out.ctypes.data, ctypes.byref(self.opts))
+        _check(st, "batch")
+        return self.out
+
+    def split(self, out=None):
+        out = self.out if out is None else out
+        return [out[self.off[p]:self.off[p + 1]] for p in range(self.ptrs.size)]
+
+
+class Server:
+    """A ggks_server: requests submitted from any thread are admitted under an
+    HBM cap and coalesced into batched launches (continuous batching)."""
+
+    def __init__(self, device=0, hbm_cap_bytes=64 << 30, max_batch=0):
+        cfg = ServerConfig(int(device), int(max_batch), int(hbm_cap_bytes))
+        h = ctypes.c_void_p()
+        _check(lib().ggks_server_create(ctypes.byref(cfg), ctypes.byref(h)), "server_create")
+        self.handle = h
+        self._keep = {}
+
+    def submit(self, ptr, n, dtype, k=None, K=None, host=False, out=None):
+        """Submit one request (k list, or K for top-k) on the vector at ptr
+        (device memory, or host memory with host=True).  Returns a ticket."""
+        dtype = np.dtype(dtype)
+        flags = REQ_HOST_VECTOR if host else 0
+        if K is not None:
+            flags |= REQ_TOPK
+            karr, num = None, int(K)
+        else:
+            karr = np.ascontiguousarray(k, dtype=np.uint32)
+            num = karr.size
+        if out is None:
+            out = np.empty(num, dtype=dtype)
+        r = Request(DTYPE_CODES[dtype], flags, ctypes.c_void_p(ptr), int(n),
+                    karr.ctypes.data if karr is not None else None, num, 0)
+        t = ctypes.c_uint64()
+        _check(lib().ggks_server_submit(self.handle, ctypes.byref(r), out.ctypes.data,
+                                        ctypes.byref(t)), "server_submit")
+        self._keep[t.value] = out
+        return t.value
+
+    def wait(self, ticket):
+        """Block until the request is done: (values, latency in ms)."""
+        lat = ctypes.c_double()
+        st = lib().ggks_server_wait(self.handle, int(ticket), ctypes.byref(lat))
+        out = self._keep.pop(ticket, None)
+        _check(st, "server_wait")
+        return out, lat.value
+
+    def stats(self):
+        s = ServerStats()
+        _check(lib().ggks_server_get_stats(self.handle, ctypes.byref(s)), "server_stats")
+        return s.as_dict()
+
+    def set_tuning(self, div, tile):
+        _check(lib().ggks_server_set_tuning(self.handle, int(div), int(tile)), "server_tuning")
+
+    def close(self):
+        if self.handle:
+            lib().ggks_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def batch_set_tuning(ctx=None, div=0, tile=0):

@@ -266,3 +266,91 @@ def batch_problems(count, seed, lo_log2=10.0, hi_log2=22.0, k_lo=1, k_hi=64):
 def batch_vector(prob):
     """The float32 data of one batch problem (numpy, seeded)."""
     return generate("f32", prob["dist"], prob["n"], prob["seed"])
+
+
+def batch_vectors_device(probs, seed, device):
+    """float32 vectors of batch_problems() generated on a CUDA device with one
+    seeded torch generator, in problem order (uniform [0,1) = rand, normal =
+    randn, Cauchy = tan(pi (u - 1/2)), integer-valued = floor(256 u))."""
+    import math
+
+    import torch
+    gen = torch.Generator(device=device)
+    gen.manual_seed(int(seed))
+    out = []
+    for p in probs:
+        n, d = p["n"], p["dist"]
+        if d == "normal":
+            v = torch.randn(n, device=device, generator=gen)
+        else:
+            u = torch.rand(n, device=device, generator=gen)
+            if d == "uniform":
+                v = u
+            elif d == "cauchy":
+                v = torch.tan(math.pi * (u - 0.5))
+            else:
+                v = torch.floor(u * 256.0)
+        out.append(v.contiguous())
+    return out
+
+
+# ---------------------------------------------------------------------------
+# served workload: a stream of mixed requests
+# ---------------------------------------------------------------------------
+
+
+def serving_pool(counts, seed, device, lo_log2=12.0, hi_log2=26.0):
+    """Resident vectors of the served workload, generated on a CUDA device:
+    counts = {"f32": a, "u32": b, "f64": c} vectors with lengths log-uniform in
+    [2^lo_log2, 2^hi_log2]; float vectors draw from uniform / normal / Cauchy /
+    integer-valued [0,256), uint32 vectors from uniform [0,2^32) / [0,2^16).
+    Returns {dtype: [tensor, ...]} (uint32 data in int32 tensors)."""
+    import math
+
+    import torch
+    r = _rng(seed)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(int(seed))
+    pool = {}
+    for dt in ("f32", "u32", "f64"):
+        pool[dt] = []
+        for _ in range(counts.get(dt, 0)):
+            n = int(2.0 ** r.uniform(lo_log2, hi_log2))
+            if dt == "u32":
+                hi = (1 << 32) if r.random() < 0.5 else (1 << 16)
+                v = torch.randint(0, hi, (n,), device=device, generator=gen, dtype=torch.int64)
+                v = (v - (v >= (1 << 31)).to(torch.int64) * (1 << 32)).to(torch.int32)  # bits
+            else:
+                fdt = torch.float32 if dt == "f32" else torch.float64
+                d = BATCH_DISTS[int(r.integers(0, len(BATCH_DISTS)))]
+                if d == "normal":
+                    v = torch.randn(n, device=device, generator=gen, dtype=fdt)
+                else:
+                    u = torch.rand(n, device=device, generator=gen, dtype=fdt)
+                    v = u if d == "uniform" else (torch.tan(math.pi * (u - 0.5)) if d == "cauchy"
+                                                  else torch.floor(u * 256.0))
+            pool[dt].append(v.contiguous())
+    return pool
+
+
+def serving_trace(pool_sizes, rate, count, seed):
+    """A Poisson request stream: arrival times (s) at `rate` requests/s; each
+    request picks float32 / uint32 / float64 in ratio 6:3:1, a vector of that
+    type from the pool, and is a multiselect with 8-1024 k's (70%) or a top-k
+    with K in [16, 4096] (30%, K <= n).  pool_sizes = {dtype: [n, ...]}."""
+    r = _rng(seed)
+    t = np.cumsum(r.exponential(1.0 / rate, count))
+    t -= t[0]
+    out = []
+    for i in range(count):
+        dt = ("f32",) * 6 + ("u32",) * 3 + ("f64",)
+        dt = dt[int(r.integers(0, 10))]
+        vi = int(r.integers(0, len(pool_sizes[dt])))
+        n = pool_sizes[dt][vi]
+        if r.random() < 0.7:
+            ks = r.integers(1, n + 1, int(r.integers(8, 1025))).astype(np.uint32)
+            out.append({"t": float(t[i]), "dtype": dt, "vec": vi, "k": ks, "K": None})
+        else:
+            out.append({"t": float(t[i]), "dtype": dt, "vec": vi, "k": None,
+                        "K": int(min(n, r.integers(16, 4097)))})
+    return out

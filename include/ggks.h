@@ -190,6 +190,72 @@ int ggks_batch_last_tuning(ggks_context *ctx, uint32_t *div, uint32_t *tile);
 int ggks_batch_set_tuning(ggks_context *ctx, uint32_t div, uint32_t tile);
 
 /* ------------------------------------------------------------------------ */
+/* Serving loop                                                              */
+/* ------------------------------------------------------------------------ */
+
+/* No counterpart in the reference (a benchmark harness that runs one
+ * selection at a time, compareMultiselect.cu:72-187).  A server accepts
+ * multiselect and top-k requests of mixed sizes and element types at any
+ * time, from any thread, and coalesces them into batched launches:
+ *   - admission: requests are taken in arrival order while the device bytes
+ *     of the admitted ones (uploaded vector + bucket-state estimate) stay
+ *     within hbm_cap_bytes; a host vector is copied to the device then, on a
+ *     copy stream that overlaps the running batch;
+ *   - execution: every request whose data is on the device (at most max_batch,
+ *     0 = no limit) joins the next batch; one persistent launch per element
+ *     type present.  Requests arriving meanwhile join the batch after it.
+ * Each result equals the result of the single-vector entry point on the same
+ * vector and k's, bit for bit. */
+typedef struct ggks_server ggks_server;
+
+typedef struct ggks_server_config {
+  int device;
+  uint32_t max_batch;     /* requests per batch at most; 0 = no limit */
+  uint64_t hbm_cap_bytes; /* admission cap on the admitted requests' device bytes */
+} ggks_server_config;
+
+#define GGKS_DTYPE_F32 0
+#define GGKS_DTYPE_F64 1
+#define GGKS_DTYPE_U32 2
+/* ggks_request.flags */
+#define GGKS_REQ_TOPK 1u        /* the num_k largest, descending (k is ignored) */
+#define GGKS_REQ_HOST_VECTOR 2u /* vec is host memory (else device memory) */
+
+typedef struct ggks_request {
+  int32_t dtype;      /* GGKS_DTYPE_* */
+  uint32_t flags;     /* GGKS_REQ_* */
+  const void *vec;    /* n elements; must stay valid until ggks_server_wait returns */
+  uint64_t n;
+  const uint32_t *k;  /* num_k k's (k-th largest, 1-based); copied by submit */
+  uint32_t num_k;     /* outputs; for top-k, K */
+  uint32_t reserved;
+} ggks_request;
+
+typedef struct ggks_server_stats {
+  uint64_t submitted, completed;
+  uint64_t batches;          /* batches formed */
+  uint64_t batched_requests; /* requests over all batches */
+  uint64_t max_batch_seen;
+  uint64_t launches;         /* batched selections run (one per element type per batch) */
+  uint64_t uploads, upload_bytes; /* host vectors copied at admission */
+  uint64_t peak_bytes;       /* largest admitted device bytes */
+  uint64_t in_flight_bytes;  /* admitted device bytes now */
+} ggks_server_stats;
+
+int ggks_server_create(const ggks_server_config *cfg, ggks_server **out);
+/* Finishes every submitted request, then stops the server's threads. */
+int ggks_server_destroy(ggks_server *srv);
+/* out: host buffer of num_k values, written before ggks_server_wait returns.
+ * GGKS_OOM: the request alone exceeds the cap. */
+int ggks_server_submit(ggks_server *srv, const ggks_request *req, void *out, uint64_t *ticket);
+/* Blocks until the request is done; returns its status; *latency_ms (may be
+ * NULL): submit to completion.  Each ticket is waited for once. */
+int ggks_server_wait(ggks_server *srv, uint64_t ticket, double *latency_ms);
+int ggks_server_get_stats(ggks_server *srv, ggks_server_stats *out);
+/* Pin the batched path's divisor / tile size (ggks_batch_set_tuning). */
+int ggks_server_set_tuning(ggks_server *srv, uint32_t div, uint32_t tile);
+
+/* ------------------------------------------------------------------------ */
 /* Contexts, statistics, utilities                                           */
 /* ------------------------------------------------------------------------ */
 
