@@ -42,6 +42,8 @@ constexpr uint32_t kBMaxNb = 8192;               // bucket budget of one problem
 constexpr uint32_t kBMaxS = 8192;                // samples of one problem (shared memory)
 constexpr int kBPhases = 5;
 constexpr uint32_t kBWarpBytes = 2048;  // shared memory of one warp-finisher buffer
+constexpr uint32_t kBRepBytes = 32768;  // per-bucket first keys of a tile (dup problems)
+constexpr uint32_t kMixed = 0x80000000u;  // tile row: the bucket holds more than one key
 
 // segments of at most this many keys are finished by one warp
 template <class K>
@@ -66,6 +68,8 @@ struct BHdr {
   uint64_t base;
   uint64_t surv_off;
   uint32_t shift, nb, heavy, num_slots;
+  uint32_t dup;  // tiles track whether each bucket holds a single key
+  uint32_t pad[3];
 };
 
 // one (problem, tile) work item (host-written)
@@ -85,6 +89,8 @@ struct BCtrl {
   uint64_t surv_top;    // survivor bump allocator
   uint64_t cap_needed;  // survivors wanted when they did not fit
   uint64_t t_ns[kBPhases + 1];  // %globaltimer at the start and after each phase (CTA 0)
+  uint32_t dbg_code, dbg_pad;   // first failed index check (builds with GGKS_BATCH_CHECKS)
+  uint64_t dbg_a, dbg_b;
 };
 
 struct BArgs {
@@ -95,8 +101,10 @@ struct BArgs {
   uint32_t num_req;  // requests of all problems (= slot index space)
   uint32_t bcap;     // finisher gather capacity (keys)
   uint64_t surv_cap;
+  uint64_t lut_words, row_words, cnt_words;  // sizes, for the index checks
   uint32_t *luts;
   uint32_t *rows;
+  void *reps;  // key per row entry: the tile's only key of the bucket (dup problems)
   uint32_t *counts;
   const Req *reqs;  // rank within the problem, output position in out[]
   uint32_t *req_bucket, *req_local;
@@ -110,6 +118,25 @@ struct BArgs {
   void *out;              // output values
   BCtrl *ctrl;
 };
+
+// Index checks of the batched kernel, compiled in with GGKS_BATCH_CHECKS: a
+// failed check records its code and operands (first failure wins), sets
+// ST_INTERNAL, and the guarded access is skipped.  Without the macro every
+// check is the constant true.
+#ifdef GGKS_BATCH_CHECKS
+static __device__ __noinline__ bool bcheck_fail(BCtrl *c, uint32_t code, uint64_t a, uint64_t b) {
+  if (atomicCAS(&c->dbg_code, 0u, code) == 0u) {
+    c->dbg_a = a;
+    c->dbg_b = b;
+  }
+  atomicOr(&c->status, ST_INTERNAL);
+  return false;
+}
+#define BCHECK(cond, code, a, b) \
+  ((cond) ? true : bcheck_fail(A.ctrl, (code), (uint64_t)(a), (uint64_t)(b)))
+#else
+#define BCHECK(cond, code, a, b) true
+#endif
 
 __device__ __forceinline__ uint64_t global_ns() {
   uint64_t t;
@@ -161,6 +188,25 @@ __device__ __forceinline__ uint32_t queue_pop(uint32_t *q, uint32_t *s_item) {
   return *s_item;
 }
 
+// Shared-memory position of bucket / slice x in the tile phases: x with its
+// low five bits XORed by the next five.  Inputs with few distinct values
+// (integer-valued floats, say) put their buckets and slices at regular
+// power-of-two strides, which without the swizzle fall into one bank.  A
+// permutation inside every group of 32 entries.
+__device__ __forceinline__ uint32_t swz(uint32_t x) { return x ^ ((x >> 5) & 31u); }
+
+// bucket_of with the splitter table stored at swizzled positions
+template <class K>
+__device__ __forceinline__ uint32_t bucket_of_sw(K key, K base, uint32_t shift, const uint32_t *lut,
+                                                 uint32_t nsl) {
+  const K d = key - base;  // wraps for key < base; that result is discarded
+  const K idx = d >> shift;
+  const uint32_t j = idx < (K)nsl ? (uint32_t)idx : nsl;
+  const uint32_t e = lut[swz(j)];
+  const uint32_t b = (uint32_t)((int32_t)e >> 7) + shr_clamp(d, e & 127u);
+  return key < base ? 0u : b;
+}
+
 __device__ __forceinline__ uint32_t ldcg_u(const uint32_t *p) { return __ldcg(p); }
 __device__ __forceinline__ uint64_t ldcg_u(const uint64_t *p) {
   return __ldcg(reinterpret_cast<const unsigned long long *>(p));
@@ -175,6 +221,7 @@ __device__ __forceinline__ BHdr load_hdr(const BHdr *h) {
   r.nb = w.y;
   r.heavy = w.z;
   r.num_slots = w.w;
+  r.dup = __ldcg(&h->dup);
   return r;
 }
 
@@ -308,6 +355,8 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
     }
     lo = block_reduce(lo, [](K u, K v) { return u < v ? u : v; }, redk);
     hi = block_reduce(hi, [](K u, K v) { return u > v ? u : v; }, redk);
+    if (!BCHECK(P.lut_off + (1u << P.nsl_bits) < A.lut_words && P.S <= kBMaxS, 1, p, P.lut_off))
+      continue;
     build_lut_cta<K, kBSpt, true>(samples, P.S, lo, hi, P.nb_max, A.luts + P.lut_off, &s_hdr,
                                   (int)P.nsl_bits);
     __syncthreads();
@@ -319,6 +368,8 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       h.nb = s_hdr.nb;
       h.heavy = s_hdr.heavy;
       h.num_slots = 0;
+      h.dup = (s_hdr.dup && P.nb_max * sizeof(K) <= kBRepBytes) ? 1u : 0u;
+      h.pad[0] = h.pad[1] = h.pad[2] = 0;
       A.hdrs[p] = h;
     }
   }
@@ -328,6 +379,8 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
   if (tid == 0) s_cur = 0xFFFFFFFFu;  // problem whose table is in shared memory
   uint32_t *lut = sm;
   uint32_t *hist = sm + kLutPadded;
+  K *rep = reinterpret_cast<K *>(hist + kBMaxNb);
+  K *reps = reinterpret_cast<K *>(A.reps);
   if (!(st & ST_FATAL)) {
     for (uint32_t t = queue_pop(&ctrl->queue[1], &s_item); t < A.num_tiles;
          t = queue_pop(&ctrl->queue[1], &s_item)) {
@@ -336,15 +389,38 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       const BHdr H = load_hdr(A.hdrs + tl.prob);
       const uint32_t nsl = 1u << P.nsl_bits;
       if (s_cur != tl.prob)
-        for (uint32_t j = tid; j <= nsl; j += nt) lut[j] = __ldcg(A.luts + P.lut_off + j);
-      for (uint32_t b = tid; b < H.nb; b += nt) hist[b] = 0;
+        for (uint32_t j = tid; j <= nsl; j += nt) lut[swz(j)] = __ldcg(A.luts + P.lut_off + j);
+      for (uint32_t b = tid; b < ((H.nb + 31) & ~31u); b += nt) {
+        hist[b] = 0;
+        if (H.dup) rep[b] = KeyMax<K>::v;
+      }
       __syncthreads();
       if (tid == 0) s_cur = tl.prob;
       const K base = (K)H.base;
       const uint32_t shift = H.shift;
-      if (H.heavy) {
+      if (H.dup) {
+        // count, and keep the bucket's first key; a second distinct key (or
+        // the largest key, which marks an empty entry) sets the mixed bit
+        for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
+          const uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
+          if (!BCHECK(ub < H.nb, 2, ub, H.nb)) return;
+          const uint32_t b = swz(ub);
+          atomicAdd(&hist[b], 1u);
+          const K r = rep[b];
+          if (r != k || k == KeyMax<K>::v) {
+            if (k != KeyMax<K>::v && r == KeyMax<K>::v) {
+              const K old = atomic_cas_key(&rep[b], KeyMax<K>::v, k);
+              if (old != KeyMax<K>::v && old != k) atomicOr(&hist[b], kMixed);
+            } else if (!(hist[b] & kMixed)) {
+              atomicOr(&hist[b], kMixed);
+            }
+          }
+        });
+      } else if (H.heavy) {
         for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool full) {
-          const uint32_t b = bucket_of<K>(k, base, shift, lut, nsl);
+          uint32_t b = bucket_of_sw<K>(k, base, shift, lut, nsl);
+          if (!BCHECK(b < H.nb, 3, b, H.nb)) b = 0;
+          b = swz(b);
           if (full)
             hist_add<true>(hist, b);
           else
@@ -352,12 +428,18 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         });
       } else {
         for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
-          atomicAdd(&hist[bucket_of<K>(k, base, shift, lut, nsl)], 1u);
+          const uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
+          if (!BCHECK(ub < H.nb, 4, ub, H.nb)) return;
+          atomicAdd(&hist[swz(ub)], 1u);
         });
       }
       __syncthreads();
-      uint32_t *row = A.rows + P.row0 + (uint64_t)tl.rank * P.nb_max;
-      for (uint32_t b = tid; b < H.nb; b += nt) row[b] = hist[b];
+      const uint64_t ro = P.row0 + (uint64_t)tl.rank * P.nb_max;
+      if (!BCHECK(ro + H.nb <= A.row_words && H.nb <= P.nb_max, 5, ro, H.nb)) continue;
+      for (uint32_t b = tid; b < H.nb; b += nt) {
+        A.rows[ro + b] = hist[swz(b)];
+        if (H.dup) reps[ro + b] = rep[swz(b)];
+      }
     }
   }
   st = grid_barrier(ctrl, &s_status, 2);
@@ -372,12 +454,20 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       uint32_t *excl = sm + kLutPadded;  // bucket prefix; later: slot of each flagged bucket
       uint8_t *flag = reinterpret_cast<uint8_t *>(excl + kBMaxNb);
       uint32_t *cnt = A.counts + P.cnt_off;
+      if (!BCHECK(P.row0 + (uint64_t)nr * P.nb_max <= A.row_words && nb <= P.nb_max &&
+                      P.cnt_off + P.nb_max <= A.cnt_words && P.req_off + P.num_req <= A.num_req,
+                  6, p, nb))
+        continue;
       for (uint32_t j = tid; j <= nsl; j += nt) lut[j] = __ldcg(A.luts + P.lut_off + j);
       // each column of the rows becomes its exclusive prefix over the tiles;
-      // a warp covers 32 neighbouring buckets of a row
+      // a warp covers 32 neighbouring buckets of a row.  Dup problems also
+      // learn which buckets hold a single key in every tile: those become
+      // flat slots (flag bit 1; the key goes to tile 0's key row).
       for (uint32_t b = tid; b < nb; b += nt) {
         uint32_t *col = A.rows + P.row0 + b;
         uint32_t run = 0, r = 0;
+        bool one = H.dup != 0;
+        K key0 = KeyMax<K>::v;
         for (; r + 8 <= nr; r += 8) {
           uint32_t v[8];
 #pragma unroll
@@ -385,17 +475,38 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
 #pragma unroll
           for (int q = 0; q < 8; ++q) {
             col[(uint64_t)(r + q) * P.nb_max] = run;
-            run += v[q];
+            run += v[q] & ~kMixed;
+          }
+          if (H.dup) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              if (v[q] & kMixed) one = false;
+              if (v[q] & ~kMixed) {
+                const K rr = ldcg_u(reps + P.row0 + (uint64_t)(r + q) * P.nb_max + b);
+                if (key0 == KeyMax<K>::v) key0 = rr;
+                one = one && rr == key0;
+              }
+            }
           }
         }
         for (; r < nr; ++r) {
           const uint32_t v = __ldcg(col + (uint64_t)r * P.nb_max);
           col[(uint64_t)r * P.nb_max] = run;
-          run += v;
+          run += v & ~kMixed;
+          if (H.dup) {
+            if (v & kMixed) one = false;
+            if (v & ~kMixed) {
+              const K rr = ldcg_u(reps + P.row0 + (uint64_t)r * P.nb_max + b);
+              if (key0 == KeyMax<K>::v) key0 = rr;
+              one = one && rr == key0;
+            }
+          }
         }
+        one = one && run > 0 && key0 != KeyMax<K>::v;
+        if (one) reps[P.row0 + b] = key0;
         cnt[b] = run;
         excl[b] = run;  // the count, until the scan below
-        flag[b] = 0;
+        flag[b] = one ? 2 : 0;
       }
       __syncthreads();
       // bucket prefix: contiguous bucket range per thread
@@ -424,21 +535,21 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
           else
             hi = mid;
         }
-        flag[lo] = 1;
+        flag[lo] |= 1;  // concurrent writers all store the same value
         A.req_bucket[P.req_off + i] = lo;
         A.req_local[P.req_off + i] = rank - excl[lo];
       }
       __syncthreads();
       // flagged buckets -> slots in bucket order; excl[] now maps bucket -> slot
       uint32_t my_slots = 0;
-      for (uint32_t b = b0; b < b1; ++b) my_slots += flag[b] ? 1u : 0u;
+      for (uint32_t b = b0; b < b1; ++b) my_slots += flag[b] & 1u;
       uint32_t tot_slots;
       {
         uint32_t slot = block_incl_scan(my_slots, &tot_slots, red32) - my_slots;
         for (uint32_t b = b0; b < b1; ++b)
-          if (flag[b]) {
+          if (flag[b] & 1u) {
             excl[b] = slot;
-            A.seg_bucket[P.req_off + slot] = b;
+            if (BCHECK(slot < P.num_req, 7, slot, P.num_req)) A.seg_bucket[P.req_off + slot] = b;
             slot++;
           }
       }
@@ -450,10 +561,15 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       for (uint32_t q = s0; q < s1; ++q) {
         const uint32_t g = P.req_off + q;
         const uint32_t b = __ldcg(A.seg_bucket + g);
-        const K klo = bucket_lo<K>(b, (K)H.base, H.shift, lut, nsl);
+        K klo = bucket_lo<K>(b, (K)H.base, H.shift, lut, nsl);
         const K knext = (b + 1 < nb) ? bucket_lo<K>(b + 1, (K)H.base, H.shift, lut, nsl) : K(0);
-        // single key iff the next bucket starts one key later (see k_plan)
-        const bool single = (knext > klo) ? (knext - klo == K(1)) : (klo == KeyMax<K>::v);
+        // single key iff the next bucket starts one key later (see k_plan), or
+        // every tile saw one and the same key in the bucket
+        bool single = (knext > klo) ? (knext - klo == K(1)) : (klo == KeyMax<K>::v);
+        if (flag[b] & 2u) {
+          single = true;
+          klo = ldcg_u(reps + P.row0 + b);
+        }
         const uint32_t cb = single ? 0u : __ldcg(cnt + b);
         A.seg_size[g] = cb;
         seg_lo[g] = klo;
@@ -531,7 +647,8 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         Req e;
         e.rank = __ldcg(A.req_local + P.req_off + i);
         e.out = rq[i].out;
-        A.klist[pos] = e;
+        if (BCHECK(pos < A.num_req && e.out < A.num_req && g < P.req_off + P.num_req, 8, pos, g))
+          A.klist[pos] = e;
       }
     }
   }
@@ -551,8 +668,8 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       const BHdr H = load_hdr(A.hdrs + tl.prob);
       const uint32_t nsl = 1u << P.nsl_bits;
       if (s_cur != tl.prob)
-        for (uint32_t j = tid; j <= nsl; j += nt) lut[j] = __ldcg(A.luts + P.lut_off + j);
-      for (uint32_t b = tid; b < H.nb; b += nt) cursor[b] = kInactive;
+        for (uint32_t j = tid; j <= nsl; j += nt) lut[swz(j)] = __ldcg(A.luts + P.lut_off + j);
+      for (uint32_t b = tid; b < ((H.nb + 31) & ~31u); b += nt) cursor[b] = kInactive;
       __syncthreads();
       if (tid == 0) s_cur = tl.prob;
       const uint32_t *row = A.rows + P.row0 + (uint64_t)tl.rank * P.nb_max;
@@ -561,7 +678,8 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         const uint32_t g = P.req_off + s;
         if (__ldcg(A.seg_size + g) == 0) continue;
         const uint32_t b = __ldcg(A.seg_bucket + g);
-        cursor[b] = (uint32_t)(ldcg_u(A.seg_off + g) - H.surv_off + __ldcg(row + b));
+        if (!BCHECK(b < H.nb && s < P.num_req, 10, b, s)) continue;
+        cursor[swz(b)] = (uint32_t)(ldcg_u(A.seg_off + g) - H.surv_off + __ldcg(row + b));
       }
       __syncthreads();
       K *sp = surv + H.surv_off;
@@ -570,7 +688,9 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       const uint32_t shift = H.shift;
       bool overrun = false;
       for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
-        const uint32_t pos = atomicAdd(&cursor[bucket_of<K>(k, base, shift, lut, nsl)], 1u);
+        uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
+        if (!BCHECK(ub < H.nb, 9, ub, H.nb)) return;
+        const uint32_t pos = atomicAdd(&cursor[swz(ub)], 1u);
         const bool active = !(pos & kInactive);
         const bool fits = pos < cap;
         st_global_if(sp + pos, k, active && fits);
@@ -586,7 +706,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         const uint32_t nxt = tl.rank + 1 < P.ntiles ? __ldcg(row + P.nb_max + b)
                                                      : __ldcg(A.counts + P.cnt_off + b);
         const uint32_t end = (uint32_t)(ldcg_u(A.seg_off + g) - H.surv_off + nxt);
-        if (cursor[b] != end) s_bad = true;
+        if (cursor[swz(b)] != end) s_bad = true;
       }
     }
     __syncthreads();
@@ -601,6 +721,25 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
     for (uint32_t i = queue_pop(&ctrl->queue[4], &s_item); i < n_big;
          i = queue_pop(&ctrl->queue[4], &s_item)) {
       const uint32_t g = __ldcg(A.big_list + i);
+      if (!BCHECK(i < A.num_req && g < A.num_req &&
+                      ldcg_u(A.seg_off + g) + __ldcg(A.seg_size + g) <= A.surv_cap &&
+                      __ldcg(A.kstart + g) + __ldcg(A.kcnt + g) <= A.num_req,
+                  11, i, g))
+        continue;
+#ifdef GGKS_BATCH_CHECKS
+      {
+        bool bad = false;
+        const uint32_t sz = __ldcg(A.seg_size + g), ks = __ldcg(A.kstart + g);
+        for (uint32_t j = tid; j < __ldcg(A.kcnt + g); j += nt) {
+          const Req e = A.klist[ks + j];
+          if (e.out >= A.num_req || (sz && e.rank >= sz)) bad = true;
+        }
+        if (__syncthreads_or(bad)) {
+          if (tid == 0) BCHECK(false, 13, g, sz);
+          continue;
+        }
+      }
+#endif
       const bool done = finish_slot<K, OutT>(
           surv + ldcg_u(A.seg_off + g), __ldcg(A.seg_size + g), ldcg_u(seg_lo + g), ldcg_u(seg_hi + g),
           A.klist + __ldcg(A.kstart + g), __ldcg(A.kcnt + g), A.bcap, sm, out);
@@ -620,6 +759,25 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       i = __shfl_sync(0xffffffffu, i, 0);
       if (i >= n_small) break;
       const uint32_t g = __ldcg(A.small_list + i);
+      if (!BCHECK(i < A.num_req && g < A.num_req && __ldcg(A.seg_size + g) <= warp_cap<K>() &&
+                      ldcg_u(A.seg_off + g) + __ldcg(A.seg_size + g) <= A.surv_cap &&
+                      __ldcg(A.kstart + g) + __ldcg(A.kcnt + g) <= A.num_req,
+                  12, i, g))
+        continue;
+#ifdef GGKS_BATCH_CHECKS
+      {
+        bool bad = false;
+        const uint32_t sz = __ldcg(A.seg_size + g), ks = __ldcg(A.kstart + g);
+        for (uint32_t j = lane; j < __ldcg(A.kcnt + g); j += 32) {
+          const Req e = A.klist[ks + j];
+          if (e.out >= A.num_req || (sz && e.rank >= sz)) bad = true;
+        }
+        if (__any_sync(0xffffffffu, bad)) {
+          if (lane == 0) BCHECK(false, 14, g, sz);
+          continue;
+        }
+      }
+#endif
       finish_warp<K, OutT>(surv + ldcg_u(A.seg_off + g), __ldcg(A.seg_size + g), ldcg_u(seg_lo + g),
                            A.klist + __ldcg(A.kstart + g), __ldcg(A.kcnt + g), wbuf, out);
     }

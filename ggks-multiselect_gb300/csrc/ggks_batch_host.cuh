@@ -3,6 +3,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -25,8 +26,9 @@ static inline int batch_smem_bytes() {
   using K = typename Traits<T>::K;
   const size_t table = (size_t)kBMaxS * sizeof(K);
   const size_t plan = kLutPadded * 4 + (size_t)kBMaxNb * 5;
-  const size_t fin = 5 * kFinBins * 4 + (size_t)(sizeof(K) == 4 ? 4096 : 2048) * sizeof(K) * 3 / 2;
-  return (int)std::max(table, std::max(plan, fin));
+  const size_t tiles = (kLutPadded + (size_t)kBMaxNb) * 4 + kBRepBytes;
+  const size_t fin = finish_smem_for<K>(sizeof(K) == 4 ? 4096u : 2048u);
+  return (int)std::max(std::max(table, tiles), std::max(plan, fin));
 }
 
 template <class T>
@@ -106,6 +108,7 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   const size_t o_hdrs = arr(P, sizeof(BHdr));
   const size_t o_luts = arr(lut_words, 4);
   const size_t o_rows = arr(row_words, 4);
+  const size_t o_reps = arr(row_words, sizeof(K));
   const size_t o_counts = arr(cnt_words, 4);
   const size_t o_req_bucket = arr(R, 4), o_req_local = arr(R, 4);
   const size_t o_seg_bucket = arr(R, 4), o_seg_size = arr(R, 4), o_kstart = arr(R, 4),
@@ -159,8 +162,12 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   a.num_tiles = num_tiles;
   a.num_req = R;
   a.bcap = bcap;
+  a.lut_words = lut_words;
+  a.row_words = row_words;
+  a.cnt_words = cnt_words;
   a.luts = reinterpret_cast<uint32_t *>(D + o_luts);
   a.rows = reinterpret_cast<uint32_t *>(D + o_rows);
+  a.reps = D + o_reps;
   a.counts = reinterpret_cast<uint32_t *>(D + o_counts);
   a.reqs = reinterpret_cast<const Req *>(D + o_reqs);
   a.req_bucket = reinterpret_cast<uint32_t *>(D + o_req_bucket);
@@ -223,6 +230,11 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   for (int round = 0;; ++round) {
     BCtrl c;
     std::memcpy(&c, h_ctrl, sizeof(BCtrl));
+#ifdef GGKS_BATCH_CHECKS
+    if (c.dbg_code)
+      fprintf(stderr, "ggks batch index check %u failed: %llu %llu (status %u)\n", c.dbg_code,
+              (unsigned long long)c.dbg_a, (unsigned long long)c.dbg_b, c.status);
+#endif
     if (c.status & ST_FATAL) return (c.status & ST_TIMEOUT) ? GGKS_TIMEOUT : GGKS_INTERNAL;
     if (c.status & ST_OVERFLOW) {
       if (round >= 3) return GGKS_INTERNAL;

@@ -98,7 +98,7 @@ struct LutHeader {
   uint32_t shift;  // slice index = (key - base) >> shift
   uint32_t nb;     // number of buckets
   uint32_t heavy;  // 1: warp-aggregate histogram updates
-  uint32_t pad;
+  uint32_t dup;    // 1: sampled keys repeat often (at least once per nb pairs)
 };
 
 // ---------------------------------------------------------------------------
@@ -239,9 +239,11 @@ __device__ __forceinline__ void st_global_if(uint64_t *p, uint64_t v, bool pred)
       : "memory");
 }
 
-// right shift that yields 0 for shift >= width
+// right shift that yields 0 for shift >= width (the splitter table's top
+// entry shifts by the key width).  __funnelshift_rc clamps the shift to 32;
+// __funnelshift_r would wrap it to shift & 31.
 __device__ __forceinline__ uint32_t shr_clamp(uint32_t d, uint32_t s) {
-  return __funnelshift_r(d, 0u, s);  // shf.r.clamp: shift clamped to 32
+  return __funnelshift_rc(d, 0u, s);
 }
 __device__ __forceinline__ uint32_t shr_clamp(uint64_t d, uint32_t s) {
   return s >= 64 ? 0u : (uint32_t)(d >> s);
@@ -513,35 +515,60 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
   uint32_t total;
   const uint32_t incl = block_incl_scan(mysum, &total, red32);
   uint32_t run = incl - mysum + 1u;  // bucket 0 is the low edge
-  uint32_t max_per_bucket = 0;
+  // the table also goes to cnt[] (its counts are no longer read) for the
+  // collision estimate below
 #pragma unroll
   for (int q = 0; q < SPT; ++q) {
     const uint32_t j = SPT * tid + q;
+    uint32_t e = 0;
     if (j >= nsl) {
-      // unused slice
+      continue;  // unused slice
     } else if (c[q]) {
       const int b = bits_of(q);
-      lut[j] = lut_pack((int32_t)run - (int32_t)(j << b), shift - (uint32_t)b);
-      const uint32_t per = c[q] >> b;
-      max_per_bucket = per > max_per_bucket ? per : max_per_bucket;
+      e = lut_pack((int32_t)run - (int32_t)(j << b), shift - (uint32_t)b);
     } else {
       // one bucket per run of empty slices
-      lut[j] = lut_pack((int32_t)(prev_nonempty[q] ? run : run - 1u) - (int32_t)j, shift);
+      e = lut_pack((int32_t)(prev_nonempty[q] ? run : run - 1u) - (int32_t)j, shift);
     }
+    lut[j] = e;
+    cnt[j] = e;
     run += my[q];
   }
-  max_per_bucket = block_reduce(max_per_bucket, [](uint32_t p, uint32_t q) { return p > q ? p : q; },
-                                red32);
+  const uint32_t top = lut_pack((int32_t)(top_run_start ? total + 1u : total),
+                                (uint32_t)KeyMax<K>::bits);
+  __syncthreads();
+  // Warp-aggregated histogram updates pay off when lanes of a warp often hit
+  // the same bucket.  The chance that two elements share a bucket (the sum of
+  // squared bucket shares) is estimated from disjoint pairs of samples.
+  uint32_t same = 0, same_key = 0;
+  for (uint32_t q = tid; q < S / 2; q += blockDim.x) {
+    const K a = SMEM ? samples[2 * q] : __ldcg(samples + 2 * q);
+    const K b = SMEM ? samples[2 * q + 1] : __ldcg(samples + 2 * q + 1);
+    auto bucket = [&](K k) {
+      const K d = k - kmin;
+      const K idx = d >> shift;
+      const uint32_t j = idx < (K)nsl ? (uint32_t)idx : nsl;
+      const uint32_t e = j == nsl ? top : cnt[j];
+      return (uint32_t)((int32_t)e >> 7) + shr_clamp(d, e & 127u);
+    };
+    same += bucket(a) == bucket(b) ? 1u : 0u;
+    same_key += a == b ? 1u : 0u;
+  }
+  same = block_reduce(same, [](uint32_t p, uint32_t q) { return p + q; }, red32);
+  same_key = block_reduce(same_key, [](uint32_t p, uint32_t q) { return p + q; }, red32);
   if (tid == 0) {
     const uint32_t nb = 1u + total + (top_run_start ? 1u : 0u);
-    lut[nsl] = lut_pack((int32_t)(top_run_start ? total + 1u : total), (uint32_t)KeyMax<K>::bits);
+    lut[nsl] = top;
     LutHeader<K> h;
     h.base = kmin;
     h.shift = shift;
     h.nb = nb;
-    // a bucket expected to hold >= 16x the mean: warp-aggregate updates
-    h.heavy = ((uint64_t)max_per_bucket * nb >= 16ull * S && S >= 256) ? 1u : 0u;
-    h.pad = 0;
+    // collision chance >= 1/32: with 32 lanes, about 15 same-bucket pairs per
+    // warp access
+    h.heavy = (S >= 256 && 32ull * same >= S / 2) ? 1u : 0u;
+    // two elements share a key with chance >= 1 / nb: buckets holding a single
+    // key (many copies of it) are likely
+    h.dup = (S >= 256 && (uint64_t)same_key * nb >= S / 2) ? 1u : 0u;
     *hdr = h;
   }
 }
@@ -1152,6 +1179,31 @@ __global__ void __launch_bounds__(1024, 1)
 constexpr int kFinBins = 1024;
 constexpr int kFinBinBits = 10;
 constexpr int kFinThreads = 256;
+constexpr uint32_t kFlatBin = 0xFFFFFFFEu;  // gather offset of a needed bin holding one key
+
+// shared memory of finish_slot with a gather buffer of bcap keys: five bin
+// arrays, the buffer, a scratch half its size, per-bin key minima and maxima
+template <class K>
+__host__ __device__ constexpr size_t finish_smem_for(uint32_t bcap) {
+  return 5 * kFinBins * sizeof(uint32_t) + (size_t)bcap * sizeof(K) * 3 / 2 +
+         2 * kFinBins * sizeof(K);
+}
+
+__device__ __forceinline__ uint32_t atomic_cas_key(uint32_t *p, uint32_t cmp, uint32_t v) {
+  return atomicCAS(p, cmp, v);
+}
+__device__ __forceinline__ uint64_t atomic_cas_key(uint64_t *p, uint64_t cmp, uint64_t v) {
+  return atomicCAS(reinterpret_cast<unsigned long long *>(p), (unsigned long long)cmp,
+                   (unsigned long long)v);
+}
+__device__ __forceinline__ void atomic_min_key(uint32_t *p, uint32_t v) { atomicMin(p, v); }
+__device__ __forceinline__ void atomic_max_key(uint32_t *p, uint32_t v) { atomicMax(p, v); }
+__device__ __forceinline__ void atomic_min_key(uint64_t *p, uint64_t v) {
+  atomicMin(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
+}
+__device__ __forceinline__ void atomic_max_key(uint64_t *p, uint64_t v) {
+  atomicMax(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
+}
 
 template <class K>
 __device__ __forceinline__ K warp_bitonic32(K v) {
@@ -1205,9 +1257,10 @@ __device__ __forceinline__ uint32_t bin_of_rank(const uint32_t *start, uint32_t 
 // Finishes one slot: its segment src[0 .. size) of survivor keys lies in the
 // key range [lo, hi] (size 0: a flat slot whose single key is lo); the m
 // requests rq[] hold local ranks and output positions.  Called by a whole CTA
-// of kFinThreads threads; smem holds 5 * kFinBins u32 followed by the gather
-// buffer (bcap keys) and the scratch (bcap / 2 keys).  Returns false when the
-// needed bins do not fit: the slot needs a recursive re-selection.
+// (a multiple of kFinThreads threads); smem is finish_smem_for<K>(bcap) bytes:
+// 5 * kFinBins u32, the gather buffer (bcap keys), the scratch (bcap / 2
+// keys), per-bin minima and maxima (kFinBins keys each).  Returns false when
+// the needed bins do not fit: the slot needs a recursive re-selection.
 template <class K, class OutT>
 __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi,
                             const Req *__restrict__ rq, uint32_t m, uint32_t bcap, uint32_t *smem,
@@ -1219,6 +1272,8 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
   uint32_t *small = cur + kFinBins;   // needed bins of 2..32 keys
   K *B = reinterpret_cast<K *>(small + kFinBins);  // gathered keys of the needed bins
   K *T = B + bcap;                                 // scratch for sorting a large bin (tcap keys)
+  K *bmin = T + bcap / 2;                          // second attempt: per-bin key range
+  K *bmax = bmin + kFinBins;
   constexpr int kMaxBig = 64;
   __shared__ K redk[33];
   __shared__ uint32_t red32[33];
@@ -1238,7 +1293,9 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
   const uint32_t nbins = 1u << nbits;
 
   // digits of (key - mn): first over the bucket's key range; if the needed
-  // bins then hold too many keys, over the segment's actual min / max
+  // bins then hold too many keys, over the segment's actual min / max, with
+  // each bin's key range tracked: a needed bin holding one distinct key is
+  // answered from its range and not gathered
   K mn = lo, mx = hi;
   uint32_t V = 0, sh = 0;
   bool flat = false, fits = false, direct = false;
@@ -1260,11 +1317,14 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
       mn = a;
       mx = z;
     }
+    const bool track = attempt == 1;
     const int bl = bitlen<K>(mx - mn);
     sh = bl > (int)nbits ? (uint32_t)(bl - (int)nbits) : 0u;
     for (uint32_t i = tid; i < nbins; i += blockDim.x) {
       hist[i] = 0;
       cur[i] = 0;
+      bmin[i] = KeyMax<K>::v;
+      bmax[i] = 0;
     }
     if (tid == 0) {
       s_nbig = 0;
@@ -1274,6 +1334,14 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
     __syncthreads();
     // keys lie in [mn, mx], so the digit is < nbins; the clamp keeps a
     // shared-memory index in range whatever the data
+    auto count = [&](K k) {
+      const uint32_t bb = min((uint32_t)((k - mn) >> sh), nbins - 1u);
+      atomicAdd(&hist[bb], 1u);
+      if (track) {
+        atomic_min_key(&bmin[bb], k);
+        atomic_max_key(&bmax[bb], k);
+      }
+    };
     {
       uint32_t i = tid;
       for (; i + 7 * blockDim.x < size; i += 8 * blockDim.x) {
@@ -1281,11 +1349,9 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
 #pragma unroll
         for (int q = 0; q < 8; ++q) kk[q] = src[i + q * blockDim.x];
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
-          atomicAdd(&hist[min((uint32_t)((kk[q] - mn) >> sh), nbins - 1u)], 1u);
+        for (int q = 0; q < 8; ++q) count(kk[q]);
       }
-      for (; i < size; i += blockDim.x)
-        atomicAdd(&hist[min((uint32_t)((src[i] - mn) >> sh), nbins - 1u)], 1u);
+      for (; i < size; i += blockDim.x) count(src[i]);
     }
     __syncthreads();
     {
@@ -1319,9 +1385,12 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
     {
       uint32_t cc[PER], sum = 0;
 #pragma unroll
+      bool one[PER];  // a needed bin of one distinct key (tracked attempt only)
+#pragma unroll
       for (uint32_t q = 0; q < PER; ++q) {
         const uint32_t bb = tid * PER + q;
-        cc[q] = (bb < nbins && gofs[bb]) ? hist[bb] : 0u;
+        one[q] = track && bb < nbins && gofs[bb] && bmin[bb] == bmax[bb];
+        cc[q] = (bb < nbins && gofs[bb] && !one[q]) ? hist[bb] : 0u;
         sum += cc[q];
       }
       uint32_t run = block_incl_scan(sum, &V, red32) - sum;
@@ -1329,8 +1398,8 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
       for (uint32_t q = 0; q < PER; ++q) {
         const uint32_t bb = tid * PER + q;
         if (bb < nbins) {
-          const bool need = gofs[bb] != 0u;
-          gofs[bb] = need ? run : kNoSlot;
+          const bool need = gofs[bb] != 0u && !one[q];
+          gofs[bb] = one[q] ? kFlatBin : (need ? run : kNoSlot);
           if (need) atomicMax(&s_maxneed, cc[q]);
           if (need && cc[q] > 32) {
             const uint32_t at = atomicAdd(&s_nbig, 1u);
@@ -1368,7 +1437,7 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
     auto put = [&](K k) {
       const uint32_t bb = min((uint32_t)((k - mn) >> sh), nbins - 1u);
       const uint32_t g = gofs[bb];
-      if (g != kNoSlot) B[g + atomicAdd(&cur[bb], 1u)] = k;
+      if (g < kFlatBin) B[g + atomicAdd(&cur[bb], 1u)] = k;
     };
     uint32_t i = tid;
     for (; i + 7 * blockDim.x < size; i += 8 * blockDim.x) {
@@ -1396,7 +1465,7 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
   for (uint32_t q = 0; q < (nbig <= (uint32_t)kMaxBig ? nbig : nbins); ++q) {
     const uint32_t bb = nbig <= (uint32_t)kMaxBig ? big[q] : q;
     const uint32_t g = gofs[bb], c = hist[bb];
-    if (g == kNoSlot || c <= 32) continue;
+    if (g >= kFlatBin || c <= 32) continue;
     uint32_t P = 64;
     while (P < c) P <<= 1;
     __syncthreads();
@@ -1411,7 +1480,8 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
   for (uint32_t j = tid; j < m; j += blockDim.x) {
     const Req e = rq[j];
     const uint32_t bb = bin_of_rank(start, nbins, e.rank);
-    out[e.out] = Traits<OutT>::value(B[gofs[bb] + (e.rank - start[bb])]);
+    const uint32_t g = gofs[bb];
+    out[e.out] = Traits<OutT>::value(g == kFlatBin ? bmin[bb] : B[g + (e.rank - start[bb])]);
   }
   __syncthreads();
   return true;

@@ -16,12 +16,13 @@ template <class T>
 static inline uint32_t cap_keys_for() {
   return sizeof(typename Traits<T>::K) == 4 ? 4096u : 2048u;
 }
-// bins (5 arrays), the gather buffer, and a scratch half its size for sorting
-// one large bin: about 44 KB, so that several finishing CTAs share an SM
+// bins (5 arrays), the gather buffer, a scratch half its size for sorting one
+// large bin, per-bin key ranges: about 52 KB (f32) / 60 KB (f64), so that
+// several finishing CTAs share an SM
 template <class T>
 static inline int finish_smem_bytes() {
   using K = typename Traits<T>::K;
-  return (int)(5 * kFinBins * sizeof(uint32_t) + (size_t)cap_keys_for<T>() * sizeof(K) * 3 / 2);
+  return (int)finish_smem_for<K>(cap_keys_for<T>());
 }
 
 static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }

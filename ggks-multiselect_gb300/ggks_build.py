@@ -16,6 +16,12 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libggks_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# GGKS_BATCH_CHECKS=1: the batched kernel checks its data-dependent indices
+# (a diagnostic build in its own object folder)
+CHECKS = os.environ.get("GGKS_BATCH_CHECKS") == "1"
+CHECK_FLAGS = ["-DGGKS_BATCH_CHECKS"] if CHECKS else []
+if CHECKS:
+    BUILD = os.path.join(HERE, "_build_checks")
 
 
 def nvcc():
@@ -30,7 +36,7 @@ def _compile(src, ptxas_verbose):
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj, ""
     cmd = [nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
-           "-I", os.path.join(ROOT, "include"), "-I", CSRC, "-c", src, "-o", obj]
+           "-I", os.path.join(ROOT, "include"), "-I", CSRC, "-c", src, "-o", obj, *CHECK_FLAGS]
     if ptxas_verbose:
         cmd[1:1] = ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -47,12 +53,18 @@ def build(ptxas_verbose=False, jobs=None):
         results = list(ex.map(lambda s: _compile(s, ptxas_verbose), srcs))
     objs = [o for o, _ in results]
     logs = "".join(l for _, l in results)
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
+    stamp = os.path.join(HERE, "_build_kind")
+    kind = "checks" if CHECKS else "release"
+    same_kind = os.path.exists(stamp) and open(stamp).read() == kind
+    if not same_kind or not os.path.exists(LIB) or \
+            os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
         cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs,
                "-Xlinker", "--no-undefined", "-lpthread", "-ldl", "-lrt"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        with open(stamp, "w") as f:
+            f.write(kind)
     return LIB, logs
 
 

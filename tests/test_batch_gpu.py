@@ -172,15 +172,17 @@ def test_batch_survivor_overflow_and_single_key_bins(g, orc):
 
 
 def test_batch_deferred_segments_recurse(g, orc):
-    """float64: 30% of the vector is exactly 1.0, the rest a narrow normal
-    around it plus a few huge values, so the buckets around 1.0 are about 2^40
-    keys wide: the bucket holding 1.0 also holds thousands of other keys and
-    its needed bin exceeds the finisher's shared memory.  The slot is selected
-    again on its keys (recursive level)."""
+    """float64: 30% of the vector is a dense cluster of distinct keys just
+    above 1.0 (within 2^22 keys), the rest a narrow normal around it plus a few
+    huge values, so the buckets around 1.0 are about 2^40 keys wide: the
+    cluster's bin holds hundreds of thousands of distinct keys and exceeds the
+    finisher's shared memory.  The slot is selected again on its keys
+    (recursive level)."""
     r = np.random.default_rng(3)
     n = 1 << 21
     x = 1.0 + r.standard_normal(n) * 1e-3
-    x[: (3 * n) // 10] = 1.0
+    m = (3 * n) // 10
+    x[:m] = 1.0 + r.integers(0, 1 << 20, m) * 2.0 ** -50
     x[-16:] = np.array([1e300, -1e300] * 8)
     r.shuffle(x)
     ctx = g.Context(0)
@@ -238,4 +240,30 @@ def test_batch_pinned_tunings_agree(g, orc):
         _check_batch(g, orc, vecs, ks, np.float32, f"div {div} tile {tile}", ctx=ctx)
         assert g.batch_last_tuning(ctx) == (div, tile)
     g.batch_set_tuning(ctx, 0, 0)
+    ctx.close()
+
+
+def test_batch_single_key_buckets(g, orc):
+    """Buckets holding one repeated key are answered without survivors only
+    when every tile saw that same key: tiles of 1.0 followed by tiles of the
+    next float up (one key per tile, two keys per bucket), the two keys
+    interleaved inside tiles, integer-valued floats, and the largest key."""
+    r = np.random.default_rng(9)
+    n = 1 << 22
+    one = np.float32(1.0)
+    up = np.nextafter(one, np.float32(2.0))
+    halves = np.concatenate([np.full(n // 2, one), np.full(n // 2, up)]).astype(np.float32)
+    halves[0], halves[-1] = -1e6, 1e6
+    mixed = np.where(r.random(n) < 0.5, one, up).astype(np.float32)
+    mixed[0], mixed[-1] = -1e6, 1e6
+    ints = np.floor(r.random(n) * 256).astype(np.float32)
+    nan_top = ints.copy()
+    nan_top[r.integers(0, n, 1000)] = np.uint32(0xFFFFFFFF).view(np.float32)  # largest key
+    vecs = [halves, mixed, ints, nan_top]
+    ks = [np.concatenate([gp_pgrid(n, 64), [n // 2 - 1, n // 2, n // 2 + 1, n // 2 + 2]]).astype(
+        np.uint32) for _ in vecs]
+    ctx = g.Context(0)
+    for div, tile in ((1024, 1 << 20), (256, 1 << 18), (4096, 1 << 16)):
+        g.batch_set_tuning(ctx, div, tile)
+        _check_batch(g, orc, vecs, ks, np.float32, f"single-key div {div} tile {tile}", ctx=ctx)
     ctx.close()

@@ -285,3 +285,30 @@ def test_pinned_host_vector_ingest(g, orc, offset):
         ks = gp.k_distinct(n, 333, offset)
         assert_same(g.multiselect_host(view, ks), orc.multiselect(x, ks), f"pinned {dtype}")
         assert_same(g.topk_host(view, 2048), orc.topk(x, 2048), f"pinned topk {dtype}")
+
+
+@pytest.mark.parametrize("dtype", ["f32", "u32", "f64"])
+def test_narrow_span_with_far_outliers(g, orc, dtype):
+    """Almost every element is one of two neighbouring keys, so the sampled
+    span is tiny; a few far outliers lie beyond every slice and take the
+    splitter table's top entry (a right shift by the whole key width)."""
+    n = 1 << 22
+    r = np.random.default_rng(11)
+    if dtype == "f32":
+        a = np.float32(1.0)
+        x = np.where(r.random(n) < 0.5, a, np.nextafter(a, np.float32(2))).astype(np.float32)
+        x[r.integers(0, n, 5)] = np.float32(1e6)
+        x[r.integers(0, n, 5)] = np.float32(-1e6)
+    elif dtype == "u32":
+        x = np.where(r.random(n) < 0.5, 1000, 1001).astype(np.uint32)
+        x[r.integers(0, n, 5)] = np.uint32(0xFFFFFF00)
+        x[r.integers(0, n, 5)] = np.uint32(3)
+    else:
+        x = np.where(r.random(n) < 0.5, 1.0, np.nextafter(1.0, 2.0))
+        x[r.integers(0, n, 5)] = 1e300
+        x[r.integers(0, n, 5)] = -1e300
+    d = DeviceArray(x)
+    ks = np.concatenate([np.arange(1, 12), np.arange(n - 11, n + 1), [n // 2, n // 2 + 1]])
+    ks = ks.astype(np.uint32)
+    assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks), orc.multiselect(x, ks), dtype)
+    assert_same(g.topk_ptr(d.ptr, n, x.dtype, 20), orc.topk(x, 20), f"topk {dtype}")
