@@ -470,7 +470,7 @@ def run_batched(torch, ggks, gp, dev, sptr, count=4096):
         "req_per_s": round(count / t_batch, 1), "ms_per_batch": round(t_batch * 1e3, 3),
         "GB/s": round(total * 4 / t_batch / 1e9, 1),
         "kernel_ms": round(sum(phase_ms.values()), 3), "phase_ms": phase_ms,
-        "launches_per_batch": round(st["launches"] / calls, 2),
+        "launches_per_batch": round(st["launches"] / calls, 2), "ctas": st["batch_grid"],
         "survivors_per_batch": int(st["survivors"] // calls),
         "recursions_per_batch": round(st["recursions"] / calls, 2),
         "tuning": {"div": tune[0], "tile": tune[1], "autotune_s": round(tune_s, 3)},

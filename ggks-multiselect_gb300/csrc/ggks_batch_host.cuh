@@ -192,13 +192,21 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   static int blocks_per_sm = -1;  // per instantiation; one GPU model per process
   if (blocks_per_sm < 0) {
     cudaFuncSetAttribute((const void *)k_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    // two CTAs of about 100 KB each per SM: ask for the largest shared-memory carveout
+    cudaFuncSetAttribute((const void *)k_batch<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         100);
     int b = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<T>, kBThreads, smem);
     if (e != cudaSuccess) return from_cuda(e);
     blocks_per_sm = b;
   }
   if (blocks_per_sm < 1) return GGKS_UNSUPPORTED;
-  const uint32_t grid = (uint32_t)blocks_per_sm * (uint32_t)ctx.sm_count;
+  // every CTA the SMs hold at once, or fewer when the batch has less work
+  // (each grid barrier waits for every CTA)
+  const uint32_t max_grid = (uint32_t)blocks_per_sm * (uint32_t)ctx.sm_count;
+  const uint32_t work = std::max(std::max(num_tiles, P), R / 8);
+  const uint32_t grid = std::max(1u, std::min(max_grid, work));
+  ctx.stats.batch_grid = grid;
 
   float ms_total = 0.f;
   auto launch = [&]() -> cudaError_t {

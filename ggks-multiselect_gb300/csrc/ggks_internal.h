@@ -17,7 +17,7 @@ namespace ggks {
 // Tunables of the batched path: bucket budget of a problem is about n / div
 // buckets; tiles of the (problem, tile) queue hold `tile` elements.
 struct BatchTune {
-  uint32_t div = 1024;
+  uint32_t div = 256;
   uint32_t tile = 1u << 18;
 };
 

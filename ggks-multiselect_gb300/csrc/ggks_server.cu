@@ -9,8 +9,10 @@
 //              requests whose data is on the device to the executor;
 //   executor   takes every device-ready request (up to max_batch), runs one
 //              batched selection per element type (select_batch: one
-//              persistent launch each), scatters the results to the callers'
-//              buffers, releases the requests' device bytes.
+//              persistent launch each; a type with a single request takes the
+//              single-vector pipeline, whose latency is lower), scatters the
+//              results to the callers' buffers, releases the requests' device
+//              bytes.
 // Requests that arrive while a batch is on the GPU are admitted and uploaded
 // meanwhile (the copy stream overlaps the compute stream) and join the next
 // batch.  Batches run one after another on the compute stream, so no two
@@ -122,6 +124,19 @@ static void admit_loop(Server *S) {
 
 template <class T>
 static void run_group(Server *S, std::vector<SReq *> &g) {
+  if (g.size() == 1) {
+    // a lone request: the single-vector pipeline has the lower latency
+    SReq *r = g[0];
+    const T *vec = static_cast<const T *>(r->host ? r->dvec : r->vec);
+    ReqSource src;
+    src.h_k = r->k.data();
+    const T *res = nullptr;
+    std::lock_guard<std::mutex> lk(S->ctx.mu);
+    r->status = select<T, T>(S->ctx, vec, r->n, src, (uint32_t)r->k.size(), nullptr, &res,
+                             S->ctx.stream, nullptr);
+    if (r->status == GGKS_OK) std::memcpy(r->out, res, r->k.size() * sizeof(T));
+    return;
+  }
   std::vector<const void *> vecs(g.size());
   std::vector<uint64_t> ns(g.size());
   std::vector<uint32_t> off(g.size() + 1, 0), ks;

@@ -283,6 +283,7 @@ typedef struct ggks_stats {
   uint64_t batch_calls;               /* batched calls completed */
   uint64_t batch_problems;            /* problems selected by batched calls */
   double batch_phase_ms[GGKS_NUM_BATCH_PHASES]; /* device time per batch phase */
+  uint64_t batch_grid;                /* CTAs of the last batched launch */
 } ggks_stats;
 
 /* phase indices of ggks_stats.batch_phase_ms (one persistent launch; each
