@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--only", choices=["batched", "served"], default=None,
+                    help="run one section alone and print it as its own JSON line (profiling)")
+    ap.add_argument("--batch-problems", type=int, default=4096)
     ap.add_argument("--log2n", type=int, default=N_LOG2)
     return ap.parse_args()
 
@@ -605,10 +608,29 @@ def read_traffic(kernel):
     return None
 
 
+def run_section(args):
+    """One section alone (for profiling): its object as one JSON line."""
+    import torch
+
+    import ggks
+    import ggks_problems as gp
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    if args.only == "batched":
+        res = run_batched(torch, ggks, gp, dev, stream.cuda_stream, count=args.batch_problems)
+    else:
+        res = run_served(torch, ggks, gp, dev, stream.cuda_stream)
+    print(json.dumps({"section": args.only, args.only: res}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.only:
+        return run_section(args)
     return run_ggks(args)
 
 
