@@ -341,25 +341,57 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
   // ---------------- phase 1: splitter tables
   for (uint32_t p = queue_pop(&ctrl->queue[0], &s_item); p < A.num_probs;
        p = queue_pop(&ctrl->queue[0], &s_item)) {
+#ifdef GGKS_BATCH_TIMING
+    const long long c0 = clock64();
+#endif
     const BProb P = A.probs[p];
     const T *x = reinterpret_cast<const T *>(P.x);
     K *samples = reinterpret_cast<K *>(sm);
     K lo = KeyMax<K>::v, hi = 0;
-    for (uint32_t i = tid; i < P.S; i += nt) {
-      const uint64_t pos =
-          (uint64_t)P.S >= P.n ? i : ((uint64_t)hash32(i * 0x9E3779B9u + 0x5EEDu) * P.n) >> 32;
-      const K k = Traits<T>::key(x[pos]);
-      samples[i] = k;
-      lo = k < lo ? k : lo;
-      hi = k > hi ? k : hi;
+    if ((uint64_t)P.S >= P.n) {
+      // small problem: every element is a sample
+      for (uint32_t i = tid; i < P.S; i += nt) {
+        const K k = Traits<T>::key(x[i]);
+        samples[i] = k;
+        lo = k < lo ? k : lo;
+        hi = k > hi ? k : hi;
+      }
+    } else {
+      // S / CH chunks of CH consecutive elements (one 32-byte sector's worth)
+      // at hashed positions: the whole grid gathers at once, and a sector read
+      // for one 4-byte key would spend 8x the DRAM traffic
+      constexpr uint32_t CH = 32 / sizeof(T);
+      const uint32_t nch = P.S / CH;
+      const uint64_t slots = P.n / CH;
+      for (uint32_t c = tid; c < nch; c += nt) {
+        const uint64_t pos = (((uint64_t)hash32(c * 0x9E3779B9u + 0x5EEDu) * slots) >> 32) * CH;
+        K k[CH];
+#pragma unroll
+        for (uint32_t e = 0; e < CH; ++e) k[e] = Traits<T>::key(x[pos + e]);
+#pragma unroll
+        for (uint32_t e = 0; e < CH; ++e) {
+          samples[c * CH + e] = k[e];
+          lo = k[e] < lo ? k[e] : lo;
+          hi = k[e] > hi ? k[e] : hi;
+        }
+      }
     }
     lo = block_reduce(lo, [](K u, K v) { return u < v ? u : v; }, redk);
     hi = block_reduce(hi, [](K u, K v) { return u > v ? u : v; }, redk);
+#ifdef GGKS_BATCH_TIMING
+    const long long c1 = clock64();
+#endif
     if (!BCHECK(P.lut_off + (1u << P.nsl_bits) < A.lut_words && P.S <= kBMaxS, 1, p, P.lut_off))
       continue;
     build_lut_cta<K, kBSpt, true>(samples, P.S, lo, hi, P.nb_max, A.luts + P.lut_off, &s_hdr,
                                   (int)P.nsl_bits);
     __syncthreads();
+#ifdef GGKS_BATCH_TIMING
+    if (tid == 0) {
+      atomicAdd((unsigned long long *)&ctrl->dbg_a, (unsigned long long)(c1 - c0));
+      atomicAdd((unsigned long long *)&ctrl->dbg_b, (unsigned long long)(clock64() - c1));
+    }
+#endif
     if (tid == 0) {
       BHdr h;
       h.base = s_hdr.base;
@@ -459,54 +491,63 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
                   6, p, nb))
         continue;
       for (uint32_t j = tid; j <= nsl; j += nt) lut[j] = __ldcg(A.luts + P.lut_off + j);
-      // each column of the rows becomes its exclusive prefix over the tiles;
-      // a warp covers 32 neighbouring buckets of a row.  Dup problems also
-      // learn which buckets hold a single key in every tile: those become
-      // flat slots (flag bit 1; the key goes to tile 0's key row).
-      for (uint32_t b = tid; b < nb; b += nt) {
-        uint32_t *col = A.rows + P.row0 + b;
-        uint32_t run = 0, r = 0;
-        bool one = H.dup != 0;
-        K key0 = KeyMax<K>::v;
-        for (; r + 8 <= nr; r += 8) {
-          uint32_t v[8];
+      // each column of the rows becomes its exclusive prefix over the tiles
+      // (tile 0's prefix is 0 and is not stored: phase 4 knows it); a warp
+      // covers 32 neighbouring buckets of a row, a thread four buckets at a
+      // time so that their loads overlap.  Dup problems also learn which
+      // buckets hold a single key in every tile: those become flat slots
+      // (flag bit 1; the key goes to tile 0's key row).
+      for (uint32_t b0 = tid; b0 < nb; b0 += 4 * nt) {
+        uint32_t run[4] = {0, 0, 0, 0};
+        bool one[4];
+        K key0[4];
 #pragma unroll
-          for (int q = 0; q < 8; ++q) v[q] = __ldcg(col + (uint64_t)(r + q) * P.nb_max);
+        for (int u = 0; u < 4; ++u) {
+          one[u] = H.dup != 0;
+          key0[u] = KeyMax<K>::v;
+        }
+        for (uint32_t r = 0; r < nr; ++r) {
+          uint32_t *row = A.rows + P.row0 + (uint64_t)r * P.nb_max;
+          uint32_t v[4];
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            col[(uint64_t)(r + q) * P.nb_max] = run;
-            run += v[q] & ~kMixed;
+          for (int u = 0; u < 4; ++u) {
+            const uint32_t b = b0 + u * nt;
+            v[u] = b < nb ? __ldcg(row + b) : 0u;
           }
           if (H.dup) {
+            K rr[4];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              if (v[q] & kMixed) one = false;
-              if (v[q] & ~kMixed) {
-                const K rr = ldcg_u(reps + P.row0 + (uint64_t)(r + q) * P.nb_max + b);
-                if (key0 == KeyMax<K>::v) key0 = rr;
-                one = one && rr == key0;
+            for (int u = 0; u < 4; ++u) {
+              const uint32_t b = b0 + u * nt;
+              rr[u] = (b < nb && (v[u] & ~kMixed)) ? ldcg_u(reps + P.row0 + (uint64_t)r * P.nb_max + b)
+                                                   : KeyMax<K>::v;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              if (v[u] & kMixed) one[u] = false;
+              if (v[u] & ~kMixed) {
+                if (key0[u] == KeyMax<K>::v) key0[u] = rr[u];
+                one[u] = one[u] && rr[u] == key0[u];
               }
             }
           }
-        }
-        for (; r < nr; ++r) {
-          const uint32_t v = __ldcg(col + (uint64_t)r * P.nb_max);
-          col[(uint64_t)r * P.nb_max] = run;
-          run += v & ~kMixed;
-          if (H.dup) {
-            if (v & kMixed) one = false;
-            if (v & ~kMixed) {
-              const K rr = ldcg_u(reps + P.row0 + (uint64_t)r * P.nb_max + b);
-              if (key0 == KeyMax<K>::v) key0 = rr;
-              one = one && rr == key0;
-            }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const uint32_t b = b0 + u * nt;
+            if (b < nb && r > 0) row[b] = run[u];
+            run[u] += v[u] & ~kMixed;
           }
         }
-        one = one && run > 0 && key0 != KeyMax<K>::v;
-        if (one) reps[P.row0 + b] = key0;
-        cnt[b] = run;
-        excl[b] = run;  // the count, until the scan below
-        flag[b] = one ? 2 : 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const uint32_t b = b0 + u * nt;
+          if (b >= nb) continue;
+          const bool o = one[u] && run[u] > 0 && key0[u] != KeyMax<K>::v;
+          if (o) reps[P.row0 + b] = key0[u];
+          cnt[b] = run[u];
+          excl[b] = run[u];  // the count, until the scan below
+          flag[b] = o ? 2 : 0;
+        }
       }
       __syncthreads();
       // bucket prefix: contiguous bucket range per thread
@@ -679,7 +720,8 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         if (__ldcg(A.seg_size + g) == 0) continue;
         const uint32_t b = __ldcg(A.seg_bucket + g);
         if (!BCHECK(b < H.nb && s < P.num_req, 10, b, s)) continue;
-        cursor[swz(b)] = (uint32_t)(ldcg_u(A.seg_off + g) - H.surv_off + __ldcg(row + b));
+        const uint32_t pre = tl.rank ? __ldcg(row + b) : 0u;  // tile 0 starts each bucket
+        cursor[swz(b)] = (uint32_t)(ldcg_u(A.seg_off + g) - H.surv_off + pre);
       }
       __syncthreads();
       K *sp = surv + H.surv_off;

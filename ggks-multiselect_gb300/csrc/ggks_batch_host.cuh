@@ -238,6 +238,10 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   for (int round = 0;; ++round) {
     BCtrl c;
     std::memcpy(&c, h_ctrl, sizeof(BCtrl));
+#ifdef GGKS_BATCH_TIMING
+    fprintf(stderr, "ggks batch timing: %u problems, gather %.0f cycles/problem, table %.0f cycles/problem\n",
+            P, (double)c.dbg_a / P, (double)c.dbg_b / P);
+#endif
 #ifdef GGKS_BATCH_CHECKS
     if (c.dbg_code)
       fprintf(stderr, "ggks batch index check %u failed: %llu %llu (status %u)\n", c.dbg_code,

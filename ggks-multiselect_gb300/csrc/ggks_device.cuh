@@ -538,12 +538,17 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
                                 (uint32_t)KeyMax<K>::bits);
   __syncthreads();
   // Warp-aggregated histogram updates pay off when lanes of a warp often hit
-  // the same bucket.  The chance that two elements share a bucket (the sum of
-  // squared bucket shares) is estimated from disjoint pairs of samples.
+  // the same bucket: the chance that two elements share a bucket is estimated
+  // from neighbouring samples (2q, 2q + 1), which are neighbouring elements
+  // when the samples come in runs, as the histogram's warps see them.  The
+  // chance that two elements share a key, a property of the whole vector, is
+  // estimated from far-apart samples (q, q + S/2).
   uint32_t same = 0, same_key = 0;
   for (uint32_t q = tid; q < S / 2; q += blockDim.x) {
     const K a = SMEM ? samples[2 * q] : __ldcg(samples + 2 * q);
     const K b = SMEM ? samples[2 * q + 1] : __ldcg(samples + 2 * q + 1);
+    const K c = SMEM ? samples[q] : __ldcg(samples + q);
+    const K d2 = SMEM ? samples[q + S / 2] : __ldcg(samples + q + S / 2);
     auto bucket = [&](K k) {
       const K d = k - kmin;
       const K idx = d >> shift;
@@ -552,7 +557,7 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
       return (uint32_t)((int32_t)e >> 7) + shr_clamp(d, e & 127u);
     };
     same += bucket(a) == bucket(b) ? 1u : 0u;
-    same_key += a == b ? 1u : 0u;
+    same_key += c == d2 ? 1u : 0u;
   }
   same = block_reduce(same, [](uint32_t p, uint32_t q) { return p + q; }, red32);
   same_key = block_reduce(same_key, [](uint32_t p, uint32_t q) { return p + q; }, red32);

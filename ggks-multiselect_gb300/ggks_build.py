@@ -20,8 +20,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # (a diagnostic build in its own object folder)
 CHECKS = os.environ.get("GGKS_BATCH_CHECKS") == "1"
 CHECK_FLAGS = ["-DGGKS_BATCH_CHECKS"] if CHECKS else []
+# GGKS_BATCH_TIMING=1: the batched kernel reports per-problem cycles of its
+# table phase (diagnostic build, own object folder)
+if os.environ.get("GGKS_BATCH_TIMING") == "1":
+    CHECKS = True
+    CHECK_FLAGS.append("-DGGKS_BATCH_TIMING")
 if CHECKS:
-    BUILD = os.path.join(HERE, "_build_checks")
+    BUILD = os.path.join(HERE, "_build_" + "_".join(f[7:].lower() for f in CHECK_FLAGS))
 
 
 def nvcc():
@@ -54,7 +59,7 @@ def build(ptxas_verbose=False, jobs=None):
     objs = [o for o, _ in results]
     logs = "".join(l for _, l in results)
     stamp = os.path.join(HERE, "_build_kind")
-    kind = "checks" if CHECKS else "release"
+    kind = " ".join(CHECK_FLAGS) if CHECKS else "release"
     same_kind = os.path.exists(stamp) and open(stamp).read() == kind
     if not same_kind or not os.path.exists(LIB) or \
             os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
