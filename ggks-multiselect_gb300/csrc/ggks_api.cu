@@ -604,7 +604,14 @@ int ggks_context_set_profiling(ggks_context *ctx, int on) {
     }
     c->events_ready = true;
   }
-  c->profiling = on != 0;
+  // on: 0 = off; GGKS_PROFILE_PASSES(mask) = the passes in mask; any other
+  // value = every pass
+  if (on == 0)
+    c->profiling = 0;
+  else if ((uint32_t)on & 0x80000000u)
+    c->profiling = (uint32_t)on & ((1u << GGKS_NUM_PASSES) - 1u);
+  else
+    c->profiling = (1u << GGKS_NUM_PASSES) - 1u;
   return GGKS_OK;
 }
 

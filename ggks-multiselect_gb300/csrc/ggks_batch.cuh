@@ -725,20 +725,18 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       }
       __syncthreads();
       K *sp = surv + H.surv_off;
-      const uint64_t cap = A.surv_cap - H.surv_off;
+      // inactive cursors carry bit 31, so one compare keeps inactive keys out
+      // and every store inside the buffer (see compact_one)
+      const uint64_t room = A.surv_cap - H.surv_off;
+      const uint32_t cap = (uint32_t)(room < (uint64_t)kInactive ? room : kInactive);
       const K base = (K)H.base;
       const uint32_t shift = H.shift;
-      bool overrun = false;
       for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
         uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
         if (!BCHECK(ub < H.nb, 9, ub, H.nb)) return;
         const uint32_t pos = atomicAdd(&cursor[swz(ub)], 1u);
-        const bool active = !(pos & kInactive);
-        const bool fits = pos < cap;
-        st_global_if(sp + pos, k, active && fits);
-        overrun |= active && !fits;
+        st_global_if(sp + pos, k, pos < cap);
       });
-      if (overrun) s_bad = true;
       __syncthreads();
       // each cursor must end where the next tile's range of the bucket starts
       for (uint32_t s = tid; s < H.num_slots; s += nt) {

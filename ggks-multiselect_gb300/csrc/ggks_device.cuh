@@ -544,7 +544,8 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
   // chance that two elements share a key, a property of the whole vector, is
   // estimated from far-apart samples (q, q + S/2).
   uint32_t same = 0, same_key = 0;
-  for (uint32_t q = tid; q < S / 2; q += blockDim.x) {
+  const uint32_t npairs = S / 2 < 4096u ? S / 2 : 4096u;  // enough for a 1/32 estimate
+  for (uint32_t q = tid; q < npairs; q += blockDim.x) {
     const K a = SMEM ? samples[2 * q] : __ldcg(samples + 2 * q);
     const K b = SMEM ? samples[2 * q + 1] : __ldcg(samples + 2 * q + 1);
     const K c = SMEM ? samples[q] : __ldcg(samples + q);
@@ -570,10 +571,10 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
     h.nb = nb;
     // collision chance >= 1/32: with 32 lanes, about 15 same-bucket pairs per
     // warp access
-    h.heavy = (S >= 256 && 32ull * same >= S / 2) ? 1u : 0u;
+    h.heavy = (S >= 256 && 32ull * same >= npairs) ? 1u : 0u;
     // two elements share a key with chance >= 1 / nb: buckets holding a single
     // key (many copies of it) are likely
-    h.dup = (S >= 256 && (uint64_t)same_key * nb >= S / 2) ? 1u : 0u;
+    h.dup = (S >= 256 && (uint64_t)same_key * nb >= npairs) ? 1u : 0u;
     *hdr = h;
   }
 }
@@ -1043,13 +1044,16 @@ __global__ void __launch_bounds__(1024, 1)
 // active bucket (< 2^31), or kInactive + (elements seen so far) for an inactive
 // one.  Every element takes one shared atomic on its bucket's cursor and the
 // returned value decides whether it is stored: no divergent branch per
-// survivor.  In heavy mode lanes of a warp that hit the same bucket share one
-// atomic (match.any) and take consecutive positions.
+// survivor.  cap = min(survivor capacity, kInactive), so the single compare
+// pos < cap rejects inactive buckets and keeps every store inside the buffer
+// (a position past the capacity can only come from an input that changed
+// between the passes; the cursor check at the end of the pass reports it).
+// In heavy mode lanes of a warp that hit the same bucket share one atomic
+// (match.any) and take consecutive positions.
 template <class T, bool HEAVY>
 __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Traits<T>::K base,
                                             uint32_t shift, const uint32_t *lut, uint32_t *cursor,
-                                            typename Traits<T>::K *__restrict__ surv,
-                                            uint64_t surv_cap, bool *overrun) {
+                                            typename Traits<T>::K *__restrict__ surv, uint32_t cap) {
   const uint32_t b = bucket_of(k, base, shift, lut);
   uint32_t pos;
   if (HEAVY) {
@@ -1064,17 +1068,14 @@ __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Tr
     pos = atomicAdd(&cursor[b], 1u);
   }
   // store without a branch: a predicated st.global
-  const bool active = !(pos & kInactive);
-  const bool fits = pos < surv_cap;
-  st_global_if(surv + pos, k, active && fits);
-  *overrun |= active && !fits;
+  st_global_if(surv + pos, k, pos < cap);
 }
 
 template <class T, int UNROLL, bool HEAVY>
 __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n, uint32_t *cursor,
                                              const uint32_t *lut, typename Traits<T>::K base,
                                              uint32_t shift, typename Traits<T>::K *__restrict__ surv,
-                                             uint64_t surv_cap, bool *overrun) {
+                                             uint32_t cap) {
   using K = typename Traits<T>::K;
   using V = typename Traits<T>::Vec;
   constexpr int PV = Traits<T>::kPerVec;
@@ -1098,7 +1099,7 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
       vec_keys<T>(v[u], kk);
 #pragma unroll
       for (int e = 0; e < PV; ++e)
-        compact_one<T, HEAVY>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun);
+        compact_one<T, HEAVY>(kk[e], base, shift, lut, cursor, surv, cap);
     }
   }
   const uint32_t owner = (uint32_t)(ntiles % gridDim.x);
@@ -1109,12 +1110,12 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
       vec_keys<T>(vv, kk);
 #pragma unroll
       for (int e = 0; e < PV; ++e)
-        compact_one<T, false>(kk[e], base, shift, lut, cursor, surv, surv_cap, overrun);
+        compact_one<T, false>(kk[e], base, shift, lut, cursor, surv, cap);
     }
     for (uint64_t e = threadIdx.x; e < sp.head; e += blockDim.x)
-      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun);
+      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, cap);
     for (uint64_t e = sp.tail0 + threadIdx.x; e < n; e += blockDim.x)
-      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, surv_cap, overrun);
+      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, cap);
   }
 }
 
@@ -1149,12 +1150,11 @@ __global__ void __launch_bounds__(1024, 1)
     cursor[b] = (uint32_t)(seg_off[s] + prefix[(uint64_t)c * nb_max + b]);
   }
   __syncthreads();
-  bool overrun = false;
+  const uint32_t cap = (uint32_t)(surv_cap < (uint64_t)kInactive ? surv_cap : kInactive);
   if (h.heavy)
-    compact_body<T, UNROLL, true>(x, n, cursor, lut, h.base, h.shift, surv, surv_cap, &overrun);
+    compact_body<T, UNROLL, true>(x, n, cursor, lut, h.base, h.shift, surv, cap);
   else
-    compact_body<T, UNROLL, false>(x, n, cursor, lut, h.base, h.shift, surv, surv_cap, &overrun);
-  if (overrun) s_bad = true;
+    compact_body<T, UNROLL, false>(x, n, cursor, lut, h.base, h.shift, surv, cap);
   __syncthreads();
   // every cursor must have reached the start of the next CTA's range (the
   // bucket's end for the last CTA); anything else means the input changed

@@ -56,7 +56,7 @@ struct Context {
   BatchTune pinned_tune{0, 0};  // div != 0: used for every batch (no autotuning)
 
   ggks_stats stats{};
-  bool profiling = false;
+  uint32_t profiling = 0;  // bit i: time pass i with CUDA events
   bool events_ready = false;
   cudaEvent_t ev0[GGKS_NUM_PASSES]{}, ev1[GGKS_NUM_PASSES]{};
   cudaEvent_t copy_done = nullptr;

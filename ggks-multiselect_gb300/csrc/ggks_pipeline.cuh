@@ -121,10 +121,10 @@ struct PassTimer {
   cudaStream_t s;
   int pass;
   PassTimer(Context &c, cudaStream_t st, int p) : ctx(c), s(st), pass(p) {
-    if (ctx.profiling) cudaEventRecord(ctx.ev0[pass], s);
+    if (ctx.profiling & (1u << pass)) cudaEventRecord(ctx.ev0[pass], s);
   }
   ~PassTimer() {
-    if (ctx.profiling) cudaEventRecord(ctx.ev1[pass], s);
+    if (ctx.profiling & (1u << pass)) cudaEventRecord(ctx.ev1[pass], s);
     ctx.stats.launches++;
     ctx.stats.pass_launches[pass]++;
   }
@@ -133,7 +133,7 @@ struct PassTimer {
 static void collect_pass_times(Context &ctx, const bool *ran) {
   if (!ctx.profiling) return;
   for (int i = 0; i < GGKS_NUM_PASSES; ++i) {
-    if (!ran[i]) continue;
+    if (!ran[i] || !(ctx.profiling & (1u << i))) continue;
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, ctx.ev0[i], ctx.ev1[i]) == cudaSuccess) ctx.stats.pass_ms[i] += ms;
   }

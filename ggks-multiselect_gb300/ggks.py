@@ -200,8 +200,8 @@ class Context:
     def reset_stats(self):
         reset_stats(self)
 
-    def set_profiling(self, on=True):
-        set_profiling(self, on)
+    def set_profiling(self, on=True, passes=None):
+        set_profiling(self, on, passes)
 
 
 def _h(ctx):
@@ -226,8 +226,19 @@ def reset_stats(ctx=None):
     _check(lib().ggks_context_reset_stats(_h(ctx)), "reset_stats")
 
 
-def set_profiling(ctx=None, on=True):
-    _check(lib().ggks_context_set_profiling(_h(ctx), 1 if on else 0), "set_profiling")
+def set_profiling(ctx=None, on=True, passes=None):
+    """Time the passes with CUDA events: all of them, or only those named in
+    passes (names of PASS_NAMES)."""
+    if not on:
+        v = 0
+    elif passes is None:
+        v = 1
+    else:
+        mask = 0
+        for p in passes:
+            mask |= 1 << PASS_NAMES.index(p)
+        v = ctypes.c_int32(0x80000000 | mask).value
+    _check(lib().ggks_context_set_profiling(_h(ctx), v), "set_profiling")
 
 
 # ---------------------------------------------------------------------------

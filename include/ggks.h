@@ -306,6 +306,9 @@ int ggks_context_get_stats(ggks_context *ctx, ggks_stats *out);
 int ggks_context_reset_stats(ggks_context *ctx);
 /* on != 0: time every pass with CUDA events on the context's stream */
 int ggks_context_set_profiling(ggks_context *ctx, int on);
+/* value for ggks_context_set_profiling: time only the passes whose bits
+ * (1 << GGKS_PASS_*) are set in mask */
+#define GGKS_PROFILE_PASSES(mask) ((int)(0x80000000u | (uint32_t)(mask)))
 const char *ggks_status_string(int status);
 int ggks_version(void);
 
