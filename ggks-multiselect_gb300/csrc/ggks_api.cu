@@ -470,6 +470,17 @@ int ggks_topk_u32(const uint32_t *d_vec, uint64_t n, uint32_t K, uint32_t *h_out
                   const ggks_opts *opts) {
   return api_topk<uint32_t>(d_vec, n, K, h_out, opts, false);
 }
+int ggks_select_f32(const float *d_vec, uint64_t n, uint32_t k, float *out, const ggks_opts *opts) {
+  return api_multiselect<float>(d_vec, n, &k, 1, out, opts, false);
+}
+int ggks_select_f64(const double *d_vec, uint64_t n, uint32_t k, double *out,
+                    const ggks_opts *opts) {
+  return api_multiselect<double>(d_vec, n, &k, 1, out, opts, false);
+}
+int ggks_select_u32(const uint32_t *d_vec, uint64_t n, uint32_t k, uint32_t *out,
+                    const ggks_opts *opts) {
+  return api_multiselect<uint32_t>(d_vec, n, &k, 1, out, opts, false);
+}
 int ggks_topk_host_f32(const float *h_vec, uint64_t n, uint32_t K, float *h_out,
                        const ggks_opts *opts) {
   return api_topk<float>(h_vec, n, K, h_out, opts, true);

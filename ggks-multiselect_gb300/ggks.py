@@ -105,6 +105,7 @@ EXPORTS = [
     "ggks_batch_last_tuning", "ggks_batch_set_tuning",
     "ggks_server_create", "ggks_server_destroy", "ggks_server_submit", "ggks_server_wait",
     "ggks_server_get_stats", "ggks_server_set_tuning",
+    "ggks_select_f32", "ggks_select_f64", "ggks_select_u32",
 ]
 
 _lib = None
@@ -123,7 +124,7 @@ def lib():
             f = getattr(L, nm + sfx)
             f.argtypes = [P, U64, P, U32, P, ctypes.POINTER(Opts)]
             f.restype = ctypes.c_int
-        for nm in ("ggks_topk_", "ggks_topk_host_"):
+        for nm in ("ggks_topk_", "ggks_topk_host_", "ggks_select_"):
             f = getattr(L, nm + sfx)
             f.argtypes = [P, U64, U32, P, ctypes.POINTER(Opts)]
             f.restype = ctypes.c_int
@@ -282,6 +283,17 @@ def topk_ptr(d_ptr, n, dtype, K, ctx=None, stream=None, out=None, out_device_ptr
         ctypes.c_void_p(d_ptr), int(n), int(K), ctypes.c_void_p(optr), ctypes.byref(o))
     _check(st, "topk")
     return out
+
+
+def select_ptr(d_ptr, n, dtype, k, ctx=None, stream=None):
+    """The k-th largest (1-based) of the device vector at d_ptr."""
+    dtype = np.dtype(dtype)
+    out = np.empty(1, dtype=dtype)
+    o = _opts(ctx, stream)
+    st = getattr(lib(), "ggks_select_" + _SFX[dtype])(ctypes.c_void_p(d_ptr), int(n), int(k),
+                                                       out.ctypes.data, ctypes.byref(o))
+    _check(st, "select")
+    return out[0]
 
 
 def multiselect_noalloc_f32(d_ptr, n, d_k_ptr, num_k, d_out_ptr, stream=None):
@@ -530,6 +542,23 @@ def bucketMultiselectWrapper(d_vector, length, kVals, numKs, outputs, blocks=0, 
     k = np.ascontiguousarray(np.asarray(kVals)[:numKs], dtype=np.uint32)
     multiselect_ptr(ptr, length, dtype, k, out=outputs)
     return 1
+
+
+def bucketSelectWrapper(d_vector, length, K, blocks=0, threads=0, dtype=None):
+    """BucketSelect::bucketSelectWrapper (bucketSelect.cu:453-471): the K-th
+    largest element of the device vector (a CUDA tensor, or a pointer with
+    dtype); blocks / threads are accepted and ignored."""
+    if hasattr(d_vector, "data_ptr"):
+        ptr, dtype = d_vector.data_ptr(), _tensor_dtype(d_vector)
+    else:
+        ptr = int(d_vector)
+    return select_ptr(ptr, length, dtype, K)
+
+
+def randomizedBucketSelectWrapper(d_vector, length, K, blocks=0, threads=0, dtype=None):
+    """RandomizedBucketSelect::randomizedBucketSelectWrapper
+    (randomizedBucketSelect.cu:861-881): same contract, same exact path."""
+    return bucketSelectWrapper(d_vector, length, K, blocks, threads, dtype)
 
 
 class Results:

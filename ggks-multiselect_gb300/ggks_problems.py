@@ -354,3 +354,28 @@ def serving_trace(pool_sizes, rate, count, seed):
             out.append({"t": float(t[i]), "dtype": dt, "vec": vi, "k": None,
                         "K": int(min(n, r.integers(16, 4097)))})
     return out
+
+
+# ---------------------------------------------------------------------------
+# the reference's names, in its order (generateProblems.cu:53-55, :369-376,
+# :425-428, :581-584): the comparison harness writes them into its CSV report
+# ---------------------------------------------------------------------------
+REFERENCE_DISTRIBUTIONS = {
+    "f32": [("uniform", "UNIFORM FLOATS"), ("normal", "NORMAL FLOATS"),
+            ("killer", "KILLER FLOATS"), ("half_normal", "HALF NORMAL FLOATS"),
+            ("normal100", "NORMAL FLOATS 100"), ("huge_uniform", "HUGE UNIFORM FLOATS"),
+            ("noisy", "NOISY FLOATS"), ("all_ones", "ALL ONES FLOATS"),
+            ("ones_twos", "ONES TWOS FLOAT"), ("cauchy", "CAUCHY FLOAT")],
+    "f64": [("uniform", "UNIFORM DOUBLES"), ("normal", "NORMAL DOUBLES"),
+            ("killer", "KILLER DOUBLES")],
+    "u32": [("uniform", "UNIFORM UNSIGNED INTEGERS"), ("sorted", "SORTED UINTS"),
+            ("zero_to_four", "UNIFORM 0-4")],
+}
+
+REFERENCE_K_DISTRIBUTIONS = [
+    ("Uniform Random Ks", lambda n, c, s: k_uniform_random(n, c, s)),
+    ("Uniform Ks", lambda n, c, s: k_uniform(n, c)),
+    ("Normal Random Ks", lambda n, c, s: k_normal(n, c, s)),
+    ("Cluster Ks", lambda n, c, s: k_cluster(n, c, s)),
+    ("Sectioned Ks", lambda n, c, s: k_sectioned(n, c, s)),
+]

@@ -111,6 +111,21 @@ int ggks_topk_host_u32(const uint32_t *h_vec, uint64_t n, uint32_t K, uint32_t *
                        const ggks_opts *opts);
 
 /* ------------------------------------------------------------------------ */
+/* Single-k select                                                           */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces BucketSelect::bucketSelectWrapper<T> (bucketSelect.cu:453-471) and
+ * RandomizedBucketSelect::randomizedBucketSelectWrapper<T>
+ * (randomizedBucketSelect.cu:861-881), which return the K-th largest element
+ * of a device vector: one output, *out = the k-th largest (1-based), host
+ * memory (device memory with GGKS_FLAG_OUT_DEVICE).  A multiselect with one k. */
+int ggks_select_f32(const float *d_vec, uint64_t n, uint32_t k, float *out, const ggks_opts *opts);
+int ggks_select_f64(const double *d_vec, uint64_t n, uint32_t k, double *out,
+                    const ggks_opts *opts);
+int ggks_select_u32(const uint32_t *d_vec, uint64_t n, uint32_t k, uint32_t *out,
+                    const ggks_opts *opts);
+
+/* ------------------------------------------------------------------------ */
 /* Multiselect without allocation                                            */
 /* ------------------------------------------------------------------------ */
 

@@ -8,6 +8,9 @@
 //   timeBucketMultiselect<T>                         multiselectTimingFunctions.cu:100-122
 //   timeBucketTopkselect<T>                          multiselectTimingFunctions.cu:205-231
 //   randomizedTopkSelectWrapper<T>                   randomizedTopkSelect.cu:210-213
+//   BucketSelect::bucketSelectWrapper<T>             bucketSelect.cu:453-471
+//   RandomizedBucketSelect::randomizedBucketSelectWrapper<T>
+//                                                    randomizedBucketSelect.cu:861-881
 //
 // T is float, double or unsigned int (the reference's uint).  Differences:
 //   - errors are not silent: the wrapper returns (T)0 instead of (T)1 and
@@ -43,6 +46,9 @@ struct Api<float> {
   static int tk_host(const float *h, uint64_t n, uint32_t K, float *o) {
     return ggks_topk_host_f32(h, n, K, o, nullptr);
   }
+  static int sel(const float *d, uint64_t n, uint32_t k, float *o) {
+    return ggks_select_f32(d, n, k, o, nullptr);
+  }
 };
 template <>
 struct Api<double> {
@@ -57,6 +63,9 @@ struct Api<double> {
   }
   static int tk_host(const double *h, uint64_t n, uint32_t K, double *o) {
     return ggks_topk_host_f64(h, n, K, o, nullptr);
+  }
+  static int sel(const double *d, uint64_t n, uint32_t k, double *o) {
+    return ggks_select_f64(d, n, k, o, nullptr);
   }
 };
 template <>
@@ -74,6 +83,9 @@ struct Api<unsigned int> {
   }
   static int tk_host(const unsigned int *h, uint64_t n, uint32_t K, unsigned int *o) {
     return ggks_topk_host_u32(h, n, K, o, nullptr);
+  }
+  static int sel(const unsigned int *d, uint64_t n, uint32_t k, unsigned int *o) {
+    return ggks_select_u32(d, n, k, o, nullptr);
   }
 };
 inline int &last_status() {
@@ -178,5 +190,40 @@ T *randomizedTopkSelectWrapper(T *list, int size, int k) {
   }
   return out;
 }
+
+namespace ggks_detail {
+template <typename T>
+T select_one(T *d_vector, int length, int K) {
+  T v = (T)0;
+  if (length <= 0 || K <= 0 || K > length) {
+    last_status() = GGKS_INVALID_ARG;
+    return v;
+  }
+  last_status() = Api<T>::sel(d_vector, (uint64_t)length, (uint32_t)K, &v);
+  return v;
+}
+}  // namespace ggks_detail
+
+// bucketSelect.cu:453-471: the K-th largest element (1-based) of the device
+// vector; BucketMultiselect::lastStatus() reports errors (the value is then 0).
+namespace BucketSelect {
+template <typename T>
+T bucketSelectWrapper(T *d_vector, int length, int K, int blocks, int threads) {
+  (void)blocks;
+  (void)threads;
+  return ggks_detail::select_one(d_vector, length, K);
+}
+}  // namespace BucketSelect
+
+// randomizedBucketSelect.cu:861-881: same contract; computed by the same
+// exact bucket path.
+namespace RandomizedBucketSelect {
+template <typename T>
+T randomizedBucketSelectWrapper(T *d_vector, int length, int K, int blocks, int threads) {
+  (void)blocks;
+  (void)threads;
+  return ggks_detail::select_one(d_vector, length, K);
+}
+}  // namespace RandomizedBucketSelect
 
 #endif  // GGKS_BUCKET_MULTISELECT_HPP_

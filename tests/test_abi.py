@@ -103,6 +103,11 @@ def test_cpp_reference_mirror_header_compiles(lib, tmp_path):
         "  results_t<float>* r = timeBucketMultiselect(out, 2u, k, 2u);\n"
         "  results_t<float>* t = timeBucketTopkselect(out, 2u, 1u);\n"
         "  float* tk = randomizedTopkSelectWrapper(d, 10, 2);\n"
+        "  float s1 = BucketSelect::bucketSelectWrapper(d, 10, 3, 152, 1024);\n"
+        "  double* dd = nullptr; unsigned int* du = nullptr;\n"
+        "  double s2 = RandomizedBucketSelect::randomizedBucketSelectWrapper(dd, 10, 3, 0, 0);\n"
+        "  unsigned int s3 = BucketSelect::bucketSelectWrapper(du, 10, 3, 0, 0);\n"
+        "  (void)s1; (void)s2; (void)s3;\n"
         "  free(tk); freeResults(r); freeResults(t);\n"
         "  return 0;\n}\n")
     import ggks
@@ -152,3 +157,18 @@ def test_batch_invalid_arguments_rejected_without_device(lib, sfx, dt):
              ctypes.byref(o)) == ggks.INVALID_ARG
     assert t(ptrs.ctypes.data, ns.ctypes.data, 2, None, out.ctypes.data,
              ctypes.byref(o)) == ggks.INVALID_ARG
+
+
+@pytest.mark.parametrize("sfx,dt", [("f32", np.float32), ("f64", np.float64), ("u32", np.uint32)])
+def test_select_invalid_arguments_rejected_without_device(lib, sfx, dt):
+    """Single-k select: null vector or output, n = 0, k outside [1, n]."""
+    import ggks
+    f = getattr(lib, "ggks_select_" + sfx)
+    o = ggks.Opts()
+    out = np.zeros(1, dtype=dt)
+    fake = 4096
+    assert f(None, 10, 1, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+    assert f(fake, 10, 1, None, ctypes.byref(o)) == ggks.INVALID_ARG
+    assert f(fake, 0, 1, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+    assert f(fake, 10, 0, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+    assert f(fake, 10, 11, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG

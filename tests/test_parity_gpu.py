@@ -312,3 +312,22 @@ def test_narrow_span_with_far_outliers(g, orc, dtype):
     ks = ks.astype(np.uint32)
     assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks), orc.multiselect(x, ks), dtype)
     assert_same(g.topk_ptr(d.ptr, n, x.dtype, 20), orc.topk(x, 20), f"topk {dtype}")
+
+
+@pytest.mark.parametrize("dtype,dist", [("f32", "normal"), ("f32", "ones_twos"), ("f64", "cauchy"),
+                                        ("u32", "uniform16"), ("u32", "sorted")])
+def test_single_k_select(g, orc, dtype, dist):
+    """bucketSelectWrapper / randomizedBucketSelectWrapper (bucketSelect.cu:453-471,
+    randomizedBucketSelect.cu:861-881): the K-th largest, one value."""
+    import ggks_problems as gp
+    for n in (1, 7, 1000, 1 << 20):
+        x = gp.generate(dtype, dist, n, seed=n)
+        d = DeviceArray(x)
+        for K in sorted({1, n, (n + 1) // 2, max(1, n // 3)}):
+            want = orc.multiselect(x, [K])
+            got = np.array([g.bucketSelectWrapper(d.ptr, n, K, 152, 1024, dtype=x.dtype)],
+                           dtype=x.dtype)
+            assert_same(got, want, f"bucketSelect {dtype}/{dist} n={n} K={K}")
+            got = np.array([g.randomizedBucketSelectWrapper(d.ptr, n, K, dtype=x.dtype)],
+                           dtype=x.dtype)
+            assert_same(got, want, f"randomizedBucketSelect {dtype}/{dist} n={n} K={K}")
