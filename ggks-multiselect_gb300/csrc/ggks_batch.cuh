@@ -44,6 +44,9 @@ constexpr int kBPhases = 5;
 constexpr uint32_t kBWarpBytes = 2048;  // shared memory of one warp-finisher buffer
 constexpr uint32_t kBRepBytes = 32768;  // per-bucket first keys of a tile (dup problems)
 constexpr uint32_t kMixed = 0x80000000u;  // tile row: the bucket holds more than one key
+// slots whose request counters fit in the plan phase's spare shared memory
+// (after the table, the bucket prefix and the flags: 81936 - 57360 bytes)
+constexpr uint32_t kBPlanSlots = 3072;
 
 // segments of at most this many keys are finished by one warp
 template <class K>
@@ -668,23 +671,42 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         }
       }
       __syncthreads();
-      for (uint32_t i = tid; i < P.num_req; i += nt)
-        atomicAdd(&A.kcnt[P.req_off + excl[__ldcg(A.req_bucket + P.req_off + i)]], 1u);
+      // per-slot request counters: in the shared memory after the flags when
+      // the slots fit (a top-k puts thousands of requests in a few slots),
+      // else the global ones
+      uint32_t *s_cnt = reinterpret_cast<uint32_t *>(flag + kBMaxNb);
+      uint32_t *s_cur = s_cnt + kBPlanSlots;
+      const bool in_smem = tot_slots <= kBPlanSlots;
+      if (in_smem)
+        for (uint32_t q = tid; q < tot_slots; q += nt) {
+          s_cnt[q] = 0;
+          s_cur[q] = 0;
+        }
+      __syncthreads();
+      for (uint32_t i = tid; i < P.num_req; i += nt) {
+        const uint32_t q = excl[__ldcg(A.req_bucket + P.req_off + i)];
+        atomicAdd(in_smem ? &s_cnt[q] : &A.kcnt[P.req_off + q], 1u);
+      }
       __syncthreads();
       {
         uint32_t mine = 0;
-        for (uint32_t q = s0; q < s1; ++q) mine += __ldcg(A.kcnt + P.req_off + q);
+        for (uint32_t q = s0; q < s1; ++q)
+          mine += in_smem ? s_cnt[q] : __ldcg(A.kcnt + P.req_off + q);
         uint32_t t2;
         uint32_t r2 = block_incl_scan(mine, &t2, red32) - mine + P.req_off;
         for (uint32_t q = s0; q < s1; ++q) {
+          const uint32_t c = in_smem ? s_cnt[q] : __ldcg(A.kcnt + P.req_off + q);
+          if (in_smem) A.kcnt[P.req_off + q] = c;  // the finisher reads the counts
           A.kstart[P.req_off + q] = r2;
-          r2 += __ldcg(A.kcnt + P.req_off + q);
+          r2 += c;
         }
       }
       __syncthreads();
       for (uint32_t i = tid; i < P.num_req; i += nt) {
-        const uint32_t g = P.req_off + excl[__ldcg(A.req_bucket + P.req_off + i)];
-        const uint32_t pos = __ldcg(A.kstart + g) + atomicAdd(&A.kcur[g], 1u);
+        const uint32_t q = excl[__ldcg(A.req_bucket + P.req_off + i)];
+        const uint32_t g = P.req_off + q;
+        const uint32_t pos =
+            __ldcg(A.kstart + g) + atomicAdd(in_smem ? &s_cur[q] : &A.kcur[g], 1u);
         Req e;
         e.rank = __ldcg(A.req_local + P.req_off + i);
         e.out = rq[i].out;

@@ -25,7 +25,7 @@ template <class T>
 static inline int batch_smem_bytes() {
   using K = typename Traits<T>::K;
   const size_t table = (size_t)kBMaxS * sizeof(K);
-  const size_t plan = kLutPadded * 4 + (size_t)kBMaxNb * 5;
+  const size_t plan = kLutPadded * 4 + (size_t)kBMaxNb * 5 + (size_t)kBPlanSlots * 8;
   const size_t tiles = (kLutPadded + (size_t)kBMaxNb) * 4 + kBRepBytes;
   const size_t fin = finish_smem_for<K>(sizeof(K) == 4 ? 4096u : 2048u);
   return (int)std::max(std::max(table, tiles), std::max(plan, fin));

@@ -1013,23 +1013,45 @@ __global__ void __launch_bounds__(1024, 1)
   }
   __syncthreads();
 
-  // requests per slot, then the request lists (local ranks)
-  for (uint32_t i = tid; i < num_req; i += nt) atomicAdd(&kcnt[excl[req_bucket[i]]], 1u);
+  // requests per slot, then the request lists (local ranks).  Many requests
+  // in few slots (a top-k) would queue on a few global counters, so the
+  // per-slot counters live in shared memory when the launch left room for
+  // them after the table, prefix and flags (the room is read from
+  // %dynamic_smem_size; a launch without it uses the global counters).
+  uint32_t dyn;
+  asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+  const uint32_t used = (uint32_t)((kLutPadded * 4 + (size_t)nb_max * 5 + 15) & ~(size_t)15);
+  const uint32_t room = dyn > used ? (dyn - used) / 8 : 0u;
+  uint32_t *s_cnt = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(smem_raw) + used);
+  uint32_t *s_cur = s_cnt + room;
+  const bool in_smem = tot_slots <= room;
+  if (in_smem)
+    for (uint32_t q = tid; q < tot_slots; q += nt) {
+      s_cnt[q] = 0;
+      s_cur[q] = 0;
+    }
+  __syncthreads();
+  for (uint32_t i = tid; i < num_req; i += nt) {
+    const uint32_t q = excl[req_bucket[i]];
+    atomicAdd(in_smem ? &s_cnt[q] : &kcnt[q], 1u);
+  }
   __syncthreads();
   {
     uint32_t mine = 0;
-    for (uint32_t q = s0; q < s1; ++q) mine += kcnt[q];
+    for (uint32_t q = s0; q < s1; ++q) mine += in_smem ? s_cnt[q] : kcnt[q];
     uint32_t tot;
     uint32_t run = block_incl_scan(mine, &tot, red32) - mine;
     for (uint32_t q = s0; q < s1; ++q) {
+      const uint32_t c = in_smem ? s_cnt[q] : kcnt[q];
+      if (in_smem) kcnt[q] = c;  // the finisher reads the counts
       kstart[q] = run;
-      run += kcnt[q];
+      run += c;
     }
   }
   __syncthreads();
   for (uint32_t i = tid; i < num_req; i += nt) {
     const uint32_t q = excl[req_bucket[i]];
-    const uint32_t pos = kstart[q] + atomicAdd(&kcur[q], 1u);
+    const uint32_t pos = kstart[q] + atomicAdd(in_smem ? &s_cur[q] : &kcur[q], 1u);
     Req e;
     e.rank = req_local[i];
     e.out = reqs[i].out;

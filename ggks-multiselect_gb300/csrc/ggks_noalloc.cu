@@ -170,7 +170,7 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
                                                 tile_state, ctrl);
   {
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kNaNbMax * 5);
-    set_smem_max<k_plan<float, float>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 5));
+    set_smem_max<k_plan<float, float>>(kPlanSmemMax);
     k_plan<float, float><<<1, 1024, smem, s>>>(hdr, lut, counts, excl, n, reqs, num_k, kNaNbMax,
                                                 ctrl, tile_state, scan_tiles, seg_bucket, seg_off,
                                                 seg_size, kstart, kcnt, kcur, seg_lo, seg_hi,

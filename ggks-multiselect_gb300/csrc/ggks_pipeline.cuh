@@ -27,6 +27,13 @@ static inline int finish_smem_bytes() {
 
 static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// k_plan's shared memory: the table, the bucket prefix and flags for the
+// largest bucket count, and room for 6144 per-slot request counters (both
+// launchers raise the kernel's limit to this one value)
+constexpr size_t kPlanSlotBytes = 6144 * 8;
+constexpr int kPlanSmemMax = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 5 + 16 +
+                                   kPlanSlotBytes);
+
 struct Plan {
   uint64_t n = 0;
   uint32_t num_req = 0;
@@ -233,9 +240,9 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   }
   // ---- (e) plan
   {
-    const int smem =
-        (int)(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 4 + (size_t)p.nb_max);
-    set_smem_max<k_plan<InT, OutT>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 5));
+    const int smem = (int)(align_up(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 5, 16) +
+                           kPlanSlotBytes);
+    set_smem_max<k_plan<InT, OutT>>(kPlanSmemMax);
     PassTimer t(ctx, s, GGKS_PASS_PLAN);
     k_plan<InT, OutT><<<1, 1024, smem, s>>>(hdr, lut, counts, excl, n, rq, num_req, p.nb_max, ctrl,
                                              tile_state, p.scan_tiles, seg_bucket, seg_off,

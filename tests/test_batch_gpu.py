@@ -267,3 +267,19 @@ def test_batch_single_key_buckets(g, orc):
         g.batch_set_tuning(ctx, div, tile)
         _check_batch(g, orc, vecs, ks, np.float32, f"single-key div {div} tile {tile}", ctx=ctx)
     ctx.close()
+
+
+def test_batch_many_slots_and_large_topk(g, orc):
+    """Per-problem request counters: a problem with more slots than the plan
+    phase's shared memory holds, and top-k problems with thousands of
+    requests in a few slots."""
+    import ggks_problems as gp
+    n = 1 << 22
+    a = gp.generate("f32", "uniform", n, seed=41)
+    b = gp.generate("f32", "normal", 300_000, seed=42)
+    ka = gp.k_distinct(n, 6000, 5)
+    kb = np.arange(1, 4097, dtype=np.uint32)  # the 4096 largest, as a k list
+    ctx = g.Context(0)
+    g.batch_set_tuning(ctx, 256, 1 << 20)
+    _check_batch(g, orc, [a, b], [ka, kb], np.float32, "many slots", ctx=ctx)
+    ctx.close()

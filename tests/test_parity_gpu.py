@@ -331,3 +331,16 @@ def test_single_k_select(g, orc, dtype, dist):
             got = np.array([g.randomizedBucketSelectWrapper(d.ptr, n, K, dtype=x.dtype)],
                            dtype=x.dtype)
             assert_same(got, want, f"randomizedBucketSelect {dtype}/{dist} n={n} K={K}")
+
+
+def test_many_slots_and_many_requests_per_slot(g, orc):
+    """Request counters per slot: thousands of requests in a few slots (top-k,
+    shared-memory counters) and more slots than shared memory holds (the
+    global counters)."""
+    import ggks_problems as gp
+    n = 1 << 22
+    x = gp.generate("f32", "normal", n, seed=31)
+    d = DeviceArray(x)
+    ks = gp.k_distinct(n, 20_000, 4)  # > 6144 slots
+    assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks), orc.multiselect(x, ks, 8), "20k ks")
+    assert_same(g.topk_ptr(d.ptr, n, x.dtype, 100_000), orc.topk(x, 100_000, 8), "top 100k")
