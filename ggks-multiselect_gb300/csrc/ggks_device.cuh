@@ -937,19 +937,38 @@ __global__ void __launch_bounds__(1024, 1)
 
   // requests -> bucket (the last b with excl[b] <= rank is never empty) and
   // the rank inside it
-  for (uint32_t i = tid; i < num_req; i += nt) {
-    const uint32_t rank = reqs[i].rank;
-    uint32_t lo = 0, hi = nb;
-    while (hi - lo > 1) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (excl[mid] <= rank)
-        lo = mid;
-      else
-        hi = mid;
+  // (four requests per thread and step: their loads and searches overlap)
+  for (uint32_t i0 = tid; i0 < num_req; i0 += 4 * nt) {
+    uint32_t rank[4], lo[4], hi[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t i = i0 + u * nt;
+      rank[u] = i < num_req ? reqs[i].rank : 0u;
+      lo[u] = 0;
+      hi[u] = i < num_req ? nb : 1u;  // no search for an absent request
     }
-    flag[lo] = 1;
-    req_bucket[i] = lo;
-    req_local[i] = rank - excl[lo];
+    for (bool more = true; more;) {
+      more = false;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (hi[u] - lo[u] > 1) {
+          const uint32_t mid = (lo[u] + hi[u]) >> 1;
+          if (excl[mid] <= rank[u])
+            lo[u] = mid;
+          else
+            hi[u] = mid;
+          more = true;
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t i = i0 + u * nt;
+      if (i < num_req) {
+        flag[lo[u]] = 1;
+        req_bucket[i] = lo[u];
+        req_local[i] = rank[u] - excl[lo[u]];
+      }
+    }
   }
   __syncthreads();
 
@@ -1023,17 +1042,22 @@ __global__ void __launch_bounds__(1024, 1)
   const uint32_t used = (uint32_t)((kLutPadded * 4 + (size_t)nb_max * 5 + 15) & ~(size_t)15);
   const uint32_t room = dyn > used ? (dyn - used) / 8 : 0u;
   uint32_t *s_cnt = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(smem_raw) + used);
-  uint32_t *s_cur = s_cnt + room;
+  uint32_t *s_cur = s_cnt + room;  // cursor = slot start + requests placed so far
   const bool in_smem = tot_slots <= room;
-  if (in_smem)
-    for (uint32_t q = tid; q < tot_slots; q += nt) {
-      s_cnt[q] = 0;
-      s_cur[q] = 0;
+  if (in_smem) {
+    for (uint32_t q = tid; q < tot_slots; q += nt) s_cnt[q] = 0;
+    __syncthreads();
+    // four requests per thread and step: the global loads overlap
+    for (uint32_t i0 = tid; i0 < num_req; i0 += 4 * nt) {
+      uint32_t b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) b[u] = i0 + u * nt < num_req ? req_bucket[i0 + u * nt] : 0u;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (i0 + u * nt < num_req) atomicAdd(&s_cnt[excl[b[u]]], 1u);
     }
-  __syncthreads();
-  for (uint32_t i = tid; i < num_req; i += nt) {
-    const uint32_t q = excl[req_bucket[i]];
-    atomicAdd(in_smem ? &s_cnt[q] : &kcnt[q], 1u);
+  } else {
+    for (uint32_t i = tid; i < num_req; i += nt) atomicAdd(&kcnt[excl[req_bucket[i]]], 1u);
   }
   __syncthreads();
   {
@@ -1043,19 +1067,44 @@ __global__ void __launch_bounds__(1024, 1)
     uint32_t run = block_incl_scan(mine, &tot, red32) - mine;
     for (uint32_t q = s0; q < s1; ++q) {
       const uint32_t c = in_smem ? s_cnt[q] : kcnt[q];
-      if (in_smem) kcnt[q] = c;  // the finisher reads the counts
+      if (in_smem) {
+        kcnt[q] = c;  // the finisher reads the counts
+        s_cur[q] = run;
+      }
       kstart[q] = run;
       run += c;
     }
   }
   __syncthreads();
-  for (uint32_t i = tid; i < num_req; i += nt) {
-    const uint32_t q = excl[req_bucket[i]];
-    const uint32_t pos = kstart[q] + atomicAdd(in_smem ? &s_cur[q] : &kcur[q], 1u);
-    Req e;
-    e.rank = req_local[i];
-    e.out = reqs[i].out;
-    klist[pos] = e;
+  if (in_smem) {
+    for (uint32_t i0 = tid; i0 < num_req; i0 += 4 * nt) {
+      uint32_t b[4], loc[4], o[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t i = i0 + u * nt;
+        const bool ok = i < num_req;
+        b[u] = ok ? req_bucket[i] : 0u;
+        loc[u] = ok ? req_local[i] : 0u;
+        o[u] = ok ? reqs[i].out : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (i0 + u * nt < num_req) {
+          Req e;
+          e.rank = loc[u];
+          e.out = o[u];
+          klist[atomicAdd(&s_cur[excl[b[u]]], 1u)] = e;
+        }
+    }
+  } else {
+    for (uint32_t i = tid; i < num_req; i += nt) {
+      const uint32_t q = excl[req_bucket[i]];
+      const uint32_t pos = kstart[q] + atomicAdd(&kcur[q], 1u);
+      Req e;
+      e.rank = req_local[i];
+      e.out = reqs[i].out;
+      klist[pos] = e;
+    }
   }
 }
 

@@ -240,8 +240,9 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   }
   // ---- (e) plan
   {
+    // shared-memory slot counters only pay when many requests share slots
     const int smem = (int)(align_up(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 5, 16) +
-                           kPlanSlotBytes);
+                           (num_req >= 4096 ? kPlanSlotBytes : 0));
     set_smem_max<k_plan<InT, OutT>>(kPlanSmemMax);
     PassTimer t(ctx, s, GGKS_PASS_PLAN);
     k_plan<InT, OutT><<<1, 1024, smem, s>>>(hdr, lut, counts, excl, n, rq, num_req, p.nb_max, ctrl,
