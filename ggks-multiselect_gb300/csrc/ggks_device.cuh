@@ -937,15 +937,18 @@ __global__ void __launch_bounds__(1024, 1)
 
   // requests -> bucket (the last b with excl[b] <= rank is never empty) and
   // the rank inside it
-  // (four requests per thread and step: their loads and searches overlap)
-  for (uint32_t i0 = tid; i0 < num_req; i0 += 4 * nt) {
+  // (with many requests, four per thread and step: their loads and searches
+  // overlap)
+  const uint32_t rstep = num_req >= 4096 ? 4u : 1u;
+  for (uint32_t i0 = tid; i0 < num_req; i0 += rstep * nt) {
     uint32_t rank[4], lo[4], hi[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const uint32_t i = i0 + u * nt;
-      rank[u] = i < num_req ? reqs[i].rank : 0u;
+      const bool ok = (uint32_t)u < rstep && i < num_req;
+      rank[u] = ok ? reqs[i].rank : 0u;
       lo[u] = 0;
-      hi[u] = i < num_req ? nb : 1u;  // no search for an absent request
+      hi[u] = ok ? nb : 1u;  // no search for an absent request
     }
     for (bool more = true; more;) {
       more = false;
@@ -963,7 +966,7 @@ __global__ void __launch_bounds__(1024, 1)
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const uint32_t i = i0 + u * nt;
-      if (i < num_req) {
+      if ((uint32_t)u < rstep && i < num_req) {
         flag[lo[u]] = 1;
         req_bucket[i] = lo[u];
         req_local[i] = rank[u] - excl[lo[u]];
