@@ -885,6 +885,88 @@ __global__ void __launch_bounds__(kScanThreads)
 // ---------------------------------------------------------------------------
 // (e) plan: requests -> buckets -> slots; request lists per slot
 // ---------------------------------------------------------------------------
+// With tens of thousands of requests the per-request work leaves the single
+// plan CTA: k_reqmap (many CTAs) maps every request to its bucket and local
+// rank, flags the bucket in a bitmap and counts requests per bucket; k_plan
+// then numbers the slots from the bitmap and takes the per-slot counts from
+// the bucket counts; k_reqplace (many CTAs) writes the request lists.
+constexpr uint32_t kPremapMin = 16384;     // requests from which the mapping is spread out
+constexpr uint32_t kReqmapPerCta = 4096;   // requests per k_reqmap CTA (1024 threads)
+
+struct Premap {
+  const uint32_t *bits = nullptr;    // bucket flags, one bit each (null: not premapped)
+  const uint32_t *bcount = nullptr;  // requests per bucket
+  uint32_t *bslot = nullptr;         // slot of each flagged bucket (written by k_plan)
+};
+
+// Bitmap and counts must start at zero.  Shared memory: the bucket prefix
+// (nb_max u32).
+static __global__ void __launch_bounds__(1024)
+    k_reqmap(const uint32_t *__restrict__ excl_g, const Ctrl *ctrl, const Req *__restrict__ reqs,
+             uint32_t num_req, uint32_t *__restrict__ req_bucket,
+             uint32_t *__restrict__ req_local, uint32_t *bits, uint32_t *bcount) {
+  extern __shared__ uint4 smem_raw[];
+  uint32_t *excl = reinterpret_cast<uint32_t *>(smem_raw);
+  if (ctrl->status & ST_FATAL) return;
+  const uint32_t nb = ctrl->nb;
+  const uint32_t nb4 = (nb + 3) >> 2;
+  for (uint32_t v = threadIdx.x; v < nb4; v += blockDim.x)
+    reinterpret_cast<uint4 *>(excl)[v] = __ldcg(reinterpret_cast<const uint4 *>(excl_g) + v);
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint32_t u = 0; u < kReqmapPerCta / 1024; ++u) {
+    const uint32_t i = blockIdx.x * kReqmapPerCta + u * 1024 + threadIdx.x;
+    const bool valid = i < num_req;
+    uint32_t b = 0xFFFFFFFFu;
+    if (valid) {
+      const uint32_t rank = reqs[i].rank;
+      uint32_t lo = 0, hi = nb;
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (excl[mid] <= rank)
+          lo = mid;
+        else
+          hi = mid;
+      }
+      b = lo;
+      req_bucket[i] = lo;
+      req_local[i] = rank - excl[lo];
+    }
+    // one count and one flag per bucket per warp (neighbouring requests often
+    // share a bucket)
+    const uint32_t peers = __match_any_sync(0xffffffffu, b);
+    if (valid && (int)lane == __ffs(peers) - 1) {
+      atomicAdd(&bcount[b], (uint32_t)__popc(peers));
+      atomicOr(&bits[b >> 5], 1u << (b & 31));
+    }
+  }
+}
+
+// klist positions: kstart[slot] + arrival order in the slot (warp-aggregated
+// cursors; kcur starts at zero, set by k_plan).
+static __global__ void __launch_bounds__(1024)
+    k_reqplace(const Ctrl *ctrl, const Req *__restrict__ reqs, uint32_t num_req,
+               const uint32_t *__restrict__ req_bucket, const uint32_t *__restrict__ req_local,
+               const uint32_t *__restrict__ bslot, const uint32_t *__restrict__ kstart,
+               uint32_t *kcur, Req *__restrict__ klist) {
+  if (ctrl->status & ST_FATAL) return;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < num_req;
+  const uint32_t q = valid ? bslot[req_bucket[i]] : 0xFFFFFFFFu;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t peers = __match_any_sync(0xffffffffu, q);
+  const int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if (valid && (int)lane == leader) base = atomicAdd(&kcur[q], (uint32_t)__popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (valid) {
+    Req e;
+    e.rank = req_local[i];
+    e.out = reqs[i].out;
+    klist[kstart[q] + base + __popc(peers & ((1u << lane) - 1u))] = e;
+  }
+}
+
 // One CTA of 1024 threads.  Dynamic shared memory: lut[kLutEntries + 1] (u32,
 // padded to 16 bytes), excl[nb_max] (u32), flags[nb_max] (u8).
 //
@@ -903,7 +985,8 @@ __global__ void __launch_bounds__(1024, 1)
            uint32_t *__restrict__ kstart, uint32_t *__restrict__ kcnt,
            uint32_t *__restrict__ kcur, typename Traits<InT>::K *__restrict__ seg_lo,
            typename Traits<InT>::K *__restrict__ seg_hi, uint32_t *__restrict__ req_bucket,
-           uint32_t *__restrict__ req_local, Req *__restrict__ klist, uint64_t surv_cap) {
+           uint32_t *__restrict__ req_local, Req *__restrict__ klist, uint64_t surv_cap,
+           Premap pm) {
   using K = typename Traits<InT>::K;
   extern __shared__ uint4 smem_raw[];
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
@@ -922,7 +1005,12 @@ __global__ void __launch_bounds__(1024, 1)
 #pragma unroll 4
   for (uint32_t v = tid; v < nb4; v += nt) {
     reinterpret_cast<uint4 *>(excl)[v] = __ldcg(reinterpret_cast<const uint4 *>(excl_g) + v);
-    reinterpret_cast<uint32_t *>(flag)[v] = 0u;
+    uint32_t fw = 0u;  // flags of buckets 4v .. 4v + 3, one byte each
+    if (pm.bits) {
+      const uint32_t f4 = (__ldcg(pm.bits + (v >> 3)) >> ((4 * v) & 31)) & 0xFu;
+      fw = (f4 & 1u) | ((f4 & 2u) << 7) | ((f4 & 4u) << 14) | ((f4 & 8u) << 21);
+    }
+    reinterpret_cast<uint32_t *>(flag)[v] = fw;
   }
 #pragma unroll 4
   for (uint32_t j = tid; j < kLutEntries; j += nt) lut[j] = __ldcg(lut_g + j);
@@ -940,7 +1028,7 @@ __global__ void __launch_bounds__(1024, 1)
   // (with many requests, four per thread and step: their loads and searches
   // overlap)
   const uint32_t rstep = num_req >= 4096 ? 4u : 1u;
-  for (uint32_t i0 = tid; i0 < num_req; i0 += rstep * nt) {
+  for (uint32_t i0 = tid; i0 < (pm.bits ? 0u : num_req); i0 += rstep * nt) {
     uint32_t rank[4], lo[4], hi[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -990,6 +1078,7 @@ __global__ void __launch_bounds__(1024, 1)
       if (flag[b]) {
         excl[b] = slot;
         seg_bucket[slot] = b;
+        if (pm.bits) pm.bslot[b] = slot;
         slot++;
       }
   }
@@ -1011,7 +1100,7 @@ __global__ void __launch_bounds__(1024, 1)
     seg_size[q] = cb;  // 0 marks a flat slot
     seg_lo[q] = klo;
     seg_hi[q] = single ? klo : (knext > klo ? knext - K(1) : KeyMax<K>::v);
-    kcnt[q] = 0;
+    kcnt[q] = pm.bits ? __ldcg(pm.bcount + b) : 0u;  // premapped: the bucket's request count
     kcur[q] = 0;
     my_surv += cb;
   }
@@ -1046,8 +1135,10 @@ __global__ void __launch_bounds__(1024, 1)
   const uint32_t room = dyn > used ? (dyn - used) / 8 : 0u;
   uint32_t *s_cnt = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(smem_raw) + used);
   uint32_t *s_cur = s_cnt + room;  // cursor = slot start + requests placed so far
-  const bool in_smem = tot_slots <= room;
-  if (in_smem) {
+  const bool in_smem = !pm.bits && tot_slots <= room;
+  if (pm.bits) {
+    // counted by k_reqmap; kcnt holds them already
+  } else if (in_smem) {
     for (uint32_t q = tid; q < tot_slots; q += nt) s_cnt[q] = 0;
     __syncthreads();
     // four requests per thread and step: the global loads overlap
@@ -1079,7 +1170,9 @@ __global__ void __launch_bounds__(1024, 1)
     }
   }
   __syncthreads();
-  if (in_smem) {
+  if (pm.bits) {
+    // k_reqplace writes the lists
+  } else if (in_smem) {
     for (uint32_t i0 = tid; i0 < num_req; i0 += 4 * nt) {
       uint32_t b[4], loc[4], o[4];
 #pragma unroll

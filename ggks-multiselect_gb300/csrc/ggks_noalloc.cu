@@ -174,7 +174,7 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
     k_plan<float, float><<<1, 1024, smem, s>>>(hdr, lut, counts, excl, n, reqs, num_k, kNaNbMax,
                                                 ctrl, tile_state, scan_tiles, seg_bucket, seg_off,
                                                 seg_size, kstart, kcnt, kcur, seg_lo, seg_hi,
-                                                req_bucket, req_local, klist, n);
+                                                req_bucket, req_local, klist, n, Premap{});
   }
   {
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kNaNbMax * 4);

@@ -48,7 +48,7 @@ struct Plan {
   size_t out = 0, ctrl = 0, reqs = 0, hdr = 0, lut = 0, samples = 0, partials = 0,
          counts = 0, excl = 0, seg_bucket = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0,
          kcur = 0, seg_lo = 0, seg_hi = 0, deferred = 0, req_bucket = 0, req_local = 0, klist = 0,
-         total = 0;
+         pm_bits = 0, pm_bcount = 0, pm_bslot = 0, total = 0;
 };
 
 template <class InT, class OutT>
@@ -108,6 +108,12 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   arr(p.req_bucket, num_req, 4);
   arr(p.req_local, num_req, 4);
   arr(p.klist, num_req, sizeof(Req));
+  // premapped plan (many requests): bucket bitmap and request counts, zeroed
+  // together before each use, and the bucket -> slot map
+  p.pm_bits = o;
+  p.pm_bcount = o + (size_t)p.nb_max / 8;
+  o = align_up(o + (size_t)p.nb_max / 8 + (size_t)p.nb_max * 4, A);
+  arr(p.pm_bslot, p.nb_max, 4);
   p.total = o;
   return p;
 }
@@ -242,13 +248,35 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   {
     // shared-memory slot counters only pay when many requests share slots
     const int smem = (int)(align_up(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 5, 16) +
-                           (num_req >= 4096 ? kPlanSlotBytes : 0));
+                           (num_req >= 4096 && num_req < kPremapMin ? kPlanSlotBytes : 0));
     set_smem_max<k_plan<InT, OutT>>(kPlanSmemMax);
     PassTimer t(ctx, s, GGKS_PASS_PLAN);
+    Premap pm;
+    const bool premap = num_req >= kPremapMin;
+    uint32_t *pm_bits = reinterpret_cast<uint32_t *>(A + p.pm_bits);
+    uint32_t *pm_bcount = reinterpret_cast<uint32_t *>(A + p.pm_bcount);
+    uint32_t *pm_bslot = reinterpret_cast<uint32_t *>(A + p.pm_bslot);
+    if (premap) {
+      // many requests: map them with many CTAs (k_reqmap), place them with
+      // many CTAs (k_reqplace); the plan CTA only numbers the slots
+      e = cudaMemsetAsync(pm_bits, 0, (size_t)p.nb_max / 8 + (size_t)p.nb_max * 4, s);
+      if (e != cudaSuccess) return from_cuda(e);
+      set_smem_max<k_reqmap>((int)(kMaxNb * 4));
+      k_reqmap<<<(num_req + kReqmapPerCta - 1) / kReqmapPerCta, 1024, p.nb_max * 4, s>>>(
+          excl, ctrl, rq, num_req, req_bucket, req_local, pm_bits, pm_bcount);
+      pm.bits = pm_bits;
+      pm.bcount = pm_bcount;
+      pm.bslot = pm_bslot;
+    }
     k_plan<InT, OutT><<<1, 1024, smem, s>>>(hdr, lut, counts, excl, n, rq, num_req, p.nb_max, ctrl,
                                              tile_state, p.scan_tiles, seg_bucket, seg_off,
                                              seg_size, kstart, kcnt, kcur, seg_lo, seg_hi,
-                                             req_bucket, req_local, klist, p.surv_cap);
+                                             req_bucket, req_local, klist, p.surv_cap, pm);
+    if (premap) {
+      k_reqplace<<<(num_req + 1023) / 1024, 1024, 0, s>>>(ctrl, rq, num_req, req_bucket, req_local,
+                                                          pm_bslot, kstart, kcur, klist);
+      ctx.stats.launches += 2;
+    }
     ran[GGKS_PASS_PLAN] = true;
   }
   uint64_t surv_cap = p.surv_cap;
