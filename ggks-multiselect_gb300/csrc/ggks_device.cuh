@@ -58,6 +58,7 @@ constexpr uint32_t kLutIdx = 1u << kLutIdxBits;  // slices over the sample span
 constexpr uint32_t kLutEntries = kLutIdx + 1;    // + one for keys above the span
 constexpr uint32_t kLutPadded = (kLutEntries + 3) & ~3u;  // 16-byte multiple
 constexpr int kMaxSubBits = 12;                  // at most 2^12 buckets per slice
+constexpr uint32_t kMaxNb = 32768;  // buckets of one vector: shared-memory histogram limit (u32)
 constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
 constexpr uint32_t kInactive = 0x80000000u;  // compaction cursor of an inactive bucket
 constexpr int kSpinLimit = 1 << 22;              // bounded device-side waits
@@ -967,6 +968,47 @@ static __global__ void __launch_bounds__(1024)
   }
 }
 
+// Flag words per lane in k_plan's slot numbering (1024 threads, kMaxNb buckets).
+constexpr uint32_t kPlanRounds = kMaxNb / 4 / 1024;
+static_assert(kPlanRounds * 4 * 1024 == kMaxNb, "k_plan slot numbering covers kMaxNb buckets");
+
+// k_plan's request mapping: bucket = the last b with excl[b] <= rank (a
+// fixed-step search over the prefix in shared memory), the request's rank
+// inside it, and the bucket's flag.  R requests per thread and step.
+template <int R>
+__device__ __forceinline__ void plan_map_requests(const uint32_t *excl, uint32_t nb,
+                                                  const Req *__restrict__ reqs, uint32_t num_req,
+                                                  uint8_t *flag, uint32_t *__restrict__ req_bucket,
+                                                  uint32_t *__restrict__ req_local) {
+  const uint32_t nt = blockDim.x;
+  const uint32_t top = nb > 1 ? 1u << (31 - __clz(nb - 1)) : 0u;  // largest step
+  for (uint32_t i0 = threadIdx.x; i0 < num_req; i0 += R * nt) {
+    uint32_t rank[R], lo[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const uint32_t i = i0 + u * nt;
+      rank[u] = i < num_req ? reqs[i].rank : 0u;
+      lo[u] = 0;
+    }
+    for (uint32_t step = top; step; step >>= 1) {
+#pragma unroll
+      for (int u = 0; u < R; ++u) {
+        const uint32_t m = lo[u] + step;
+        if (m < nb && excl[m] <= rank[u]) lo[u] = m;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const uint32_t i = i0 + u * nt;
+      if (i < num_req) {
+        flag[lo[u]] = 1;
+        req_bucket[i] = lo[u];
+        req_local[i] = rank[u] - excl[lo[u]];
+      }
+    }
+  }
+}
+
 // One CTA of 1024 threads.  Dynamic shared memory: lut[kLutEntries + 1] (u32,
 // padded to 16 bytes), excl[nb_max] (u32), flags[nb_max] (u8).
 //
@@ -992,8 +1034,10 @@ __global__ void __launch_bounds__(1024, 1)
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
   uint32_t *excl = lut + kLutPadded;  // 16-byte aligned; later: slot of each bucket
   uint8_t *flag = reinterpret_cast<uint8_t *>(excl + nb_max);
+  uint32_t *s_segb = reinterpret_cast<uint32_t *>(flag);  // once the flags are in registers
   __shared__ uint32_t red32[33];
   __shared__ uint64_t red64[33];
+  __shared__ uint32_t s_wbase[33];
   const uint32_t tid = threadIdx.x, nt = blockDim.x;
 
   if (ctrl->status & ST_FATAL) return;
@@ -1024,63 +1068,65 @@ __global__ void __launch_bounds__(1024, 1)
   __syncthreads();
 
   // requests -> bucket (the last b with excl[b] <= rank is never empty) and
-  // the rank inside it
-  // (with many requests, four per thread and step: their loads and searches
-  // overlap)
-  const uint32_t rstep = num_req >= 4096 ? 4u : 1u;
-  for (uint32_t i0 = tid; i0 < (pm.bits ? 0u : num_req); i0 += rstep * nt) {
-    uint32_t rank[4], lo[4], hi[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint32_t i = i0 + u * nt;
-      const bool ok = (uint32_t)u < rstep && i < num_req;
-      rank[u] = ok ? reqs[i].rank : 0u;
-      lo[u] = 0;
-      hi[u] = ok ? nb : 1u;  // no search for an absent request
-    }
-    for (bool more = true; more;) {
-      more = false;
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (hi[u] - lo[u] > 1) {
-          const uint32_t mid = (lo[u] + hi[u]) >> 1;
-          if (excl[mid] <= rank[u])
-            lo[u] = mid;
-          else
-            hi[u] = mid;
-          more = true;
-        }
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint32_t i = i0 + u * nt;
-      if ((uint32_t)u < rstep && i < num_req) {
-        flag[lo[u]] = 1;
-        req_bucket[i] = lo[u];
-        req_local[i] = rank[u] - excl[lo[u]];
-      }
-    }
+  // the rank inside it; with many requests, four per thread and step, so that
+  // their loads and searches overlap
+  if (!pm.bits) {
+    if (num_req >= 4096)
+      plan_map_requests<4>(excl, nb, reqs, num_req, flag, req_bucket, req_local);
+    else
+      plan_map_requests<1>(excl, nb, reqs, num_req, flag, req_bucket, req_local);
   }
   __syncthreads();
 
-  // Slots in bucket order.  A block scan over the flags (contiguous bucket
-  // range per thread) numbers the flagged buckets; excl[] is dead from here on
-  // and maps each flagged bucket to its slot, seg_bucket[] lists the slots'
-  // buckets.
-  const uint32_t per = (nb + nt - 1) / nt;
-  const uint32_t b0 = min(nb, tid * per), b1 = min(nb, b0 + per);
-  uint32_t my_slots = 0;
-  for (uint32_t b = b0; b < b1; ++b) my_slots += flag[b] ? 1u : 0u;
-  uint32_t tot_slots;
+  // Slots in bucket order.  Warp w owns the flag words [w wpw, (w + 1) wpw)
+  // (one byte per bucket, 0 or 1), read in rounds of 32 neighbouring words;
+  // the flags stay in registers, so from the warp-total scan on the flag
+  // bytes can hold the slot -> bucket list (s_segb, while it fits).  excl[]
+  // is dead from here on and maps each flagged bucket to its slot.
+  const uint32_t lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+  const uint32_t nw = (nb + 3) >> 2;
+  const uint32_t wpw = (((nw + nwarps - 1) / nwarps) + 31) & ~31u;
+  const uint32_t rounds = wpw >> 5;  // <= kPlanRounds for 1024 threads
+  uint32_t fw[kPlanRounds];
+  uint32_t mine = 0;
+#pragma unroll
+  for (uint32_t r = 0; r < kPlanRounds; ++r) {
+    const uint32_t w = warp * wpw + r * 32 + lane;
+    fw[r] = (r < rounds && w < nw) ? reinterpret_cast<const uint32_t *>(flag)[w] : 0u;
+    mine += __popc(fw[r]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+  if (lane == 0) s_wbase[warp] = mine;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t v = lane < nwarps ? s_wbase[lane] : 0u;
+    const uint32_t incl = warp_incl_scan(v);
+    if (lane < nwarps) s_wbase[lane] = incl - v;
+    if (lane == 31) s_wbase[32] = incl;
+  }
+  __syncthreads();
+  const uint32_t tot_slots = s_wbase[32];
+  const bool segb_smem = tot_slots <= nb_max / 4;
   {
-    uint32_t slot = block_incl_scan(my_slots, &tot_slots, red32) - my_slots;
-    for (uint32_t b = b0; b < b1; ++b)
-      if (flag[b]) {
+    uint32_t slot0 = s_wbase[warp];
+#pragma unroll
+    for (uint32_t r = 0; r < kPlanRounds; ++r) {
+      if (r >= rounds) break;
+      const uint32_t c = __popc(fw[r]);
+      const uint32_t incl = warp_incl_scan(c);
+      uint32_t slot = slot0 + incl - c;
+      const uint32_t b4 = 4u * (warp * wpw + r * 32 + lane);
+      for (uint32_t bits = fw[r]; bits; bits &= bits - 1u) {
+        const uint32_t b = b4 + ((__ffs(bits) - 1) >> 3);
         excl[b] = slot;
         seg_bucket[slot] = b;
+        if (segb_smem) s_segb[slot] = b;
         if (pm.bits) pm.bslot[b] = slot;
-        slot++;
+        ++slot;
       }
+      slot0 += __shfl_sync(0xffffffffu, incl, 31);
+    }
   }
   __syncthreads();
   // one thread per slot (contiguous slot range per thread for the offsets):
@@ -1089,7 +1135,7 @@ __global__ void __launch_bounds__(1024, 1)
   const uint32_t s0 = min(tot_slots, tid * sper), s1 = min(tot_slots, s0 + sper);
   uint64_t my_surv = 0;
   for (uint32_t q = s0; q < s1; ++q) {
-    const uint32_t b = __ldcg(seg_bucket + q);
+    const uint32_t b = segb_smem ? s_segb[q] : __ldcg(seg_bucket + q);
     const K klo = bucket_lo<K>(b, h.base, h.shift, lut);
     const K knext = (b + 1 < nb) ? bucket_lo<K>(b + 1, h.base, h.shift, lut) : K(0);
     // single key iff the next bucket starts one key later; the start of the
@@ -1106,10 +1152,12 @@ __global__ void __launch_bounds__(1024, 1)
   }
   uint64_t tot_surv;
   {
+    // the sizes of all but a thread's last slot are read back (none for one
+    // slot per thread)
     uint64_t off = block_incl_scan(my_surv, &tot_surv, red64) - my_surv;
     for (uint32_t q = s0; q < s1; ++q) {
       seg_off[q] = off;
-      off += __ldcg(seg_size + q);
+      if (q + 1 < s1) off += __ldcg(seg_size + q);
     }
   }
   if (tid == 0) {

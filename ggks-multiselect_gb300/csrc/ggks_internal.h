@@ -80,7 +80,6 @@ cudaError_t ensure_pin(Context &ctx, size_t bytes);
 
 // fixed-offset persistent state at the start of the arena
 constexpr size_t kTileStateBytes = 8192;  // >= (65536 / kScanTile) * 8
-constexpr uint32_t kMaxNb = 32768;        // shared-memory histogram limit (u32 counters)
 
 // Where the requests of one selection come from.
 struct ReqSource {

@@ -246,9 +246,9 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   }
   // ---- (e) plan
   {
-    // shared-memory slot counters only pay when many requests share slots
+    // per-slot request counters in shared memory unless the requests are premapped
     const int smem = (int)(align_up(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 5, 16) +
-                           (num_req >= 4096 && num_req < kPremapMin ? kPlanSlotBytes : 0));
+                           (num_req < kPremapMin ? kPlanSlotBytes : 0));
     set_smem_max<k_plan<InT, OutT>>(kPlanSmemMax);
     PassTimer t(ctx, s, GGKS_PASS_PLAN);
     Premap pm;
