@@ -802,7 +802,9 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         }
       }
 #endif
-      const bool done = finish_slot<K, OutT>(
+      // one vector per thread and chunk: the kernel's other phases already
+      // hold its register budget
+      const bool done = finish_slot<K, OutT, 1>(
           surv + ldcg_u(A.seg_off + g), __ldcg(A.seg_size + g), ldcg_u(seg_lo + g), ldcg_u(seg_hi + g),
           A.klist + __ldcg(A.kstart + g), __ldcg(A.kcnt + g), A.bcap, sm, out);
       if (!done && tid == 0) {

@@ -21,21 +21,23 @@
 //                 sample shows heavy duplicates); one row of counts per CTA.
 //                 Replaces assignSmartBucket (bucketMultiselect.cu:129-205)
 //                 without its 4n-byte element-to-bucket array.
-//   (d) scan      k_scan: sums the per-CTA rows per bucket (rewriting each
-//                 column as its exclusive prefix over the CTAs) and computes
-//                 the global exclusive prefix with a single-pass decoupled
-//                 look-back scan (bounded spin).  Replaces sumCounts
-//                 (:214-221) and the host walk of findKBuckets (:87-111).
-//   (e) plan      k_plan: one CTA maps every requested rank to its bucket and
-//                 local rank, answers ranks that fall in single-key buckets
+//   (d) totals    k_colsum: sums the per-CTA rows per bucket.  Replaces
+//                 sumCounts (:214-221).
+//   (e) plan      k_plan: one CTA takes the exclusive bucket prefix in shared
+//                 memory, maps every requested rank to its bucket and local
+//                 rank, answers ranks that fall in single-key buckets
 //                 directly, assigns compact slots to the active buckets and
-//                 groups the requests by slot.  Replaces the host reindex loop
-//                 and reindexCounts (:714-756).
+//                 groups the requests by slot; k_colprefix then turns the
+//                 active buckets' columns of the per-CTA rows into prefixes
+//                 over the CTAs.  Replaces the host walk of findKBuckets
+//                 (:87-111), the host reindex loop and reindexCounts
+//                 (:714-756).
 //   (f) compact   k_compact: second pass over the input with the same
 //                 CTA-to-tile assignment as (c); every CTA starts a private
-//                 shared-memory cursor per active bucket at its prefix from
-//                 (d), so elements of active buckets land in their segment of
-//                 the survivor buffer with shared-memory atomics only.
+//                 shared-memory cursor per active bucket at its column prefix
+//                 from (e), so elements of active buckets land in their
+//                 segment of the survivor buffer with shared-memory atomics
+//                 only.
 //                 Replaces copyElements (:249-308) and reindexCounts
 //                 (:229-241).
 //   (g) finish    k_finish: per segment, an in-shared-memory sort of the
@@ -86,7 +88,6 @@ struct Ctrl {
   uint64_t total_surv;
   uint32_t deferred_count;
   uint32_t sample_done;  // last-CTA ticket of k_sample_lut (reset by that CTA)
-  uint32_t scan_ticket;  // dynamic tile ids of k_scan (reset by k_plan)
   uint32_t nb;           // buckets in use
   uint64_t cap_needed;
   uint64_t kmin_inv;     // ~(smallest sampled key), by atomicMax
@@ -426,10 +427,18 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
   for (uint32_t j = tid; j < kLutIdx; j += blockDim.x) cnt[j] = 0;
   if (tid < 36) lch[tid] = 0;
   __syncthreads();
-#pragma unroll 16
-  for (uint32_t s = tid; s < S; s += blockDim.x) {
-    const K k = SMEM ? samples[s] : __ldcg(samples + s);
-    atomicAdd(&cnt[(uint32_t)((k - kmin) >> shift)], 1u);
+  // 16 loads per thread in flight before their atomics (loads and shared
+  // atomics interleaved in one loop body complete one at a time)
+  for (uint32_t s0 = tid; s0 < S; s0 += 16 * blockDim.x) {
+    K kk[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const uint32_t s = s0 + u * blockDim.x;
+      kk[u] = s < S ? (SMEM ? samples[s] : __ldcg(samples + s)) : kmin;
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u)
+      if (s0 + u * blockDim.x < S) atomicAdd(&cnt[(uint32_t)((kk[u] - kmin) >> shift)], 1u);
   }
   __syncthreads();
 
@@ -546,20 +555,32 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
   // estimated from far-apart samples (q, q + S/2).
   uint32_t same = 0, same_key = 0;
   const uint32_t npairs = S / 2 < 4096u ? S / 2 : 4096u;  // enough for a 1/32 estimate
-  for (uint32_t q = tid; q < npairs; q += blockDim.x) {
-    const K a = SMEM ? samples[2 * q] : __ldcg(samples + 2 * q);
-    const K b = SMEM ? samples[2 * q + 1] : __ldcg(samples + 2 * q + 1);
-    const K c = SMEM ? samples[q] : __ldcg(samples + q);
-    const K d2 = SMEM ? samples[q + S / 2] : __ldcg(samples + q + S / 2);
-    auto bucket = [&](K k) {
-      const K d = k - kmin;
-      const K idx = d >> shift;
-      const uint32_t j = idx < (K)nsl ? (uint32_t)idx : nsl;
-      const uint32_t e = j == nsl ? top : cnt[j];
-      return (uint32_t)((int32_t)e >> 7) + shr_clamp(d, e & 127u);
-    };
-    same += bucket(a) == bucket(b) ? 1u : 0u;
-    same_key += c == d2 ? 1u : 0u;
+  auto bucket = [&](K k) {
+    const K d = k - kmin;
+    const K idx = d >> shift;
+    const uint32_t j = idx < (K)nsl ? (uint32_t)idx : nsl;
+    const uint32_t e = j == nsl ? top : cnt[j];
+    return (uint32_t)((int32_t)e >> 7) + shr_clamp(d, e & 127u);
+  };
+  auto ld = [&](uint32_t i) -> K { return SMEM ? samples[i] : __ldcg(samples + i); };
+  // four pairs of each kind per thread and step, all loads issued first
+  for (uint32_t q0 = tid; q0 < npairs; q0 += 4 * blockDim.x) {
+    K a[4], b[4], c[4], d2[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t q = q0 + u * blockDim.x;
+      const bool ok = q < npairs;
+      a[u] = ok ? ld(2 * q) : K(0);
+      b[u] = ok ? ld(2 * q + 1) : K(0);
+      c[u] = ok ? ld(q) : K(0);
+      d2[u] = ok ? ld(q + S / 2) : K(1);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (q0 + u * blockDim.x < npairs) {
+        same += bucket(a[u]) == bucket(b[u]) ? 1u : 0u;
+        same_key += c[u] == d2[u] ? 1u : 0u;
+      }
   }
   same = block_reduce(same, [](uint32_t p, uint32_t q) { return p + q; }, red32);
   same_key = block_reduce(same_key, [](uint32_t p, uint32_t q) { return p + q; }, red32);
@@ -758,129 +779,97 @@ __global__ void __launch_bounds__(1024, 1)
 }
 
 // ---------------------------------------------------------------------------
-// (d) reduce the per-CTA rows and scan (decoupled look-back, one pass)
+// (d) bucket totals: column sums of the per-CTA rows
 // ---------------------------------------------------------------------------
+// The bucket prefix itself is taken in shared memory by the kernels that
+// search it (k_plan, k_reqmap: smem_excl_scan), which load the totals anyway;
+// a grid-wide scan here would make every tile wait on its predecessors.
 constexpr int kScanThreads = 256;
 constexpr int kScanGroups = 4;                            // row groups per bucket
 constexpr int kScanTile = kScanThreads / kScanGroups;     // buckets per CTA
-constexpr uint64_t kFlagAgg = 1ull << 62, kFlagIncl = 2ull << 62;
-constexpr uint64_t kValMask = (1ull << 62) - 1;
 
-// Thread t handles bucket tile * kScanTile + (t % kScanTile) over row group
-// t / kScanTile, so a warp reads 32 neighbouring buckets of one row (128
-// bytes).  The rows are read twice from L2: once to sum, once to rewrite them
-// as their exclusive prefix.
+// Thread t handles bucket blockIdx.x * kScanTile + (t % kScanTile) over row
+// group t / kScanTile, so a warp reads 32 neighbouring buckets of one row (128
+// bytes).  The rows are read once; only the columns of the buckets that get a
+// slot become prefixes over the rows, later (k_colprefix).
 template <class K>
 __global__ void __launch_bounds__(kScanThreads)
-    k_scan(uint32_t *__restrict__ partials, uint32_t rows, uint32_t nb_max,
-           const LutHeader<K> *hdr, uint32_t *__restrict__ counts, uint32_t *__restrict__ excl,
-           uint64_t *tile_state, Ctrl *ctrl) {
-  __shared__ uint32_t s_tile;
-  __shared__ uint32_t red[33];
+    k_colsum(const uint32_t *__restrict__ partials, uint32_t rows, uint32_t nb_max,
+             const LutHeader<K> *hdr, uint32_t *__restrict__ counts, const Ctrl *ctrl) {
   __shared__ uint32_t gsum[kScanGroups][kScanTile];
-  __shared__ uint64_t s_prefix;
   if (ctrl->status & ST_FATAL) return;
   const uint32_t nb = hdr->nb;
-  if (threadIdx.x == 0) s_tile = atomicAdd(&ctrl->scan_ticket, 1u);
-  __syncthreads();
-  const uint32_t tile = s_tile;
-  if ((uint64_t)tile * kScanTile >= nb) return;
+  if ((uint64_t)blockIdx.x * kScanTile >= nb) return;
   const uint32_t col = threadIdx.x % kScanTile, grp = threadIdx.x / kScanTile;
-  const uint32_t b = tile * kScanTile + col;
+  const uint32_t b = blockIdx.x * kScanTile + col;
   const uint32_t per = (rows + kScanGroups - 1) / kScanGroups;
   const uint32_t r0 = grp * per, r1 = min(rows, r0 + per);
-  uint32_t *p = partials + b;
+  const uint32_t *p = partials + b;
   uint32_t gs = 0;
   if (b < nb) {
-    uint32_t r = r0;
-    for (; r + 8 <= r1; r += 8) {
-      uint32_t v[8];
+    // predicated batches: every load of a batch is in flight at once (a
+    // remainder loop of single loads would wait for each)
+    for (uint32_t r = r0; r < r1; r += 20) {
+      uint32_t v[20];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) v[q] = __ldcg(p + (uint64_t)(r + q) * nb_max);
+      for (int q = 0; q < 20; ++q) v[q] = r + q < r1 ? __ldcg(p + (uint64_t)(r + q) * nb_max) : 0u;
 #pragma unroll
-      for (int q = 0; q < 8; ++q) gs += v[q];
+      for (int q = 0; q < 20; ++q) gs += v[q];
     }
-    for (; r < r1; ++r) gs += __ldcg(p + (uint64_t)r * nb_max);
   }
   gsum[grp][col] = gs;
   __syncthreads();
-  uint32_t c = 0, before = 0;  // bucket total; rows of the groups before mine
+  if (grp == 0 && b < nb) {
+    uint32_t c = 0;
 #pragma unroll
-  for (int g = 0; g < kScanGroups; ++g) {
-    const uint32_t v = gsum[g][col];
-    before += (g < (int)grp) ? v : 0u;
-    c += v;
+    for (int g = 0; g < kScanGroups; ++g) c += gsum[g][col];
+    counts[b] = c;
   }
-  if (b < nb) {
-    // column b becomes its exclusive prefix over the rows: the compaction
-    // pass starts CTA r's cursor for bucket b there
-    uint32_t run = before;
-    uint32_t r = r0;
-    for (; r + 8 <= r1; r += 8) {
-      uint32_t v[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) v[q] = __ldcg(p + (uint64_t)(r + q) * nb_max);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        p[(uint64_t)(r + q) * nb_max] = run;
-        run += v[q];
-      }
-    }
-    for (; r < r1; ++r) {
-      const uint32_t v = __ldcg(p + (uint64_t)r * nb_max);
-      p[(uint64_t)r * nb_max] = run;
-      run += v;
-    }
-  }
-  // scan of the tile's bucket totals (group 0's threads hold one bucket each)
-  uint32_t agg;
-  const uint32_t incl = block_incl_scan(grp == 0 ? c : 0u, &agg, red);
+}
 
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
-    uint64_t prefix = 0;
-    if (tile == 0) {
-      if (lane == 0) st_release_u64(&tile_state[0], kFlagIncl | agg);
-    } else {
-      if (lane == 0) st_release_u64(&tile_state[tile], kFlagAgg | agg);
-      int64_t pred = (int64_t)tile - 1;
-      bool timed_out = false;
-      while (true) {
-        const int64_t pp = pred - lane;
-        uint64_t st = 0;
-        int iters = 0;
-        while (true) {
-          st = pp >= 0 ? ld_acquire_u64(&tile_state[pp]) : kFlagIncl;
-          if (__all_sync(0xffffffffu, (st >> 62) != 0)) break;
-          if (++iters > kSpinLimit) {
-            timed_out = true;
-            break;
-          }
-          __nanosleep(64);
-        }
-        if (timed_out) break;
-        const uint32_t incl_mask = __ballot_sync(0xffffffffu, (st >> 62) == 2);
-        const int first = incl_mask ? __ffs(incl_mask) - 1 : 32;
-        uint64_t v = (lane <= first) ? (st & kValMask) : 0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        prefix += v;
-        if (incl_mask) break;
-        pred -= 32;
-      }
-      if (timed_out) {
-        if (lane == 0) atomicOr(&ctrl->status, ST_TIMEOUT);
-        prefix = 0;
-      }
-      if (lane == 0) st_release_u64(&tile_state[tile], kFlagIncl | (prefix + agg));
+// In place: a[0 .. nb) (bucket totals, 16-byte aligned, zero from nb up to
+// the next multiple of 4) becomes its exclusive prefix; returns the total.
+// Warp w owns a contiguous run of 16-byte vectors, read in rounds of 32
+// neighbouring vectors (conflict-free); one pass sums, one pass writes.
+static __device__ uint64_t smem_excl_scan(uint32_t *a, uint32_t nb, uint32_t *s_w /* >= 33 */) {
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  uint4 *a4 = reinterpret_cast<uint4 *>(a);
+  const uint32_t nv = (nb + 3) >> 2;
+  const uint32_t span = (((nv + nwarps - 1) / nwarps) + 31) & ~31u;  // vectors per warp
+  const uint32_t v0 = warp * span;
+  uint32_t mine = 0;
+  for (uint32_t r = 0; r < span; r += 32) {
+    const uint32_t v = v0 + r + lane;
+    if (v < nv) {
+      const uint4 c = a4[v];
+      mine += c.x + c.y + c.z + c.w;
     }
-    if (lane == 0) s_prefix = prefix;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+  if (lane == 0) s_w[warp] = mine;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = lane < nwarps ? s_w[lane] : 0u;
+    const uint32_t incl = warp_incl_scan(w);
+    if (lane < nwarps) s_w[lane] = incl - w;
+    if (lane == 31) s_w[32] = incl;
   }
   __syncthreads();
-  if (grp == 0 && b < nb) {
-    counts[b] = c;
-    excl[b] = (uint32_t)(s_prefix + incl - c);
+  uint32_t base = s_w[warp];
+  for (uint32_t r = 0; r < span; r += 32) {
+    const uint32_t v = v0 + r + lane;
+    uint4 c = make_uint4(0, 0, 0, 0);
+    if (v < nv) c = a4[v];
+    const uint32_t sum = c.x + c.y + c.z + c.w;
+    const uint32_t incl = warp_incl_scan(sum);
+    const uint32_t pre = base + incl - sum;
+    if (v < nv) a4[v] = make_uint4(pre, pre + c.x, pre + c.x + c.y, pre + c.x + c.y + c.z);
+    base += __shfl_sync(0xffffffffu, incl, 31);
   }
+  const uint64_t total = s_w[32];
+  __syncthreads();
+  return total;
 }
 
 // ---------------------------------------------------------------------------
@@ -900,20 +889,49 @@ struct Premap {
   uint32_t *bslot = nullptr;         // slot of each flagged bucket (written by k_plan)
 };
 
+// Bucket totals counts_g[0 .. nb) -> a[] (shared, 16-byte aligned), zero up
+// to the next multiple of 4; every load of a step in flight before the
+// stores.
+__device__ __forceinline__ void load_totals(const uint32_t *__restrict__ counts_g, uint32_t nb,
+                                            uint32_t *a) {
+  const uint32_t nb4 = (nb + 3) >> 2;
+  for (uint32_t v0 = threadIdx.x; v0 < nb4; v0 += 4 * blockDim.x) {
+    uint4 e[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t v = v0 + u * blockDim.x;
+      e[u] = v < nb4 ? __ldcg(reinterpret_cast<const uint4 *>(counts_g) + v) : make_uint4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t v = v0 + u * blockDim.x;
+      if (v < nb4) {
+        if (4 * v + 4 > nb) {  // the last vector: totals past nb are stale
+          const uint32_t k = nb - 4 * v;
+          if (k < 2) e[u].y = 0;
+          if (k < 3) e[u].z = 0;
+          e[u].w = 0;
+        }
+        reinterpret_cast<uint4 *>(a)[v] = e[u];
+      }
+    }
+  }
+}
+
 // Bitmap and counts must start at zero.  Shared memory: the bucket prefix
-// (nb_max u32).
+// (nb_max u32), scanned here from the bucket totals.
 static __global__ void __launch_bounds__(1024)
-    k_reqmap(const uint32_t *__restrict__ excl_g, const Ctrl *ctrl, const Req *__restrict__ reqs,
+    k_reqmap(const uint32_t *__restrict__ counts_g, const Ctrl *ctrl, const Req *__restrict__ reqs,
              uint32_t num_req, uint32_t *__restrict__ req_bucket,
              uint32_t *__restrict__ req_local, uint32_t *bits, uint32_t *bcount) {
   extern __shared__ uint4 smem_raw[];
   uint32_t *excl = reinterpret_cast<uint32_t *>(smem_raw);
+  __shared__ uint32_t s_w[33];
   if (ctrl->status & ST_FATAL) return;
   const uint32_t nb = ctrl->nb;
-  const uint32_t nb4 = (nb + 3) >> 2;
-  for (uint32_t v = threadIdx.x; v < nb4; v += blockDim.x)
-    reinterpret_cast<uint4 *>(excl)[v] = __ldcg(reinterpret_cast<const uint4 *>(excl_g) + v);
+  load_totals(counts_g, nb, excl);
   __syncthreads();
+  smem_excl_scan(excl, nb, s_w);
   const uint32_t lane = threadIdx.x & 31;
   for (uint32_t u = 0; u < kReqmapPerCta / 1024; ++u) {
     const uint32_t i = blockIdx.x * kReqmapPerCta + u * 1024 + threadIdx.x;
@@ -965,6 +983,42 @@ static __global__ void __launch_bounds__(1024)
     e.rank = req_local[i];
     e.out = reqs[i].out;
     klist[kstart[q] + base + __popc(peers & ((1u << lane) - 1u))] = e;
+  }
+}
+
+// Column b of the per-CTA histogram rows becomes its exclusive prefix over the
+// rows for every slot bucket with survivors: the compaction pass starts CTA
+// r's cursor for bucket b there.  One warp per slot, four warps per CTA: the
+// column accesses are scattered (one sector per row), so they are spread over
+// every SM; the other columns are never read again.
+constexpr int kColpThreads = 128;
+static __global__ void __launch_bounds__(kColpThreads)
+    k_colprefix(uint32_t *partials, uint32_t rows, uint32_t nb_max, const Ctrl *ctrl,
+                const uint32_t *__restrict__ seg_bucket, const uint32_t *__restrict__ seg_size) {
+  if (ctrl->status & ST_FATAL) return;
+  const uint32_t num_slots = ctrl->num_slots;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; slot < num_slots;
+       slot += warps) {
+    if (__ldcg(seg_size + slot) == 0) continue;  // flat slot: no survivors
+    uint32_t *col = partials + __ldcg(seg_bucket + slot);
+    uint32_t run = 0;
+    for (uint32_t r0 = 0; r0 < rows; r0 += 8 * 32) {
+      uint32_t v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const uint32_t r = r0 + q * 32 + lane;
+        v[q] = r < rows ? __ldcg(col + (uint64_t)r * nb_max) : 0u;
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const uint32_t r = r0 + q * 32 + lane;
+        const uint32_t incl = warp_incl_scan(v[q]);
+        if (r < rows) col[(uint64_t)r * nb_max] = run + incl - v[q];
+        run += __shfl_sync(0xffffffffu, incl, 31);
+      }
+    }
   }
 }
 
@@ -1020,9 +1074,9 @@ __device__ __forceinline__ void plan_map_requests(const uint32_t *excl, uint32_t
 template <class InT, class OutT>
 __global__ void __launch_bounds__(1024, 1)
     k_plan(const LutHeader<typename Traits<InT>::K> *hdr, const uint32_t *__restrict__ lut_g,
-           const uint32_t *__restrict__ counts, const uint32_t *__restrict__ excl_g, uint64_t n,
+           const uint32_t *__restrict__ counts, uint64_t n,
            const Req *__restrict__ reqs, uint32_t num_req, uint32_t nb_max, Ctrl *ctrl,
-           uint64_t *tile_state, uint32_t scan_tiles, uint32_t *__restrict__ seg_bucket,
+           uint32_t *__restrict__ seg_bucket,
            uint64_t *__restrict__ seg_off, uint32_t *__restrict__ seg_size,
            uint32_t *__restrict__ kstart, uint32_t *__restrict__ kcnt,
            uint32_t *__restrict__ kcur, typename Traits<InT>::K *__restrict__ seg_lo,
@@ -1043,29 +1097,45 @@ __global__ void __launch_bounds__(1024, 1)
   if (ctrl->status & ST_FATAL) return;
   const LutHeader<K> h = *hdr;
   const uint32_t nb = h.nb;
-  // 16-byte loads: the buffers are 16-byte aligned and hold nb_max (a
-  // multiple of 4) entries
+  // bucket totals (becoming the prefix below) and flags, one 16-byte vector
+  // and one flag word per four buckets; every load of a step is issued before
+  // the first shared store (loads and stores interleaved in one loop body
+  // complete one at a time)
+  load_totals(counts, nb, excl);
   const uint32_t nb4 = (nb + 3) >> 2;
-#pragma unroll 4
-  for (uint32_t v = tid; v < nb4; v += nt) {
-    reinterpret_cast<uint4 *>(excl)[v] = __ldcg(reinterpret_cast<const uint4 *>(excl_g) + v);
-    uint32_t fw = 0u;  // flags of buckets 4v .. 4v + 3, one byte each
-    if (pm.bits) {
-      const uint32_t f4 = (__ldcg(pm.bits + (v >> 3)) >> ((4 * v) & 31)) & 0xFu;
-      fw = (f4 & 1u) | ((f4 & 2u) << 7) | ((f4 & 4u) << 14) | ((f4 & 8u) << 21);
+  for (uint32_t v0 = tid; v0 < nb4; v0 += 4 * nt) {
+    uint32_t f[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t v = v0 + u * nt;
+      f[u] = v < nb4 && pm.bits ? __ldcg(pm.bits + (v >> 3)) : 0u;
     }
-    reinterpret_cast<uint32_t *>(flag)[v] = fw;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t v = v0 + u * nt;
+      if (v < nb4) {
+        // flags of buckets 4v .. 4v + 3, one byte each
+        const uint32_t f4 = (f[u] >> ((4 * v) & 31)) & 0xFu;
+        reinterpret_cast<uint32_t *>(flag)[v] =
+            (f4 & 1u) | ((f4 & 2u) << 7) | ((f4 & 4u) << 14) | ((f4 & 8u) << 21);
+      }
+    }
   }
-#pragma unroll 4
-  for (uint32_t j = tid; j < kLutEntries; j += nt) lut[j] = __ldcg(lut_g + j);
-  // re-arm the scan's state for the next call on this workspace
-  for (uint32_t t = tid; t < scan_tiles; t += nt) tile_state[t] = 0;
-  if (tid == 0) {
-    ctrl->scan_ticket = 0;
-    ctrl->deferred_count = 0;
-    if ((uint64_t)excl_g[nb - 1] + counts[nb - 1] != n) atomicOr(&ctrl->status, ST_INTERNAL);
+  for (uint32_t j0 = tid; j0 < kLutEntries; j0 += 8 * nt) {
+    uint32_t e[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const uint32_t j = j0 + u * nt;
+      e[u] = j < kLutEntries ? __ldcg(lut_g + j) : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (j0 + u * nt < kLutEntries) lut[j0 + u * nt] = e[u];
   }
+  if (tid == 0) ctrl->deferred_count = 0;
   __syncthreads();
+  // the totals must add up to n (else the input changed under the histogram)
+  if (smem_excl_scan(excl, nb, s_wbase) != n && tid == 0) atomicOr(&ctrl->status, ST_INTERNAL);
 
   // requests -> bucket (the last b with excl[b] <= rank is never empty) and
   // the rank inside it; with many requests, four per thread and step, so that
@@ -1481,7 +1551,29 @@ __device__ __forceinline__ uint32_t bin_of_rank(const uint32_t *start, uint32_t 
 // 5 * kFinBins u32, the gather buffer (bcap keys), the scratch (bcap / 2
 // keys), per-bin minima and maxima (kFinBins keys each).  Returns false when
 // the needed bins do not fit: the slot needs a recursive re-selection.
-template <class K, class OutT>
+// 16-byte vectors of survivor keys, read past L1 (the survivors may have been
+// written earlier in the same kernel)
+template <class K>
+struct KeyVec;
+template <>
+struct KeyVec<uint32_t> {
+  using V = uint4;
+  static constexpr int kKeys = 4;
+  static __device__ __forceinline__ V load(const V *p) { return __ldcg(p); }
+  static __device__ __forceinline__ uint32_t key(const V &v, int e) {
+    return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
+  }
+};
+template <>
+struct KeyVec<uint64_t> {
+  using V = ulonglong2;
+  static constexpr int kKeys = 2;
+  static __device__ __forceinline__ V load(const V *p) { return __ldcg(p); }
+  static __device__ __forceinline__ uint64_t key(const V &v, int e) { return e == 0 ? v.x : v.y; }
+};
+constexpr int kFinVecs = 2;  // vectors per thread and chunk in k_finish (63 registers)
+
+template <class K, class OutT, int VECS = kFinVecs>
 __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi,
                             const Req *__restrict__ rq, uint32_t m, uint32_t bcap, uint32_t *smem,
                             OutT *__restrict__ out) {
@@ -1503,10 +1595,52 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
   const uint32_t tcap = bcap / 2;                   // scratch T holds one bin of <= tcap keys
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t nwarps = blockDim.x >> 5;
+  // each thread's first request, loaded ahead of the phases that read it
+  Req my_rq;
+  my_rq.rank = 0;
+  my_rq.out = 0;
+  if (tid < m) my_rq = rq[tid];
+  auto req_at = [&](uint32_t j) -> Req { return j == tid ? my_rq : rq[j]; };
   if (size == 0) {  // flat slot: every rank in the bucket is its single key
-    for (uint32_t j = tid; j < m; j += blockDim.x) out[rq[j].out] = Traits<OutT>::value(lo);
+    for (uint32_t j = tid; j < m; j += blockDim.x) out[req_at(j).out] = Traits<OutT>::value(lo);
     return true;
   }
+  // The segment is read as aligned 16-byte vectors, VECS per thread and
+  // chunk, every load of a chunk in flight before its keys are used (each
+  // vector in flight costs about 15 registers once its keys' bodies are
+  // scheduled).  The first and last vector may hold keys of the neighbouring
+  // segments (an
+  // aligned 16-byte granule lies within one page, so reading it is safe);
+  // those keys are masked out.
+  using KV = KeyVec<K>;
+  using VecT = typename KV::V;
+  constexpr uint32_t KPV = KV::kKeys;
+  const uintptr_t a0 = reinterpret_cast<uintptr_t>(src) & ~uintptr_t(15);
+  const uint32_t head = (uint32_t)((reinterpret_cast<uintptr_t>(src) - a0) / sizeof(K));
+  const VecT *vsrc = reinterpret_cast<const VecT *>(a0);
+  const uint32_t nvec = (uint32_t)(((uint64_t)head + size + KPV - 1) / KPV);
+  const uint32_t chunk = VECS * blockDim.x;
+  auto each_key = [&](auto &&fn) {
+    for (uint32_t c0 = 0; c0 < nvec; c0 += chunk) {
+      VecT tv[VECS];
+#pragma unroll
+      for (int u = 0; u < VECS; ++u) {
+        const uint32_t v = c0 + u * blockDim.x + tid;
+        if (v < nvec) tv[u] = KV::load(vsrc + v);
+      }
+#pragma unroll
+      for (int u = 0; u < VECS; ++u) {
+        const uint32_t v = c0 + u * blockDim.x + tid;
+        if (v < nvec) {
+#pragma unroll
+          for (uint32_t e = 0; e < KPV; ++e) {
+            const uint32_t i = v * KPV + e;  // key index from the first vector's start
+            if (i >= head && i - head < size) fn(KV::key(tv[u], (int)e));
+          }
+        }
+      }
+    }
+  };
   // about four keys per bin
   uint32_t nbits = 8;
   while (nbits < (uint32_t)kFinBinBits && (4u << nbits) < size) ++nbits;
@@ -1522,11 +1656,10 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
   for (int attempt = 0; attempt < 2 && !fits && !flat && !direct; ++attempt) {
     if (attempt == 1) {
       K a = KeyMax<K>::v, z = 0;
-      for (uint32_t i = tid; i < size; i += blockDim.x) {
-        const K k = src[i];
+      each_key([&](K k) {
         a = k < a ? k : a;
         z = k > z ? k : z;
-      }
+      });
       a = block_reduce(a, [](K p, K q) { return p < q ? p : q; }, redk);
       z = block_reduce(z, [](K p, K q) { return p > q ? p : q; }, redk);
       if (a == z) {
@@ -1562,17 +1695,7 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
         atomic_max_key(&bmax[bb], k);
       }
     };
-    {
-      uint32_t i = tid;
-      for (; i + 7 * blockDim.x < size; i += 8 * blockDim.x) {
-        K kk[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) kk[q] = src[i + q * blockDim.x];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) count(kk[q]);
-      }
-      for (; i < size; i += blockDim.x) count(src[i]);
-    }
+    each_key(count);
     __syncthreads();
     {
       uint32_t cc[PER], sum = 0;
@@ -1600,11 +1723,10 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
       break;
     }
     for (uint32_t j = tid; j < m; j += blockDim.x)
-      gofs[bin_of_rank(start, nbins, rq[j].rank)] = 1u;
+      gofs[bin_of_rank(start, nbins, req_at(j).rank)] = 1u;
     __syncthreads();
     {
       uint32_t cc[PER], sum = 0;
-#pragma unroll
       bool one[PER];  // a needed bin of one distinct key (tracked attempt only)
 #pragma unroll
       for (uint32_t q = 0; q < PER; ++q) {
@@ -1635,13 +1757,13 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
     fits = V <= bcap && s_maxneed <= tcap;
   }
   if (flat) {  // one distinct key: every rank is that key
-    for (uint32_t j = tid; j < m; j += blockDim.x) out[rq[j].out] = Traits<OutT>::value(mn);
+    for (uint32_t j = tid; j < m; j += blockDim.x) out[req_at(j).out] = Traits<OutT>::value(mn);
     __syncthreads();
     return true;
   }
   if (direct) {  // bins of one key each (few distinct keys, many copies)
     for (uint32_t j = tid; j < m; j += blockDim.x) {
-      const Req e = rq[j];
+      const Req e = req_at(j);
       out[e.out] = Traits<OutT>::value(mn + (K)bin_of_rank(start, nbins, e.rank));
     }
     __syncthreads();
@@ -1659,15 +1781,7 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
       const uint32_t g = gofs[bb];
       if (g < kFlatBin) B[g + atomicAdd(&cur[bb], 1u)] = k;
     };
-    uint32_t i = tid;
-    for (; i + 7 * blockDim.x < size; i += 8 * blockDim.x) {
-      K kk[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) kk[q] = src[i + q * blockDim.x];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) put(kk[q]);
-    }
-    for (; i < size; i += blockDim.x) put(src[i]);
+    each_key(put);
   }
   __syncthreads();
 
@@ -1698,7 +1812,7 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
 
   // ---- answer
   for (uint32_t j = tid; j < m; j += blockDim.x) {
-    const Req e = rq[j];
+    const Req e = req_at(j);
     const uint32_t bb = bin_of_rank(start, nbins, e.rank);
     const uint32_t g = gofs[bb];
     out[e.out] = Traits<OutT>::value(g == kFlatBin ? bmin[bb] : B[g + (e.rank - start[bb])]);

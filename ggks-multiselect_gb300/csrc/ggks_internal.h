@@ -32,7 +32,7 @@ struct Context {
   cudaStream_t stream = nullptr;
   std::mutex mu;
 
-  char *arena = nullptr;  // [tile_state | out | ctrl | reqs | ... ]
+  char *arena = nullptr;  // [out | ctrl | reqs | ... ]
   size_t arena_bytes = 0;
   void *surv = nullptr;
   size_t surv_bytes = 0;
@@ -79,7 +79,6 @@ cudaError_t ensure_dvec(Context &ctx, size_t bytes);
 cudaError_t ensure_pin(Context &ctx, size_t bytes);
 
 // fixed-offset persistent state at the start of the arena
-constexpr size_t kTileStateBytes = 8192;  // >= (65536 / kScanTile) * 8
 
 // Where the requests of one selection come from.
 struct ReqSource {

@@ -35,17 +35,15 @@ constexpr uint32_t kNaMaxG = 64;     // histogram / compaction CTAs
 constexpr uint32_t kNaS = 65536;     // sample size
 
 constexpr size_t na_align(size_t v) { return (v + 255) / 256 * 256; }
-// scratch layout (byte offsets); tile_state must start at offset 0
-constexpr size_t kNaTile = 0;
-constexpr size_t kNaCtrl = na_align(kNaTile + kTileStateBytes);
+// scratch layout (byte offsets)
+constexpr size_t kNaCtrl = 0;
 constexpr size_t kNaReqs = na_align(kNaCtrl + sizeof(Ctrl));
 constexpr size_t kNaHdr = na_align(kNaReqs + kNaMaxK * sizeof(Req));
 constexpr size_t kNaLut = na_align(kNaHdr + sizeof(LutHeader<uint32_t>));
 constexpr size_t kNaSamples = na_align(kNaLut + kLutPadded * sizeof(uint32_t));
 constexpr size_t kNaPartials = na_align(kNaSamples + kNaS * sizeof(uint32_t));
 constexpr size_t kNaCounts = na_align(kNaPartials + (size_t)kNaMaxG * kNaNbMax * 4);
-constexpr size_t kNaExcl = na_align(kNaCounts + kNaNbMax * 4);
-constexpr size_t kNaSegBucket = na_align(kNaExcl + kNaNbMax * 4);
+constexpr size_t kNaSegBucket = na_align(kNaCounts + kNaNbMax * 4);
 constexpr size_t kNaSegOff = na_align(kNaSegBucket + kNaNbMax * 4);
 constexpr size_t kNaSegSize = na_align(kNaSegOff + kNaNbMax * 8);
 constexpr size_t kNaKstart = na_align(kNaSegSize + kNaNbMax * 4);
@@ -128,8 +126,6 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
   K *samples = reinterpret_cast<K *>(A + kNaSamples);
   uint32_t *partials = reinterpret_cast<uint32_t *>(A + kNaPartials);
   uint32_t *counts = reinterpret_cast<uint32_t *>(A + kNaCounts);
-  uint32_t *excl = reinterpret_cast<uint32_t *>(A + kNaExcl);
-  uint64_t *tile_state = reinterpret_cast<uint64_t *>(A + kNaTile);
   uint32_t *seg_bucket = reinterpret_cast<uint32_t *>(A + kNaSegBucket);
   uint64_t *seg_off = reinterpret_cast<uint64_t *>(A + kNaSegOff);
   uint32_t *seg_size = reinterpret_cast<uint32_t *>(A + kNaSegSize);
@@ -148,14 +144,13 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
   const uint32_t S = n <= kNaS ? (uint32_t)n : kNaS;
   uint64_t g = (n + 65535) / 65536;
   const uint32_t G = (uint32_t)(g < 1 ? 1 : (g > kNaMaxG ? kNaMaxG : (g > (uint64_t)sms ? sms : g)));
-  const uint32_t scan_tiles = (kNaNbMax + kScanTile - 1) / kScanTile;
+  const uint32_t col_tiles = (kNaNbMax + kScanTile - 1) / kScanTile;
   const uint32_t cap_keys = cap_keys_for<float>();
   const uint32_t fg = 5u * (uint32_t)sms;
   const uint32_t fin_grid = num_k < fg ? num_k : fg;
 
-  // state that must start at zero: the control block and the look-back flags
-  // (the scan re-arms the flags itself, but a call that stopped early may not)
-  e = cudaMemsetAsync(A + kNaTile, 0, kNaCtrl + sizeof(Ctrl), s);
+  // the control block starts at zero
+  e = cudaMemsetAsync(A + kNaCtrl, 0, sizeof(Ctrl), s);
   if (e != cudaSuccess) return from_cuda(e);
   k_na_reqs<<<(num_k + 255) / 256, 256, 0, s>>>(d_k, num_k, n, reqs, ctrl);
   k_sample_lut<float><<<(S + 1023) / 1024, 1024, 0, s>>>(d_vec, n, S, 0x5EEDu, samples, ctrl, hdr,
@@ -166,15 +161,21 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
     k_hist<float, UNROLL><<<G, 1024, smem, s>>>(d_vec, n, hdr, lut, partials, kNaNbMax, ctrl,
                                                 nullptr);
   }
-  k_scan<K><<<scan_tiles, kScanThreads, 0, s>>>(partials, G, kNaNbMax, hdr, counts, excl,
-                                                tile_state, ctrl);
+  k_colsum<K><<<col_tiles, kScanThreads, 0, s>>>(partials, G, kNaNbMax, hdr, counts, ctrl);
   {
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kNaNbMax * 5);
     set_smem_max<k_plan<float, float>>(kPlanSmemMax);
-    k_plan<float, float><<<1, 1024, smem, s>>>(hdr, lut, counts, excl, n, reqs, num_k, kNaNbMax,
-                                                ctrl, tile_state, scan_tiles, seg_bucket, seg_off,
+    k_plan<float, float><<<1, 1024, smem, s>>>(hdr, lut, counts, n, reqs, num_k, kNaNbMax,
+                                                ctrl, seg_bucket, seg_off,
                                                 seg_size, kstart, kcnt, kcur, seg_lo, seg_hi,
                                                 req_bucket, req_local, klist, n, Premap{});
+  }
+  {
+    // the slot buckets' columns of the histogram rows become prefixes
+    const uint32_t wpc = kColpThreads / 32;
+    const uint32_t cg = (num_k + wpc - 1) / wpc, cg_max = 16u * (uint32_t)sms;
+    k_colprefix<<<cg > cg_max ? cg_max : cg, kColpThreads, 0, s>>>(partials, G, kNaNbMax, ctrl,
+                                                                    seg_bucket, seg_size);
   }
   {
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kNaNbMax * 4);

@@ -43,10 +43,11 @@ struct Plan {
   uint32_t scan_tiles = 0;
   uint32_t cap_keys = 0;
   uint32_t fin_grid = 0;
+  uint32_t colp_grid = 0;
   uint64_t surv_cap = 0;
   // arena offsets
   size_t out = 0, ctrl = 0, reqs = 0, hdr = 0, lut = 0, samples = 0, partials = 0,
-         counts = 0, excl = 0, seg_bucket = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0,
+         counts = 0, seg_bucket = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0,
          kcur = 0, seg_lo = 0, seg_hi = 0, deferred = 0, req_bucket = 0, req_local = 0, klist = 0,
          pm_bits = 0, pm_bcount = 0, pm_bslot = 0, total = 0;
 };
@@ -70,12 +71,16 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   uint32_t slots_bound = num_req < p.nb_max ? num_req : p.nb_max;
   uint32_t fg = 5u * (uint32_t)ctx.sm_count;
   p.fin_grid = slots_bound < fg ? (slots_bound ? slots_bound : 1) : fg;
+  // one warp per slot, at most 16 CTAs per SM
+  const uint32_t wpc = kColpThreads / 32;
+  const uint32_t cg = (slots_bound + wpc - 1) / wpc, cg_max = 16u * (uint32_t)ctx.sm_count;
+  p.colp_grid = cg < 1 ? 1 : (cg > cg_max ? cg_max : cg);
   uint64_t cap = n / 8;
   p.surv_cap = cap < (1u << 20) ? (1u << 20) : cap;
   if (p.surv_cap > n) p.surv_cap = n;
 
   const size_t A = 256;
-  size_t o = kTileStateBytes;
+  size_t o = 0;
   p.out = o;
   o = align_up(o + (size_t)num_req * sizeof(OutT), A);
   p.ctrl = o;
@@ -95,7 +100,6 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
     o = align_up(o + elems * esz, A);
   };
   arr(p.counts, p.nb_max, 4);
-  arr(p.excl, p.nb_max, 4);
   arr(p.seg_bucket, p.nb_max, 4);
   arr(p.seg_off, p.nb_max, 8);
   arr(p.seg_size, p.nb_max, 4);
@@ -173,8 +177,6 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   K *samples = reinterpret_cast<K *>(A + p.samples);
   uint32_t *partials = reinterpret_cast<uint32_t *>(A + p.partials);
   uint32_t *counts = reinterpret_cast<uint32_t *>(A + p.counts);
-  uint32_t *excl = reinterpret_cast<uint32_t *>(A + p.excl);
-  uint64_t *tile_state = reinterpret_cast<uint64_t *>(A);
   uint32_t *seg_bucket = reinterpret_cast<uint32_t *>(A + p.seg_bucket);
   uint64_t *seg_off = reinterpret_cast<uint64_t *>(A + p.seg_off);
   uint32_t *seg_size = reinterpret_cast<uint32_t *>(A + p.seg_size);
@@ -240,8 +242,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   // ---- (d) reduce + decoupled look-back scan
   {
     PassTimer t(ctx, s, GGKS_PASS_SCAN);
-    k_scan<K><<<p.scan_tiles, kScanThreads, 0, s>>>(partials, p.G, p.nb_max, hdr, counts, excl,
-                                                  tile_state, ctrl);
+    k_colsum<K><<<p.scan_tiles, kScanThreads, 0, s>>>(partials, p.G, p.nb_max, hdr, counts, ctrl);
     ran[GGKS_PASS_SCAN] = true;
   }
   // ---- (e) plan
@@ -263,13 +264,13 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       if (e != cudaSuccess) return from_cuda(e);
       set_smem_max<k_reqmap>((int)(kMaxNb * 4));
       k_reqmap<<<(num_req + kReqmapPerCta - 1) / kReqmapPerCta, 1024, p.nb_max * 4, s>>>(
-          excl, ctrl, rq, num_req, req_bucket, req_local, pm_bits, pm_bcount);
+          counts, ctrl, rq, num_req, req_bucket, req_local, pm_bits, pm_bcount);
       pm.bits = pm_bits;
       pm.bcount = pm_bcount;
       pm.bslot = pm_bslot;
     }
-    k_plan<InT, OutT><<<1, 1024, smem, s>>>(hdr, lut, counts, excl, n, rq, num_req, p.nb_max, ctrl,
-                                             tile_state, p.scan_tiles, seg_bucket, seg_off,
+    k_plan<InT, OutT><<<1, 1024, smem, s>>>(hdr, lut, counts, n, rq, num_req, p.nb_max, ctrl,
+                                             seg_bucket, seg_off,
                                              seg_size, kstart, kcnt, kcur, seg_lo, seg_hi,
                                              req_bucket, req_local, klist, p.surv_cap, pm);
     if (premap) {
@@ -277,6 +278,10 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
                                                           pm_bslot, kstart, kcur, klist);
       ctx.stats.launches += 2;
     }
+    // the slot buckets' columns of the histogram rows become prefixes
+    k_colprefix<<<p.colp_grid, kColpThreads, 0, s>>>(partials, p.G, p.nb_max, ctrl, seg_bucket,
+                                                      seg_size);
+    ctx.stats.launches++;
     ran[GGKS_PASS_PLAN] = true;
   }
   uint64_t surv_cap = p.surv_cap;
@@ -323,11 +328,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
 
   for (int round = 0; round < 4; ++round) {
     const Ctrl c = *h_ctrl;
-    if (c.status & ST_FATAL) {
-      cudaMemsetAsync(tile_state, 0, kTileStateBytes, s);
-      cudaStreamSynchronize(s);
-      return (c.status & ST_TIMEOUT) ? GGKS_TIMEOUT : GGKS_INTERNAL;
-    }
+    if (c.status & ST_FATAL) return (c.status & ST_TIMEOUT) ? GGKS_TIMEOUT : GGKS_INTERNAL;
     if (c.status & ST_OVERFLOW) {
       // survivors did not fit: grow the buffer, re-run compaction + finish
       const uint64_t need = c.cap_needed + (c.cap_needed >> 3);
