@@ -16,6 +16,7 @@ namespace ggks {
 // top-k requests: output i receives the (i+1)-th largest, i.e. ascending rank
 // n-1-i (multiselectTimingFunctions.cu:207-209 builds k = 1..K for this)
 __global__ void k_make_topk_reqs(Req *reqs, uint64_t n, uint32_t K) {
+  pdl_start();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < K) {
     Req r;

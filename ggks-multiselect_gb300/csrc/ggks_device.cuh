@@ -65,6 +65,19 @@ constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
 constexpr uint32_t kInactive = 0x80000000u;  // compaction cursor of an inactive bucket
 constexpr int kSpinLimit = 1 << 22;              // bounded device-side waits
 
+// Programmatic dependent launch.  The pipeline's kernels are launched so that
+// each may be scheduled while its predecessor in the stream still runs;
+// griddepcontrol.wait blocks until that predecessor has completed and its
+// memory is visible (a no-op after a plain launch), and comes before a
+// kernel's first global access.  griddepcontrol.launch_dependents lets the
+// successor be scheduled at once: it orders nothing, the successor's own wait
+// does.  No kernel of the pipeline waits on other CTAs, so successors that sit
+// resident while waiting cannot hold up the running grid.
+__device__ __forceinline__ void pdl_start() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // status bits in Ctrl::status
 enum : uint32_t {
   ST_OVERFLOW = 1u,  // survivors exceed the survivor buffer: host regrows, re-runs (f)+(g)
@@ -608,6 +621,7 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
                                                      Ctrl *ctrl,
                                                      LutHeader<typename Traits<T>::K> *hdr,
                                                      uint32_t *lut, uint32_t nb_max) {
+  pdl_start();
   using K = typename Traits<T>::K;
   __shared__ K redk[33];
   __shared__ uint32_t s_last;
@@ -753,6 +767,7 @@ __global__ void __launch_bounds__(1024, 1)
     k_hist(const T *__restrict__ x, uint64_t n, const LutHeader<typename Traits<T>::K> *hdr,
            const uint32_t *__restrict__ lut_g, uint32_t *__restrict__ partials, uint32_t nb_max,
            const Ctrl *ctrl, T *__restrict__ copy_to) {
+  pdl_start();
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
@@ -796,6 +811,7 @@ template <class K>
 __global__ void __launch_bounds__(kScanThreads)
     k_colsum(const uint32_t *__restrict__ partials, uint32_t rows, uint32_t nb_max,
              const LutHeader<K> *hdr, uint32_t *__restrict__ counts, const Ctrl *ctrl) {
+  pdl_start();
   __shared__ uint32_t gsum[kScanGroups][kScanTile];
   if (ctrl->status & ST_FATAL) return;
   const uint32_t nb = hdr->nb;
@@ -924,6 +940,7 @@ static __global__ void __launch_bounds__(1024)
     k_reqmap(const uint32_t *__restrict__ counts_g, const Ctrl *ctrl, const Req *__restrict__ reqs,
              uint32_t num_req, uint32_t *__restrict__ req_bucket,
              uint32_t *__restrict__ req_local, uint32_t *bits, uint32_t *bcount) {
+  pdl_start();
   extern __shared__ uint4 smem_raw[];
   uint32_t *excl = reinterpret_cast<uint32_t *>(smem_raw);
   __shared__ uint32_t s_w[33];
@@ -968,6 +985,7 @@ static __global__ void __launch_bounds__(1024)
                const uint32_t *__restrict__ req_bucket, const uint32_t *__restrict__ req_local,
                const uint32_t *__restrict__ bslot, const uint32_t *__restrict__ kstart,
                uint32_t *kcur, Req *__restrict__ klist) {
+  pdl_start();
   if (ctrl->status & ST_FATAL) return;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < num_req;
@@ -995,6 +1013,7 @@ constexpr int kColpThreads = 128;
 static __global__ void __launch_bounds__(kColpThreads)
     k_colprefix(uint32_t *partials, uint32_t rows, uint32_t nb_max, const Ctrl *ctrl,
                 const uint32_t *__restrict__ seg_bucket, const uint32_t *__restrict__ seg_size) {
+  pdl_start();
   if (ctrl->status & ST_FATAL) return;
   const uint32_t num_slots = ctrl->num_slots;
   const uint32_t lane = threadIdx.x & 31;
@@ -1083,6 +1102,7 @@ __global__ void __launch_bounds__(1024, 1)
            typename Traits<InT>::K *__restrict__ seg_hi, uint32_t *__restrict__ req_bucket,
            uint32_t *__restrict__ req_local, Req *__restrict__ klist, uint64_t surv_cap,
            Premap pm) {
+  pdl_start();
   using K = typename Traits<InT>::K;
   extern __shared__ uint4 smem_raw[];
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
@@ -1414,6 +1434,7 @@ __global__ void __launch_bounds__(1024, 1)
               const uint32_t *__restrict__ prefix, const uint32_t *__restrict__ counts,
               uint32_t nb_max,
               typename Traits<T>::K *__restrict__ surv, uint64_t surv_cap, Ctrl *ctrl) {
+  pdl_start();
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
@@ -1828,6 +1849,7 @@ __global__ void __launch_bounds__(kFinThreads)
              const K *__restrict__ seg_hi, const uint32_t *__restrict__ kstart,
              const uint32_t *__restrict__ kcnt, const Req *__restrict__ klist,
              uint32_t *__restrict__ deferred, uint32_t bcap, OutT *__restrict__ out) {
+  pdl_start();
   extern __shared__ uint4 smem_raw[];
   if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
   const uint32_t num_slots = ctrl->num_slots;

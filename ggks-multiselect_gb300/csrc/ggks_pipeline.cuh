@@ -133,6 +133,26 @@ static void set_smem_max(int bytes) {
   (void)done;
 }
 
+// Launches a pipeline kernel with programmatic stream serialization: it may be
+// scheduled while the previous kernel in the stream still runs, and waits for
+// that kernel in its own first instructions (pdl_start).  The arguments are
+// converted to the kernel's parameter types.
+template <class... P, class... A>
+static cudaError_t launch(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                          A &&...args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
+
 struct PassTimer {
   Context &ctx;
   cudaStream_t s;
@@ -216,16 +236,20 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   if (e != cudaSuccess) return from_cuda(e);
   const Req *rq = src.d_reqs ? src.d_reqs : reqs;
   bool ran[GGKS_NUM_PASSES] = {false, false, false, false, false, false};
+  cudaError_t le = cudaSuccess;  // the first failed launch
+  auto L = [&le](cudaError_t r) {
+    if (le == cudaSuccess) le = r;
+  };
   if (src.topk) {
-    k_make_topk_reqs<<<(num_req + 255) / 256, 256, 0, s>>>(reqs, n, num_req);
+    L(launch(k_make_topk_reqs, (num_req + 255) / 256, 256, 0, s, reqs, n, num_req));
     ctx.stats.launches++;
   }
 
   // ---- (b) sample + splitter table
   {
     PassTimer t(ctx, s, GGKS_PASS_SAMPLE);
-    k_sample_lut<InT><<<p.sample_grid, 1024, 0, s>>>(ingest ? ingest : d_in, n, p.S, 0x5EEDu,
-                                                      samples, ctrl, hdr, lut, p.nb_max);
+    L(launch(k_sample_lut<InT>, p.sample_grid, 1024, 0, s, ingest ? ingest : d_in, n, p.S, 0x5EEDu,
+             samples, ctrl, hdr, lut, p.nb_max));
     ran[GGKS_PASS_SAMPLE] = true;
   }
   // ---- (c) histogram
@@ -234,15 +258,15 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     set_smem_max<k_hist<InT, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
     PassTimer t(ctx, s, GGKS_PASS_HIST);
     // with a mapped host vector, this pass also writes the device copy d_in
-    k_hist<InT, UNROLL><<<p.G, 1024, smem, s>>>(ingest ? ingest : d_in, n, hdr, lut, partials,
-                                                p.nb_max, ctrl,
-                                                ingest ? const_cast<InT *>(d_in) : nullptr);
+    L(launch(k_hist<InT, UNROLL>, p.G, 1024, smem, s, ingest ? ingest : d_in, n, hdr, lut, partials,
+             p.nb_max, ctrl, ingest ? const_cast<InT *>(d_in) : nullptr));
     ran[GGKS_PASS_HIST] = true;
   }
   // ---- (d) reduce + decoupled look-back scan
   {
     PassTimer t(ctx, s, GGKS_PASS_SCAN);
-    k_colsum<K><<<p.scan_tiles, kScanThreads, 0, s>>>(partials, p.G, p.nb_max, hdr, counts, ctrl);
+    L(launch(k_colsum<K>, p.scan_tiles, kScanThreads, 0, s, partials, p.G, p.nb_max, hdr, counts,
+             ctrl));
     ran[GGKS_PASS_SCAN] = true;
   }
   // ---- (e) plan
@@ -263,24 +287,23 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       e = cudaMemsetAsync(pm_bits, 0, (size_t)p.nb_max / 8 + (size_t)p.nb_max * 4, s);
       if (e != cudaSuccess) return from_cuda(e);
       set_smem_max<k_reqmap>((int)(kMaxNb * 4));
-      k_reqmap<<<(num_req + kReqmapPerCta - 1) / kReqmapPerCta, 1024, p.nb_max * 4, s>>>(
-          counts, ctrl, rq, num_req, req_bucket, req_local, pm_bits, pm_bcount);
+      L(launch(k_reqmap, (num_req + kReqmapPerCta - 1) / kReqmapPerCta, 1024, p.nb_max * 4, s,
+               counts, ctrl, rq, num_req, req_bucket, req_local, pm_bits, pm_bcount));
       pm.bits = pm_bits;
       pm.bcount = pm_bcount;
       pm.bslot = pm_bslot;
     }
-    k_plan<InT, OutT><<<1, 1024, smem, s>>>(hdr, lut, counts, n, rq, num_req, p.nb_max, ctrl,
-                                             seg_bucket, seg_off,
-                                             seg_size, kstart, kcnt, kcur, seg_lo, seg_hi,
-                                             req_bucket, req_local, klist, p.surv_cap, pm);
+    L(launch(k_plan<InT, OutT>, 1, 1024, smem, s, hdr, lut, counts, n, rq, num_req, p.nb_max, ctrl,
+             seg_bucket, seg_off, seg_size, kstart, kcnt, kcur, seg_lo, seg_hi, req_bucket,
+             req_local, klist, p.surv_cap, pm));
     if (premap) {
-      k_reqplace<<<(num_req + 1023) / 1024, 1024, 0, s>>>(ctrl, rq, num_req, req_bucket, req_local,
-                                                          pm_bslot, kstart, kcur, klist);
+      L(launch(k_reqplace, (num_req + 1023) / 1024, 1024, 0, s, ctrl, rq, num_req, req_bucket,
+               req_local, pm_bslot, kstart, kcur, klist));
       ctx.stats.launches += 2;
     }
     // the slot buckets' columns of the histogram rows become prefixes
-    k_colprefix<<<p.colp_grid, kColpThreads, 0, s>>>(partials, p.G, p.nb_max, ctrl, seg_bucket,
-                                                      seg_size);
+    L(launch(k_colprefix, p.colp_grid, kColpThreads, 0, s, partials, p.G, p.nb_max, ctrl,
+             seg_bucket, seg_size));
     ctx.stats.launches++;
     ran[GGKS_PASS_PLAN] = true;
   }
@@ -290,23 +313,21 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 4);
       set_smem_max<k_compact<InT, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
       PassTimer t(ctx, s, GGKS_PASS_COMPACT);
-      k_compact<InT, UNROLL><<<p.G, 1024, smem, s>>>(d_in, n, hdr, lut, seg_bucket, seg_off, seg_size,
-                                                     partials, counts, p.nb_max, surv, surv_cap,
-                                                     ctrl);
+      L(launch(k_compact<InT, UNROLL>, p.G, 1024, smem, s, d_in, n, hdr, lut, seg_bucket, seg_off,
+               seg_size, partials, counts, p.nb_max, surv, surv_cap, ctrl));
       ran[GGKS_PASS_COMPACT] = true;
     }
     {
       const int smem = finish_smem_bytes<InT>();
       set_smem_max<k_finish<K, OutT>>(smem);
       PassTimer t(ctx, s, GGKS_PASS_FINISH);
-      k_finish<K, OutT><<<p.fin_grid, kFinThreads, smem, s>>>(surv, ctrl, seg_off, seg_size, seg_lo,
-                                                              seg_hi, kstart, kcnt, klist, deferred,
-                                                              p.cap_keys, d_out);
+      L(launch(k_finish<K, OutT>, p.fin_grid, kFinThreads, smem, s, surv, ctrl, seg_off, seg_size,
+               seg_lo, seg_hi, kstart, kcnt, klist, deferred, p.cap_keys, d_out));
       ran[GGKS_PASS_FINISH] = true;
     }
   };
   launch_tail();
-  e = cudaGetLastError();
+  e = le != cudaSuccess ? le : cudaGetLastError();
   if (e != cudaSuccess) return from_cuda(e);
 
   // results and control block come back in one copy when the output is ours
@@ -341,6 +362,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       if (e != cudaSuccess) return from_cuda(e);
       for (int i = 0; i < GGKS_NUM_PASSES; ++i) ran[i] = false;
       launch_tail();
+      if (le != cudaSuccess) return from_cuda(le);
       e = pull(want_host);
       if (e != cudaSuccess) return from_cuda(e);
       collect_pass_times(ctx, ran);
