@@ -95,7 +95,7 @@ static cudaError_t grow(void **p, size_t *have, size_t need, bool zero) {
 }
 
 cudaError_t ensure_arena(Context &ctx, size_t bytes) {
-  // the arena's head holds state that must start zeroed (look-back flags)
+  // the arena's head holds state that must start zeroed (slice counts)
   if (bytes <= ctx.arena_bytes && ctx.arena) return cudaSuccess;
   cudaError_t e = cudaStreamSynchronize(ctx.stream);
   if (e != cudaSuccess) return e;

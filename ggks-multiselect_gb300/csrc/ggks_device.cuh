@@ -100,8 +100,10 @@ struct Ctrl {
   uint32_t num_slots;
   uint64_t total_surv;
   uint32_t deferred_count;
-  uint32_t sample_done;  // last-CTA ticket of k_sample_lut (reset by that CTA)
-  uint32_t nb;           // buckets in use
+  uint32_t sample_done;    // last-CTA ticket of k_sample_lut (reset by that CTA)
+  uint32_t sample_arrive;  // k_sample_lut's grid barrier (arrivals)
+  uint32_t same_key;       // far-apart sample pairs holding one key (k_sample_lut)
+  uint32_t nb;             // buckets in use
   uint64_t cap_needed;
   uint64_t kmin_inv;     // ~(smallest sampled key), by atomicMax
   uint64_t kmax;         // largest sampled key, by atomicMax
@@ -423,7 +425,8 @@ __device__ __forceinline__ V block_reduce(V v, Op op, V *sh /* >= 32 */) {
 // CTAs (read past L1).
 template <class K, int SPT, bool SMEM>
 __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint32_t nb_max,
-                              uint32_t *lut, LutHeader<K> *hdr, int nsl_bits = kLutIdxBits) {
+                              uint32_t *lut, LutHeader<K> *hdr, int nsl_bits = kLutIdxBits,
+                              uint32_t *pre_cnt = nullptr, int64_t pre_same_key = -1) {
   __shared__ uint32_t cnt[kLutIdx];
   __shared__ uint32_t lch[36];  // [0, 33): slices by ceil(log2 c); [34]: empty-run starts
   __shared__ uint32_t red32[33];
@@ -436,13 +439,34 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
   const uint32_t shift = bl > nsl_bits ? (uint32_t)(bl - nsl_bits) : 0u;
   const int bcap = (int)(shift < (uint32_t)kMaxSubBits ? shift : (uint32_t)kMaxSubBits);
 
-  // --- sample counts per slice
-  for (uint32_t j = tid; j < kLutIdx; j += blockDim.x) cnt[j] = 0;
+  // --- sample counts per slice: counted by the caller (pre_cnt, global, left
+  // zero here for the next call), or from the samples
   if (tid < 36) lch[tid] = 0;
-  __syncthreads();
+  if (pre_cnt) {
+    for (uint32_t j0 = tid; j0 < kLutIdx; j0 += 4 * blockDim.x) {
+      uint32_t c4[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t j = j0 + u * blockDim.x;
+        c4[u] = j < kLutIdx ? __ldcg(pre_cnt + j) : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t j = j0 + u * blockDim.x;
+        if (j < kLutIdx) {
+          cnt[j] = c4[u];
+          pre_cnt[j] = 0;
+        }
+      }
+    }
+    __syncthreads();
+  } else {
+    for (uint32_t j = tid; j < kLutIdx; j += blockDim.x) cnt[j] = 0;
+    __syncthreads();
+  }
   // 16 loads per thread in flight before their atomics (loads and shared
   // atomics interleaved in one loop body complete one at a time)
-  for (uint32_t s0 = tid; s0 < S; s0 += 16 * blockDim.x) {
+  for (uint32_t s0 = tid; s0 < (pre_cnt ? 0u : S); s0 += 16 * blockDim.x) {
     K kk[16];
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
@@ -576,7 +600,9 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
     return (uint32_t)((int32_t)e >> 7) + shr_clamp(d, e & 127u);
   };
   auto ld = [&](uint32_t i) -> K { return SMEM ? samples[i] : __ldcg(samples + i); };
-  // four pairs of each kind per thread and step, all loads issued first
+  // four pairs of each kind per thread and step, all loads issued first (the
+  // far-apart pairs only when the caller has not counted them)
+  const bool far = pre_same_key < 0;
   for (uint32_t q0 = tid; q0 < npairs; q0 += 4 * blockDim.x) {
     K a[4], b[4], c[4], d2[4];
 #pragma unroll
@@ -585,8 +611,8 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
       const bool ok = q < npairs;
       a[u] = ok ? ld(2 * q) : K(0);
       b[u] = ok ? ld(2 * q + 1) : K(0);
-      c[u] = ok ? ld(q) : K(0);
-      d2[u] = ok ? ld(q + S / 2) : K(1);
+      c[u] = ok && far ? ld(q) : K(0);
+      d2[u] = ok && far ? ld(q + S / 2) : K(1);
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u)
@@ -596,7 +622,8 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
       }
   }
   same = block_reduce(same, [](uint32_t p, uint32_t q) { return p + q; }, red32);
-  same_key = block_reduce(same_key, [](uint32_t p, uint32_t q) { return p + q; }, red32);
+  same_key = far ? block_reduce(same_key, [](uint32_t p, uint32_t q) { return p + q; }, red32)
+                 : (uint32_t)pre_same_key;
   if (tid == 0) {
     const uint32_t nb = 1u + total + (top_run_start ? 1u : 0u);
     lut[nsl] = top;
@@ -614,39 +641,83 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
   }
 }
 
+// Cooperative launch (every CTA resident): each CTA gathers 1024 samples
+// (one per thread, kept in a register) and folds its min / max into Ctrl; a
+// grid barrier (bounded wait) publishes the sample's span; each CTA then bins
+// its own samples by slice in shared memory, adds its non-zero slice counts to
+// slice_cnt (global, zero on entry) and counts the far-apart pairs (q, q + S/2)
+// that hold one key; the last CTA to finish builds the table from slice_cnt
+// (leaving it zero) and reads back only the neighbouring samples its bucket
+// collision estimate needs.
 template <class T>
 __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, uint64_t n,
                                                      uint32_t S, uint32_t seed,
                                                      typename Traits<T>::K *samples,
                                                      Ctrl *ctrl,
                                                      LutHeader<typename Traits<T>::K> *hdr,
-                                                     uint32_t *lut, uint32_t nb_max) {
+                                                     uint32_t *lut, uint32_t nb_max,
+                                                     uint32_t *slice_cnt) {
   pdl_start();
   using K = typename Traits<T>::K;
   __shared__ K redk[33];
-  __shared__ uint32_t s_last;
+  __shared__ uint32_t red32[33];
+  __shared__ uint32_t s_last, s_timeout;
+  __shared__ uint32_t ccnt[kLutIdx];
 
   const uint32_t tid = threadIdx.x;
   const uint32_t i = blockIdx.x * blockDim.x + tid;
-  K mine_lo = KeyMax<K>::v, mine_hi = 0;
+  for (uint32_t j = tid; j < kLutIdx; j += blockDim.x) ccnt[j] = 0;
+  K k = 0, mine_lo = KeyMax<K>::v, mine_hi = 0;
   if (i < S) {
     uint64_t pos;
     if ((uint64_t)S >= n)
       pos = i;
     else
       pos = ((uint64_t)hash32(i * 0x9E3779B9u + seed) * n) >> 32;
-    const K k = Traits<T>::key(x[pos]);
+    k = Traits<T>::key(x[pos]);
     samples[i] = k;
     mine_lo = k;
     mine_hi = k;
   }
   mine_lo = block_reduce(mine_lo, [](K p, K q) { return p < q ? p : q; }, redk);
   mine_hi = block_reduce(mine_hi, [](K p, K q) { return p > q ? p : q; }, redk);
-  // block_reduce ended with a barrier: the CTA's sample stores happen before
-  // thread 0's fence, which orders them (cumulatively) before the ticket
+  // grid barrier: the CTA's sample stores and extremes before its arrival
   if (tid == 0) {
     atomicMax((unsigned long long *)&ctrl->kmin_inv, (unsigned long long)~(uint64_t)mine_lo);
     atomicMax((unsigned long long *)&ctrl->kmax, (unsigned long long)mine_hi);
+    __threadfence();
+    atomicAdd(&ctrl->sample_arrive, 1u);
+    uint32_t it = 0, to = 0;
+    while (ld_volatile_u32(&ctrl->sample_arrive) < gridDim.x) {
+      if (++it > (uint32_t)kSpinLimit) {
+        atomicOr(&ctrl->status, ST_TIMEOUT);
+        to = 1;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+    s_timeout = to;
+  }
+  __syncthreads();
+  if (s_timeout) return;
+
+  const K kmin = (K)~__ldcg((const unsigned long long *)&ctrl->kmin_inv);
+  const K kmax = (K)__ldcg((const unsigned long long *)&ctrl->kmax);
+  const int bl = bitlen<K>(kmax - kmin);
+  const uint32_t shift = bl > kLutIdxBits ? (uint32_t)(bl - kLutIdxBits) : 0u;
+  if (i < S) atomicAdd(&ccnt[(uint32_t)((k - kmin) >> shift)], 1u);
+  // far-apart pairs (q, q + S/2): does the vector hold many copies of a key
+  const uint32_t npairs = S / 2 < 4096u ? S / 2 : 4096u;
+  uint32_t sk = 0;
+  if (i < npairs) sk = __ldcg(samples + i + S / 2) == k ? 1u : 0u;
+  sk = block_reduce(sk, [](uint32_t p, uint32_t q) { return p + q; }, red32);
+  for (uint32_t j = tid; j < kLutIdx; j += blockDim.x) {
+    const uint32_t c = ccnt[j];
+    if (c) atomicAdd(&slice_cnt[j], c);
+  }
+  if (tid == 0) {
+    if (sk) atomicAdd(&ctrl->same_key, sk);
     __threadfence();
     s_last = (atomicAdd(&ctrl->sample_done, 1u) == gridDim.x - 1) ? 1u : 0u;
     if (s_last) __threadfence();
@@ -654,12 +725,12 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
   __syncthreads();
   if (!s_last) return;
 
-  const K kmin = (K)~__ldcg((const unsigned long long *)&ctrl->kmin_inv);
-  const K kmax = (K)__ldcg((const unsigned long long *)&ctrl->kmax);
-  build_lut_cta<K, 4, false>(samples, S, kmin, kmax, nb_max, lut, hdr);
+  build_lut_cta<K, 4, false>(samples, S, kmin, kmax, nb_max, lut, hdr, kLutIdxBits, slice_cnt,
+                             (int64_t)__ldcg(&ctrl->same_key));
   if (tid == 0) {
     ctrl->nb = hdr->nb;
     ctrl->sample_done = 0;  // re-arm for the next call on this workspace
+    ctrl->sample_arrive = 0;
   }
 }
 

@@ -32,7 +32,7 @@ struct Context {
   cudaStream_t stream = nullptr;
   std::mutex mu;
 
-  char *arena = nullptr;  // [out | ctrl | reqs | ... ]
+  char *arena = nullptr;  // [slice counts | out | ctrl | reqs | ... ]
   size_t arena_bytes = 0;
   void *surv = nullptr;
   size_t surv_bytes = 0;
@@ -78,7 +78,9 @@ cudaError_t ensure_surv(Context &ctx, size_t bytes);
 cudaError_t ensure_dvec(Context &ctx, size_t bytes);
 cudaError_t ensure_pin(Context &ctx, size_t bytes);
 
-// fixed-offset persistent state at the start of the arena
+// fixed-offset persistent state at the start of the arena: k_sample_lut's
+// per-slice sample counts, zero between calls
+constexpr size_t kSliceCntBytes = kLutIdx * sizeof(uint32_t);
 
 // Where the requests of one selection come from.
 struct ReqSource {

@@ -35,9 +35,11 @@ constexpr uint32_t kNaMaxG = 64;     // histogram / compaction CTAs
 constexpr uint32_t kNaS = 65536;     // sample size
 
 constexpr size_t na_align(size_t v) { return (v + 255) / 256 * 256; }
-// scratch layout (byte offsets)
+// scratch layout (byte offsets); the control block and the slice counts are
+// zeroed together at the start of each call
 constexpr size_t kNaCtrl = 0;
-constexpr size_t kNaReqs = na_align(kNaCtrl + sizeof(Ctrl));
+constexpr size_t kNaSliceCnt = na_align(kNaCtrl + sizeof(Ctrl));
+constexpr size_t kNaReqs = na_align(kNaSliceCnt + kSliceCntBytes);
 constexpr size_t kNaHdr = na_align(kNaReqs + kNaMaxK * sizeof(Req));
 constexpr size_t kNaLut = na_align(kNaHdr + sizeof(LutHeader<uint32_t>));
 constexpr size_t kNaSamples = na_align(kNaLut + kLutPadded * sizeof(uint32_t));
@@ -149,12 +151,14 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
   const uint32_t fg = 5u * (uint32_t)sms;
   const uint32_t fin_grid = num_k < fg ? num_k : fg;
 
-  // the control block starts at zero
-  e = cudaMemsetAsync(A + kNaCtrl, 0, sizeof(Ctrl), s);
+  // the control block and the slice counts start at zero
+  e = cudaMemsetAsync(A + kNaCtrl, 0, kNaSliceCnt + kSliceCntBytes, s);
   if (e != cudaSuccess) return from_cuda(e);
   k_na_reqs<<<(num_k + 255) / 256, 256, 0, s>>>(d_k, num_k, n, reqs, ctrl);
-  k_sample_lut<float><<<(S + 1023) / 1024, 1024, 0, s>>>(d_vec, n, S, 0x5EEDu, samples, ctrl, hdr,
-                                                          lut, kNaNbMax);
+  e = launch_cooperative(k_sample_lut<float>, (S + 1023) / 1024, 1024, 0, s, d_vec, n, S, 0x5EEDu,
+                         samples, ctrl, hdr, lut, kNaNbMax,
+                         reinterpret_cast<uint32_t *>(A + kNaSliceCnt));
+  if (e != cudaSuccess) return from_cuda(e);
   {
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kNaNbMax * 4);
     set_smem_max<k_hist<float, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));

@@ -80,7 +80,9 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   if (p.surv_cap > n) p.surv_cap = n;
 
   const size_t A = 256;
-  size_t o = 0;
+  // the arena's head: per-slice sample counts of k_sample_lut, zero between
+  // calls (the arena starts zeroed; every call leaves them zero)
+  size_t o = kSliceCntBytes;
   p.out = o;
   o = align_up(o + (size_t)num_req * sizeof(OutT), A);
   p.ctrl = o;
@@ -153,6 +155,24 @@ static cudaError_t launch(void (*kern)(P...), dim3 grid, dim3 block, size_t smem
   return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
 }
 
+// Cooperative launch: every CTA of the grid is resident at once (a kernel
+// with a grid barrier).
+template <class... P, class... A>
+static cudaError_t launch_cooperative(void (*kern)(P...), dim3 grid, dim3 block, size_t smem,
+                                      cudaStream_t s, A &&...args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
+
 struct PassTimer {
   Context &ctx;
   cudaStream_t s;
@@ -195,6 +215,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   LutHeader<K> *hdr = reinterpret_cast<LutHeader<K> *>(A + p.hdr);
   uint32_t *lut = reinterpret_cast<uint32_t *>(A + p.lut);
   K *samples = reinterpret_cast<K *>(A + p.samples);
+  uint32_t *slice_cnt = reinterpret_cast<uint32_t *>(A);
   uint32_t *partials = reinterpret_cast<uint32_t *>(A + p.partials);
   uint32_t *counts = reinterpret_cast<uint32_t *>(A + p.counts);
   uint32_t *seg_bucket = reinterpret_cast<uint32_t *>(A + p.seg_bucket);
@@ -248,8 +269,8 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   // ---- (b) sample + splitter table
   {
     PassTimer t(ctx, s, GGKS_PASS_SAMPLE);
-    L(launch(k_sample_lut<InT>, p.sample_grid, 1024, 0, s, ingest ? ingest : d_in, n, p.S, 0x5EEDu,
-             samples, ctrl, hdr, lut, p.nb_max));
+    L(launch_cooperative(k_sample_lut<InT>, p.sample_grid, 1024, 0, s, ingest ? ingest : d_in, n,
+                         p.S, 0x5EEDu, samples, ctrl, hdr, lut, p.nb_max, slice_cnt));
     ran[GGKS_PASS_SAMPLE] = true;
   }
   // ---- (c) histogram
@@ -349,7 +370,12 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
 
   for (int round = 0; round < 4; ++round) {
     const Ctrl c = *h_ctrl;
-    if (c.status & ST_FATAL) return (c.status & ST_TIMEOUT) ? GGKS_TIMEOUT : GGKS_INTERNAL;
+    if (c.status & ST_FATAL) {
+      // a stopped call may leave slice counts behind
+      cudaMemsetAsync(slice_cnt, 0, kSliceCntBytes, s);
+      cudaStreamSynchronize(s);
+      return (c.status & ST_TIMEOUT) ? GGKS_TIMEOUT : GGKS_INTERNAL;
+    }
     if (c.status & ST_OVERFLOW) {
       // survivors did not fit: grow the buffer, re-run compaction + finish
       const uint64_t need = c.cap_needed + (c.cap_needed >> 3);
