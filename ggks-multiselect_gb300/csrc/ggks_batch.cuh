@@ -41,6 +41,7 @@ constexpr int kBSpt = (int)kLutIdx / kBThreads;  // slices per thread in the tab
 constexpr uint32_t kBMaxNb = 8192;               // bucket budget of one problem
 constexpr uint32_t kBMaxS = 8192;                // samples of one problem (shared memory)
 constexpr int kBPhases = 5;
+constexpr int kBColBatch = 4;  // tile rows per lane and load step of the plan phase's single-key scan
 constexpr uint32_t kBWarpBytes = 2048;  // shared memory of one warp-finisher buffer
 constexpr uint32_t kBRepBytes = 32768;  // per-bucket first keys of a tile (dup problems)
 constexpr uint32_t kMixed = 0x80000000u;  // tile row: the bucket holds more than one key
@@ -112,6 +113,7 @@ struct BArgs {
   const Req *reqs;  // rank within the problem, output position in out[]
   uint32_t *req_bucket, *req_local;
   uint32_t *seg_bucket, *seg_size, *kstart, *kcnt, *kcur;
+  uint32_t *fill;  // per slot: survivor positions handed out to tiles (phase 4)
   uint64_t *seg_off;
   void *seg_lo, *seg_hi;  // key arrays
   Req *klist;
@@ -407,6 +409,8 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       h.pad[0] = h.pad[1] = h.pad[2] = 0;
       A.hdrs[p] = h;
     }
+    // the bucket totals start at zero: the tiles of phase 2 add to them
+    for (uint32_t b = tid; b < P.nb_max; b += nt) A.counts[P.cnt_off + b] = 0;
   }
   uint32_t st = grid_barrier(ctrl, &s_status, 1);
 
@@ -471,8 +475,12 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       __syncthreads();
       const uint64_t ro = P.row0 + (uint64_t)tl.rank * P.nb_max;
       if (!BCHECK(ro + H.nb <= A.row_words && H.nb <= P.nb_max, 5, ro, H.nb)) continue;
+      // the tile's row, and its counts added to the problem's bucket totals
+      uint32_t *tot = A.counts + P.cnt_off;
       for (uint32_t b = tid; b < H.nb; b += nt) {
-        A.rows[ro + b] = hist[swz(b)];
+        const uint32_t c = hist[swz(b)];
+        A.rows[ro + b] = c;
+        if (c & ~kMixed) atomicAdd(tot + b, c & ~kMixed);
         if (H.dup) reps[ro + b] = rep[swz(b)];
       }
     }
@@ -494,79 +502,15 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
                   6, p, nb))
         continue;
       for (uint32_t j = tid; j <= nsl; j += nt) lut[j] = __ldcg(A.luts + P.lut_off + j);
-      // each column of the rows becomes its exclusive prefix over the tiles
-      // (tile 0's prefix is 0 and is not stored: phase 4 knows it); a warp
-      // covers 32 neighbouring buckets of a row, a thread four buckets at a
-      // time so that their loads overlap.  Dup problems also learn which
-      // buckets hold a single key in every tile: those become flat slots
-      // (flag bit 1; the key goes to tile 0's key row).
-      for (uint32_t b0 = tid; b0 < nb; b0 += 4 * nt) {
-        uint32_t run[4] = {0, 0, 0, 0};
-        bool one[4];
-        K key0[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          one[u] = H.dup != 0;
-          key0[u] = KeyMax<K>::v;
-        }
-        for (uint32_t r = 0; r < nr; ++r) {
-          uint32_t *row = A.rows + P.row0 + (uint64_t)r * P.nb_max;
-          uint32_t v[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const uint32_t b = b0 + u * nt;
-            v[u] = b < nb ? __ldcg(row + b) : 0u;
-          }
-          if (H.dup) {
-            K rr[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const uint32_t b = b0 + u * nt;
-              rr[u] = (b < nb && (v[u] & ~kMixed)) ? ldcg_u(reps + P.row0 + (uint64_t)r * P.nb_max + b)
-                                                   : KeyMax<K>::v;
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              if (v[u] & kMixed) one[u] = false;
-              if (v[u] & ~kMixed) {
-                if (key0[u] == KeyMax<K>::v) key0[u] = rr[u];
-                one[u] = one[u] && rr[u] == key0[u];
-              }
-            }
-          }
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const uint32_t b = b0 + u * nt;
-            if (b < nb && r > 0) row[b] = run[u];
-            run[u] += v[u] & ~kMixed;
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const uint32_t b = b0 + u * nt;
-          if (b >= nb) continue;
-          const bool o = one[u] && run[u] > 0 && key0[u] != KeyMax<K>::v;
-          if (o) reps[P.row0 + b] = key0[u];
-          cnt[b] = run[u];
-          excl[b] = run[u];  // the count, until the scan below
-          flag[b] = o ? 2 : 0;
-        }
-      }
+      // bucket totals (added by the tiles of phase 2) -> exclusive prefix in
+      // shared memory; the flags start clear
+      load_totals(cnt, nb, excl);
+      for (uint32_t v = tid; v < ((nb + 3) >> 2); v += nt) reinterpret_cast<uint32_t *>(flag)[v] = 0;
       __syncthreads();
-      // bucket prefix: contiguous bucket range per thread
+      if (smem_excl_scan(excl, nb, red32) != P.n && tid == 0) atomicOr(&ctrl->status, ST_INTERNAL);
+      // contiguous bucket range per thread (slot numbering below)
       const uint32_t per = (nb + nt - 1) / nt;
       const uint32_t b0 = min(nb, tid * per), b1 = min(nb, b0 + per);
-      uint32_t mysum = 0;
-      for (uint32_t b = b0; b < b1; ++b) mysum += excl[b];
-      uint32_t tot;
-      uint32_t run = block_incl_scan(mysum, &tot, red32) - mysum;
-      for (uint32_t b = b0; b < b1; ++b) {
-        const uint32_t c = excl[b];
-        excl[b] = run;
-        run += c;
-      }
-      if (tid == 0 && (uint64_t)tot != P.n) atomicOr(&ctrl->status, ST_INTERNAL);
-      __syncthreads();
       // requests -> bucket (the last b with excl[b] <= rank) and local rank
       const Req *rq = A.reqs + P.req_off;
       for (uint32_t i = tid; i < P.num_req; i += nt) {
@@ -598,6 +542,59 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
           }
       }
       __syncthreads();
+      // Dup problems learn which slot buckets hold one and the same key in
+      // every tile: those become flat slots (flag bit 1; the key goes to tile
+      // 0's key row).  A warp per slot, its lanes over the tiles, kBColBatch
+      // loads per lane in flight.
+      if (H.dup) {
+        const uint32_t lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+        for (uint32_t q = warp; q < tot_slots; q += nwarps) {
+          const uint32_t b = __ldcg(A.seg_bucket + P.req_off + q);
+          const uint32_t *col = A.rows + P.row0 + b;
+          const K *rcol = reps + P.row0 + b;
+          bool mixed = false, any = false;
+          K kmin = KeyMax<K>::v, kmax = 0;
+          for (uint32_t r0 = 0; r0 < nr; r0 += 32 * kBColBatch) {
+            uint32_t v[kBColBatch];
+#pragma unroll
+            for (int j = 0; j < kBColBatch; ++j) {
+              const uint32_t r = r0 + j * 32 + lane;
+              v[j] = r < nr ? __ldcg(col + (uint64_t)r * P.nb_max) : 0u;
+            }
+            K rr[kBColBatch];
+#pragma unroll
+            for (int j = 0; j < kBColBatch; ++j) {
+              const uint32_t r = r0 + j * 32 + lane;
+              rr[j] = (r < nr && (v[j] & ~kMixed)) ? ldcg_u(rcol + (uint64_t)r * P.nb_max)
+                                                    : KeyMax<K>::v;
+            }
+#pragma unroll
+            for (int j = 0; j < kBColBatch; ++j) {
+              mixed |= (v[j] & kMixed) != 0;
+              if (v[j] & ~kMixed) {
+                any = true;
+                kmin = rr[j] < kmin ? rr[j] : kmin;
+                kmax = rr[j] > kmax ? rr[j] : kmax;
+              }
+            }
+          }
+          mixed = __any_sync(0xffffffffu, mixed);
+          any = __any_sync(0xffffffffu, any);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            const K a2 = __shfl_xor_sync(0xffffffffu, kmin, o);
+            const K z2 = __shfl_xor_sync(0xffffffffu, kmax, o);
+            kmin = a2 < kmin ? a2 : kmin;
+            kmax = z2 > kmax ? z2 : kmax;
+          }
+          // one key in every tile that saw the bucket, no tile with two
+          if (lane == 0 && any && !mixed && kmin == kmax && kmin != KeyMax<K>::v) {
+            flag[b] |= 2;
+            reps[P.row0 + b] = kmin;
+          }
+        }
+        __syncthreads();
+      }
       // key range, flat test and survivor count of each slot
       const uint32_t sper = (tot_slots + nt - 1) / nt;
       const uint32_t s0 = min(tot_slots, tid * sper), s1 = min(tot_slots, s0 + sper);
@@ -620,6 +617,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         seg_hi[g] = single ? klo : (knext > klo ? knext - K(1) : KeyMax<K>::v);
         A.kcnt[g] = 0;
         A.kcur[g] = 0;
+        A.fill[g] = 0;
         my_surv += cb;
       }
       uint64_t tot_surv;
@@ -735,15 +733,22 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       for (uint32_t b = tid; b < ((H.nb + 31) & ~31u); b += nt) cursor[b] = kInactive;
       __syncthreads();
       if (tid == 0) s_cur = tl.prob;
-      const uint32_t *row = A.rows + P.row0 + (uint64_t)tl.rank * P.nb_max;
-      // positions relative to the problem's survivor range (flat slots have none)
+      uint32_t *row = A.rows + P.row0 + (uint64_t)tl.rank * P.nb_max;
+      // Positions relative to the problem's survivor range (flat slots have
+      // none): the tile takes its share of each slot's segment with one
+      // atomic on the slot's fill counter (tiles take their shares in any
+      // order; the order of a segment's keys does not matter), and leaves the
+      // end of its share in its row for the check below.
       for (uint32_t s = tid; s < H.num_slots; s += nt) {
         const uint32_t g = P.req_off + s;
         if (__ldcg(A.seg_size + g) == 0) continue;
         const uint32_t b = __ldcg(A.seg_bucket + g);
         if (!BCHECK(b < H.nb && s < P.num_req, 10, b, s)) continue;
-        const uint32_t pre = tl.rank ? __ldcg(row + b) : 0u;  // tile 0 starts each bucket
-        cursor[swz(b)] = (uint32_t)(ldcg_u(A.seg_off + g) - H.surv_off + pre);
+        const uint32_t c = __ldcg(row + b) & ~kMixed;
+        const uint32_t pre = c ? atomicAdd(A.fill + g, c) : 0u;
+        const uint32_t at = (uint32_t)(ldcg_u(A.seg_off + g) - H.surv_off + pre);
+        cursor[swz(b)] = at;
+        row[b] = at + c;
       }
       __syncthreads();
       K *sp = surv + H.surv_off;
@@ -760,15 +765,12 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         st_global_if(sp + pos, k, pos < cap);
       });
       __syncthreads();
-      // each cursor must end where the next tile's range of the bucket starts
+      // each cursor must end where the tile's share of the segment ends
       for (uint32_t s = tid; s < H.num_slots; s += nt) {
         const uint32_t g = P.req_off + s;
         if (__ldcg(A.seg_size + g) == 0) continue;
         const uint32_t b = __ldcg(A.seg_bucket + g);
-        const uint32_t nxt = tl.rank + 1 < P.ntiles ? __ldcg(row + P.nb_max + b)
-                                                     : __ldcg(A.counts + P.cnt_off + b);
-        const uint32_t end = (uint32_t)(ldcg_u(A.seg_off + g) - H.surv_off + nxt);
-        if (cursor[swz(b)] != end) s_bad = true;
+        if (cursor[swz(b)] != __ldcg(row + b)) s_bad = true;
       }
     }
     __syncthreads();

@@ -112,7 +112,7 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   const size_t o_counts = arr(cnt_words, 4);
   const size_t o_req_bucket = arr(R, 4), o_req_local = arr(R, 4);
   const size_t o_seg_bucket = arr(R, 4), o_seg_size = arr(R, 4), o_kstart = arr(R, 4),
-               o_kcnt = arr(R, 4), o_kcur = arr(R, 4);
+               o_kcnt = arr(R, 4), o_kcur = arr(R, 4), o_fill = arr(R, 4);
   const size_t o_seg_off = arr(R, 8), o_seg_lo = arr(R, sizeof(K)), o_seg_hi = arr(R, sizeof(K));
   const size_t o_klist = arr(R, sizeof(Req)), o_deferred = arr(R, 4);
   const size_t o_big = arr(R, 4), o_small = arr(R, 4);
@@ -177,6 +177,7 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   a.kstart = reinterpret_cast<uint32_t *>(D + o_kstart);
   a.kcnt = reinterpret_cast<uint32_t *>(D + o_kcnt);
   a.kcur = reinterpret_cast<uint32_t *>(D + o_kcur);
+  a.fill = reinterpret_cast<uint32_t *>(D + o_fill);
   a.seg_off = reinterpret_cast<uint64_t *>(D + o_seg_off);
   a.seg_lo = D + o_seg_lo;
   a.seg_hi = D + o_seg_hi;

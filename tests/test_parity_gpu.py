@@ -141,7 +141,8 @@ def test_duplicate_and_unsorted_ks(g, orc):
 
 
 def test_repeated_calls_one_context(g, orc):
-    """Device state (look-back flags, tickets) re-arms between calls."""
+    """Device state (per-slice sample counts at the workspace head, grid-barrier
+    counters, tickets) re-arms between calls of different shapes."""
     import ggks_problems as gp
     ctx = g.Context(0)
     prev = None
