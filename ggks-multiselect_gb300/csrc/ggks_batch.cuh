@@ -41,6 +41,7 @@ constexpr int kBSpt = (int)kLutIdx / kBThreads;  // slices per thread in the tab
 constexpr uint32_t kBMaxNb = 8192;               // bucket budget of one problem
 constexpr uint32_t kBMaxS = 8192;                // samples of one problem (shared memory)
 constexpr int kBPhases = 5;
+constexpr uint64_t kBMinTile = 1u << 16;  // smallest tile the host picks for a small batch
 constexpr int kBColBatch = 4;  // tile rows per lane and load step of the plan phase's single-key scan
 constexpr uint32_t kBWarpBytes = 2048;  // shared memory of one warp-finisher buffer
 constexpr uint32_t kBRepBytes = 32768;  // per-bucket first keys of a tile (dup problems)

@@ -38,13 +38,37 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   const uint32_t bcap = sizeof(K) == 4 ? 4096u : 2048u;
   const uint32_t R = in.k_off[in.num_problems];
 
-  // ---- plan: problems with requests, their bucket budgets and tiles
+  // co-resident grid: every CTA the SMs hold at once
+  const int smem = batch_smem_bytes<T>();
+  static int blocks_per_sm = -1;  // per instantiation; one GPU model per process
+  if (blocks_per_sm < 0) {
+    cudaFuncSetAttribute((const void *)k_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    // two CTAs of about 100 KB each per SM: ask for the largest shared-memory carveout
+    cudaFuncSetAttribute((const void *)k_batch<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         100);
+    int b = 0;
+    const cudaError_t oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<T>, kBThreads,
+                                                                           smem);
+    if (oe != cudaSuccess) return from_cuda(oe);
+    blocks_per_sm = b;
+  }
+  if (blocks_per_sm < 1) return GGKS_UNSUPPORTED;
+  const uint32_t max_grid = (uint32_t)blocks_per_sm * (uint32_t)ctx.sm_count;
+
+  // ---- plan: problems with requests, their bucket budgets and tiles.  The
+  // tile size is the tuned one, or smaller when the batch holds fewer than
+  // two tiles per resident CTA of that size (a few large tiles would leave
+  // most CTAs idle in the streaming phases).
+  uint64_t total_n = 0;
+  for (uint32_t p = 0; p < in.num_problems; ++p)
+    if (in.k_off[p + 1] > in.k_off[p]) total_n += in.n[p];
+  uint64_t tile = std::max<uint64_t>(64, tune.tile & ~63ull);
+  while (tile > kBMinTile && total_n / tile < 2ull * max_grid) tile >>= 1;
   std::vector<BProb> probs;
   std::vector<uint32_t> orig;  // problem index in the caller's arrays
   probs.reserve(in.num_problems);
   uint64_t lut_words = 0, cnt_words = 0, row_words = 0, surv_est = 0;
   uint32_t num_tiles = 0;
-  const uint64_t tile = std::max<uint64_t>(64, tune.tile & ~63ull);
   for (uint32_t p = 0; p < in.num_problems; ++p) {
     const uint32_t nr = in.k_off[p + 1] - in.k_off[p];
     if (nr == 0) continue;
@@ -188,23 +212,9 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   a.out = d_out;
   a.ctrl = ctrl;
 
-  // co-resident grid: every CTA the SMs hold at once
-  const int smem = batch_smem_bytes<T>();
-  static int blocks_per_sm = -1;  // per instantiation; one GPU model per process
-  if (blocks_per_sm < 0) {
-    cudaFuncSetAttribute((const void *)k_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    // two CTAs of about 100 KB each per SM: ask for the largest shared-memory carveout
-    cudaFuncSetAttribute((const void *)k_batch<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                         100);
-    int b = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<T>, kBThreads, smem);
-    if (e != cudaSuccess) return from_cuda(e);
-    blocks_per_sm = b;
-  }
-  if (blocks_per_sm < 1) return GGKS_UNSUPPORTED;
+
   // every CTA the SMs hold at once, or fewer when the batch has less work
   // (each grid barrier waits for every CTA)
-  const uint32_t max_grid = (uint32_t)blocks_per_sm * (uint32_t)ctx.sm_count;
   const uint32_t work = std::max(std::max(num_tiles, P), R / 8);
   const uint32_t grid = std::max(1u, std::min(max_grid, work));
   ctx.stats.batch_grid = grid;
