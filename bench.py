@@ -507,7 +507,7 @@ def run_batched(torch, ggks, gp, dev, sptr, count=4096):
 SERVE_RATES = (1000, 5000, 20000, 50000)
 
 
-def run_served(torch, ggks, gp, dev, sptr, per_rate=1500):
+def run_served(torch, ggks, gp, dev, sptr, per_rate=4000):
     """The served workload: Poisson arrivals at each rate of SERVE_RATES over
     a resident pool of mixed vectors (float32 : uint32 : float64 = 6 : 3 : 1,
     lengths log-uniform in [2^12, 2^26]); 70% multiselects with 8-1024 k's,

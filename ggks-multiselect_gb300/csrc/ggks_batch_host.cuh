@@ -220,6 +220,9 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   ctx.stats.batch_grid = grid;
 
   float ms_total = 0.f;
+  // the results come back with the control block (one synchronisation); a
+  // rerun or a deferred slot makes them stale and they are copied again
+  bool res_fresh = false;
   auto launch = [&]() -> cudaError_t {
     a.surv = ctx.surv;
     a.surv_cap = surv_cap;
@@ -237,6 +240,11 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
     if (r != cudaSuccess) return r;
     r = cudaMemcpyAsync(h_ctrl, ctrl, sizeof(BCtrl), cudaMemcpyDeviceToHost, s);
     if (r != cudaSuccess) return r;
+    if (h_out) {
+      r = cudaMemcpyAsync(h_res, d_out, out_bytes, cudaMemcpyDeviceToHost, s);
+      if (r != cudaSuccess) return r;
+      res_fresh = true;
+    }
     r = cudaStreamSynchronize(s);
     float ms = 0.f;
     if (r == cudaSuccess && cudaEventElapsedTime(&ms, ctx.bev0, ctx.bev1) == cudaSuccess)
@@ -277,6 +285,7 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
     if (c.status & ST_DEFERRED) {
       // slots whose needed bins exceed shared memory: select each again on
       // its survivor keys (recursively, single-vector path)
+      res_fresh = false;
       const uint32_t Dn = c.deferred_count;
       std::vector<uint32_t> dl(Dn);
       e = cudaMemcpyAsync(dl.data(), a.deferred, (size_t)Dn * 4, cudaMemcpyDeviceToHost, s);
@@ -306,9 +315,11 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
     break;
   }
   if (h_out) {
-    e = cudaMemcpyAsync(h_res, d_out, out_bytes, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return from_cuda(e);
+    if (!res_fresh) {
+      e = cudaMemcpyAsync(h_res, d_out, out_bytes, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) return from_cuda(e);
+    }
     std::memcpy(h_out, h_res, out_bytes);
   }
   if (kernel_ms) *kernel_ms = ms_total;
