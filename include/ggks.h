@@ -305,15 +305,16 @@ typedef struct ggks_stats {
  * phase is timed from the grid barrier before it to the one after it) */
 #define GGKS_BATCH_TABLE 0    /* samples + splitter table of every problem */
 #define GGKS_BATCH_HIST 1     /* histogram rows of every (problem, tile) */
-#define GGKS_BATCH_PLAN 2     /* per-problem scan, k -> bucket, slots */
+#define GGKS_BATCH_PLAN 2     /* per-problem bucket prefix, k -> bucket, slots */
 #define GGKS_BATCH_COMPACT 3  /* compaction of every (problem, tile) */
 #define GGKS_BATCH_FINISH 4   /* every slot's in-shared-memory selection */
 
 /* pass indices of ggks_stats.pass_* */
 #define GGKS_PASS_SAMPLE 0   /* sample + splitter table build */
 #define GGKS_PASS_HIST 1     /* bucket histogram over the input */
-#define GGKS_PASS_SCAN 2     /* bucket-count reduce + decoupled-lookback scan */
-#define GGKS_PASS_PLAN 3     /* k -> bucket marker, slot and request layout */
+#define GGKS_PASS_SCAN 2     /* bucket totals: column sums of the per-CTA rows */
+#define GGKS_PASS_PLAN 3     /* bucket prefix, k -> bucket marker, slot and request
+                                layout, per-CTA column prefixes of the slot buckets */
 #define GGKS_PASS_COMPACT 4  /* compaction of active-bucket elements */
 #define GGKS_PASS_FINISH 5   /* per-segment in-shared-memory selection */
 
