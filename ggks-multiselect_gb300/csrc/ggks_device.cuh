@@ -27,17 +27,15 @@
 //                 memory, maps every requested rank to its bucket and local
 //                 rank, answers ranks that fall in single-key buckets
 //                 directly, assigns compact slots to the active buckets and
-//                 groups the requests by slot; k_colprefix then turns the
-//                 active buckets' columns of the per-CTA rows into prefixes
-//                 over the CTAs.  Replaces the host walk of findKBuckets
+//                 groups the requests by slot.  Replaces the host walk of findKBuckets
 //                 (:87-111), the host reindex loop and reindexCounts
 //                 (:714-756).
 //   (f) compact   k_compact: second pass over the input with the same
-//                 CTA-to-tile assignment as (c); every CTA starts a private
-//                 shared-memory cursor per active bucket at its column prefix
-//                 from (e), so elements of active buckets land in their
-//                 segment of the survivor buffer with shared-memory atomics
-//                 only.
+//                 CTA-to-tile assignment as (c); every CTA takes its share of
+//                 each active bucket's segment with one global atomic and
+//                 starts a private shared-memory cursor there, so elements of
+//                 active buckets land in their segment of the survivor buffer
+//                 with shared-memory atomics only.
 //                 Replaces copyElements (:249-308) and reindexCounts
 //                 (:229-241).
 //   (g) finish    k_finish: per segment, an in-shared-memory sort of the
@@ -876,8 +874,8 @@ constexpr int kScanTile = kScanThreads / kScanGroups;     // buckets per CTA
 
 // Thread t handles bucket blockIdx.x * kScanTile + (t % kScanTile) over row
 // group t / kScanTile, so a warp reads 32 neighbouring buckets of one row (128
-// bytes).  The rows are read once; only the columns of the buckets that get a
-// slot become prefixes over the rows, later (k_colprefix).
+// bytes).  The rows are read once; compaction later takes each CTA's share of
+// a bucket's segment from its own row.
 template <class K>
 __global__ void __launch_bounds__(kScanThreads)
     k_colsum(const uint32_t *__restrict__ partials, uint32_t rows, uint32_t nb_max,
@@ -1075,43 +1073,6 @@ static __global__ void __launch_bounds__(1024)
   }
 }
 
-// Column b of the per-CTA histogram rows becomes its exclusive prefix over the
-// rows for every slot bucket with survivors: the compaction pass starts CTA
-// r's cursor for bucket b there.  One warp per slot, four warps per CTA: the
-// column accesses are scattered (one sector per row), so they are spread over
-// every SM; the other columns are never read again.
-constexpr int kColpThreads = 128;
-static __global__ void __launch_bounds__(kColpThreads)
-    k_colprefix(uint32_t *partials, uint32_t rows, uint32_t nb_max, const Ctrl *ctrl,
-                const uint32_t *__restrict__ seg_bucket, const uint32_t *__restrict__ seg_size) {
-  pdl_start();
-  if (ctrl->status & ST_FATAL) return;
-  const uint32_t num_slots = ctrl->num_slots;
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; slot < num_slots;
-       slot += warps) {
-    if (__ldcg(seg_size + slot) == 0) continue;  // flat slot: no survivors
-    uint32_t *col = partials + __ldcg(seg_bucket + slot);
-    uint32_t run = 0;
-    for (uint32_t r0 = 0; r0 < rows; r0 += 8 * 32) {
-      uint32_t v[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const uint32_t r = r0 + q * 32 + lane;
-        v[q] = r < rows ? __ldcg(col + (uint64_t)r * nb_max) : 0u;
-      }
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const uint32_t r = r0 + q * 32 + lane;
-        const uint32_t incl = warp_incl_scan(v[q]);
-        if (r < rows) col[(uint64_t)r * nb_max] = run + incl - v[q];
-        run += __shfl_sync(0xffffffffu, incl, 31);
-      }
-    }
-  }
-}
-
 // Flag words per lane in k_plan's slot numbering (1024 threads, kMaxNb buckets).
 constexpr uint32_t kPlanRounds = kMaxNb / 4 / 1024;
 static_assert(kPlanRounds * 4 * 1024 == kMaxNb, "k_plan slot numbering covers kMaxNb buckets");
@@ -1169,7 +1130,8 @@ __global__ void __launch_bounds__(1024, 1)
            uint32_t *__restrict__ seg_bucket,
            uint64_t *__restrict__ seg_off, uint32_t *__restrict__ seg_size,
            uint32_t *__restrict__ kstart, uint32_t *__restrict__ kcnt,
-           uint32_t *__restrict__ kcur, typename Traits<InT>::K *__restrict__ seg_lo,
+           uint32_t *__restrict__ kcur, uint32_t *__restrict__ fill,
+           typename Traits<InT>::K *__restrict__ seg_lo,
            typename Traits<InT>::K *__restrict__ seg_hi, uint32_t *__restrict__ req_bucket,
            uint32_t *__restrict__ req_local, Req *__restrict__ klist, uint64_t surv_cap,
            Premap pm) {
@@ -1309,6 +1271,7 @@ __global__ void __launch_bounds__(1024, 1)
     seg_hi[q] = single ? klo : (knext > klo ? knext - K(1) : KeyMax<K>::v);
     kcnt[q] = pm.bits ? __ldcg(pm.bcount + b) : 0u;  // premapped: the bucket's request count
     kcur[q] = 0;
+    fill[q] = 0;
     my_surv += cb;
   }
   uint64_t tot_surv;
@@ -1496,14 +1459,19 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
 }
 
 // Grid and tile assignment must equal k_hist's (same G, same owner of the
-// leftovers), so that CTA c meets exactly the elements it counted.
+// leftovers), so that CTA c meets exactly the elements it counted.  CTA c
+// takes its share of each slot's segment with one atomic on the slot's fill
+// counter (CTAs take their shares in any order: the order of a segment's keys
+// never matters) and leaves the share's end in its row of the per-CTA counts
+// for the check at the end.  A call that overflows the survivor buffer stops
+// here before touching the rows or the counters, so its re-run finds both as
+// the plan left them.
 template <class T, int UNROLL>
 __global__ void __launch_bounds__(1024, 1)
     k_compact(const T *__restrict__ x, uint64_t n, const LutHeader<typename Traits<T>::K> *hdr,
               const uint32_t *__restrict__ lut_g, const uint32_t *__restrict__ seg_bucket,
               const uint64_t *__restrict__ seg_off, const uint32_t *__restrict__ seg_size,
-              const uint32_t *__restrict__ prefix, const uint32_t *__restrict__ counts,
-              uint32_t nb_max,
+              uint32_t *__restrict__ rows, uint32_t *__restrict__ fill, uint32_t nb_max,
               typename Traits<T>::K *__restrict__ surv, uint64_t surv_cap, Ctrl *ctrl) {
   pdl_start();
   using K = typename Traits<T>::K;
@@ -1520,11 +1488,16 @@ __global__ void __launch_bounds__(1024, 1)
   if (threadIdx.x == 0) s_bad = false;
   __syncthreads();
   // flat slots (seg_size 0: a single-key bucket) are answered without survivors
+  uint32_t *row = rows + (uint64_t)c * nb_max;
   for (uint32_t s = threadIdx.x; s < num_slots; s += blockDim.x) {
     const uint32_t sz = seg_size[s];
     if (sz == 0) continue;
     const uint32_t b = seg_bucket[s];
-    cursor[b] = (uint32_t)(seg_off[s] + prefix[(uint64_t)c * nb_max + b]);
+    const uint32_t cnt = row[b];
+    const uint32_t pre = cnt ? atomicAdd(fill + s, cnt) : 0u;
+    const uint32_t at = (uint32_t)(seg_off[s] + pre);
+    cursor[b] = at;
+    row[b] = at + cnt;
   }
   __syncthreads();
   const uint32_t cap = (uint32_t)(surv_cap < (uint64_t)kInactive ? surv_cap : kInactive);
@@ -1533,16 +1506,11 @@ __global__ void __launch_bounds__(1024, 1)
   else
     compact_body<T, UNROLL, false>(x, n, cursor, lut, h.base, h.shift, surv, cap);
   __syncthreads();
-  // every cursor must have reached the start of the next CTA's range (the
-  // bucket's end for the last CTA); anything else means the input changed
-  // between the two passes
+  // every cursor must have reached the end of the CTA's share; anything else
+  // means the input changed between the two passes
   for (uint32_t s = threadIdx.x; s < num_slots; s += blockDim.x) {
     if (seg_size[s] == 0) continue;
-    const uint32_t b = seg_bucket[s];
-    const uint32_t end = (uint32_t)(seg_off[s] + (c + 1 < gridDim.x
-                                                       ? prefix[(uint64_t)(c + 1) * nb_max + b]
-                                                       : counts[b]));
-    if (cursor[b] != end) s_bad = true;
+    if (cursor[seg_bucket[s]] != row[seg_bucket[s]]) s_bad = true;
   }
   __syncthreads();
   if (threadIdx.x == 0 && s_bad) atomicOr(&ctrl->status, ST_INTERNAL);

@@ -51,7 +51,8 @@ constexpr size_t kNaSegSize = na_align(kNaSegOff + kNaNbMax * 8);
 constexpr size_t kNaKstart = na_align(kNaSegSize + kNaNbMax * 4);
 constexpr size_t kNaKcnt = na_align(kNaKstart + kNaNbMax * 4);
 constexpr size_t kNaKcur = na_align(kNaKcnt + kNaNbMax * 4);
-constexpr size_t kNaSegLo = na_align(kNaKcur + kNaNbMax * 4);
+constexpr size_t kNaFill = na_align(kNaKcur + kNaNbMax * 4);
+constexpr size_t kNaSegLo = na_align(kNaFill + kNaNbMax * 4);
 constexpr size_t kNaSegHi = na_align(kNaSegLo + kNaNbMax * 4);
 constexpr size_t kNaDeferred = na_align(kNaSegHi + kNaNbMax * 4);
 constexpr size_t kNaReqBucket = na_align(kNaDeferred + kNaNbMax * 4);
@@ -134,6 +135,7 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
   uint32_t *kstart = reinterpret_cast<uint32_t *>(A + kNaKstart);
   uint32_t *kcnt = reinterpret_cast<uint32_t *>(A + kNaKcnt);
   uint32_t *kcur = reinterpret_cast<uint32_t *>(A + kNaKcur);
+  uint32_t *fill = reinterpret_cast<uint32_t *>(A + kNaFill);
   K *seg_lo = reinterpret_cast<K *>(A + kNaSegLo);
   K *seg_hi = reinterpret_cast<K *>(A + kNaSegHi);
   uint32_t *deferred = reinterpret_cast<uint32_t *>(A + kNaDeferred);
@@ -171,22 +173,15 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
     set_smem_max<k_plan<float, float>>(kPlanSmemMax);
     k_plan<float, float><<<1, 1024, smem, s>>>(hdr, lut, counts, n, reqs, num_k, kNaNbMax,
                                                 ctrl, seg_bucket, seg_off,
-                                                seg_size, kstart, kcnt, kcur, seg_lo, seg_hi,
+                                                seg_size, kstart, kcnt, kcur, fill, seg_lo, seg_hi,
                                                 req_bucket, req_local, klist, n, Premap{});
-  }
-  {
-    // the slot buckets' columns of the histogram rows become prefixes
-    const uint32_t wpc = kColpThreads / 32;
-    const uint32_t cg = (num_k + wpc - 1) / wpc, cg_max = 16u * (uint32_t)sms;
-    k_colprefix<<<cg > cg_max ? cg_max : cg, kColpThreads, 0, s>>>(partials, G, kNaNbMax, ctrl,
-                                                                    seg_bucket, seg_size);
   }
   {
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kNaNbMax * 4);
     set_smem_max<k_compact<float, UNROLL>>(
         (int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
     k_compact<float, UNROLL><<<G, 1024, smem, s>>>(d_vec, n, hdr, lut, seg_bucket, seg_off,
-                                                   seg_size, partials, counts, kNaNbMax, surv, n,
+                                                   seg_size, partials, fill, kNaNbMax, surv, n,
                                                    ctrl);
   }
   {

@@ -43,11 +43,10 @@ struct Plan {
   uint32_t scan_tiles = 0;
   uint32_t cap_keys = 0;
   uint32_t fin_grid = 0;
-  uint32_t colp_grid = 0;
   uint64_t surv_cap = 0;
   // arena offsets
   size_t out = 0, ctrl = 0, reqs = 0, hdr = 0, lut = 0, samples = 0, partials = 0,
-         counts = 0, seg_bucket = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0,
+         counts = 0, seg_bucket = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0, fill = 0,
          kcur = 0, seg_lo = 0, seg_hi = 0, deferred = 0, req_bucket = 0, req_local = 0, klist = 0,
          pm_bits = 0, pm_bcount = 0, pm_bslot = 0, total = 0;
 };
@@ -71,10 +70,6 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   uint32_t slots_bound = num_req < p.nb_max ? num_req : p.nb_max;
   uint32_t fg = 5u * (uint32_t)ctx.sm_count;
   p.fin_grid = slots_bound < fg ? (slots_bound ? slots_bound : 1) : fg;
-  // one warp per slot, at most 16 CTAs per SM
-  const uint32_t wpc = kColpThreads / 32;
-  const uint32_t cg = (slots_bound + wpc - 1) / wpc, cg_max = 16u * (uint32_t)ctx.sm_count;
-  p.colp_grid = cg < 1 ? 1 : (cg > cg_max ? cg_max : cg);
   uint64_t cap = n / 8;
   p.surv_cap = cap < (1u << 20) ? (1u << 20) : cap;
   if (p.surv_cap > n) p.surv_cap = n;
@@ -108,6 +103,7 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   arr(p.kstart, p.nb_max, 4);
   arr(p.kcnt, p.nb_max, 4);
   arr(p.kcur, p.nb_max, 4);
+  arr(p.fill, p.nb_max, 4);
   arr(p.seg_lo, p.nb_max, sizeof(K));
   arr(p.seg_hi, p.nb_max, sizeof(K));
   arr(p.deferred, p.nb_max, 4);
@@ -224,6 +220,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   uint32_t *kstart = reinterpret_cast<uint32_t *>(A + p.kstart);
   uint32_t *kcnt = reinterpret_cast<uint32_t *>(A + p.kcnt);
   uint32_t *kcur = reinterpret_cast<uint32_t *>(A + p.kcur);
+  uint32_t *fill = reinterpret_cast<uint32_t *>(A + p.fill);
   K *seg_lo = reinterpret_cast<K *>(A + p.seg_lo);
   K *seg_hi = reinterpret_cast<K *>(A + p.seg_hi);
   uint32_t *deferred = reinterpret_cast<uint32_t *>(A + p.deferred);
@@ -315,17 +312,13 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       pm.bslot = pm_bslot;
     }
     L(launch(k_plan<InT, OutT>, 1, 1024, smem, s, hdr, lut, counts, n, rq, num_req, p.nb_max, ctrl,
-             seg_bucket, seg_off, seg_size, kstart, kcnt, kcur, seg_lo, seg_hi, req_bucket,
+             seg_bucket, seg_off, seg_size, kstart, kcnt, kcur, fill, seg_lo, seg_hi, req_bucket,
              req_local, klist, p.surv_cap, pm));
     if (premap) {
       L(launch(k_reqplace, (num_req + 1023) / 1024, 1024, 0, s, ctrl, rq, num_req, req_bucket,
                req_local, pm_bslot, kstart, kcur, klist));
       ctx.stats.launches += 2;
     }
-    // the slot buckets' columns of the histogram rows become prefixes
-    L(launch(k_colprefix, p.colp_grid, kColpThreads, 0, s, partials, p.G, p.nb_max, ctrl,
-             seg_bucket, seg_size));
-    ctx.stats.launches++;
     ran[GGKS_PASS_PLAN] = true;
   }
   uint64_t surv_cap = p.surv_cap;
@@ -335,7 +328,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       set_smem_max<k_compact<InT, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
       PassTimer t(ctx, s, GGKS_PASS_COMPACT);
       L(launch(k_compact<InT, UNROLL>, p.G, 1024, smem, s, d_in, n, hdr, lut, seg_bucket, seg_off,
-               seg_size, partials, counts, p.nb_max, surv, surv_cap, ctrl));
+               seg_size, partials, fill, p.nb_max, surv, surv_cap, ctrl));
       ran[GGKS_PASS_COMPACT] = true;
     }
     {

@@ -314,7 +314,7 @@ typedef struct ggks_stats {
 #define GGKS_PASS_HIST 1     /* bucket histogram over the input */
 #define GGKS_PASS_SCAN 2     /* bucket totals: column sums of the per-CTA rows */
 #define GGKS_PASS_PLAN 3     /* bucket prefix, k -> bucket marker, slot and request
-                                layout, per-CTA column prefixes of the slot buckets */
+                                layout */
 #define GGKS_PASS_COMPACT 4  /* compaction of active-bucket elements */
 #define GGKS_PASS_FINISH 5   /* per-segment in-shared-memory selection */
 
