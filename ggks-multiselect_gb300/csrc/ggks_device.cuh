@@ -71,9 +71,13 @@ constexpr int kSpinLimit = 1 << 22;              // bounded device-side waits
 // successor be scheduled at once: it orders nothing, the successor's own wait
 // does.  No kernel of the pipeline waits on other CTAs, so successors that sit
 // resident while waiting cannot hold up the running grid.
-__device__ __forceinline__ void pdl_start() {
+__device__ __forceinline__ void pdl_trigger() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_start() {
+  pdl_trigger();
+  pdl_wait();
 }
 
 // status bits in Ctrl::status
@@ -1135,7 +1139,17 @@ __global__ void __launch_bounds__(1024, 1)
            typename Traits<InT>::K *__restrict__ seg_hi, uint32_t *__restrict__ req_bucket,
            uint32_t *__restrict__ req_local, Req *__restrict__ klist, uint64_t surv_cap,
            Premap pm) {
-  pdl_start();
+  // The requests are complete before the call's first kernel (uploaded, made
+  // by a kernel the plainly launched sample kernel waits for, or left by an
+  // earlier call): with at most one per thread, each thread loads its own
+  // ahead of the dependency wait.
+  pdl_trigger();
+  const bool own = num_req <= blockDim.x;
+  Req my_rq;
+  my_rq.rank = 0;
+  my_rq.out = 0;
+  if (own && !pm.bits && threadIdx.x < num_req) my_rq = reqs[threadIdx.x];
+  pdl_wait();
   using K = typename Traits<InT>::K;
   extern __shared__ uint4 smem_raw[];
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
@@ -1193,19 +1207,34 @@ __global__ void __launch_bounds__(1024, 1)
   // requests -> bucket (the last b with excl[b] <= rank is never empty) and
   // the rank inside it; with many requests, four per thread and step, so that
   // their loads and searches overlap
+  uint32_t my_b = 0;  // the bucket of the thread's own request
   if (!pm.bits) {
-    if (num_req >= 4096)
+    if (own) {
+      if (tid < num_req) {
+        const uint32_t top = nb > 1 ? 1u << (31 - __clz(nb - 1)) : 0u;
+        uint32_t lo = 0;
+        for (uint32_t step = top; step; step >>= 1) {
+          const uint32_t m = lo + step;
+          if (m < nb && excl[m] <= my_rq.rank) lo = m;
+        }
+        flag[lo] = 1;
+        my_b = lo;
+        my_rq.rank -= excl[lo];  // now the rank inside the bucket
+      }
+    } else if (num_req >= 4096) {
       plan_map_requests<4>(excl, nb, reqs, num_req, flag, req_bucket, req_local);
-    else
+    } else {
       plan_map_requests<1>(excl, nb, reqs, num_req, flag, req_bucket, req_local);
+    }
   }
   __syncthreads();
 
   // Slots in bucket order.  Warp w owns the flag words [w wpw, (w + 1) wpw)
   // (one byte per bucket, 0 or 1), read in rounds of 32 neighbouring words;
   // the flags stay in registers, so from the warp-total scan on the flag
-  // bytes can hold the slot -> bucket list (s_segb, while it fits).  excl[]
-  // is dead from here on and maps each flagged bucket to its slot.
+  // bytes can hold the slot -> bucket list (s_segb, while it fits).  Once the
+  // slots have read their buckets' sizes from excl[], it maps each flagged
+  // bucket to its slot.
   const uint32_t lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
   const uint32_t nw = (nb + 3) >> 2;
   const uint32_t wpw = (((nw + nwarps - 1) / nwarps) + 31) & ~31u;
@@ -1242,7 +1271,6 @@ __global__ void __launch_bounds__(1024, 1)
       const uint32_t b4 = 4u * (warp * wpw + r * 32 + lane);
       for (uint32_t bits = fw[r]; bits; bits &= bits - 1u) {
         const uint32_t b = b4 + ((__ffs(bits) - 1) >> 3);
-        excl[b] = slot;
         seg_bucket[slot] = b;
         if (segb_smem) s_segb[slot] = b;
         if (pm.bits) pm.bslot[b] = slot;
@@ -1265,7 +1293,7 @@ __global__ void __launch_bounds__(1024, 1)
     // top entry's bucket can wrap past the key width, and then bucket b runs
     // up to the largest key
     const bool single = (knext > klo) ? (knext - klo == K(1)) : (klo == KeyMax<K>::v);
-    const uint32_t cb = single ? 0u : __ldg(counts + b);
+    const uint32_t cb = single ? 0u : (uint32_t)((b + 1 < nb ? excl[b + 1] : n) - excl[b]);
     seg_size[q] = cb;  // 0 marks a flat slot
     seg_lo[q] = klo;
     seg_hi[q] = single ? klo : (knext > klo ? knext - K(1) : KeyMax<K>::v);
@@ -1282,6 +1310,8 @@ __global__ void __launch_bounds__(1024, 1)
     for (uint32_t q = s0; q < s1; ++q) {
       seg_off[q] = off;
       if (q + 1 < s1) off += __ldcg(seg_size + q);
+      // the sizes are read (the scan's barriers passed): bucket -> slot
+      excl[segb_smem ? s_segb[q] : __ldcg(seg_bucket + q)] = q;
     }
   }
   if (tid == 0) {
@@ -1310,6 +1340,13 @@ __global__ void __launch_bounds__(1024, 1)
   const bool in_smem = !pm.bits && tot_slots <= room;
   if (pm.bits) {
     // counted by k_reqmap; kcnt holds them already
+  } else if (own) {
+    // one request per thread, its bucket in a register
+    if (in_smem) {
+      for (uint32_t q = tid; q < tot_slots; q += nt) s_cnt[q] = 0;
+      __syncthreads();
+    }
+    if (tid < num_req) atomicAdd(in_smem ? &s_cnt[excl[my_b]] : &kcnt[excl[my_b]], 1u);
   } else if (in_smem) {
     for (uint32_t q = tid; q < tot_slots; q += nt) s_cnt[q] = 0;
     __syncthreads();
@@ -1344,6 +1381,11 @@ __global__ void __launch_bounds__(1024, 1)
   __syncthreads();
   if (pm.bits) {
     // k_reqplace writes the lists
+  } else if (own) {
+    if (tid < num_req) {
+      const uint32_t q = excl[my_b];
+      klist[in_smem ? atomicAdd(&s_cur[q], 1u) : kstart[q] + atomicAdd(&kcur[q], 1u)] = my_rq;
+    }
   } else if (in_smem) {
     for (uint32_t i0 = tid; i0 < num_req; i0 += 4 * nt) {
       uint32_t b[4], loc[4], o[4];
@@ -1650,7 +1692,7 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
   __shared__ K redk[33];
   __shared__ uint32_t red32[33];
   __shared__ uint32_t big[kMaxBig];
-  __shared__ uint32_t s_nbig, s_nsmall, s_maxneed;
+  __shared__ uint32_t s_nbig, s_nsmall, s_maxneed, s_v;
   constexpr uint32_t PER = kFinBins / kFinThreads;  // bins per thread (at most)
   const uint32_t tcap = bcap / 2;                   // scratch T holds one bin of <= tcap keys
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1772,7 +1814,9 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
         const uint32_t bb = tid * PER + q;
         if (bb < nbins) {
           start[bb] = run;
-          gofs[bb] = 0;  // "needed" flag until the next scan
+          // few requests: "not needed" until warp 0 marks the needed bins;
+          // else the "needed" flag until the next scan
+          gofs[bb] = m <= 32 ? kNoSlot : 0u;
         }
         run += cc[q];
       }
@@ -1781,6 +1825,36 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
     if (sh == 0) {  // every bin is a single key: the ranks read their bins
       direct = true;
       break;
+    }
+    if (m <= 32) {
+      // One warp finds the requests' bins, drops repeats (match.any) and
+      // numbers the needed bins with a warp scan: no block-wide scan over
+      // the bins.  The gather order of the bins does not matter.
+      if (warp == 0) {
+        const uint32_t bb = lane < m ? bin_of_rank(start, nbins, req_at(lane).rank) : kNoSlot;
+        const uint32_t same = __match_any_sync(0xffffffffu, bb);
+        const bool lead = bb != kNoSlot && (int)lane == __ffs(same) - 1;
+        const bool one = lead && track && bmin[bb] == bmax[bb];
+        const uint32_t c = lead && !one ? hist[bb] : 0u;
+        const uint32_t incl = warp_incl_scan(c);
+        if (lead) {
+          gofs[bb] = one ? kFlatBin : incl - c;
+          if (!one) {
+            atomicMax(&s_maxneed, c);
+            if (c > 32) {
+              const uint32_t at = atomicAdd(&s_nbig, 1u);
+              if (at < kMaxBig) big[at] = bb;
+            } else if (c > 1) {
+              small[atomicAdd(&s_nsmall, 1u)] = bb;
+            }
+          }
+        }
+        if (lane == 31) s_v = incl;
+      }
+      __syncthreads();
+      V = s_v;
+      fits = V <= bcap && s_maxneed <= tcap;
+      continue;
     }
     for (uint32_t j = tid; j < m; j += blockDim.x)
       gofs[bin_of_rank(start, nbins, req_at(j).rank)] = 1u;
