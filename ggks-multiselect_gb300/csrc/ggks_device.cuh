@@ -869,9 +869,11 @@ __global__ void __launch_bounds__(1024, 1)
 // ---------------------------------------------------------------------------
 // (d) bucket totals: column sums of the per-CTA rows
 // ---------------------------------------------------------------------------
-// The bucket prefix itself is taken in shared memory by the kernels that
-// search it (k_plan, k_reqmap: smem_excl_scan), which load the totals anyway;
-// a grid-wide scan here would make every tile wait on its predecessors.
+// Each CTA sums kScanTile buckets over the rows and writes their exclusive
+// prefix inside the tile and the tile's total; the kernels that search the
+// bucket prefix (k_plan, k_reqmap: load_prefix) add the tiles' offsets in
+// shared memory.  A grid-wide scan here would make every tile wait on its
+// predecessors.
 constexpr int kScanThreads = 256;
 constexpr int kScanGroups = 4;                            // row groups per bucket
 constexpr int kScanTile = kScanThreads / kScanGroups;     // buckets per CTA
@@ -883,9 +885,11 @@ constexpr int kScanTile = kScanThreads / kScanGroups;     // buckets per CTA
 template <class K>
 __global__ void __launch_bounds__(kScanThreads)
     k_colsum(const uint32_t *__restrict__ partials, uint32_t rows, uint32_t nb_max,
-             const LutHeader<K> *hdr, uint32_t *__restrict__ counts, const Ctrl *ctrl) {
+             const LutHeader<K> *hdr, uint32_t *__restrict__ bpre, uint32_t *__restrict__ ttot,
+             const Ctrl *ctrl) {
   pdl_start();
   __shared__ uint32_t gsum[kScanGroups][kScanTile];
+  __shared__ uint32_t s_w2[2];
   if (ctrl->status & ST_FATAL) return;
   const uint32_t nb = hdr->nb;
   if ((uint64_t)blockIdx.x * kScanTile >= nb) return;
@@ -908,13 +912,22 @@ __global__ void __launch_bounds__(kScanThreads)
   }
   gsum[grp][col] = gs;
   __syncthreads();
-  if (grp == 0 && b < nb) {
-    uint32_t c = 0;
+  // the tile's kScanTile buckets (group 0: two warps) -> their exclusive
+  // prefix inside the tile, and the tile's total
+  uint32_t c = 0, incl = 0;
+  if (grp == 0) {
 #pragma unroll
     for (int g = 0; g < kScanGroups; ++g) c += gsum[g][col];
-    counts[b] = c;
+    incl = warp_incl_scan(c);
+    if ((threadIdx.x & 31) == 31) s_w2[threadIdx.x >> 5] = incl;
+  }
+  __syncthreads();
+  if (grp == 0) {
+    if (b < nb) bpre[b] = incl - c + (threadIdx.x >= 32 ? s_w2[0] : 0u);
+    if (threadIdx.x == 0) ttot[blockIdx.x] = s_w2[0] + s_w2[1];
   }
 }
+static_assert(kScanTile == 64, "k_colsum's tile prefix covers two warps");
 
 // In place: a[0 .. nb) (bucket totals, 16-byte aligned, zero from nb up to
 // the next multiple of 4) becomes its exclusive prefix; returns the total.
@@ -1007,21 +1020,51 @@ __device__ __forceinline__ void load_totals(const uint32_t *__restrict__ counts_
   }
 }
 
+// The exclusive bucket prefix into a[] (shared, 16-byte aligned): bpre_g holds
+// each bucket's prefix inside its tile of kScanTile buckets, ttot_g the tiles'
+// totals (k_colsum).  The tile totals are scanned (one per thread: at most
+// kMaxNb / kScanTile tiles), then every bucket adds its tile's offset.
+// Returns the total.
+static __device__ uint64_t load_prefix(const uint32_t *__restrict__ bpre_g,
+                                       const uint32_t *__restrict__ ttot_g, uint32_t nb,
+                                       uint32_t *a, uint32_t *s_tile /* kMaxNb / kScanTile */,
+                                       uint32_t *red /* 33 */) {
+  const uint32_t ntile = (nb + kScanTile - 1) / kScanTile;
+  const uint32_t t = threadIdx.x < ntile ? __ldcg(ttot_g + threadIdx.x) : 0u;
+  load_totals(bpre_g, nb, a);
+  uint32_t tot;
+  const uint32_t ex = block_incl_scan(t, &tot, red) - t;  // ends with a barrier
+  if (threadIdx.x < ntile) s_tile[threadIdx.x] = ex;
+  __syncthreads();
+  uint4 *a4 = reinterpret_cast<uint4 *>(a);
+  for (uint32_t v = threadIdx.x; v < ((nb + 3) >> 2); v += blockDim.x) {
+    const uint32_t o = s_tile[v / (kScanTile / 4)];  // four buckets of one tile
+    uint4 x = a4[v];
+    x.x += o;
+    x.y += o;
+    x.z += o;
+    x.w += o;
+    a4[v] = x;
+  }
+  __syncthreads();
+  return tot;
+}
+
 // Bitmap and counts must start at zero.  Shared memory: the bucket prefix
-// (nb_max u32), scanned here from the bucket totals.
+// (nb_max u32), from the tile prefixes and totals.
 static __global__ void __launch_bounds__(1024)
-    k_reqmap(const uint32_t *__restrict__ counts_g, const Ctrl *ctrl, const Req *__restrict__ reqs,
-             uint32_t num_req, uint32_t *__restrict__ req_bucket,
-             uint32_t *__restrict__ req_local, uint32_t *bits, uint32_t *bcount) {
+    k_reqmap(const uint32_t *__restrict__ bpre_g, const uint32_t *__restrict__ ttot_g,
+             const Ctrl *ctrl, const Req *__restrict__ reqs, uint32_t num_req,
+             uint32_t *__restrict__ req_bucket, uint32_t *__restrict__ req_local, uint32_t *bits,
+             uint32_t *bcount) {
   pdl_start();
   extern __shared__ uint4 smem_raw[];
   uint32_t *excl = reinterpret_cast<uint32_t *>(smem_raw);
   __shared__ uint32_t s_w[33];
+  __shared__ uint32_t s_tile[kMaxNb / kScanTile];
   if (ctrl->status & ST_FATAL) return;
   const uint32_t nb = ctrl->nb;
-  load_totals(counts_g, nb, excl);
-  __syncthreads();
-  smem_excl_scan(excl, nb, s_w);
+  load_prefix(bpre_g, ttot_g, nb, excl, s_tile, s_w);
   const uint32_t lane = threadIdx.x & 31;
   for (uint32_t u = 0; u < kReqmapPerCta / 1024; ++u) {
     const uint32_t i = blockIdx.x * kReqmapPerCta + u * 1024 + threadIdx.x;
@@ -1129,7 +1172,7 @@ __device__ __forceinline__ void plan_map_requests(const uint32_t *excl, uint32_t
 template <class InT, class OutT>
 __global__ void __launch_bounds__(1024, 1)
     k_plan(const LutHeader<typename Traits<InT>::K> *hdr, const uint32_t *__restrict__ lut_g,
-           const uint32_t *__restrict__ counts, uint64_t n,
+           const uint32_t *__restrict__ bpre, const uint32_t *__restrict__ ttot, uint64_t n,
            const Req *__restrict__ reqs, uint32_t num_req, uint32_t nb_max, Ctrl *ctrl,
            uint32_t *__restrict__ seg_bucket,
            uint64_t *__restrict__ seg_off, uint32_t *__restrict__ seg_size,
@@ -1159,16 +1202,15 @@ __global__ void __launch_bounds__(1024, 1)
   __shared__ uint32_t red32[33];
   __shared__ uint64_t red64[33];
   __shared__ uint32_t s_wbase[33];
+  __shared__ uint32_t s_tile[kMaxNb / kScanTile];
   const uint32_t tid = threadIdx.x, nt = blockDim.x;
 
   if (ctrl->status & ST_FATAL) return;
   const LutHeader<K> h = *hdr;
   const uint32_t nb = h.nb;
-  // bucket totals (becoming the prefix below) and flags, one 16-byte vector
-  // and one flag word per four buckets; every load of a step is issued before
+  // flags, one word per four buckets; every load of a step is issued before
   // the first shared store (loads and stores interleaved in one loop body
   // complete one at a time)
-  load_totals(counts, nb, excl);
   const uint32_t nb4 = (nb + 3) >> 2;
   for (uint32_t v0 = tid; v0 < nb4; v0 += 4 * nt) {
     uint32_t f[4];
@@ -1201,8 +1243,10 @@ __global__ void __launch_bounds__(1024, 1)
   }
   if (tid == 0) ctrl->deferred_count = 0;
   __syncthreads();
-  // the totals must add up to n (else the input changed under the histogram)
-  if (smem_excl_scan(excl, nb, s_wbase) != n && tid == 0) atomicOr(&ctrl->status, ST_INTERNAL);
+  // the bucket prefix; the totals must add up to n (else the input changed
+  // under the histogram)
+  if (load_prefix(bpre, ttot, nb, excl, s_tile, s_wbase) != n && tid == 0)
+    atomicOr(&ctrl->status, ST_INTERNAL);
 
   // requests -> bucket (the last b with excl[b] <= rank is never empty) and
   // the rank inside it; with many requests, four per thread and step, so that

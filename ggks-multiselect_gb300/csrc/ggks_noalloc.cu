@@ -45,7 +45,8 @@ constexpr size_t kNaLut = na_align(kNaHdr + sizeof(LutHeader<uint32_t>));
 constexpr size_t kNaSamples = na_align(kNaLut + kLutPadded * sizeof(uint32_t));
 constexpr size_t kNaPartials = na_align(kNaSamples + kNaS * sizeof(uint32_t));
 constexpr size_t kNaCounts = na_align(kNaPartials + (size_t)kNaMaxG * kNaNbMax * 4);
-constexpr size_t kNaSegBucket = na_align(kNaCounts + kNaNbMax * 4);
+constexpr size_t kNaTtot = na_align(kNaCounts + kNaNbMax * 4);
+constexpr size_t kNaSegBucket = na_align(kNaTtot + kNaNbMax / kScanTile * 4);
 constexpr size_t kNaSegOff = na_align(kNaSegBucket + kNaNbMax * 4);
 constexpr size_t kNaSegSize = na_align(kNaSegOff + kNaNbMax * 8);
 constexpr size_t kNaKstart = na_align(kNaSegSize + kNaNbMax * 4);
@@ -128,7 +129,8 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
   uint32_t *lut = reinterpret_cast<uint32_t *>(A + kNaLut);
   K *samples = reinterpret_cast<K *>(A + kNaSamples);
   uint32_t *partials = reinterpret_cast<uint32_t *>(A + kNaPartials);
-  uint32_t *counts = reinterpret_cast<uint32_t *>(A + kNaCounts);
+  uint32_t *bpre = reinterpret_cast<uint32_t *>(A + kNaCounts);  // prefix inside 64-bucket tiles
+  uint32_t *ttot = reinterpret_cast<uint32_t *>(A + kNaTtot);
   uint32_t *seg_bucket = reinterpret_cast<uint32_t *>(A + kNaSegBucket);
   uint64_t *seg_off = reinterpret_cast<uint64_t *>(A + kNaSegOff);
   uint32_t *seg_size = reinterpret_cast<uint32_t *>(A + kNaSegSize);
@@ -167,11 +169,11 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
     k_hist<float, UNROLL><<<G, 1024, smem, s>>>(d_vec, n, hdr, lut, partials, kNaNbMax, ctrl,
                                                 nullptr);
   }
-  k_colsum<K><<<col_tiles, kScanThreads, 0, s>>>(partials, G, kNaNbMax, hdr, counts, ctrl);
+  k_colsum<K><<<col_tiles, kScanThreads, 0, s>>>(partials, G, kNaNbMax, hdr, bpre, ttot, ctrl);
   {
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kNaNbMax * 5);
     set_smem_max<k_plan<float, float>>(kPlanSmemMax);
-    k_plan<float, float><<<1, 1024, smem, s>>>(hdr, lut, counts, n, reqs, num_k, kNaNbMax,
+    k_plan<float, float><<<1, 1024, smem, s>>>(hdr, lut, bpre, ttot, n, reqs, num_k, kNaNbMax,
                                                 ctrl, seg_bucket, seg_off,
                                                 seg_size, kstart, kcnt, kcur, fill, seg_lo, seg_hi,
                                                 req_bucket, req_local, klist, n, Premap{});

@@ -46,7 +46,7 @@ struct Plan {
   uint64_t surv_cap = 0;
   // arena offsets
   size_t out = 0, ctrl = 0, reqs = 0, hdr = 0, lut = 0, samples = 0, partials = 0,
-         counts = 0, seg_bucket = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0, fill = 0,
+         bpre = 0, ttot = 0, seg_bucket = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0, fill = 0,
          kcur = 0, seg_lo = 0, seg_hi = 0, deferred = 0, req_bucket = 0, req_local = 0, klist = 0,
          pm_bits = 0, pm_bcount = 0, pm_bslot = 0, total = 0;
 };
@@ -96,7 +96,8 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
     off = o;
     o = align_up(o + elems * esz, A);
   };
-  arr(p.counts, p.nb_max, 4);
+  arr(p.bpre, p.nb_max, 4);
+  arr(p.ttot, p.scan_tiles, 4);
   arr(p.seg_bucket, p.nb_max, 4);
   arr(p.seg_off, p.nb_max, 8);
   arr(p.seg_size, p.nb_max, 4);
@@ -213,7 +214,8 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   K *samples = reinterpret_cast<K *>(A + p.samples);
   uint32_t *slice_cnt = reinterpret_cast<uint32_t *>(A);
   uint32_t *partials = reinterpret_cast<uint32_t *>(A + p.partials);
-  uint32_t *counts = reinterpret_cast<uint32_t *>(A + p.counts);
+  uint32_t *bpre = reinterpret_cast<uint32_t *>(A + p.bpre);  // prefix inside 64-bucket tiles
+  uint32_t *ttot = reinterpret_cast<uint32_t *>(A + p.ttot);  // the tiles' totals
   uint32_t *seg_bucket = reinterpret_cast<uint32_t *>(A + p.seg_bucket);
   uint64_t *seg_off = reinterpret_cast<uint64_t *>(A + p.seg_off);
   uint32_t *seg_size = reinterpret_cast<uint32_t *>(A + p.seg_size);
@@ -283,8 +285,8 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   // ---- (d) reduce + decoupled look-back scan
   {
     PassTimer t(ctx, s, GGKS_PASS_SCAN);
-    L(launch(k_colsum<K>, p.scan_tiles, kScanThreads, 0, s, partials, p.G, p.nb_max, hdr, counts,
-             ctrl));
+    L(launch(k_colsum<K>, p.scan_tiles, kScanThreads, 0, s, partials, p.G, p.nb_max, hdr, bpre,
+             ttot, ctrl));
     ran[GGKS_PASS_SCAN] = true;
   }
   // ---- (e) plan
@@ -306,14 +308,14 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       if (e != cudaSuccess) return from_cuda(e);
       set_smem_max<k_reqmap>((int)(kMaxNb * 4));
       L(launch(k_reqmap, (num_req + kReqmapPerCta - 1) / kReqmapPerCta, 1024, p.nb_max * 4, s,
-               counts, ctrl, rq, num_req, req_bucket, req_local, pm_bits, pm_bcount));
+               bpre, ttot, ctrl, rq, num_req, req_bucket, req_local, pm_bits, pm_bcount));
       pm.bits = pm_bits;
       pm.bcount = pm_bcount;
       pm.bslot = pm_bslot;
     }
-    L(launch(k_plan<InT, OutT>, 1, 1024, smem, s, hdr, lut, counts, n, rq, num_req, p.nb_max, ctrl,
-             seg_bucket, seg_off, seg_size, kstart, kcnt, kcur, fill, seg_lo, seg_hi, req_bucket,
-             req_local, klist, p.surv_cap, pm));
+    L(launch(k_plan<InT, OutT>, 1, 1024, smem, s, hdr, lut, bpre, ttot, n, rq, num_req, p.nb_max,
+             ctrl, seg_bucket, seg_off, seg_size, kstart, kcnt, kcur, fill, seg_lo, seg_hi,
+             req_bucket, req_local, klist, p.surv_cap, pm));
     if (premap) {
       L(launch(k_reqplace, (num_req + 1023) / 1024, 1024, 0, s, ctrl, rq, num_req, req_bucket,
                req_local, pm_bslot, kstart, kcur, klist));
