@@ -1717,6 +1717,7 @@ struct KeyVec<uint64_t> {
   static __device__ __forceinline__ V load(const V *p) { return __ldcg(p); }
   static __device__ __forceinline__ uint64_t key(const V &v, int e) { return e == 0 ? v.x : v.y; }
 };
+constexpr uint32_t kSpecBins = 24;  // bins kept either side of a request's predicted bin
 constexpr int kFinVecs = 2;  // vectors per thread and chunk in k_finish (63 registers)
 
 template <class K, class OutT, int VECS = kFinVecs>
@@ -1736,7 +1737,8 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
   __shared__ K redk[33];
   __shared__ uint32_t red32[33];
   __shared__ uint32_t big[kMaxBig];
-  __shared__ uint32_t s_nbig, s_nsmall, s_maxneed, s_v;
+  __shared__ uint32_t s_nbig, s_nsmall, s_maxneed, s_v, s_spec, s_wlo, s_wsp;
+  __shared__ uint32_t s_wn[32];  // speculative gather: keys kept per warp
   constexpr uint32_t PER = kFinBins / kFinThreads;  // bins per thread (at most)
   const uint32_t tcap = bcap / 2;                   // scratch T holds one bin of <= tcap keys
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1755,9 +1757,8 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
   // chunk, every load of a chunk in flight before its keys are used (each
   // vector in flight costs about 15 registers once its keys' bodies are
   // scheduled).  The first and last vector may hold keys of the neighbouring
-  // segments (an
-  // aligned 16-byte granule lies within one page, so reading it is safe);
-  // those keys are masked out.
+  // segments (an aligned 16-byte granule lies within one page, so reading it
+  // is safe); those keys are masked out.
   using KV = KeyVec<K>;
   using VecT = typename KV::V;
   constexpr uint32_t KPV = KV::kKeys;
@@ -1825,20 +1826,43 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
       bmin[i] = KeyMax<K>::v;
       bmax[i] = 0;
     }
+    // Speculative gather (first attempt, a slot with one request): within a
+    // bucket the keys are close to linear in their rank, so the request's bin
+    // is predicted from its rank, and the counting pass keeps the keys of the
+    // kSpecBins bins either side of it in T (one region per warp).  If the
+    // request's bin lies in the window (and no region overflowed), the needed
+    // bin is filled from T and the segment is not read a second time.
+    const bool spec = attempt == 0 && m == 1;
     if (tid == 0) {
+      if (spec) {
+        const uint32_t span = min((uint32_t)((mx - mn) >> sh), nbins - 1u) + 1u;  // bins in use
+        const float at = ((float)my_rq.rank + 0.5f) * ((float)span / (float)size);
+        const uint32_t pb = at < (float)(span - 1) ? (uint32_t)at : span - 1u;
+        s_wlo = pb > kSpecBins ? pb - kSpecBins : 0u;
+        s_wsp = min(pb + kSpecBins, nbins - 1u) - s_wlo;
+      }
       s_nbig = 0;
       s_nsmall = 0;
       s_maxneed = 0;
+      s_spec = 0;
     }
+    if (spec && tid < nwarps) s_wn[tid] = 0;
     __syncthreads();
     // keys lie in [mn, mx], so the digit is < nbins; the clamp keeps a
     // shared-memory index in range whatever the data
+    const uint32_t wlo = spec ? s_wlo : 0u, wsp = spec ? s_wsp : 0u;
+    const uint32_t wcap = tcap / nwarps;  // keys per warp region of T
+    K *wreg = T + warp * wcap;
     auto count = [&](K k) {
       const uint32_t bb = min((uint32_t)((k - mn) >> sh), nbins - 1u);
       atomicAdd(&hist[bb], 1u);
       if (track) {
         atomic_min_key(&bmin[bb], k);
         atomic_max_key(&bmax[bb], k);
+      }
+      if (spec && bb - wlo <= wsp) {
+        const uint32_t p = atomicAdd(&s_wn[warp], 1u);
+        if (p < wcap) wreg[p] = k;
       }
     };
     each_key(count);
@@ -1894,6 +1918,12 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
           }
         }
         if (lane == 31) s_v = incl;
+        // the speculative gather holds the needed bin, no region overflowed
+        if (spec && lane == 0 && bb - wlo <= wsp) {
+          bool fit = true;
+          for (uint32_t w = 0; w < nwarps; ++w) fit = fit && s_wn[w] <= wcap;
+          s_spec = fit ? 1u : 0u;
+        }
       }
       __syncthreads();
       V = s_v;
@@ -1959,7 +1989,13 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
       const uint32_t g = gofs[bb];
       if (g < kFlatBin) B[g + atomicAdd(&cur[bb], 1u)] = k;
     };
-    each_key(put);
+    if (s_spec) {
+      const uint32_t wcap = tcap / nwarps;
+      for (uint32_t w = 0; w < nwarps; ++w)
+        for (uint32_t i = tid; i < s_wn[w]; i += blockDim.x) put(T[w * wcap + i]);
+    } else {
+      each_key(put);
+    }
   }
   __syncthreads();
 
