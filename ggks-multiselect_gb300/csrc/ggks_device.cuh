@@ -5,8 +5,8 @@
 //
 //   (a) keys      order-preserving float/double -> uint key map
 //                 (keyConversion.cu:9-23), applied on load, never stored.
-//   (b) sample    k_sample_lut: S pseudo-random keys are gathered; the last
-//                 CTA builds a range-adaptive splitter table (LUT) from them:
+//   (b) sample    k_sample + k_lut: S pseudo-random keys are gathered; the
+//                 last CTA builds a range-adaptive splitter table (LUT) from them:
 //                 4096 equal-width slices of the sample's key span, each
 //                 slice cut into 2^b sub-buckets with b chosen from the
 //                 slice's sample count, so that buckets hold about equal
@@ -102,9 +102,8 @@ struct Ctrl {
   uint32_t num_slots;
   uint64_t total_surv;
   uint32_t deferred_count;
-  uint32_t sample_done;    // last-CTA ticket of k_sample_lut (reset by that CTA)
-  uint32_t sample_arrive;  // k_sample_lut's grid barrier (arrivals)
-  uint32_t same_key;       // far-apart sample pairs holding one key (k_sample_lut)
+  uint32_t sample_done;    // last-CTA ticket of k_lut (reset by that CTA)
+  uint32_t same_key;       // far-apart sample pairs holding one key (k_lut)
   uint32_t nb;             // buckets in use
   uint64_t cap_needed;
   uint64_t kmin_inv;     // ~(smallest sampled key), by atomicMax
@@ -643,76 +642,67 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
   }
 }
 
-// Cooperative launch (every CTA resident): each CTA gathers 1024 samples
-// (one per thread, kept in a register) and folds its min / max into Ctrl; a
-// grid barrier (bounded wait) publishes the sample's span; each CTA then bins
-// its own samples by slice in shared memory, adds its non-zero slice counts to
-// slice_cnt (global, zero on entry) and counts the far-apart pairs (q, q + S/2)
-// that hold one key; the last CTA to finish builds the table from slice_cnt
-// (leaving it zero) and reads back only the neighbouring samples its bucket
-// collision estimate needs.
+// Two kernels of ceil(S / 1024) CTAs.  k_sample: each thread gathers one
+// sample at a hashed position and each CTA folds its min / max into Ctrl.
+// k_lut (after it in the stream): each CTA re-reads its 1024 samples, bins
+// them by slice in shared memory against the sample's span, adds its non-zero
+// slice counts to slice_cnt (global, zero on entry) and counts the far-apart
+// pairs (q, q + S/2) that hold one key; the last CTA to finish builds the
+// table from slice_cnt (leaving it zero) and reads back only the neighbouring
+// samples its bucket collision estimate needs.  The kernel boundary takes the
+// place of a grid barrier, so no launch needs every CTA resident at once.
 template <class T>
-__global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, uint64_t n,
-                                                     uint32_t S, uint32_t seed,
-                                                     typename Traits<T>::K *samples,
-                                                     Ctrl *ctrl,
-                                                     LutHeader<typename Traits<T>::K> *hdr,
-                                                     uint32_t *lut, uint32_t nb_max,
-                                                     uint32_t *slice_cnt) {
+__global__ void __launch_bounds__(1024) k_sample(const T *__restrict__ x, uint64_t n, uint32_t S,
+                                                 uint32_t seed,
+                                                 typename Traits<T>::K *__restrict__ samples,
+                                                 Ctrl *ctrl) {
   pdl_start();
   using K = typename Traits<T>::K;
   __shared__ K redk[33];
-  __shared__ uint32_t red32[33];
-  __shared__ uint32_t s_last, s_timeout;
-  __shared__ uint32_t ccnt[kLutIdx];
-
-  const uint32_t tid = threadIdx.x;
-  const uint32_t i = blockIdx.x * blockDim.x + tid;
-  for (uint32_t j = tid; j < kLutIdx; j += blockDim.x) ccnt[j] = 0;
-  K k = 0, mine_lo = KeyMax<K>::v, mine_hi = 0;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  K mine_lo = KeyMax<K>::v, mine_hi = 0;
   if (i < S) {
     uint64_t pos;
     if ((uint64_t)S >= n)
       pos = i;
     else
       pos = ((uint64_t)hash32(i * 0x9E3779B9u + seed) * n) >> 32;
-    k = Traits<T>::key(x[pos]);
+    const K k = Traits<T>::key(x[pos]);
     samples[i] = k;
     mine_lo = k;
     mine_hi = k;
   }
   mine_lo = block_reduce(mine_lo, [](K p, K q) { return p < q ? p : q; }, redk);
   mine_hi = block_reduce(mine_hi, [](K p, K q) { return p > q ? p : q; }, redk);
-  // grid barrier: the CTA's sample stores and extremes before its arrival
-  if (tid == 0) {
+  if (threadIdx.x == 0) {
     atomicMax((unsigned long long *)&ctrl->kmin_inv, (unsigned long long)~(uint64_t)mine_lo);
     atomicMax((unsigned long long *)&ctrl->kmax, (unsigned long long)mine_hi);
-    __threadfence();
-    atomicAdd(&ctrl->sample_arrive, 1u);
-    uint32_t it = 0, to = 0;
-    while (ld_volatile_u32(&ctrl->sample_arrive) < gridDim.x) {
-      if (++it > (uint32_t)kSpinLimit) {
-        atomicOr(&ctrl->status, ST_TIMEOUT);
-        to = 1;
-        break;
-      }
-      __nanosleep(32);
-    }
-    __threadfence();
-    s_timeout = to;
   }
-  __syncthreads();
-  if (s_timeout) return;
+}
 
+template <class K>
+__global__ void __launch_bounds__(1024) k_lut(const K *__restrict__ samples, uint32_t S,
+                                              Ctrl *ctrl, LutHeader<K> *hdr, uint32_t *lut,
+                                              uint32_t nb_max, uint32_t *slice_cnt) {
+  pdl_start();
+  __shared__ uint32_t red32[33];
+  __shared__ uint32_t s_last;
+  __shared__ uint32_t ccnt[kLutIdx];
+
+  const uint32_t tid = threadIdx.x;
+  const uint32_t i = blockIdx.x * blockDim.x + tid;
+  for (uint32_t j = tid; j < kLutIdx; j += blockDim.x) ccnt[j] = 0;
+  const uint32_t npairs = S / 2 < 4096u ? S / 2 : 4096u;
+  const K k = i < S ? __ldcg(samples + i) : K(0);
+  const K other = i < npairs ? __ldcg(samples + i + S / 2) : K(0);
   const K kmin = (K)~__ldcg((const unsigned long long *)&ctrl->kmin_inv);
   const K kmax = (K)__ldcg((const unsigned long long *)&ctrl->kmax);
   const int bl = bitlen<K>(kmax - kmin);
   const uint32_t shift = bl > kLutIdxBits ? (uint32_t)(bl - kLutIdxBits) : 0u;
+  __syncthreads();
   if (i < S) atomicAdd(&ccnt[(uint32_t)((k - kmin) >> shift)], 1u);
   // far-apart pairs (q, q + S/2): does the vector hold many copies of a key
-  const uint32_t npairs = S / 2 < 4096u ? S / 2 : 4096u;
-  uint32_t sk = 0;
-  if (i < npairs) sk = __ldcg(samples + i + S / 2) == k ? 1u : 0u;
+  uint32_t sk = i < npairs && other == k ? 1u : 0u;
   sk = block_reduce(sk, [](uint32_t p, uint32_t q) { return p + q; }, red32);
   for (uint32_t j = tid; j < kLutIdx; j += blockDim.x) {
     const uint32_t c = ccnt[j];
@@ -732,7 +722,6 @@ __global__ void __launch_bounds__(1024) k_sample_lut(const T *__restrict__ x, ui
   if (tid == 0) {
     ctrl->nb = hdr->nb;
     ctrl->sample_done = 0;  // re-arm for the next call on this workspace
-    ctrl->sample_arrive = 0;
   }
 }
 

@@ -78,7 +78,7 @@ cudaError_t ensure_surv(Context &ctx, size_t bytes);
 cudaError_t ensure_dvec(Context &ctx, size_t bytes);
 cudaError_t ensure_pin(Context &ctx, size_t bytes);
 
-// fixed-offset persistent state at the start of the arena: k_sample_lut's
+// fixed-offset persistent state at the start of the arena: k_lut's
 // per-slice sample counts, zero between calls
 constexpr size_t kSliceCntBytes = kLutIdx * sizeof(uint32_t);
 

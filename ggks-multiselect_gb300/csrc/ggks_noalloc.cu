@@ -159,10 +159,9 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
   e = cudaMemsetAsync(A + kNaCtrl, 0, kNaSliceCnt + kSliceCntBytes, s);
   if (e != cudaSuccess) return from_cuda(e);
   k_na_reqs<<<(num_k + 255) / 256, 256, 0, s>>>(d_k, num_k, n, reqs, ctrl);
-  e = launch_cooperative(k_sample_lut<float>, (S + 1023) / 1024, 1024, 0, s, d_vec, n, S, 0x5EEDu,
-                         samples, ctrl, hdr, lut, kNaNbMax,
-                         reinterpret_cast<uint32_t *>(A + kNaSliceCnt));
-  if (e != cudaSuccess) return from_cuda(e);
+  k_sample<float><<<(S + 1023) / 1024, 1024, 0, s>>>(d_vec, n, S, 0x5EEDu, samples, ctrl);
+  k_lut<K><<<(S + 1023) / 1024, 1024, 0, s>>>(samples, S, ctrl, hdr, lut, kNaNbMax,
+                                               reinterpret_cast<uint32_t *>(A + kNaSliceCnt));
   {
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kNaNbMax * 4);
     set_smem_max<k_hist<float, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));

@@ -75,7 +75,7 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   if (p.surv_cap > n) p.surv_cap = n;
 
   const size_t A = 256;
-  // the arena's head: per-slice sample counts of k_sample_lut, zero between
+  // the arena's head: per-slice sample counts of k_lut, zero between
   // calls (the arena starts zeroed; every call leaves them zero)
   size_t o = kSliceCntBytes;
   p.out = o;
@@ -142,24 +142,6 @@ static cudaError_t launch(void (*kern)(P...), dim3 grid, dim3 block, size_t smem
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   at[0].val.programmaticStreamSerializationAllowed = 1;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
-}
-
-// Cooperative launch: every CTA of the grid is resident at once (a kernel
-// with a grid barrier).
-template <class... P, class... A>
-static cudaError_t launch_cooperative(void (*kern)(P...), dim3 grid, dim3 block, size_t smem,
-                                      cudaStream_t s, A &&...args) {
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeCooperative;
-  at[0].val.cooperative = 1;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
@@ -268,8 +250,11 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   // ---- (b) sample + splitter table
   {
     PassTimer t(ctx, s, GGKS_PASS_SAMPLE);
-    L(launch_cooperative(k_sample_lut<InT>, p.sample_grid, 1024, 0, s, ingest ? ingest : d_in, n,
-                         p.S, 0x5EEDu, samples, ctrl, hdr, lut, p.nb_max, slice_cnt));
+    L(launch(k_sample<InT>, p.sample_grid, 1024, 0, s, ingest ? ingest : d_in, n, p.S, 0x5EEDu,
+             samples, ctrl));
+    L(launch(k_lut<K>, p.sample_grid, 1024, 0, s, samples, p.S, ctrl, hdr, lut, p.nb_max,
+             slice_cnt));
+    ctx.stats.launches++;
     ran[GGKS_PASS_SAMPLE] = true;
   }
   // ---- (c) histogram
