@@ -186,6 +186,9 @@ class Context:
 
     def close(self):
         if self.handle:
+            hv = self.handle.value if isinstance(self.handle, ctypes.c_void_p) else self.handle
+            for key in [k for k in _opts_refs if k[0] == hv]:
+                del _opts_refs[key]
             lib().ggks_context_destroy(self.handle)
             self.handle = None
 
@@ -215,6 +218,26 @@ def _opts(ctx=None, stream=None, flags=0):
     o.stream = stream
     o.flags = flags
     return o
+
+
+_opts_refs = {}
+
+
+def _opts_ref(ctx, stream, flags):
+    """A reference to an Opts for (context, stream, flags), built once: a call
+    of the pointer entry points then costs no structure construction."""
+    h = _h(ctx)
+    key = (h.value if isinstance(h, ctypes.c_void_p) else h, stream, flags)
+    r = _opts_refs.get(key)
+    if r is None:
+        o = _opts(ctx, stream, flags)
+        r = _opts_refs[key] = (o, ctypes.byref(o))  # the Opts lives as long as its reference
+    return r[1]
+
+
+def _addr(a):
+    """Data address of a numpy array (cheaper than a.ctypes.data)."""
+    return a.__array_interface__["data"][0]
 
 
 def get_stats(ctx=None):
@@ -259,11 +282,9 @@ def multiselect_ptr(d_ptr, n, dtype, k, ctx=None, stream=None, out=None, out_dev
     else:
         if out is None:
             out = np.empty(k.size, dtype=dtype)
-        optr = out.ctypes.data
-    o = _opts(ctx, stream, flags)
+        optr = _addr(out)
     st = getattr(lib(), "ggks_multiselect_" + _SFX[dtype])(
-        ctypes.c_void_p(d_ptr), int(n), k.ctypes.data, k.size, ctypes.c_void_p(optr),
-        ctypes.byref(o))
+        d_ptr, int(n), _addr(k), k.size, optr, _opts_ref(ctx, stream, flags))
     _check(st, "multiselect")
     return out
 
@@ -277,10 +298,9 @@ def topk_ptr(d_ptr, n, dtype, K, ctx=None, stream=None, out=None, out_device_ptr
     else:
         if out is None:
             out = np.empty(int(K), dtype=dtype)
-        optr = out.ctypes.data
-    o = _opts(ctx, stream, flags)
+        optr = _addr(out)
     st = getattr(lib(), "ggks_topk_" + _SFX[dtype])(
-        ctypes.c_void_p(d_ptr), int(n), int(K), ctypes.c_void_p(optr), ctypes.byref(o))
+        d_ptr, int(n), int(K), optr, _opts_ref(ctx, stream, flags))
     _check(st, "topk")
     return out
 
