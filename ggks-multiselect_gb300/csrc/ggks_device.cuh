@@ -43,6 +43,15 @@
 //                 thrust::sort of all survivors + copyValuesInChunk
 //                 (:799-818).  Segments larger than shared memory are listed
 //                 for a recursive re-selection by the host.
+//
+// Speculative compaction.  When the requested ranks cluster (top-k, one k, a
+// few k's near each other or near both ends), the host sends one or two rank
+// windows; (b) widens them by the sample's rank error and, if the predicted
+// buckets hold few elements, (c) also writes the elements of those buckets to
+// per-warp regions of the survivor buffer's upper half, and (f) reads those
+// candidates in place of the input whenever every active bucket was
+// predicted (a CTA whose regions overflowed reads its tiles).  The result
+// never depends on the prediction, only the second pass's traffic does.
 #pragma once
 
 #include <cstdint>
@@ -62,6 +71,7 @@ constexpr uint32_t kMaxNb = 32768;  // buckets of one vector: shared-memory hist
 constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
 constexpr uint32_t kInactive = 0x80000000u;  // compaction cursor of an inactive bucket
 constexpr int kSpinLimit = 1 << 22;              // bounded device-side waits
+constexpr uint32_t kCandWarps = 32;  // warps of a histogram / compaction CTA (1024 threads)
 
 // Programmatic dependent launch.  The pipeline's kernels are launched so that
 // each may be scheduled while its predecessor in the stream still runs;
@@ -108,6 +118,13 @@ struct Ctrl {
   uint64_t cap_needed;
   uint64_t kmin_inv;     // ~(smallest sampled key), by atomicMax
   uint64_t kmax;         // largest sampled key, by atomicMax
+  // rank windows of the call's requests, written by the host into the
+  // uploaded image (0 windows: the requests are spread out or unknown)
+  uint32_t spec_nwin;
+  uint32_t spec_pad;
+  uint64_t spec_lo[2], spec_hi[2];  // ascending 0-based ranks, inclusive
+  uint32_t spec_on;    // the table keeps candidate buckets (k_lut)
+  uint32_t spec_ctas;  // compaction CTAs that read candidates
 };
 
 template <class K>
@@ -117,7 +134,27 @@ struct LutHeader {
   uint32_t nb;     // number of buckets
   uint32_t heavy;  // 1: warp-aggregate histogram updates
   uint32_t dup;    // 1: sampled keys repeat often (at least once per nb pairs)
+  // speculative compaction: the histogram pass also keeps every element whose
+  // bucket lies in [spec_lo[i], spec_lo[i] + spec_len[i]) (i < 2), at most
+  // cand_cap per CTA; spec == 0: off
+  uint32_t spec;
+  uint32_t cand_cap;
+  uint32_t spec_lo[2];
+  uint32_t spec_len[2];
 };
+
+// Inputs of the candidate-window computation (k_lut's last CTA).
+struct SpecArgs {
+  const Ctrl *ctrl;     // spec_nwin, spec_lo, spec_hi
+  uint64_t n;           // elements of the vector
+  uint32_t cand_cap;    // candidate slots per histogram CTA (0: off)
+  uint32_t G;           // histogram CTAs
+};
+
+template <class K>
+__device__ __forceinline__ bool in_spec(const LutHeader<K> &h, uint32_t b) {
+  return (b - h.spec_lo[0] < h.spec_len[0]) | (b - h.spec_lo[1] < h.spec_len[1]);
+}
 
 // ---------------------------------------------------------------------------
 // (a) order-preserving keys (keyConversion.cu:9-23 preProcess, :29-42
@@ -427,7 +464,8 @@ __device__ __forceinline__ V block_reduce(V v, Op op, V *sh /* >= 32 */) {
 template <class K, int SPT, bool SMEM>
 __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint32_t nb_max,
                               uint32_t *lut, LutHeader<K> *hdr, int nsl_bits = kLutIdxBits,
-                              uint32_t *pre_cnt = nullptr, int64_t pre_same_key = -1) {
+                              uint32_t *pre_cnt = nullptr, int64_t pre_same_key = -1,
+                              const SpecArgs *sp = nullptr) {
   __shared__ uint32_t cnt[kLutIdx];
   __shared__ uint32_t lch[36];  // [0, 33): slices by ceil(log2 c); [34]: empty-run starts
   __shared__ uint32_t red32[33];
@@ -563,6 +601,44 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
   uint32_t total;
   const uint32_t incl = block_incl_scan(mysum, &total, red32);
   uint32_t run = incl - mysum + 1u;  // bucket 0 is the low edge
+
+  // Candidate windows.  The number of samples below the element of rank r is
+  // about Binomial(S, r / n); each window [lo, hi] of ranks is widened to the
+  // sample ranks E - 6 sd - 4 .. E + 6 sd + 4 of its ends, and the slices
+  // holding those two samples bound its buckets.  A window reaching past the
+  // sample's first or last key takes bucket 0 or the top bucket as well.  The
+  // prediction only decides what the histogram pass keeps: compaction checks
+  // that every segment's bucket was kept before it reads the candidates.
+  __shared__ uint32_t s_sp[8];  // per window: first bucket, last bucket, first / end sample rank
+  const bool spec_on = sp != nullptr && sp->cand_cap != 0 && sp->ctrl->spec_nwin != 0;
+  uint32_t wa[2] = {0, 0}, wb[2] = {0, 0}, nwin = 0;
+  bool wlo_open[2] = {false, false}, whi_open[2] = {false, false};
+  uint32_t cpre = 0;
+  if (spec_on) {
+    nwin = sp->ctrl->spec_nwin < 2u ? sp->ctrl->spec_nwin : 2u;
+    // single precision (float64 is slow on this part; sample ranks need
+    // about one unit of 2^16)
+    const float dn = (float)sp->n, dS = (float)S;
+#pragma unroll
+    for (uint32_t w = 0; w < 2; ++w) {
+      if (w >= nwin) break;
+      const float pl = (float)sp->ctrl->spec_lo[w] / dn;
+      const float ph = fminf((float)(sp->ctrl->spec_hi[w] + 1) / dn, 1.0f);
+      const float a = pl * dS - (6.0f * sqrtf(dS * pl * (1.0f - pl)) + 4.0f);
+      const float b = ph * dS + (6.0f * sqrtf(dS * ph * (1.0f - ph)) + 4.0f);
+      wlo_open[w] = a <= 0.0f;
+      whi_open[w] = b >= dS - 1.0f;
+      wa[w] = wlo_open[w] ? 0u : (a >= dS - 1.0f ? S - 1u : (uint32_t)a);
+      wb[w] = whi_open[w] ? S - 1u : (uint32_t)b;
+    }
+    // defaults (replaced below; no slice left unmatched): every bucket, every sample
+    if (tid < 8) s_sp[tid] = (tid & 3) == 1 ? 0xFFFFFFFEu : ((tid & 3) == 3 ? S : 0u);
+    uint32_t csum = 0;
+#pragma unroll
+    for (int q = 0; q < SPT; ++q) csum += c[q];
+    uint32_t ctot;
+    cpre = block_incl_scan(csum, &ctot, red32) - csum;
+  }
   // the table also goes to cnt[] (its counts are no longer read) for the
   // collision estimate below
 #pragma unroll
@@ -574,6 +650,22 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
     } else if (c[q]) {
       const int b = bits_of(q);
       e = lut_pack((int32_t)run - (int32_t)(j << b), shift - (uint32_t)b);
+      if (spec_on) {
+        // the slices with samples split the sample ranks [0, S) in order
+#pragma unroll
+        for (uint32_t w = 0; w < 2; ++w) {
+          if (w >= nwin) break;
+          if (cpre <= wa[w] && wa[w] < cpre + c[q]) {
+            s_sp[4 * w + 0] = run;
+            s_sp[4 * w + 2] = cpre;
+          }
+          if (cpre <= wb[w] && wb[w] < cpre + c[q]) {
+            s_sp[4 * w + 1] = run + my[q] - 1u;
+            s_sp[4 * w + 3] = cpre + c[q];
+          }
+        }
+        cpre += c[q];
+      }
     } else {
       // one bucket per run of empty slices
       e = lut_pack((int32_t)(prev_nonempty[q] ? run : run - 1u) - (int32_t)j, shift);
@@ -638,6 +730,54 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
     // two elements share a key with chance >= 1 / nb: buckets holding a single
     // key (many copies of it) are likely
     h.dup = (S >= 256 && (uint64_t)same_key * nb >= npairs) ? 1u : 0u;
+    h.spec = 0;
+    h.cand_cap = 0;
+    h.spec_lo[0] = h.spec_lo[1] = 0;
+    h.spec_len[0] = h.spec_len[1] = 0;
+    if (spec_on) {
+      // bucket intervals and the sample ranks they hold, ordered and merged
+      uint32_t blo[2], bhi[2], clo[2], chi[2];
+#pragma unroll
+      for (uint32_t w = 0; w < 2; ++w) {
+        if (w >= nwin) break;
+        blo[w] = wlo_open[w] ? 0u : s_sp[4 * w + 0];
+        bhi[w] = whi_open[w] ? nb - 1u : s_sp[4 * w + 1];
+        clo[w] = wlo_open[w] ? 0u : s_sp[4 * w + 2];
+        chi[w] = whi_open[w] ? S : s_sp[4 * w + 3];
+      }
+      uint32_t ni = nwin;
+      if (ni == 2) {
+        if (blo[1] < blo[0]) {
+          uint32_t t0 = blo[0]; blo[0] = blo[1]; blo[1] = t0;
+          t0 = bhi[0]; bhi[0] = bhi[1]; bhi[1] = t0;
+          t0 = clo[0]; clo[0] = clo[1]; clo[1] = t0;
+          t0 = chi[0]; chi[0] = chi[1]; chi[1] = t0;
+        }
+        if (blo[1] <= bhi[0] + 1u) {
+          bhi[0] = bhi[1] > bhi[0] ? bhi[1] : bhi[0];
+          chi[0] = chi[1] > chi[0] ? chi[1] : chi[0];
+          ni = 1;
+        }
+      }
+      uint32_t pred = 0;  // samples inside the intervals
+#pragma unroll
+      for (uint32_t i = 0; i < 2; ++i)
+        if (i < ni) pred += chi[i] - clo[i];
+      // expected candidates of the fullest CTA (its tiles plus the leftovers)
+      // with half as much again and 32 per warp to spare must fit its slots
+      const float per_cta = (float)((sp->n + sp->G - 1) / sp->G + 16384u);
+      const float want = 1.5f * per_cta * (float)pred / (float)S + 32.0f * kCandWarps;
+      if (want <= (float)sp->cand_cap) {
+        h.spec = ni;
+        h.cand_cap = sp->cand_cap;
+#pragma unroll
+        for (uint32_t i = 0; i < 2; ++i)
+          if (i < ni) {
+            h.spec_lo[i] = blo[i];
+            h.spec_len[i] = bhi[i] - blo[i] + 1u;
+          }
+      }
+    }
     *hdr = h;
   }
 }
@@ -651,6 +791,9 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
 // table from slice_cnt (leaving it zero) and reads back only the neighbouring
 // samples its bucket collision estimate needs.  The kernel boundary takes the
 // place of a grid barrier, so no launch needs every CTA resident at once.
+// The table builder also turns the call's rank windows (Ctrl::spec_*) into
+// the candidate buckets of speculative compaction (n, cand_cap: slots per
+// histogram CTA, 0 for none; G: histogram CTAs).
 template <class T>
 __global__ void __launch_bounds__(1024) k_sample(const T *__restrict__ x, uint64_t n, uint32_t S,
                                                  uint32_t seed,
@@ -683,7 +826,8 @@ __global__ void __launch_bounds__(1024) k_sample(const T *__restrict__ x, uint64
 template <class K>
 __global__ void __launch_bounds__(1024) k_lut(const K *__restrict__ samples, uint32_t S,
                                               Ctrl *ctrl, LutHeader<K> *hdr, uint32_t *lut,
-                                              uint32_t nb_max, uint32_t *slice_cnt) {
+                                              uint32_t nb_max, uint32_t *slice_cnt, uint64_t n,
+                                              uint32_t cand_cap, uint32_t G) {
   pdl_start();
   __shared__ uint32_t red32[33];
   __shared__ uint32_t s_last;
@@ -717,10 +861,12 @@ __global__ void __launch_bounds__(1024) k_lut(const K *__restrict__ samples, uin
   __syncthreads();
   if (!s_last) return;
 
+  const SpecArgs sa{ctrl, n, cand_cap, G};
   build_lut_cta<K, 4, false>(samples, S, kmin, kmax, nb_max, lut, hdr, kLutIdxBits, slice_cnt,
-                             (int64_t)__ldcg(&ctrl->same_key));
+                             (int64_t)__ldcg(&ctrl->same_key), &sa);
   if (tid == 0) {
     ctrl->nb = hdr->nb;
+    ctrl->spec_on = hdr->spec != 0 ? 1u : 0u;
     ctrl->sample_done = 0;  // re-arm for the next call on this workspace
   }
 }
@@ -760,14 +906,55 @@ __device__ __forceinline__ void hist_add(uint32_t *hist, uint32_t b) {
   }
 }
 
+// A warp's candidates (speculative compaction): its region of the candidate
+// buffer (each of a CTA's kCandWarps warps owns cap slots of the CTA's
+// region), and the kept buckets.  The count may run past cap: the region then
+// holds only part of the warp's candidates.
+template <class K>
+struct CandRow {
+  K *row;
+  uint32_t cap;
+  uint32_t lo0, len0, lo1, len1;
+  __device__ __forceinline__ bool keep(uint32_t b) const {
+    return (b - lo0 < len0) | (b - lo1 < len1);
+  }
+};
+
+// Every lane of the warp calls this (the tile loop): lanes keeping their key
+// take consecutive slots; the count is warp-uniform and lives in a register.
+template <class K>
+__device__ __forceinline__ void cand_put_warp(const CandRow<K> &cr, K k, uint32_t b,
+                                              uint32_t &count) {
+  const bool keep = cr.keep(b);
+  const uint32_t m = __ballot_sync(0xffffffffu, keep);
+  if (m) {
+    const uint32_t pos = count + __popc(m & ((1u << (threadIdx.x & 31)) - 1u));
+    if (keep && pos < cr.cap) cr.row[pos] = k;
+    count += __popc(m);
+  }
+}
+// any subset of lanes (the leftover vectors and the scalar head / tail):
+// the warp's count is in shared memory
+template <class K>
+__device__ __forceinline__ void cand_put_lane(const CandRow<K> &cr, K k, uint32_t b,
+                                              uint32_t *count) {
+  if (cr.keep(b)) {
+    const uint32_t pos = atomicAdd(count, 1u);
+    if (pos < cr.cap) cr.row[pos] = k;
+  }
+}
+
 // INGEST: x is a host vector mapped into the device address space (pinned
 // memory read over NVLink-C2C); every tile is also written to copy_to, the
 // device copy that the later passes read.  copy_to has the same alignment
-// modulo 16 bytes as x.
-template <class T, int UNROLL, bool HEAVY, bool INGEST>
+// modulo 16 bytes as x.  SPEC: keys of the kept buckets also go to the CTA's
+// candidate region.
+template <class T, int UNROLL, bool HEAVY, bool INGEST, bool SPEC>
 __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, uint32_t *hist,
                                           const uint32_t *lut, typename Traits<T>::K base,
-                                          uint32_t shift, T *__restrict__ copy_to) {
+                                          uint32_t shift, T *__restrict__ copy_to,
+                                          const CandRow<typename Traits<T>::K> &cr,
+                                          uint32_t *wcount) {
   using K = typename Traits<T>::K;
   using V = typename Traits<T>::Vec;
   constexpr int PV = Traits<T>::kPerVec;
@@ -776,6 +963,7 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
   V *cv = reinterpret_cast<V *>(copy_to + sp.head);
   const uint64_t tile_v = (uint64_t)blockDim.x * UNROLL;
   const uint64_t ntiles = sp.nvec / tile_v;
+  uint32_t count = 0;  // this warp's candidates (SPEC)
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const uint64_t off = tile * tile_v + threadIdx.x;
     V v[UNROLL];
@@ -794,9 +982,24 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
     for (int u = 0; u < UNROLL; ++u) {
       K k[PV];
       vec_keys<T>(v[u], k);
+      uint32_t b[PV];
+      bool any = false;
 #pragma unroll
-      for (int e = 0; e < PV; ++e) hist_add<HEAVY>(hist, bucket_of<K>(k[e], base, shift, lut));
+      for (int e = 0; e < PV; ++e) {
+        b[e] = bucket_of<K>(k[e], base, shift, lut);
+        hist_add<HEAVY>(hist, b[e]);
+        if (SPEC) any |= cr.keep(b[e]);
+      }
+      // one vote per vector; the per-key votes only when a lane keeps one
+      if (SPEC && __any_sync(0xffffffffu, any)) {
+#pragma unroll
+        for (int e = 0; e < PV; ++e) cand_put_warp<K>(cr, k[e], b[e], count);
+      }
     }
+  }
+  if (SPEC) {
+    if ((threadIdx.x & 31) == 0) *wcount = count;
+    __syncwarp();
   }
   // leftover vectors (fewer than one tile) and the scalar head / tail
   const uint32_t owner = (uint32_t)(ntiles % gridDim.x);
@@ -807,52 +1010,94 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
       K k[PV];
       vec_keys<T>(vv, k);
 #pragma unroll
-      for (int e = 0; e < PV; ++e) atomicAdd(&hist[bucket_of<K>(k[e], base, shift, lut)], 1u);
+      for (int e = 0; e < PV; ++e) {
+        const uint32_t b = bucket_of<K>(k[e], base, shift, lut);
+        atomicAdd(&hist[b], 1u);
+        if (SPEC) cand_put_lane<K>(cr, k[e], b, wcount);
+      }
     }
     for (uint64_t e = threadIdx.x; e < sp.head; e += blockDim.x) {
       const T v = x[e];
       if (INGEST) copy_to[e] = v;
-      atomicAdd(&hist[bucket_of<K>(Traits<T>::key(v), base, shift, lut)], 1u);
+      const K k = Traits<T>::key(v);
+      const uint32_t b = bucket_of<K>(k, base, shift, lut);
+      atomicAdd(&hist[b], 1u);
+      if (SPEC) cand_put_lane<K>(cr, k, b, wcount);
     }
     for (uint64_t e = sp.tail0 + threadIdx.x; e < n; e += blockDim.x) {
       const T v = x[e];
       if (INGEST) copy_to[e] = v;
-      atomicAdd(&hist[bucket_of<K>(Traits<T>::key(v), base, shift, lut)], 1u);
+      const K k = Traits<T>::key(v);
+      const uint32_t b = bucket_of<K>(k, base, shift, lut);
+      atomicAdd(&hist[b], 1u);
+      if (SPEC) cand_put_lane<K>(cr, k, b, wcount);
     }
   }
 }
 
+template <class T, int UNROLL, bool INGEST, bool SPEC>
+__device__ __forceinline__ void hist_dispatch(const T *__restrict__ x, uint64_t n, uint32_t *hist,
+                                              const uint32_t *lut,
+                                              const LutHeader<typename Traits<T>::K> &h,
+                                              T *__restrict__ copy_to,
+                                              const CandRow<typename Traits<T>::K> &cr,
+                                              uint32_t *wcount) {
+  if (h.heavy)
+    hist_body<T, UNROLL, true, INGEST, SPEC>(x, n, hist, lut, h.base, h.shift, copy_to, cr,
+                                             wcount);
+  else
+    hist_body<T, UNROLL, false, INGEST, SPEC>(x, n, hist, lut, h.base, h.shift, copy_to, cr,
+                                              wcount);
+}
+
 // copy_to == nullptr: x is the device vector.  Otherwise x is a mapped host
-// vector and this pass also writes the device copy (see hist_body).
+// vector and this pass also writes the device copy (see hist_body).  cand:
+// the candidate buffer (nullptr: no speculation); when the table keeps
+// buckets, warp w of CTA c writes its candidates to
+// cand[c * cand_cap + w * cand_cap / kCandWarps ...) and their count (which may
+// exceed the region) to cand_cnt[c * kCandWarps + w].
 template <class T, int UNROLL>
 __global__ void __launch_bounds__(1024, 1)
     k_hist(const T *__restrict__ x, uint64_t n, const LutHeader<typename Traits<T>::K> *hdr,
            const uint32_t *__restrict__ lut_g, uint32_t *__restrict__ partials, uint32_t nb_max,
-           const Ctrl *ctrl, T *__restrict__ copy_to) {
+           const Ctrl *ctrl, T *__restrict__ copy_to, typename Traits<T>::K *__restrict__ cand,
+           uint32_t *__restrict__ cand_cnt) {
   pdl_start();
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
   uint32_t *hist = (lut + kLutPadded);
+  __shared__ uint32_t s_wcnt[kCandWarps];
   if (ctrl->status & ST_FATAL) return;
   const LutHeader<K> h = *hdr;
   for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
   for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) hist[b] = 0;
   __syncthreads();
+  const bool spec = cand != nullptr && h.spec != 0;
+  const uint32_t warp = threadIdx.x >> 5;
+  CandRow<K> cr;
+  cr.cap = h.cand_cap / kCandWarps;
+  cr.row = spec ? cand + (uint64_t)blockIdx.x * h.cand_cap + (uint64_t)warp * cr.cap : nullptr;
+  cr.lo0 = h.spec_lo[0];
+  cr.len0 = h.spec_len[0];
+  cr.lo1 = h.spec_lo[1];
+  cr.len1 = h.spec_len[1];
   if (copy_to) {
-    if (h.heavy)
-      hist_body<T, UNROLL, true, true>(x, n, hist, lut, h.base, h.shift, copy_to);
+    if (spec)
+      hist_dispatch<T, UNROLL, true, true>(x, n, hist, lut, h, copy_to, cr, s_wcnt + warp);
     else
-      hist_body<T, UNROLL, false, true>(x, n, hist, lut, h.base, h.shift, copy_to);
+      hist_dispatch<T, UNROLL, true, false>(x, n, hist, lut, h, copy_to, cr, s_wcnt + warp);
   } else {
-    if (h.heavy)
-      hist_body<T, UNROLL, true, false>(x, n, hist, lut, h.base, h.shift, nullptr);
+    if (spec)
+      hist_dispatch<T, UNROLL, false, true>(x, n, hist, lut, h, nullptr, cr, s_wcnt + warp);
     else
-      hist_body<T, UNROLL, false, false>(x, n, hist, lut, h.base, h.shift, nullptr);
+      hist_dispatch<T, UNROLL, false, false>(x, n, hist, lut, h, nullptr, cr, s_wcnt + warp);
   }
   __syncthreads();
   uint32_t *row = partials + (uint64_t)blockIdx.x * nb_max;
   for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) row[b] = hist[b];
+  if (spec && threadIdx.x < kCandWarps)
+    cand_cnt[(uint64_t)blockIdx.x * kCandWarps + threadIdx.x] = s_wcnt[threadIdx.x];
 }
 
 // ---------------------------------------------------------------------------
@@ -1541,27 +1786,49 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
 // for the check at the end.  A call that overflows the survivor buffer stops
 // here before touching the rows or the counters, so its re-run finds both as
 // the plan left them.
+//
+// Speculative compaction: when the histogram pass kept candidates (cand not
+// null, the table's spec on) and every segment's bucket is a kept one, CTA c's
+// candidates hold all of its elements of the segments' buckets, so it reads
+// them in place of its tiles -- unless its candidates overflowed their region
+// (it reads its tiles).  The candidates lie in the survivor buffer above
+// surv_half, so candidate mode also needs the survivors to end below it.
 template <class T, int UNROLL>
 __global__ void __launch_bounds__(1024, 1)
     k_compact(const T *__restrict__ x, uint64_t n, const LutHeader<typename Traits<T>::K> *hdr,
               const uint32_t *__restrict__ lut_g, const uint32_t *__restrict__ seg_bucket,
               const uint64_t *__restrict__ seg_off, const uint32_t *__restrict__ seg_size,
               uint32_t *__restrict__ rows, uint32_t *__restrict__ fill, uint32_t nb_max,
-              typename Traits<T>::K *__restrict__ surv, uint64_t surv_cap, Ctrl *ctrl) {
+              typename Traits<T>::K *__restrict__ surv, uint64_t surv_cap, Ctrl *ctrl,
+              const typename Traits<T>::K *__restrict__ cand,
+              const uint32_t *__restrict__ cand_cnt, uint64_t surv_half) {
   pdl_start();
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
   uint32_t *cursor = (lut + kLutPadded);
   __shared__ bool s_bad;
+  __shared__ bool s_spec_miss;
+  __shared__ uint32_t s_wcnt[kCandWarps];
   if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
   const LutHeader<K> h = *hdr;
   const uint32_t c = blockIdx.x;
   for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
   const uint32_t num_slots = ctrl->num_slots;
+  const bool spec = cand != nullptr && h.spec != 0;
   for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) cursor[b] = kInactive;
-  if (threadIdx.x == 0) s_bad = false;
+  if (threadIdx.x == 0) {
+    s_bad = false;
+    s_spec_miss = false;
+  }
+  const uint32_t wcap = h.cand_cap / kCandWarps;
   __syncthreads();
+  // a warp whose candidates overflowed their region sends the CTA to its tiles
+  if (spec && threadIdx.x < kCandWarps) {
+    const uint32_t wc = cand_cnt[(uint64_t)c * kCandWarps + threadIdx.x];
+    s_wcnt[threadIdx.x] = wc;
+    if (wc > wcap) s_spec_miss = true;
+  }
   // flat slots (seg_size 0: a single-key bucket) are answered without survivors
   uint32_t *row = rows + (uint64_t)c * nb_max;
   for (uint32_t s = threadIdx.x; s < num_slots; s += blockDim.x) {
@@ -1573,13 +1840,24 @@ __global__ void __launch_bounds__(1024, 1)
     const uint32_t at = (uint32_t)(seg_off[s] + pre);
     cursor[b] = at;
     row[b] = at + cnt;
+    if (spec && !in_spec(h, b)) s_spec_miss = true;
   }
   __syncthreads();
   const uint32_t cap = (uint32_t)(surv_cap < (uint64_t)kInactive ? surv_cap : kInactive);
-  if (h.heavy)
+  if (spec && !s_spec_miss && ctrl->total_surv <= surv_half) {
+    // warp w reads the candidates of the histogram pass's warp w
+    const uint32_t w = threadIdx.x >> 5;
+    const K *mine = cand + (uint64_t)c * h.cand_cap + (uint64_t)w * wcap;
+    const uint32_t cw = s_wcnt[w];
+    const uint32_t cap_lo = (uint32_t)(surv_half < (uint64_t)cap ? surv_half : cap);
+    for (uint32_t i = threadIdx.x & 31; i < cw; i += 32)
+      compact_one<T, false>(mine[i], h.base, h.shift, lut, cursor, surv, cap_lo);
+    if (threadIdx.x == 0) atomicAdd(&ctrl->spec_ctas, 1u);
+  } else if (h.heavy) {
     compact_body<T, UNROLL, true>(x, n, cursor, lut, h.base, h.shift, surv, cap);
-  else
+  } else {
     compact_body<T, UNROLL, false>(x, n, cursor, lut, h.base, h.shift, surv, cap);
+  }
   __syncthreads();
   // every cursor must have reached the end of the CTA's share; anything else
   // means the input changed between the two passes

@@ -3,6 +3,7 @@
 // per-type instantiation units.
 #pragma once
 
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -48,8 +49,13 @@ struct Plan {
   size_t out = 0, ctrl = 0, reqs = 0, hdr = 0, lut = 0, samples = 0, partials = 0,
          bpre = 0, ttot = 0, seg_bucket = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0, fill = 0,
          kcur = 0, seg_lo = 0, seg_hi = 0, deferred = 0, req_bucket = 0, req_local = 0, klist = 0,
-         pm_bits = 0, pm_bcount = 0, pm_bslot = 0, total = 0;
+         pm_bits = 0, pm_bcount = 0, pm_bslot = 0, cand_cnt = 0, total = 0;
+  // speculative compaction: candidates live in the survivor buffer at
+  // [surv_half, surv_half + G * cand_cap)
+  uint64_t surv_half = 0;
+  uint32_t cand_cap = 0;
 };
+static_assert(sizeof(Ctrl) <= 256, "the control block travels in one 256-byte image");
 
 template <class InT, class OutT>
 static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
@@ -73,6 +79,9 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   uint64_t cap = n / 8;
   p.surv_cap = cap < (1u << 20) ? (1u << 20) : cap;
   if (p.surv_cap > n) p.surv_cap = n;
+  // per-warp regions of 16-byte multiples
+  p.surv_half = (p.surv_cap / 2) & ~(uint64_t)3;
+  p.cand_cap = (uint32_t)(((p.surv_cap - p.surv_half) / p.G) & ~(uint64_t)(4 * kCandWarps - 1));
 
   const size_t A = 256;
   // the arena's head: per-slice sample counts of k_lut, zero between
@@ -117,6 +126,7 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   p.pm_bcount = o + (size_t)p.nb_max / 8;
   o = align_up(o + (size_t)p.nb_max / 8 + (size_t)p.nb_max * 4, A);
   arr(p.pm_bslot, p.nb_max, 4);
+  arr(p.cand_cnt, (size_t)p.G * kCandWarps, 4);
   p.total = o;
   return p;
 }
@@ -177,6 +187,49 @@ static void collect_pass_times(Context &ctx, const bool *ran) {
 
 __global__ void k_make_topk_reqs(Req *reqs, uint64_t n, uint32_t K);
 
+// Rank windows for speculative compaction: one window over all requested
+// ranks, or, for up to 64 requests, two windows split at the widest gap
+// between neighbouring ranks.  The table builder widens them by the sample's
+// error and turns speculation off when they would keep too many elements;
+// windows spanning more than n / 16 ranks are not sent at all.
+static inline void set_windows_any(Ctrl *ci, const Req *hr, uint32_t num_req) {
+  if (num_req == 0) return;
+  if (num_req > 64) {
+    uint32_t lo = hr[0].rank, hi = hr[0].rank;
+    for (uint32_t i = 1; i < num_req; ++i) {
+      lo = hr[i].rank < lo ? hr[i].rank : lo;
+      hi = hr[i].rank > hi ? hr[i].rank : hi;
+    }
+    ci->spec_nwin = 1;
+    ci->spec_lo[0] = lo;
+    ci->spec_hi[0] = hi;
+    return;
+  }
+  uint32_t r[64];
+  for (uint32_t i = 0; i < num_req; ++i) r[i] = hr[i].rank;
+  std::sort(r, r + num_req);
+  uint32_t cut = 0, gap = 0;  // the second window starts at r[cut] (0: one window)
+  for (uint32_t i = 1; i < num_req; ++i)
+    if (r[i] - r[i - 1] > gap) {
+      gap = r[i] - r[i - 1];
+      cut = i;
+    }
+  if (gap <= 1) cut = 0;
+  ci->spec_nwin = cut ? 2 : 1;
+  ci->spec_lo[0] = r[0];
+  ci->spec_hi[0] = cut ? r[cut - 1] : r[num_req - 1];
+  if (cut) {
+    ci->spec_lo[1] = r[cut];
+    ci->spec_hi[1] = r[num_req - 1];
+  }
+}
+static inline void set_windows(Ctrl *ci, const Req *hr, uint32_t num_req, uint64_t n) {
+  set_windows_any(ci, hr, num_req);
+  uint64_t span = 0;
+  for (uint32_t w = 0; w < ci->spec_nwin; ++w) span += ci->spec_hi[w] - ci->spec_lo[w] + 1;
+  if (span > n / 16) ci->spec_nwin = 0;
+}
+
 template <class InT, class OutT>
 int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint32_t num_req,
            OutT *d_out_user, const OutT **host_results, cudaStream_t s, const InT *ingest) {
@@ -212,6 +265,8 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   uint32_t *req_local = reinterpret_cast<uint32_t *>(A + p.req_local);
   Req *klist = reinterpret_cast<Req *>(A + p.klist);
   K *surv = reinterpret_cast<K *>(ctx.surv);
+  K *cand = surv + p.surv_half;
+  uint32_t *cand_cnt = reinterpret_cast<uint32_t *>(A + p.cand_cnt);
   OutT *d_out = d_out_user ? d_out_user : reinterpret_cast<OutT *>(A + p.out);
   const bool out_in_arena = d_out_user == nullptr;
 
@@ -227,12 +282,18 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   // every call ends with a stream synchronisation, so no earlier copy still
   // reads the pinned buffer here
   std::memset(pin_up, 0, 256);
+  Ctrl *ci = reinterpret_cast<Ctrl *>(pin_up);
   if (src.h_k) {
     Req *hr = reinterpret_cast<Req *>(pin_up + 256);
     for (uint32_t i = 0; i < num_req; ++i) {
       hr[i].rank = (uint32_t)(n - src.h_k[i]);
       hr[i].out = i;
     }
+    set_windows(ci, hr, num_req, n);
+  } else if (src.topk && num_req && (uint64_t)num_req <= n / 16) {
+    ci->spec_nwin = 1;
+    ci->spec_lo[0] = n - num_req;
+    ci->spec_hi[0] = n - 1;
   }
   e = cudaMemcpyAsync(ctrl, pin_up, up_bytes, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return from_cuda(e);
@@ -253,7 +314,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     L(launch(k_sample<InT>, p.sample_grid, 1024, 0, s, ingest ? ingest : d_in, n, p.S, 0x5EEDu,
              samples, ctrl));
     L(launch(k_lut<K>, p.sample_grid, 1024, 0, s, samples, p.S, ctrl, hdr, lut, p.nb_max,
-             slice_cnt));
+             slice_cnt, n, p.cand_cap, p.G));
     ctx.stats.launches++;
     ran[GGKS_PASS_SAMPLE] = true;
   }
@@ -264,7 +325,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     PassTimer t(ctx, s, GGKS_PASS_HIST);
     // with a mapped host vector, this pass also writes the device copy d_in
     L(launch(k_hist<InT, UNROLL>, p.G, 1024, smem, s, ingest ? ingest : d_in, n, hdr, lut, partials,
-             p.nb_max, ctrl, ingest ? const_cast<InT *>(d_in) : nullptr));
+             p.nb_max, ctrl, ingest ? const_cast<InT *>(d_in) : nullptr, cand, cand_cnt));
     ran[GGKS_PASS_HIST] = true;
   }
   // ---- (d) reduce + decoupled look-back scan
@@ -309,13 +370,15 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     ran[GGKS_PASS_PLAN] = true;
   }
   uint64_t surv_cap = p.surv_cap;
+  const K *cand_live = cand;  // no candidates once the survivor buffer is replaced
   auto launch_tail = [&]() {
     {
       const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 4);
       set_smem_max<k_compact<InT, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
       PassTimer t(ctx, s, GGKS_PASS_COMPACT);
       L(launch(k_compact<InT, UNROLL>, p.G, 1024, smem, s, d_in, n, hdr, lut, seg_bucket, seg_off,
-               seg_size, partials, fill, p.nb_max, surv, surv_cap, ctrl));
+               seg_size, partials, fill, p.nb_max, surv, surv_cap, ctrl, cand_live, cand_cnt,
+               p.surv_half));
       ran[GGKS_PASS_COMPACT] = true;
     }
     {
@@ -363,6 +426,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       if (e != cudaSuccess) return from_cuda(e);
       surv = reinterpret_cast<K *>(ctx.surv);
       surv_cap = need;
+      cand_live = nullptr;
       ctx.stats.retries++;
       e = cudaMemsetAsync(&ctrl->status, 0, sizeof(uint32_t), s);
       if (e != cudaSuccess) return from_cuda(e);
@@ -406,6 +470,8 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     break;
   }
   ctx.stats.survivors += h_ctrl->total_surv;
+  ctx.stats.spec_calls += h_ctrl->spec_on;
+  ctx.stats.spec_ctas += h_ctrl->spec_ctas;
   if (want_host) *host_results = reinterpret_cast<const OutT *>(pin_down);
   return GGKS_OK;
 }

@@ -52,7 +52,8 @@ class Stats(ctypes.Structure):
                 ("host_ingested", ctypes.c_uint64), ("host_staged", ctypes.c_uint64),
                 ("batch_calls", ctypes.c_uint64), ("batch_problems", ctypes.c_uint64),
                 ("batch_phase_ms", ctypes.c_double * NUM_BATCH_PHASES),
-                ("batch_grid", ctypes.c_uint64)]
+                ("batch_grid", ctypes.c_uint64), ("spec_calls", ctypes.c_uint64),
+                ("spec_ctas", ctypes.c_uint64)]
 
     def as_dict(self):
         return {"calls": self.calls, "launches": self.launches,
@@ -63,7 +64,8 @@ class Stats(ctypes.Structure):
                 "host_ingested": self.host_ingested, "host_staged": self.host_staged,
                 "batch_calls": self.batch_calls, "batch_problems": self.batch_problems,
                 "batch_phase_ms": dict(zip(BATCH_PHASE_NAMES, list(self.batch_phase_ms))),
-                "batch_grid": self.batch_grid}
+                "batch_grid": self.batch_grid, "spec_calls": self.spec_calls,
+                "spec_ctas": self.spec_ctas}
 
 
 DTYPE_CODES = {np.dtype(np.float32): 0, np.dtype(np.float64): 1, np.dtype(np.uint32): 2}

@@ -299,6 +299,10 @@ typedef struct ggks_stats {
   uint64_t batch_problems;            /* problems selected by batched calls */
   double batch_phase_ms[GGKS_NUM_BATCH_PHASES]; /* device time per batch phase */
   uint64_t batch_grid;                /* CTAs of the last batched launch */
+  uint64_t spec_calls;                /* calls whose first pass also kept the predicted
+                                         candidates (top-k, few clustered k's) */
+  uint64_t spec_ctas;                 /* compaction CTAs that read those candidates
+                                         in place of their share of the vector */
 } ggks_stats;
 
 /* phase indices of ggks_stats.batch_phase_ms (one persistent launch; each
