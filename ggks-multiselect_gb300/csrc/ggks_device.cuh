@@ -90,6 +90,53 @@ __device__ __forceinline__ void pdl_start() {
   pdl_wait();
 }
 
+// Bulk asynchronous copies global -> shared (the copy engine's untiled form):
+// 16-byte aligned addresses, sizes in multiples of 16 bytes, completion
+// counted in bytes on an mbarrier.  One thread initialises the barrier and
+// issues the copies; a barrier of the block orders the initialisation before
+// any wait; waits are bounded.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+__device__ __forceinline__ void mbar_init(uint64_t *bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// bytes: a multiple of 16, issued in pieces of at most 32 KB
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+  for (uint32_t o = 0; o < bytes; o += 32768u) {
+    const uint32_t m = bytes - o < 32768u ? bytes - o : 32768u;
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_addr(static_cast<char *>(dst) + o)),
+        "l"(static_cast<const char *>(src) + o), "r"(m), "r"(smem_addr(bar))
+        : "memory");
+  }
+}
+// true once the barrier's phase `parity` has completed; false after
+// kSpinLimit tries
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  const uint32_t a = smem_addr(bar);
+  for (int i = 0; i < kSpinLimit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // status bits in Ctrl::status
 enum : uint32_t {
   ST_OVERFLOW = 1u,  // survivors exceed the survivor buffer: host regrows, re-runs (f)+(g)
@@ -1259,15 +1306,36 @@ __device__ __forceinline__ void load_totals(const uint32_t *__restrict__ counts_
 // totals (k_colsum).  The tile totals are scanned (one per thread: at most
 // kMaxNb / kScanTile tiles), then every bucket adds its tile's offset.
 // Returns the total.
+//
+// With bar set, the tile prefixes come by one bulk copy that completes on bar
+// (phase 0) while the tile totals are scanned: issued here by thread 0 when
+// issue is set, else already issued by the caller (bulk_prefix_bytes(nb)
+// bytes).  A wait that gives up marks the call timed out in *status.
+__device__ __forceinline__ uint32_t bulk_prefix_bytes(uint32_t nb) { return ((nb + 3) >> 2) * 16u; }
+
 static __device__ uint64_t load_prefix(const uint32_t *__restrict__ bpre_g,
                                        const uint32_t *__restrict__ ttot_g, uint32_t nb,
                                        uint32_t *a, uint32_t *s_tile /* kMaxNb / kScanTile */,
-                                       uint32_t *red /* 33 */) {
+                                       uint32_t *red /* 33 */, uint64_t *bar = nullptr,
+                                       bool issue = false, uint32_t *status = nullptr) {
   const uint32_t ntile = (nb + kScanTile - 1) / kScanTile;
+  if (bar && issue && threadIdx.x == 0) {
+    mbar_init(bar);
+    mbar_expect_tx(bar, bulk_prefix_bytes(nb));
+    bulk_g2s(a, bpre_g, bulk_prefix_bytes(nb), bar);
+  }
   const uint32_t t = threadIdx.x < ntile ? __ldcg(ttot_g + threadIdx.x) : 0u;
-  load_totals(bpre_g, nb, a);
+  if (!bar) load_totals(bpre_g, nb, a);
   uint32_t tot;
   const uint32_t ex = block_incl_scan(t, &tot, red) - t;  // ends with a barrier
+  if (bar) {
+    if (!mbar_wait(bar, 0)) {
+      if (status) atomicOr(status, ST_TIMEOUT);
+      mbar_wait(bar, 0);  // once more for the copy in flight, then go on
+    }
+    // the last vector's entries past nb are stale
+    if (threadIdx.x < 4u * ((nb + 3) >> 2) - nb) a[nb + threadIdx.x] = 0;
+  }
   if (threadIdx.x < ntile) s_tile[threadIdx.x] = ex;
   __syncthreads();
   uint4 *a4 = reinterpret_cast<uint4 *>(a);
@@ -1296,9 +1364,12 @@ static __global__ void __launch_bounds__(1024)
   uint32_t *excl = reinterpret_cast<uint32_t *>(smem_raw);
   __shared__ uint32_t s_w[33];
   __shared__ uint32_t s_tile[kMaxNb / kScanTile];
+  __shared__ uint64_t s_bar;
   if (ctrl->status & ST_FATAL) return;
   const uint32_t nb = ctrl->nb;
-  load_prefix(bpre_g, ttot_g, nb, excl, s_tile, s_w);
+  const bool bulk = aligned16(bpre_g) && aligned16(excl);
+  load_prefix(bpre_g, ttot_g, nb, excl, s_tile, s_w, bulk ? &s_bar : nullptr, true,
+              const_cast<uint32_t *>(&ctrl->status));
   const uint32_t lane = threadIdx.x & 31;
   for (uint32_t u = 0; u < kReqmapPerCta / 1024; ++u) {
     const uint32_t i = blockIdx.x * kReqmapPerCta + u * 1024 + threadIdx.x;
@@ -1439,9 +1510,19 @@ __global__ void __launch_bounds__(1024, 1)
   __shared__ uint32_t s_tile[kMaxNb / kScanTile];
   const uint32_t tid = threadIdx.x, nt = blockDim.x;
 
+  __shared__ uint64_t s_bar;
   if (ctrl->status & ST_FATAL) return;
   const LutHeader<K> h = *hdr;
   const uint32_t nb = h.nb;
+  // the table and the tile prefixes come by bulk copies that run while the
+  // flags are loaded and the tile totals scanned
+  const bool bulk = aligned16(bpre) && aligned16(lut_g) && aligned16(lut) && aligned16(excl);
+  if (bulk && tid == 0) {
+    mbar_init(&s_bar);
+    mbar_expect_tx(&s_bar, bulk_prefix_bytes(nb) + kLutPadded * 4u);
+    bulk_g2s(lut, lut_g, kLutPadded * 4u, &s_bar);
+    bulk_g2s(excl, bpre, bulk_prefix_bytes(nb), &s_bar);
+  }
   // flags, one word per four buckets; every load of a step is issued before
   // the first shared store (loads and stores interleaved in one loop body
   // complete one at a time)
@@ -1464,7 +1545,7 @@ __global__ void __launch_bounds__(1024, 1)
       }
     }
   }
-  for (uint32_t j0 = tid; j0 < kLutEntries; j0 += 8 * nt) {
+  for (uint32_t j0 = tid; j0 < (bulk ? 0u : kLutEntries); j0 += 8 * nt) {
     uint32_t e[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -1479,7 +1560,9 @@ __global__ void __launch_bounds__(1024, 1)
   __syncthreads();
   // the bucket prefix; the totals must add up to n (else the input changed
   // under the histogram)
-  if (load_prefix(bpre, ttot, nb, excl, s_tile, s_wbase) != n && tid == 0)
+  if (load_prefix(bpre, ttot, nb, excl, s_tile, s_wbase, bulk ? &s_bar : nullptr, false,
+                  &ctrl->status) != n &&
+      tid == 0)
     atomicOr(&ctrl->status, ST_INTERNAL);
 
   // requests -> bucket (the last b with excl[b] <= rank is never empty) and
