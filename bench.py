@@ -429,6 +429,27 @@ def run_variants(torch, ggks, gp, ctx, stream, sptr, dev, log2n):
         "pass_ms": {p: round(st["pass_ms"][p] / max(1, st["pass_launches"][p]), 4)
                     for p in ggks.PASS_NAMES},
         "recursions": st["recursions"], "survivors": st["survivors"] // 5}
+    # the rest of the top-k configuration: K in {32, 1024, 65536} on 2^26 float32
+    # uniform, uint32 uniform over [0, 2^16) and the ascending float32 copy (ms per call)
+    u16 = gp.uniform_u32(n, 1, 1 << 16)
+    inputs = [("f32_uniform", d, np.float32),
+              ("u32_uniform16", torch.from_numpy(u16.view(np.int32)).to(dev), np.uint32),
+              ("f32_sorted", torch.sort(d)[0], np.float32)]
+    grid = {}
+    for name, dt, npdt in inputs:
+        row = {}
+        for K in (32, 1024, 65536):
+            o = np.empty(K, dtype=npdt)
+
+            def tkk():
+                ggks.topk_ptr(dt.data_ptr(), n, npdt, K, ctx=ctx, stream=sptr, out=o)
+
+            ms, _, _ = timed_steps(tkk, 10, 3, stream, torch)
+            row[str(K)] = round(ms, 4)
+        grid[name] = row
+        if dt is not d:
+            del dt
+    res["topk_grid_2^26_ms"] = grid
     return res
 
 
