@@ -76,7 +76,13 @@ int context_init(Context &ctx, int device) {
   return from_cuda(e);
 }
 
-static cudaError_t grow(void **p, size_t *have, size_t need, bool zero) {
+// zero: clear the new buffer on `stream` (the stream that uses it), so that
+// the clearing is ordered before that stream's work; a plain cudaMemset would
+// go to the legacy default stream, which a non-blocking stream does not wait
+// for, and could land in the middle of a call while other work keeps the
+// default stream busy.
+static cudaError_t grow(void **p, size_t *have, size_t need, bool zero,
+                        cudaStream_t stream = nullptr) {
   if (need <= *have && *p) return cudaSuccess;
   size_t want = need + need / 4 + 4096;
   if (*p) {
@@ -90,7 +96,7 @@ static cudaError_t grow(void **p, size_t *have, size_t need, bool zero) {
     return e;
   }
   *have = want;
-  if (zero) e = cudaMemset(*p, 0, want);
+  if (zero) e = cudaMemsetAsync(*p, 0, want, stream);
   return e;
 }
 
@@ -100,7 +106,7 @@ cudaError_t ensure_arena(Context &ctx, size_t bytes) {
   cudaError_t e = cudaStreamSynchronize(ctx.stream);
   if (e != cudaSuccess) return e;
   void *p = ctx.arena;
-  e = grow(&p, &ctx.arena_bytes, bytes, true);
+  e = grow(&p, &ctx.arena_bytes, bytes, true, ctx.stream);
   ctx.arena = static_cast<char *>(p);
   return e;
 }

@@ -17,8 +17,7 @@
 //                 :534-547, :659-667).
 //   (c) hist      k_hist: persistent grid-stride pass over the input with
 //                 128-bit loads; per-CTA shared-memory histogram of up to
-//                 nb_max buckets (warp-aggregated with match.any when the
-//                 sample shows heavy duplicates); one row of counts per CTA.
+//                 nb_max buckets; one row of counts per CTA.
 //                 Replaces assignSmartBucket (bucketMultiselect.cu:129-205)
 //                 without its 4n-byte element-to-bucket array.
 //   (d) totals    k_colsum: sums the per-CTA rows per bucket.  Replaces
@@ -72,6 +71,8 @@ constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
 constexpr uint32_t kInactive = 0x80000000u;  // compaction cursor of an inactive bucket
 constexpr int kSpinLimit = 1 << 22;              // bounded device-side waits
 constexpr uint32_t kCandWarps = 32;  // warps of a histogram / compaction CTA (1024 threads)
+constexpr uint32_t kCandChunk = 256;          // candidate keys per pool chunk
+constexpr uint32_t kCandChunksPerWarp = 64;   // chunks one warp's list can hold
 
 // Programmatic dependent launch.  The pipeline's kernels are launched so that
 // each may be scheduled while its predecessor in the stream still runs;
@@ -172,6 +173,7 @@ struct Ctrl {
   uint64_t spec_lo[2], spec_hi[2];  // ascending 0-based ranks, inclusive
   uint32_t spec_on;    // the table keeps candidate buckets (k_lut)
   uint32_t spec_ctas;  // compaction CTAs that read candidates
+  uint32_t cand_next;  // candidate chunks handed out (k_hist)
 };
 
 template <class K>
@@ -179,11 +181,11 @@ struct LutHeader {
   K base;          // smallest sampled key
   uint32_t shift;  // slice index = (key - base) >> shift
   uint32_t nb;     // number of buckets
-  uint32_t heavy;  // 1: warp-aggregate histogram updates
+  uint32_t heavy;  // 1: warp-aggregate compaction's cursor updates
   uint32_t dup;    // 1: sampled keys repeat often (at least once per nb pairs)
   // speculative compaction: the histogram pass also keeps every element whose
-  // bucket lies in [spec_lo[i], spec_lo[i] + spec_len[i]) (i < 2), at most
-  // cand_cap per CTA; spec == 0: off
+  // bucket lies in [spec_lo[i], spec_lo[i] + spec_len[i]) (i < 2) in a pool of
+  // cand_cap chunks; spec == 0: off
   uint32_t spec;
   uint32_t cand_cap;
   uint32_t spec_lo[2];
@@ -194,7 +196,7 @@ struct LutHeader {
 struct SpecArgs {
   const Ctrl *ctrl;     // spec_nwin, spec_lo, spec_hi
   uint64_t n;           // elements of the vector
-  uint32_t cand_cap;    // candidate slots per histogram CTA (0: off)
+  uint32_t cand_cap;    // candidate chunks in the pool (0: off)
   uint32_t G;           // histogram CTAs
 };
 
@@ -724,10 +726,12 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
   const uint32_t top = lut_pack((int32_t)(top_run_start ? total + 1u : total),
                                 (uint32_t)KeyMax<K>::bits);
   __syncthreads();
-  // Warp-aggregated histogram updates pay off when lanes of a warp often hit
-  // the same bucket: the chance that two elements share a bucket is estimated
-  // from neighbouring samples (2q, 2q + 1), which are neighbouring elements
-  // when the samples come in runs, as the histogram's warps see them.  The
+  // Warp-aggregated cursor updates in compaction pay off when lanes of a warp
+  // often hit the same bucket (its atomics return positions, which lanes of
+  // one address receive one at a time): the chance that two elements share a
+  // bucket is estimated from neighbouring samples (2q, 2q + 1), which are
+  // neighbouring elements when the samples come in pairs or runs, as the
+  // passes' warps see them.  The
   // chance that two elements share a key, a property of the whole vector, is
   // estimated from far-apart samples (q, q + S/2).
   uint32_t same = 0, same_key = 0;
@@ -810,11 +814,11 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
 #pragma unroll
       for (uint32_t i = 0; i < 2; ++i)
         if (i < ni) pred += chi[i] - clo[i];
-      // expected candidates of the fullest CTA (its tiles plus the leftovers)
-      // with half as much again and 32 per warp to spare must fit its slots
-      const float per_cta = (float)((sp->n + sp->G - 1) / sp->G + 16384u);
-      const float want = 1.5f * per_cta * (float)pred / (float)S + 32.0f * kCandWarps;
-      if (want <= (float)sp->cand_cap) {
+      // the expected candidates with half as much again, plus one partly
+      // filled chunk per histogram warp, must fit the pool
+      const float want = 1.5f * (float)sp->n * (float)pred / (float)S +
+                         (float)sp->G * kCandWarps * kCandChunk;
+      if (want <= (float)sp->cand_cap * kCandChunk) {
         h.spec = ni;
         h.cand_cap = sp->cand_cap;
 #pragma unroll
@@ -830,7 +834,8 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
 }
 
 // Two kernels of ceil(S / 1024) CTAs.  k_sample: each thread gathers one
-// sample at a hashed position and each CTA folds its min / max into Ctrl.
+// sample (pairs of neighbouring elements at hashed positions) and each CTA
+// folds its min / max into Ctrl.
 // k_lut (after it in the stream): each CTA re-reads its 1024 samples, bins
 // them by slice in shared memory against the sample's span, adds its non-zero
 // slice counts to slice_cnt (global, zero on entry) and counts the far-apart
@@ -839,8 +844,8 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
 // samples its bucket collision estimate needs.  The kernel boundary takes the
 // place of a grid barrier, so no launch needs every CTA resident at once.
 // The table builder also turns the call's rank windows (Ctrl::spec_*) into
-// the candidate buckets of speculative compaction (n, cand_cap: slots per
-// histogram CTA, 0 for none; G: histogram CTAs).
+// the candidate buckets of speculative compaction (n, cand_cap: chunks in the
+// candidate pool, 0 for none; G: histogram CTAs).
 template <class T>
 __global__ void __launch_bounds__(1024) k_sample(const T *__restrict__ x, uint64_t n, uint32_t S,
                                                  uint32_t seed,
@@ -853,10 +858,14 @@ __global__ void __launch_bounds__(1024) k_sample(const T *__restrict__ x, uint64
   K mine_lo = KeyMax<K>::v, mine_hi = 0;
   if (i < S) {
     uint64_t pos;
-    if ((uint64_t)S >= n)
+    if ((uint64_t)S >= n) {
       pos = i;
-    else
-      pos = ((uint64_t)hash32(i * 0x9E3779B9u + seed) * n) >> 32;
+    } else {
+      // pairs of neighbouring elements at hashed positions: samples 2q and
+      // 2q + 1 are neighbours, so the table builder's collision estimate sees
+      // runs of equal buckets (sorted input) as the histogram's warps do
+      pos = (((uint64_t)hash32((i >> 1) * 0x9E3779B9u + seed) * (n - 1)) >> 32) + (i & 1u);
+    }
     const K k = Traits<T>::key(x[pos]);
     samples[i] = k;
     mine_lo = k;
@@ -953,41 +962,60 @@ __device__ __forceinline__ void hist_add(uint32_t *hist, uint32_t b) {
   }
 }
 
-// A warp's candidates (speculative compaction): its region of the candidate
-// buffer (each of a CTA's kCandWarps warps owns cap slots of the CTA's
-// region), and the kept buckets.  The count may run past cap: the region then
-// holds only part of the warp's candidates.
+// A warp's candidates (speculative compaction) go to chunks of kCandChunk
+// keys taken from one pool (the upper half of the survivor buffer) with one
+// global atomic each and listed in the warp's table of kCandChunksPerWarp
+// entries (shared memory while the pass runs).  A chunk index at or past the
+// pool's size means the pool ran out, and a count past the table's reach means
+// the table did: either way the warp's list is incomplete and compaction reads
+// the CTA's tiles instead.  Chunks follow the keys wherever they lie, so a
+// sorted input whose candidates fill a few CTAs' tiles still fits.
 template <class K>
-struct CandRow {
-  K *row;
-  uint32_t cap;
+struct CandPool {
+  K *pool;
+  uint32_t chunks;  // chunks in the pool
+  uint32_t *next;   // chunks handed out so far (global)
   uint32_t lo0, len0, lo1, len1;
   __device__ __forceinline__ bool keep(uint32_t b) const {
     return (b - lo0 < len0) | (b - lo1 < len1);
   }
 };
 
-// Every lane of the warp calls this (the tile loop): lanes keeping their key
-// take consecutive slots; the count is warp-uniform and lives in a register.
+// A warp's list while the pass runs: its length and the chunk holding its
+// last key, both warp-uniform in registers.
+struct CandList {
+  uint32_t count = 0;
+  uint32_t cur = 0xFFFFFFFFu;
+};
+
+// Every lane of the warp calls this with its key and whether it keeps it:
+// the keeping lanes take consecutive positions of the warp's list.  A new
+// chunk (a vote adds at most 32 keys, so at most one) is taken by lane 0,
+// recorded in the warp's table tab and broadcast; the table is not read here.
 template <class K>
-__device__ __forceinline__ void cand_put_warp(const CandRow<K> &cr, K k, uint32_t b,
-                                              uint32_t &count) {
-  const bool keep = cr.keep(b);
+__device__ __forceinline__ void cand_put_warp(const CandPool<K> &cp, K k, bool keep,
+                                              CandList &cl, uint32_t *tab) {
   const uint32_t m = __ballot_sync(0xffffffffu, keep);
   if (m) {
-    const uint32_t pos = count + __popc(m & ((1u << (threadIdx.x & 31)) - 1u));
-    if (keep && pos < cr.cap) cr.row[pos] = k;
-    count += __popc(m);
-  }
-}
-// any subset of lanes (the leftover vectors and the scalar head / tail):
-// the warp's count is in shared memory
-template <class K>
-__device__ __forceinline__ void cand_put_lane(const CandRow<K> &cr, K k, uint32_t b,
-                                              uint32_t *count) {
-  if (cr.keep(b)) {
-    const uint32_t pos = atomicAdd(count, 1u);
-    if (pos < cr.cap) cr.row[pos] = k;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t have = (cl.count + kCandChunk - 1) / kCandChunk;  // chunks the list holds
+    const uint32_t end = cl.count + __popc(m);
+    uint32_t nxt = cl.cur;
+    if (end > have * kCandChunk) {
+      uint32_t c = 0xFFFFFFFFu;  // no chunk: the table is full
+      if (lane == 0 && have < kCandChunksPerWarp) {
+        c = atomicAdd(cp.next, 1u);
+        tab[have] = c;
+      }
+      nxt = __shfl_sync(0xffffffffu, c, 0);
+    }
+    if (keep) {
+      const uint32_t pos = cl.count + __popc(m & ((1u << lane) - 1u));
+      const uint32_t c = pos >= have * kCandChunk ? nxt : cl.cur;
+      if (c < cp.chunks) cp.pool[(uint64_t)c * kCandChunk + pos % kCandChunk] = k;
+    }
+    cl.cur = nxt;
+    cl.count = end;
   }
 }
 
@@ -1000,8 +1028,8 @@ template <class T, int UNROLL, bool HEAVY, bool INGEST, bool SPEC>
 __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, uint32_t *hist,
                                           const uint32_t *lut, typename Traits<T>::K base,
                                           uint32_t shift, T *__restrict__ copy_to,
-                                          const CandRow<typename Traits<T>::K> &cr,
-                                          uint32_t *wcount) {
+                                          const CandPool<typename Traits<T>::K> &cr,
+                                          uint32_t *wcount, uint32_t *wtab) {
   using K = typename Traits<T>::K;
   using V = typename Traits<T>::Vec;
   constexpr int PV = Traits<T>::kPerVec;
@@ -1010,7 +1038,7 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
   V *cv = reinterpret_cast<V *>(copy_to + sp.head);
   const uint64_t tile_v = (uint64_t)blockDim.x * UNROLL;
   const uint64_t ntiles = sp.nvec / tile_v;
-  uint32_t count = 0;  // this warp's candidates (SPEC)
+  CandList cl;  // this warp's candidates (SPEC)
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const uint64_t off = tile * tile_v + threadIdx.x;
     V v[UNROLL];
@@ -1040,46 +1068,51 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
       // one vote per vector; the per-key votes only when a lane keeps one
       if (SPEC && __any_sync(0xffffffffu, any)) {
 #pragma unroll
-        for (int e = 0; e < PV; ++e) cand_put_warp<K>(cr, k[e], b[e], count);
+        for (int e = 0; e < PV; ++e) cand_put_warp<K>(cr, k[e], cr.keep(b[e]), cl, wtab);
       }
     }
   }
-  if (SPEC) {
-    if ((threadIdx.x & 31) == 0) *wcount = count;
-    __syncwarp();
-  }
-  // leftover vectors (fewer than one tile) and the scalar head / tail
+  // leftover vectors (fewer than one tile) and the scalar head / tail; every
+  // lane runs every round (the candidate votes need the whole warp)
   const uint32_t owner = (uint32_t)(ntiles % gridDim.x);
   if (blockIdx.x == owner) {
-    for (uint64_t vi = ntiles * tile_v + threadIdx.x; vi < sp.nvec; vi += blockDim.x) {
-      V vv = INGEST ? xv[vi] : ldg_stream(xv + vi);
-      if (INGEST) cv[vi] = vv;
+    for (uint64_t vb = ntiles * tile_v; vb < sp.nvec; vb += blockDim.x) {
+      const uint64_t vi = vb + threadIdx.x;
+      const bool valid = vi < sp.nvec;
+      V vv{};
+      if (valid) {
+        vv = INGEST ? xv[vi] : ldg_stream(xv + vi);
+        if (INGEST) cv[vi] = vv;
+      }
       K k[PV];
       vec_keys<T>(vv, k);
 #pragma unroll
       for (int e = 0; e < PV; ++e) {
-        const uint32_t b = bucket_of<K>(k[e], base, shift, lut);
-        atomicAdd(&hist[b], 1u);
-        if (SPEC) cand_put_lane<K>(cr, k[e], b, wcount);
+        const uint32_t b = valid ? bucket_of<K>(k[e], base, shift, lut) : 0u;
+        if (valid) atomicAdd(&hist[b], 1u);
+        if (SPEC) cand_put_warp<K>(cr, k[e], valid && cr.keep(b), cl, wtab);
       }
     }
-    for (uint64_t e = threadIdx.x; e < sp.head; e += blockDim.x) {
-      const T v = x[e];
-      if (INGEST) copy_to[e] = v;
-      const K k = Traits<T>::key(v);
-      const uint32_t b = bucket_of<K>(k, base, shift, lut);
-      atomicAdd(&hist[b], 1u);
-      if (SPEC) cand_put_lane<K>(cr, k, b, wcount);
-    }
-    for (uint64_t e = sp.tail0 + threadIdx.x; e < n; e += blockDim.x) {
-      const T v = x[e];
-      if (INGEST) copy_to[e] = v;
-      const K k = Traits<T>::key(v);
-      const uint32_t b = bucket_of<K>(k, base, shift, lut);
-      atomicAdd(&hist[b], 1u);
-      if (SPEC) cand_put_lane<K>(cr, k, b, wcount);
-    }
+    auto scalar = [&](uint64_t e0, uint64_t e1) {
+      for (uint64_t eb = e0; eb < e1; eb += blockDim.x) {
+        const uint64_t e = eb + threadIdx.x;
+        const bool valid = e < e1;
+        K k = 0;
+        uint32_t b = 0;
+        if (valid) {
+          const T v = x[e];
+          if (INGEST) copy_to[e] = v;
+          k = Traits<T>::key(v);
+          b = bucket_of<K>(k, base, shift, lut);
+          atomicAdd(&hist[b], 1u);
+        }
+        if (SPEC) cand_put_warp<K>(cr, k, valid && cr.keep(b), cl, wtab);
+      }
+    };
+    scalar(0, sp.head);
+    scalar(sp.tail0, n);
   }
+  if (SPEC && (threadIdx.x & 31) == 0) *wcount = cl.count;
 }
 
 template <class T, int UNROLL, bool INGEST, bool SPEC>
@@ -1087,34 +1120,38 @@ __device__ __forceinline__ void hist_dispatch(const T *__restrict__ x, uint64_t 
                                               const uint32_t *lut,
                                               const LutHeader<typename Traits<T>::K> &h,
                                               T *__restrict__ copy_to,
-                                              const CandRow<typename Traits<T>::K> &cr,
-                                              uint32_t *wcount) {
-  if (h.heavy)
-    hist_body<T, UNROLL, true, INGEST, SPEC>(x, n, hist, lut, h.base, h.shift, copy_to, cr,
-                                             wcount);
-  else
-    hist_body<T, UNROLL, false, INGEST, SPEC>(x, n, hist, lut, h.base, h.shift, copy_to, cr,
-                                              wcount);
+                                              const CandPool<typename Traits<T>::K> &cr,
+                                              uint32_t *wcount, uint32_t *wtab) {
+  // The histogram's atomics return nothing; lanes of a warp adding to one
+  // counter cost no more than lanes adding to different ones, so the warp
+  // aggregation that compaction uses (h.heavy) only slows this pass down
+  // (measured at 2^26: two-valued, constant and sorted inputs 74 -> 55 us).
+  (void)h;
+  hist_body<T, UNROLL, false, INGEST, SPEC>(x, n, hist, lut, h.base, h.shift, copy_to, cr,
+                                            wcount, wtab);
 }
 
 // copy_to == nullptr: x is the device vector.  Otherwise x is a mapped host
 // vector and this pass also writes the device copy (see hist_body).  cand:
-// the candidate buffer (nullptr: no speculation); when the table keeps
-// buckets, warp w of CTA c writes its candidates to
-// cand[c * cand_cap + w * cand_cap / kCandWarps ...) and their count (which may
-// exceed the region) to cand_cnt[c * kCandWarps + w].
+// the candidate pool (nullptr: no speculation); when the table keeps
+// buckets, warp w of CTA c lists its candidates in pool chunks and leaves its
+// count in cand_cnt[c * kCandWarps + w] and its chunk table in
+// cand_tab[(c * kCandWarps + w) * kCandChunksPerWarp ...); cand_next counts
+// the chunks handed out (zero on entry).
 template <class T, int UNROLL>
 __global__ void __launch_bounds__(1024, 1)
     k_hist(const T *__restrict__ x, uint64_t n, const LutHeader<typename Traits<T>::K> *hdr,
            const uint32_t *__restrict__ lut_g, uint32_t *__restrict__ partials, uint32_t nb_max,
            const Ctrl *ctrl, T *__restrict__ copy_to, typename Traits<T>::K *__restrict__ cand,
-           uint32_t *__restrict__ cand_cnt) {
+           uint32_t *__restrict__ cand_cnt, uint32_t *__restrict__ cand_tab,
+           uint32_t *cand_next) {
   pdl_start();
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
   uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
   uint32_t *hist = (lut + kLutPadded);
   __shared__ uint32_t s_wcnt[kCandWarps];
+  __shared__ uint32_t s_tab[kCandWarps * kCandChunksPerWarp];
   if (ctrl->status & ST_FATAL) return;
   const LutHeader<K> h = *hdr;
   for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
@@ -1122,29 +1159,36 @@ __global__ void __launch_bounds__(1024, 1)
   __syncthreads();
   const bool spec = cand != nullptr && h.spec != 0;
   const uint32_t warp = threadIdx.x >> 5;
-  CandRow<K> cr;
-  cr.cap = h.cand_cap / kCandWarps;
-  cr.row = spec ? cand + (uint64_t)blockIdx.x * h.cand_cap + (uint64_t)warp * cr.cap : nullptr;
+  CandPool<K> cr;
+  cr.pool = cand;
+  cr.chunks = h.cand_cap;
+  cr.next = cand_next;
   cr.lo0 = h.spec_lo[0];
   cr.len0 = h.spec_len[0];
   cr.lo1 = h.spec_lo[1];
   cr.len1 = h.spec_len[1];
+  uint32_t *wc = s_wcnt + warp, *wt = s_tab + warp * kCandChunksPerWarp;
   if (copy_to) {
     if (spec)
-      hist_dispatch<T, UNROLL, true, true>(x, n, hist, lut, h, copy_to, cr, s_wcnt + warp);
+      hist_dispatch<T, UNROLL, true, true>(x, n, hist, lut, h, copy_to, cr, wc, wt);
     else
-      hist_dispatch<T, UNROLL, true, false>(x, n, hist, lut, h, copy_to, cr, s_wcnt + warp);
+      hist_dispatch<T, UNROLL, true, false>(x, n, hist, lut, h, copy_to, cr, wc, wt);
   } else {
     if (spec)
-      hist_dispatch<T, UNROLL, false, true>(x, n, hist, lut, h, nullptr, cr, s_wcnt + warp);
+      hist_dispatch<T, UNROLL, false, true>(x, n, hist, lut, h, nullptr, cr, wc, wt);
     else
-      hist_dispatch<T, UNROLL, false, false>(x, n, hist, lut, h, nullptr, cr, s_wcnt + warp);
+      hist_dispatch<T, UNROLL, false, false>(x, n, hist, lut, h, nullptr, cr, wc, wt);
   }
   __syncthreads();
   uint32_t *row = partials + (uint64_t)blockIdx.x * nb_max;
   for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) row[b] = hist[b];
-  if (spec && threadIdx.x < kCandWarps)
-    cand_cnt[(uint64_t)blockIdx.x * kCandWarps + threadIdx.x] = s_wcnt[threadIdx.x];
+  if (spec) {
+    if (threadIdx.x < kCandWarps)
+      cand_cnt[(uint64_t)blockIdx.x * kCandWarps + threadIdx.x] = s_wcnt[threadIdx.x];
+    // entries past a warp's chunks are never read
+    for (uint32_t i = threadIdx.x; i < kCandWarps * kCandChunksPerWarp; i += blockDim.x)
+      cand_tab[(uint64_t)blockIdx.x * kCandWarps * kCandChunksPerWarp + i] = s_tab[i];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1873,7 +1917,7 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
 // Speculative compaction: when the histogram pass kept candidates (cand not
 // null, the table's spec on) and every segment's bucket is a kept one, CTA c's
 // candidates hold all of its elements of the segments' buckets, so it reads
-// them in place of its tiles -- unless its candidates overflowed their region
+// them in place of its tiles -- unless one of its warps' lists is incomplete
 // (it reads its tiles).  The candidates lie in the survivor buffer above
 // surv_half, so candidate mode also needs the survivors to end below it.
 template <class T, int UNROLL>
@@ -1884,7 +1928,8 @@ __global__ void __launch_bounds__(1024, 1)
               uint32_t *__restrict__ rows, uint32_t *__restrict__ fill, uint32_t nb_max,
               typename Traits<T>::K *__restrict__ surv, uint64_t surv_cap, Ctrl *ctrl,
               const typename Traits<T>::K *__restrict__ cand,
-              const uint32_t *__restrict__ cand_cnt, uint64_t surv_half) {
+              const uint32_t *__restrict__ cand_cnt, const uint32_t *__restrict__ cand_tab,
+              uint64_t surv_half) {
   pdl_start();
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
@@ -1893,7 +1938,10 @@ __global__ void __launch_bounds__(1024, 1)
   __shared__ bool s_bad;
   __shared__ bool s_spec_miss;
   __shared__ uint32_t s_wcnt[kCandWarps];
-  if (ctrl->status & (ST_FATAL | ST_OVERFLOW)) return;
+  __shared__ uint32_t s_tab[kCandWarps * kCandChunksPerWarp];
+  // nothing to compact when every slot is a single-key one (answered by the
+  // finisher from its key alone), and then no cursor needs checking either
+  if ((ctrl->status & (ST_FATAL | ST_OVERFLOW)) || ctrl->total_surv == 0) return;
   const LutHeader<K> h = *hdr;
   const uint32_t c = blockIdx.x;
   for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
@@ -1904,13 +1952,24 @@ __global__ void __launch_bounds__(1024, 1)
     s_bad = false;
     s_spec_miss = false;
   }
-  const uint32_t wcap = h.cand_cap / kCandWarps;
   __syncthreads();
-  // a warp whose candidates overflowed their region sends the CTA to its tiles
-  if (spec && threadIdx.x < kCandWarps) {
-    const uint32_t wc = cand_cnt[(uint64_t)c * kCandWarps + threadIdx.x];
-    s_wcnt[threadIdx.x] = wc;
-    if (wc > wcap) s_spec_miss = true;
+  // a warp whose list is incomplete (its table or the pool ran out) sends the
+  // CTA to its tiles
+  if (spec) {
+    const uint32_t *tab = cand_tab + (uint64_t)c * kCandWarps * kCandChunksPerWarp;
+    for (uint32_t i = threadIdx.x; i < kCandWarps * kCandChunksPerWarp; i += blockDim.x)
+      s_tab[i] = tab[i];
+    if (threadIdx.x < kCandWarps) {
+      const uint32_t wc = cand_cnt[(uint64_t)c * kCandWarps + threadIdx.x];
+      s_wcnt[threadIdx.x] = wc;
+      const uint32_t nch = (wc + kCandChunk - 1) / kCandChunk;
+      if (nch > kCandChunksPerWarp) {
+        s_spec_miss = true;
+      } else {
+        for (uint32_t q = 0; q < nch; ++q)
+          if (tab[threadIdx.x * kCandChunksPerWarp + q] >= h.cand_cap) s_spec_miss = true;
+      }
+    }
   }
   // flat slots (seg_size 0: a single-key bucket) are answered without survivors
   uint32_t *row = rows + (uint64_t)c * nb_max;
@@ -1930,11 +1989,12 @@ __global__ void __launch_bounds__(1024, 1)
   if (spec && !s_spec_miss && ctrl->total_surv <= surv_half) {
     // warp w reads the candidates of the histogram pass's warp w
     const uint32_t w = threadIdx.x >> 5;
-    const K *mine = cand + (uint64_t)c * h.cand_cap + (uint64_t)w * wcap;
+    const uint32_t *wt = s_tab + w * kCandChunksPerWarp;
     const uint32_t cw = s_wcnt[w];
     const uint32_t cap_lo = (uint32_t)(surv_half < (uint64_t)cap ? surv_half : cap);
     for (uint32_t i = threadIdx.x & 31; i < cw; i += 32)
-      compact_one<T, false>(mine[i], h.base, h.shift, lut, cursor, surv, cap_lo);
+      compact_one<T, false>(cand[(uint64_t)wt[i / kCandChunk] * kCandChunk + i % kCandChunk],
+                            h.base, h.shift, lut, cursor, surv, cap_lo);
     if (threadIdx.x == 0) atomicAdd(&ctrl->spec_ctas, 1u);
   } else if (h.heavy) {
     compact_body<T, UNROLL, true>(x, n, cursor, lut, h.base, h.shift, surv, cap);

@@ -4,6 +4,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -41,6 +42,7 @@ struct Plan {
   uint32_t S = 0, sample_grid = 0;
   uint32_t nb_max = 0;
   uint32_t G = 0;           // hist / compact grid
+  bool unroll8 = true;      // tiles of 8 (else 4) vectors per thread in hist / compact
   uint32_t scan_tiles = 0;
   uint32_t cap_keys = 0;
   uint32_t fin_grid = 0;
@@ -49,11 +51,11 @@ struct Plan {
   size_t out = 0, ctrl = 0, reqs = 0, hdr = 0, lut = 0, samples = 0, partials = 0,
          bpre = 0, ttot = 0, seg_bucket = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0, fill = 0,
          kcur = 0, seg_lo = 0, seg_hi = 0, deferred = 0, req_bucket = 0, req_local = 0, klist = 0,
-         pm_bits = 0, pm_bcount = 0, pm_bslot = 0, cand_cnt = 0, total = 0;
-  // speculative compaction: candidates live in the survivor buffer at
-  // [surv_half, surv_half + G * cand_cap)
+         pm_bits = 0, pm_bcount = 0, pm_bslot = 0, cand_cnt = 0, cand_tab = 0, total = 0;
+  // speculative compaction: the candidate pool is the survivor buffer from
+  // surv_half on, cand_chunks chunks of kCandChunk keys
   uint64_t surv_half = 0;
-  uint32_t cand_cap = 0;
+  uint32_t cand_chunks = 0;
 };
 static_assert(sizeof(Ctrl) <= 256, "the control block travels in one 256-byte image");
 
@@ -72,16 +74,31 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   uint64_t g = (n + 65535) / 65536;
   p.G = (uint32_t)(g < 1 ? 1 : (g > (uint64_t)ctx.sm_count ? ctx.sm_count : g));
   p.scan_tiles = (p.nb_max + kScanTile - 1) / kScanTile;
+  // Tiles of 8 vectors per thread stream a little faster than tiles of 4, but
+  // the grid's last round of tiles is then coarser: keep 8 unless 4 spreads
+  // the tiles over the CTAs better by more than 1 % (the busiest CTA's tiles
+  // against the average).
+  {
+    const double nv = (double)(n * sizeof(InT) / 16);
+    auto spread = [&](double tile_v) {
+      const double t = std::floor(nv / tile_v);
+      return t < 1 ? 1e9 : std::ceil(t / p.G) * p.G / t;
+    };
+    p.unroll8 = spread(8.0 * 1024) <= spread(4.0 * 1024) * 1.01;
+  }
   p.cap_keys = cap_keys_for<InT>();
   uint32_t slots_bound = num_req < p.nb_max ? num_req : p.nb_max;
   uint32_t fg = 5u * (uint32_t)ctx.sm_count;
   p.fin_grid = slots_bound < fg ? (slots_bound ? slots_bound : 1) : fg;
   uint64_t cap = n / 8;
-  p.surv_cap = cap < (1u << 20) ? (1u << 20) : cap;
-  if (p.surv_cap > n) p.surv_cap = n;
-  // per-warp regions of 16-byte multiples
-  p.surv_half = (p.surv_cap / 2) & ~(uint64_t)3;
-  p.cand_cap = (uint32_t)(((p.surv_cap - p.surv_half) / p.G) & ~(uint64_t)(4 * kCandWarps - 1));
+  cap = cap < (1u << 20) ? (1u << 20) : cap;
+  if (cap > n) cap = n;
+  // survivors below surv_half; from there the candidate pool, which also
+  // holds one partly filled chunk per histogram warp
+  p.surv_half = (cap / 2) & ~(uint64_t)3;  // 16-byte aligned pool
+  p.surv_cap = cap + (uint64_t)p.G * kCandWarps * kCandChunk;
+  const uint64_t chunks = (p.surv_cap - p.surv_half) / kCandChunk;
+  p.cand_chunks = (uint32_t)(chunks < 0xFFFFFFFFull ? chunks : 0xFFFFFFFFull);
 
   const size_t A = 256;
   // the arena's head: per-slice sample counts of k_lut, zero between
@@ -127,6 +144,7 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   o = align_up(o + (size_t)p.nb_max / 8 + (size_t)p.nb_max * 4, A);
   arr(p.pm_bslot, p.nb_max, 4);
   arr(p.cand_cnt, (size_t)p.G * kCandWarps, 4);
+  arr(p.cand_tab, (size_t)p.G * kCandWarps * kCandChunksPerWarp, 4);
   p.total = o;
   return p;
 }
@@ -234,7 +252,6 @@ template <class InT, class OutT>
 int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint32_t num_req,
            OutT *d_out_user, const OutT **host_results, cudaStream_t s, const InT *ingest) {
   using K = typename Traits<InT>::K;
-  constexpr int UNROLL = 4;
   if (ctx.depth > 12) return GGKS_INTERNAL;
   const Plan p = make_plan<InT, OutT>(ctx, n, num_req);
   cudaError_t e = ensure_arena(ctx, p.total);
@@ -267,6 +284,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   K *surv = reinterpret_cast<K *>(ctx.surv);
   K *cand = surv + p.surv_half;
   uint32_t *cand_cnt = reinterpret_cast<uint32_t *>(A + p.cand_cnt);
+  uint32_t *cand_tab = reinterpret_cast<uint32_t *>(A + p.cand_tab);
   OutT *d_out = d_out_user ? d_out_user : reinterpret_cast<OutT *>(A + p.out);
   const bool out_in_arena = d_out_user == nullptr;
 
@@ -314,18 +332,20 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     L(launch(k_sample<InT>, p.sample_grid, 1024, 0, s, ingest ? ingest : d_in, n, p.S, 0x5EEDu,
              samples, ctrl));
     L(launch(k_lut<K>, p.sample_grid, 1024, 0, s, samples, p.S, ctrl, hdr, lut, p.nb_max,
-             slice_cnt, n, p.cand_cap, p.G));
+             slice_cnt, n, p.cand_chunks, p.G));
     ctx.stats.launches++;
     ran[GGKS_PASS_SAMPLE] = true;
   }
   // ---- (c) histogram
   {
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 4);
-    set_smem_max<k_hist<InT, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
+    set_smem_max<k_hist<InT, 8>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
+    set_smem_max<k_hist<InT, 4>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
     PassTimer t(ctx, s, GGKS_PASS_HIST);
     // with a mapped host vector, this pass also writes the device copy d_in
-    L(launch(k_hist<InT, UNROLL>, p.G, 1024, smem, s, ingest ? ingest : d_in, n, hdr, lut, partials,
-             p.nb_max, ctrl, ingest ? const_cast<InT *>(d_in) : nullptr, cand, cand_cnt));
+    L(launch(p.unroll8 ? k_hist<InT, 8> : k_hist<InT, 4>, p.G, 1024, smem, s, ingest ? ingest : d_in, n, hdr, lut, partials,
+             p.nb_max, ctrl, ingest ? const_cast<InT *>(d_in) : nullptr, cand, cand_cnt, cand_tab,
+             &ctrl->cand_next));
     ran[GGKS_PASS_HIST] = true;
   }
   // ---- (d) reduce + decoupled look-back scan
@@ -374,11 +394,12 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   auto launch_tail = [&]() {
     {
       const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 4);
-      set_smem_max<k_compact<InT, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
+      set_smem_max<k_compact<InT, 8>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
+      set_smem_max<k_compact<InT, 4>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
       PassTimer t(ctx, s, GGKS_PASS_COMPACT);
-      L(launch(k_compact<InT, UNROLL>, p.G, 1024, smem, s, d_in, n, hdr, lut, seg_bucket, seg_off,
+      L(launch(p.unroll8 ? k_compact<InT, 8> : k_compact<InT, 4>, p.G, 1024, smem, s, d_in, n, hdr, lut, seg_bucket, seg_off,
                seg_size, partials, fill, p.nb_max, surv, surv_cap, ctrl, cand_live, cand_cnt,
-               p.surv_half));
+               cand_tab, p.surv_half));
       ran[GGKS_PASS_COMPACT] = true;
     }
     {

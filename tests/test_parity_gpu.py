@@ -160,6 +160,30 @@ def test_repeated_calls_one_context(g, orc):
     ctx.close()
 
 
+def test_fresh_context_while_default_stream_busy(g, orc):
+    """A context's workspace is cleared when it is allocated.  The clearing
+    must be ordered on the context's own (non-blocking) stream: issued to the
+    legacy default stream while other work keeps that stream busy, it would
+    run whenever that work ends -- in the middle of whichever call is then in
+    flight.  The default stream is held by a bounded spin while calls on a
+    fresh context run back to back past its end; every result must be exact."""
+    import torch
+
+    import ggks_problems as gp
+    n = 1 << 24
+    x = gp.uniform_f32(n, 8)
+    ks = gp.k_distinct(n, 1001, 3)
+    want = orc.multiselect(x, ks, 8)
+    d = DeviceArray(x)
+    torch.cuda.synchronize()
+    ctx = g.Context(0)
+    torch.cuda._sleep(40_000_000)  # ~20 ms on the default stream
+    for i in range(120):
+        assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks, ctx=ctx), want, f"call {i}")
+    torch.cuda.synchronize()
+    ctx.close()
+
+
 def test_host_vector_entry_points(g, orc):
     import ggks_problems as gp
     for dtype, dist in (("f32", "normal"), ("f64", "uniform"), ("u32", "uniform")):

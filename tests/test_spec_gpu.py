@@ -35,14 +35,16 @@ def orc():
 
 def sampled_positions(n):
     """Positions the sampling pass reads for a vector of n > 65536 elements:
-    murmur3's 32-bit finaliser of i * 0x9E3779B9 + seed, scaled to [0, n)."""
-    a = (np.arange(SAMPLES, dtype=np.uint64) * 0x9E3779B9 + SEED) & 0xFFFFFFFF
+    pairs of neighbours, sample i at murmur3's 32-bit finaliser of
+    (i / 2) * 0x9E3779B9 + seed scaled to [0, n - 1), plus i mod 2."""
+    i = np.arange(SAMPLES, dtype=np.uint64)
+    a = ((i >> np.uint64(1)) * 0x9E3779B9 + SEED) & 0xFFFFFFFF
     a ^= a >> 16
     a = (a * 0x85EBCA6B) & 0xFFFFFFFF
     a ^= a >> 13
     a = (a * 0xC2B2AE35) & 0xFFFFFFFF
     a ^= a >> 16
-    return (a * np.uint64(n)) >> np.uint64(32)
+    return ((a * np.uint64(n - 1)) >> np.uint64(32)) + (i & np.uint64(1))
 
 
 def run(g, fn, *args, **kw):
@@ -121,10 +123,10 @@ def test_prediction_miss_falls_back(g, orc):
     assert st["spec_calls"] == 1 and st["spec_ctas"] == 0
 
 
-def test_presorted_candidates_overflow_per_cta(g, orc):
-    """Ascending input: the top elements sit in the last tiles, so the CTAs
-    owning them exceed their candidate regions and read their tiles, while
-    the others read their (empty) candidate lists."""
+def test_presorted_candidates_fill_few_ctas(g, orc):
+    """Ascending input: the top elements sit in the last tiles, so a few CTAs
+    hold every candidate.  Their warps take as many pool chunks as they need,
+    and every CTA reads its candidate lists (most of them empty)."""
     import ggks_problems as gp
     n = 1 << 22
     x = np.sort(gp.uniform_f32(n, 14))
@@ -133,8 +135,7 @@ def test_presorted_candidates_overflow_per_cta(g, orc):
         got, st = run(g, g.topk_ptr, d.ptr, n, x.dtype, K)
         assert_same(got, orc.topk(x, K, 8), f"sorted K={K}")
         assert st["spec_calls"] == 1
-        grid = min(n // 65536, 152)
-        assert 0 < st["spec_ctas"] < grid
+        assert st["spec_ctas"] == min(n // 65536, 152)
 
 
 def test_speculation_with_survivor_overflow(g, orc):
@@ -143,7 +144,8 @@ def test_speculation_with_survivor_overflow(g, orc):
     keeps them, but the top bucket (keys above the sampled span) holds the
     whole cluster, so its survivors exceed the survivor buffer.  The buffer is
     regrown and the re-run compaction reads the vector (the candidates were in
-    the old buffer)."""
+    the old buffer).  The cluster's elements are all candidates: the pool runs
+    out long before, so no CTA could have read candidates anyway."""
     r = np.random.default_rng(3)
     n = 1 << 23
     x = 3.0 + r.integers(0, 1 << 16, n) * 2.0 ** -50
