@@ -352,7 +352,8 @@ def run_ggks(args):
 
     if rank == 0:
         line = {
-            "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": ws,
+            "metric": METRIC.replace("2^28", f"2^{args.log2n}"), "value": round(value, 2),
+            "unit": "GB/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
             "data": "synthetic (numpy PCG64)",
@@ -360,7 +361,9 @@ def run_ggks(args):
                                    f"{NUM_K} distinct k's uniform in [1,n]",
                        "n": n, "num_k": NUM_K, "elem": "float32 (ordered as u32 keys)",
                        "parallelism": "replicas" if ws > 1 else "single GPU",
-                       "l2": "input (1 GiB) larger than L2 (129 MB); no flush needed"},
+                       "l2": (f"input ({n * 4 >> 20} MiB) larger than L2 (129 MB); no flush needed"
+                              if n * 4 > 129 * 10**6 else
+                              f"input ({n * 4 >> 20} MiB) smaller than L2 (129 MB): not flushed")},
             "elements_per_s": round(ws * n / (ms_max * 1e-3), 1),
             "roofline": roofline,
             "pass_ms": {p: round(v, 4) for p, v in pass_ms.items()},
