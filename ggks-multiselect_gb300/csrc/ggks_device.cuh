@@ -46,11 +46,11 @@
 // Speculative compaction.  When the requested ranks cluster (top-k, one k, a
 // few k's near each other or near both ends), the host sends one or two rank
 // windows; (b) widens them by the sample's rank error and, if the predicted
-// buckets hold few elements, (c) also writes the elements of those buckets to
-// per-warp regions of the survivor buffer's upper half, and (f) reads those
-// candidates in place of the input whenever every active bucket was
-// predicted (a CTA whose regions overflowed reads its tiles).  The result
-// never depends on the prediction, only the second pass's traffic does.
+// buckets hold few elements, (c) also lists the elements of those buckets per
+// warp, in chunks taken from a pool in the survivor buffer's upper half, and
+// (f) reads those candidates in place of the input whenever every active
+// bucket was predicted (a CTA with an incomplete list reads its tiles).  The
+// result never depends on the prediction, only the second pass's traffic does.
 #pragma once
 
 #include <cstdint>
@@ -1022,8 +1022,8 @@ __device__ __forceinline__ void cand_put_warp(const CandPool<K> &cp, K k, bool k
 // INGEST: x is a host vector mapped into the device address space (pinned
 // memory read over NVLink-C2C); every tile is also written to copy_to, the
 // device copy that the later passes read.  copy_to has the same alignment
-// modulo 16 bytes as x.  SPEC: keys of the kept buckets also go to the CTA's
-// candidate region.
+// modulo 16 bytes as x.  SPEC: keys of the kept buckets also go to the warp's
+// candidate list (cand_put_warp).
 template <class T, int UNROLL, bool HEAVY, bool INGEST, bool SPEC>
 __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, uint32_t *hist,
                                           const uint32_t *lut, typename Traits<T>::K base,
