@@ -1200,56 +1200,72 @@ __global__ void __launch_bounds__(1024, 1)
 // shared memory.  A grid-wide scan here would make every tile wait on its
 // predecessors.
 constexpr int kScanThreads = 256;
-constexpr int kScanGroups = 4;                            // row groups per bucket
-constexpr int kScanTile = kScanThreads / kScanGroups;     // buckets per CTA
+constexpr int kScanTile = 64;  // buckets per CTA
 
-// Thread t handles bucket blockIdx.x * kScanTile + (t % kScanTile) over row
-// group t / kScanTile, so a warp reads 32 neighbouring buckets of one row (128
-// bytes).  The rows are read once; compaction later takes each CTA's share of
-// a bucket's segment from its own row.
+// 16 lanes read a row's 64 buckets of the tile as 16-byte vectors, and the
+// CTA's 16 groups of 16 lanes split the rows between them (at most 12 rows per
+// thread at once: one round of loads for 152 rows).  The rows are read once;
+// compaction later takes each CTA's share of a bucket's segment from its own
+// row.
 template <class K>
 __global__ void __launch_bounds__(kScanThreads)
     k_colsum(const uint32_t *__restrict__ partials, uint32_t rows, uint32_t nb_max,
              const LutHeader<K> *hdr, uint32_t *__restrict__ bpre, uint32_t *__restrict__ ttot,
              const Ctrl *ctrl) {
   pdl_start();
-  __shared__ uint32_t gsum[kScanGroups][kScanTile];
+  constexpr uint32_t kVecs = kScanTile / 4;              // 16-byte vectors per tile row
+  constexpr uint32_t kGroups = kScanThreads / kVecs;     // row groups
+  constexpr uint32_t kBatch = 12;                        // loads in flight per thread
+  __shared__ uint32_t gsum[kGroups][kScanTile];
   __shared__ uint32_t s_w2[2];
   if (ctrl->status & ST_FATAL) return;
   const uint32_t nb = hdr->nb;
   if ((uint64_t)blockIdx.x * kScanTile >= nb) return;
-  const uint32_t col = threadIdx.x % kScanTile, grp = threadIdx.x / kScanTile;
-  const uint32_t b = blockIdx.x * kScanTile + col;
-  const uint32_t per = (rows + kScanGroups - 1) / kScanGroups;
+  // thread t sums buckets 4 (t % kVecs) .. + 3 of the tile over row group
+  // t / kVecs: a row's 64 buckets are one 256-byte span read by 16 lanes
+  const uint32_t v = threadIdx.x % kVecs, grp = threadIdx.x / kVecs;
+  const uint32_t b0 = blockIdx.x * kScanTile + 4 * v;
+  const uint32_t per = (rows + kGroups - 1) / kGroups;
   const uint32_t r0 = grp * per, r1 = min(rows, r0 + per);
-  const uint32_t *p = partials + b;
-  uint32_t gs = 0;
-  if (b < nb) {
-    // predicated batches: every load of a batch is in flight at once (a
-    // remainder loop of single loads would wait for each)
-    for (uint32_t r = r0; r < r1; r += 20) {
-      uint32_t v[20];
+  const uint4 *p = reinterpret_cast<const uint4 *>(partials + b0);
+  const uint32_t row4 = nb_max / 4;  // nb_max is a multiple of 4
+  uint4 gs = make_uint4(0, 0, 0, 0);
+  if (b0 < nb) {
+    for (uint32_t r = r0; r < r1; r += kBatch) {
+      uint4 e[kBatch];
 #pragma unroll
-      for (int q = 0; q < 20; ++q) v[q] = r + q < r1 ? __ldcg(p + (uint64_t)(r + q) * nb_max) : 0u;
+      for (uint32_t q = 0; q < kBatch; ++q)
+        e[q] = r + q < r1 ? __ldcg(p + (uint64_t)(r + q) * row4) : make_uint4(0, 0, 0, 0);
 #pragma unroll
-      for (int q = 0; q < 20; ++q) gs += v[q];
+      for (uint32_t q = 0; q < kBatch; ++q) {
+        gs.x += e[q].x;
+        gs.y += e[q].y;
+        gs.z += e[q].z;
+        gs.w += e[q].w;
+      }
     }
   }
-  gsum[grp][col] = gs;
+  // rows hold stale counts past nb
+  gsum[grp][4 * v + 0] = b0 + 0 < nb ? gs.x : 0u;
+  gsum[grp][4 * v + 1] = b0 + 1 < nb ? gs.y : 0u;
+  gsum[grp][4 * v + 2] = b0 + 2 < nb ? gs.z : 0u;
+  gsum[grp][4 * v + 3] = b0 + 3 < nb ? gs.w : 0u;
   __syncthreads();
-  // the tile's kScanTile buckets (group 0: two warps) -> their exclusive
-  // prefix inside the tile, and the tile's total
+  // the tile's kScanTile buckets (two warps) -> their exclusive prefix inside
+  // the tile, and the tile's total
+  const uint32_t col = threadIdx.x;
   uint32_t c = 0, incl = 0;
-  if (grp == 0) {
+  if (col < kScanTile) {
 #pragma unroll
-    for (int g = 0; g < kScanGroups; ++g) c += gsum[g][col];
+    for (uint32_t g = 0; g < kGroups; ++g) c += gsum[g][col];
     incl = warp_incl_scan(c);
-    if ((threadIdx.x & 31) == 31) s_w2[threadIdx.x >> 5] = incl;
+    if ((col & 31) == 31) s_w2[col >> 5] = incl;
   }
   __syncthreads();
-  if (grp == 0) {
-    if (b < nb) bpre[b] = incl - c + (threadIdx.x >= 32 ? s_w2[0] : 0u);
-    if (threadIdx.x == 0) ttot[blockIdx.x] = s_w2[0] + s_w2[1];
+  if (col < kScanTile) {
+    const uint32_t b = blockIdx.x * kScanTile + col;
+    if (b < nb) bpre[b] = incl - c + (col >= 32 ? s_w2[0] : 0u);
+    if (col == 0) ttot[blockIdx.x] = s_w2[0] + s_w2[1];
   }
 }
 static_assert(kScanTile == 64, "k_colsum's tile prefix covers two warps");
