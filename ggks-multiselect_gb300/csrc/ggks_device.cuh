@@ -951,6 +951,17 @@ __device__ __forceinline__ Span<T> split_span(const T *x, uint64_t n) {
   return s;
 }
 
+// Shared-memory position of bucket b in the histogram of a table whose keys
+// repeat often (LutHeader::dup): the low five bits XOR the next five (a
+// permutation inside every block of 1024 buckets), so that buckets at
+// power-of-two strides -- integer-valued floats put theirs 512 apart -- do not
+// all fall into one bank (2^26 floats in [0, 256): 232 -> 79 us).  Other
+// tables keep plain positions: the two operations per key cost the histogram
+// of a constant or two-valued vector 10 %.
+__device__ __forceinline__ uint32_t bank_swz(uint32_t b) { return b ^ ((b >> 5) & 31u); }
+// buckets [0, nb) occupy positions [0, bank_span(nb)) once swizzled
+__device__ __forceinline__ uint32_t bank_span(uint32_t nb) { return (nb + 1023u) & ~1023u; }
+
 template <bool HEAVY>
 __device__ __forceinline__ void hist_add(uint32_t *hist, uint32_t b) {
   if (HEAVY) {
@@ -1024,7 +1035,7 @@ __device__ __forceinline__ void cand_put_warp(const CandPool<K> &cp, K k, bool k
 // device copy that the later passes read.  copy_to has the same alignment
 // modulo 16 bytes as x.  SPEC: keys of the kept buckets also go to the warp's
 // candidate list (cand_put_warp).
-template <class T, int UNROLL, bool HEAVY, bool INGEST, bool SPEC>
+template <class T, int UNROLL, bool HEAVY, bool INGEST, bool SPEC, bool SWZ>
 __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, uint32_t *hist,
                                           const uint32_t *lut, typename Traits<T>::K base,
                                           uint32_t shift, T *__restrict__ copy_to,
@@ -1062,7 +1073,7 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
 #pragma unroll
       for (int e = 0; e < PV; ++e) {
         b[e] = bucket_of<K>(k[e], base, shift, lut);
-        hist_add<HEAVY>(hist, b[e]);
+        hist_add<HEAVY>(hist, SWZ ? bank_swz(b[e]) : b[e]);
         if (SPEC) any |= cr.keep(b[e]);
       }
       // one vote per vector; the per-key votes only when a lane keeps one
@@ -1089,7 +1100,7 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
 #pragma unroll
       for (int e = 0; e < PV; ++e) {
         const uint32_t b = valid ? bucket_of<K>(k[e], base, shift, lut) : 0u;
-        if (valid) atomicAdd(&hist[b], 1u);
+        if (valid) atomicAdd(&hist[SWZ ? bank_swz(b) : b], 1u);
         if (SPEC) cand_put_warp<K>(cr, k[e], valid && cr.keep(b), cl, wtab);
       }
     }
@@ -1104,7 +1115,7 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
           if (INGEST) copy_to[e] = v;
           k = Traits<T>::key(v);
           b = bucket_of<K>(k, base, shift, lut);
-          atomicAdd(&hist[b], 1u);
+          atomicAdd(&hist[SWZ ? bank_swz(b) : b], 1u);
         }
         if (SPEC) cand_put_warp<K>(cr, k, valid && cr.keep(b), cl, wtab);
       }
@@ -1126,9 +1137,12 @@ __device__ __forceinline__ void hist_dispatch(const T *__restrict__ x, uint64_t 
   // counter cost no more than lanes adding to different ones, so the warp
   // aggregation that compaction uses (h.heavy) only slows this pass down
   // (measured at 2^26: two-valued, constant and sorted inputs 74 -> 55 us).
-  (void)h;
-  hist_body<T, UNROLL, false, INGEST, SPEC>(x, n, hist, lut, h.base, h.shift, copy_to, cr,
-                                            wcount, wtab);
+  if (h.dup)
+    hist_body<T, UNROLL, false, INGEST, SPEC, true>(x, n, hist, lut, h.base, h.shift, copy_to,
+                                                    cr, wcount, wtab);
+  else
+    hist_body<T, UNROLL, false, INGEST, SPEC, false>(x, n, hist, lut, h.base, h.shift, copy_to,
+                                                     cr, wcount, wtab);
 }
 
 // copy_to == nullptr: x is the device vector.  Otherwise x is a mapped host
@@ -1155,7 +1169,8 @@ __global__ void __launch_bounds__(1024, 1)
   if (ctrl->status & ST_FATAL) return;
   const LutHeader<K> h = *hdr;
   for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
-  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) hist[b] = 0;
+  const uint32_t span = min(bank_span(h.nb), nb_max);
+  for (uint32_t b = threadIdx.x; b < span; b += blockDim.x) hist[b] = 0;
   __syncthreads();
   const bool spec = cand != nullptr && h.spec != 0;
   const uint32_t warp = threadIdx.x >> 5;
@@ -1181,7 +1196,8 @@ __global__ void __launch_bounds__(1024, 1)
   }
   __syncthreads();
   uint32_t *row = partials + (uint64_t)blockIdx.x * nb_max;
-  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) row[b] = hist[b];
+  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x)
+    row[b] = hist[h.dup ? bank_swz(b) : b];
   if (spec) {
     if (threadIdx.x < kCandWarps)
       cand_cnt[(uint64_t)blockIdx.x * kCandWarps + threadIdx.x] = s_wcnt[threadIdx.x];
