@@ -1035,7 +1035,7 @@ __device__ __forceinline__ void cand_put_warp(const CandPool<K> &cp, K k, bool k
 // device copy that the later passes read.  copy_to has the same alignment
 // modulo 16 bytes as x.  SPEC: keys of the kept buckets also go to the warp's
 // candidate list (cand_put_warp).
-template <class T, int UNROLL, bool HEAVY, bool INGEST, bool SPEC, bool SWZ>
+template <class T, int UNROLL, bool INGEST, bool SPEC, bool SWZ>
 __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, uint32_t *hist,
                                           const uint32_t *lut, typename Traits<T>::K base,
                                           uint32_t shift, T *__restrict__ copy_to,
@@ -1073,7 +1073,7 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
 #pragma unroll
       for (int e = 0; e < PV; ++e) {
         b[e] = bucket_of<K>(k[e], base, shift, lut);
-        hist_add<HEAVY>(hist, SWZ ? bank_swz(b[e]) : b[e]);
+        atomicAdd(&hist[SWZ ? bank_swz(b[e]) : b[e]], 1u);
         if (SPEC) any |= cr.keep(b[e]);
       }
       // one vote per vector; the per-key votes only when a lane keeps one
@@ -1138,11 +1138,11 @@ __device__ __forceinline__ void hist_dispatch(const T *__restrict__ x, uint64_t 
   // aggregation that compaction uses (h.heavy) only slows this pass down
   // (measured at 2^26: two-valued, constant and sorted inputs 74 -> 55 us).
   if (h.dup)
-    hist_body<T, UNROLL, false, INGEST, SPEC, true>(x, n, hist, lut, h.base, h.shift, copy_to,
-                                                    cr, wcount, wtab);
+    hist_body<T, UNROLL, INGEST, SPEC, true>(x, n, hist, lut, h.base, h.shift, copy_to, cr,
+                                             wcount, wtab);
   else
-    hist_body<T, UNROLL, false, INGEST, SPEC, false>(x, n, hist, lut, h.base, h.shift, copy_to,
-                                                     cr, wcount, wtab);
+    hist_body<T, UNROLL, INGEST, SPEC, false>(x, n, hist, lut, h.base, h.shift, copy_to, cr,
+                                              wcount, wtab);
 }
 
 // copy_to == nullptr: x is the device vector.  Otherwise x is a mapped host
