@@ -456,17 +456,11 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
             }
           }
         });
-      } else if (H.heavy) {
-        for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool full) {
-          uint32_t b = bucket_of_sw<K>(k, base, shift, lut, nsl);
-          if (!BCHECK(b < H.nb, 3, b, H.nb)) b = 0;
-          b = swz(b);
-          if (full)
-            hist_add<true>(hist, b);
-          else
-            atomicAdd(&hist[b], 1u);
-        });
       } else {
+        // also for heavy problems: the histogram's atomics return nothing, and
+        // lanes adding to one counter cost no more than lanes adding to
+        // different ones, so warp aggregation (compaction's) would only slow
+        // this phase down
         for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
           const uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
           if (!BCHECK(ub < H.nb, 4, ub, H.nb)) return;
@@ -759,12 +753,38 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       const uint32_t cap = (uint32_t)(room < (uint64_t)kInactive ? room : kInactive);
       const K base = (K)H.base;
       const uint32_t shift = H.shift;
-      for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
-        uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
-        if (!BCHECK(ub < H.nb, 9, ub, H.nb)) return;
-        const uint32_t pos = atomicAdd(&cursor[swz(ub)], 1u);
-        st_global_if(sp + pos, k, pos < cap);
-      });
+      if (H.heavy) {
+        // Sorted runs and few distinct keys: the cursor atomics return
+        // positions, which lanes of one address receive one at a time, so
+        // lanes of a warp sharing a bucket take one atomic (match.any) and
+        // consecutive positions.  A key whose bucket fails the check (the call
+        // is then failed) stays in the vote under bucket 0 but is not stored.
+        for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool full) {
+          uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
+          const bool ok = BCHECK(ub < H.nb, 9, ub, H.nb);
+          if (!ok) ub = 0;
+          uint32_t pos;
+          if (full) {
+            const uint32_t peers = __match_any_sync(0xffffffffu, ub);
+            const uint32_t lane = threadIdx.x & 31;
+            const int leader = __ffs(peers) - 1;
+            uint32_t p0 = 0;
+            if ((int)lane == leader) p0 = atomicAdd(&cursor[swz(ub)], (uint32_t)__popc(peers));
+            p0 = __shfl_sync(peers, p0, leader);
+            pos = p0 + __popc(peers & ((1u << lane) - 1u));
+          } else {
+            pos = atomicAdd(&cursor[swz(ub)], 1u);
+          }
+          st_global_if(sp + pos, k, ok && pos < cap);
+        });
+      } else {
+        for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
+          uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
+          if (!BCHECK(ub < H.nb, 9, ub, H.nb)) return;
+          const uint32_t pos = atomicAdd(&cursor[swz(ub)], 1u);
+          st_global_if(sp + pos, k, pos < cap);
+        });
+      }
       __syncthreads();
       // each cursor must end where the tile's share of the segment ends
       for (uint32_t s = tid; s < H.num_slots; s += nt) {
