@@ -45,7 +45,6 @@ constexpr uint64_t kBMinTile = 1u << 16;  // smallest tile the host picks for a 
 constexpr int kBColBatch = 4;  // tile rows per lane and load step of the plan phase's single-key scan
 constexpr uint32_t kBWarpBytes = 2048;  // shared memory of one warp-finisher buffer
 constexpr uint32_t kBRepBytes = 32768;  // per-bucket first keys of a tile (dup problems)
-constexpr uint32_t kMixed = 0x80000000u;  // tile row: the bucket holds more than one key
 // slots whose request counters fit in the plan phase's spare shared memory
 // (after the table, the bucket prefix and the flags: 81936 - 57360 bytes)
 constexpr uint32_t kBPlanSlots = 3072;

@@ -70,6 +70,14 @@ constexpr uint32_t kMaxNb = 32768;  // buckets of one vector: shared-memory hist
 constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
 constexpr uint32_t kInactive = 0x80000000u;  // compaction cursor of an inactive bucket
 constexpr int kSpinLimit = 1 << 22;              // bounded device-side waits
+constexpr uint32_t kMixed = 0x80000000u;  // count word: the bucket holds more than one key
+// Buckets of a table that tracks single-key buckets in the histogram pass:
+// its counts and first keys share the shared memory of nb_max counts.  0: no
+// tracking (the splitter table needs more than 4098 buckets to be feasible).
+template <class K>
+__host__ __device__ constexpr uint32_t dup_nb_cap(uint32_t nb_max) {
+  return nb_max / (sizeof(K) == 4 ? 2u : 4u) >= 8192u ? nb_max / (sizeof(K) == 4 ? 2u : 4u) : 0u;
+}
 constexpr uint32_t kCandWarps = 32;  // warps of a histogram / compaction CTA (1024 threads)
 constexpr uint32_t kCandChunk = 256;          // candidate keys per pool chunk
 constexpr uint32_t kCandChunksPerWarp = 64;   // chunks one warp's list can hold
@@ -514,7 +522,7 @@ template <class K, int SPT, bool SMEM>
 __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint32_t nb_max,
                               uint32_t *lut, LutHeader<K> *hdr, int nsl_bits = kLutIdxBits,
                               uint32_t *pre_cnt = nullptr, int64_t pre_same_key = -1,
-                              const SpecArgs *sp = nullptr) {
+                              const SpecArgs *sp = nullptr, uint32_t dup_cap = 0) {
   __shared__ uint32_t cnt[kLutIdx];
   __shared__ uint32_t lch[36];  // [0, 33): slices by ceil(log2 c); [34]: empty-run starts
   __shared__ uint32_t red32[33];
@@ -523,6 +531,13 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
   __shared__ uint32_t s_cost[34];
   const uint32_t tid = threadIdx.x;
   const uint32_t nsl = 1u << nsl_bits;
+  // A caller that tracks single-key buckets (dup_cap) needs at most dup_cap
+  // buckets when keys repeat often; the counted far-apart pairs tell that
+  // before the table exists (with nb_max >= the final bucket count, this test
+  // holds whenever the table's dup flag will).
+  if (dup_cap && pre_same_key >= 0 && S >= 256 &&
+      (uint64_t)pre_same_key * nb_max >= (S / 2 < 4096u ? S / 2 : 4096u) && nb_max > dup_cap)
+    nb_max = dup_cap;
   const int bl = bitlen<K>(kmax - kmin);
   const uint32_t shift = bl > nsl_bits ? (uint32_t)(bl - nsl_bits) : 0u;
   const int bcap = (int)(shift < (uint32_t)kMaxSubBits ? shift : (uint32_t)kMaxSubBits);
@@ -919,7 +934,7 @@ __global__ void __launch_bounds__(1024) k_lut(const K *__restrict__ samples, uin
 
   const SpecArgs sa{ctrl, n, cand_cap, G};
   build_lut_cta<K, 4, false>(samples, S, kmin, kmax, nb_max, lut, hdr, kLutIdxBits, slice_cnt,
-                             (int64_t)__ldcg(&ctrl->same_key), &sa);
+                             (int64_t)__ldcg(&ctrl->same_key), &sa, dup_nb_cap<K>(nb_max));
   if (tid == 0) {
     ctrl->nb = hdr->nb;
     ctrl->spec_on = hdr->spec != 0 ? 1u : 0u;
@@ -951,6 +966,23 @@ __device__ __forceinline__ Span<T> split_span(const T *x, uint64_t n) {
   return s;
 }
 
+// Atomics on order-preserving keys in shared memory.
+__device__ __forceinline__ uint32_t atomic_cas_key(uint32_t *p, uint32_t cmp, uint32_t v) {
+  return atomicCAS(p, cmp, v);
+}
+__device__ __forceinline__ uint64_t atomic_cas_key(uint64_t *p, uint64_t cmp, uint64_t v) {
+  return atomicCAS(reinterpret_cast<unsigned long long *>(p), (unsigned long long)cmp,
+                   (unsigned long long)v);
+}
+__device__ __forceinline__ void atomic_min_key(uint32_t *p, uint32_t v) { atomicMin(p, v); }
+__device__ __forceinline__ void atomic_max_key(uint32_t *p, uint32_t v) { atomicMax(p, v); }
+__device__ __forceinline__ void atomic_min_key(uint64_t *p, uint64_t v) {
+  atomicMin(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
+}
+__device__ __forceinline__ void atomic_max_key(uint64_t *p, uint64_t v) {
+  atomicMax(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
+}
+
 // Shared-memory position of bucket b in the histogram of a table whose keys
 // repeat often (LutHeader::dup): the low five bits XOR the next five (a
 // permutation inside every block of 1024 buckets), so that buckets at
@@ -961,6 +993,22 @@ __device__ __forceinline__ Span<T> split_span(const T *x, uint64_t n) {
 __device__ __forceinline__ uint32_t bank_swz(uint32_t b) { return b ^ ((b >> 5) & 31u); }
 // buckets [0, nb) occupy positions [0, bank_span(nb)) once swizzled
 __device__ __forceinline__ uint32_t bank_span(uint32_t nb) { return (nb + 1023u) & ~1023u; }
+
+// Single-key tracking (a table whose keys repeat often): rep[i] keeps the
+// first key counted at position i (KeyMax: none yet); a second distinct key --
+// or the largest key, which marks an empty entry -- sets kMixed in the count.
+template <class K>
+__device__ __forceinline__ void track_key(uint32_t *hist, K *rep, uint32_t i, K k) {
+  const K r = rep[i];
+  if (r != k || k == KeyMax<K>::v) {
+    if (k != KeyMax<K>::v && r == KeyMax<K>::v) {
+      const K old = atomic_cas_key(&rep[i], KeyMax<K>::v, k);
+      if (old != KeyMax<K>::v && old != k) atomicOr(&hist[i], kMixed);
+    } else if (!(hist[i] & kMixed)) {
+      atomicOr(&hist[i], kMixed);
+    }
+  }
+}
 
 template <bool HEAVY>
 __device__ __forceinline__ void hist_add(uint32_t *hist, uint32_t b) {
@@ -1034,13 +1082,15 @@ __device__ __forceinline__ void cand_put_warp(const CandPool<K> &cp, K k, bool k
 // memory read over NVLink-C2C); every tile is also written to copy_to, the
 // device copy that the later passes read.  copy_to has the same alignment
 // modulo 16 bytes as x.  SPEC: keys of the kept buckets also go to the warp's
-// candidate list (cand_put_warp).
+// candidate list (cand_put_warp).  SWZ: swizzled positions (bank_swz) and
+// single-key tracking in rep (track_key).
 template <class T, int UNROLL, bool INGEST, bool SPEC, bool SWZ>
 __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, uint32_t *hist,
                                           const uint32_t *lut, typename Traits<T>::K base,
                                           uint32_t shift, T *__restrict__ copy_to,
                                           const CandPool<typename Traits<T>::K> &cr,
-                                          uint32_t *wcount, uint32_t *wtab) {
+                                          uint32_t *wcount, uint32_t *wtab,
+                                          typename Traits<T>::K *rep) {
   using K = typename Traits<T>::K;
   using V = typename Traits<T>::Vec;
   constexpr int PV = Traits<T>::kPerVec;
@@ -1073,7 +1123,9 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
 #pragma unroll
       for (int e = 0; e < PV; ++e) {
         b[e] = bucket_of<K>(k[e], base, shift, lut);
-        atomicAdd(&hist[SWZ ? bank_swz(b[e]) : b[e]], 1u);
+        const uint32_t i = SWZ ? bank_swz(b[e]) : b[e];
+        atomicAdd(&hist[i], 1u);
+        if (SWZ) track_key<K>(hist, rep, i, k[e]);
         if (SPEC) any |= cr.keep(b[e]);
       }
       // one vote per vector; the per-key votes only when a lane keeps one
@@ -1100,7 +1152,11 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
 #pragma unroll
       for (int e = 0; e < PV; ++e) {
         const uint32_t b = valid ? bucket_of<K>(k[e], base, shift, lut) : 0u;
-        if (valid) atomicAdd(&hist[SWZ ? bank_swz(b) : b], 1u);
+        if (valid) {
+          const uint32_t i = SWZ ? bank_swz(b) : b;
+          atomicAdd(&hist[i], 1u);
+          if (SWZ) track_key<K>(hist, rep, i, k[e]);
+        }
         if (SPEC) cand_put_warp<K>(cr, k[e], valid && cr.keep(b), cl, wtab);
       }
     }
@@ -1115,7 +1171,9 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
           if (INGEST) copy_to[e] = v;
           k = Traits<T>::key(v);
           b = bucket_of<K>(k, base, shift, lut);
-          atomicAdd(&hist[SWZ ? bank_swz(b) : b], 1u);
+          const uint32_t i = SWZ ? bank_swz(b) : b;
+          atomicAdd(&hist[i], 1u);
+          if (SWZ) track_key<K>(hist, rep, i, k);
         }
         if (SPEC) cand_put_warp<K>(cr, k, valid && cr.keep(b), cl, wtab);
       }
@@ -1132,17 +1190,19 @@ __device__ __forceinline__ void hist_dispatch(const T *__restrict__ x, uint64_t 
                                               const LutHeader<typename Traits<T>::K> &h,
                                               T *__restrict__ copy_to,
                                               const CandPool<typename Traits<T>::K> &cr,
-                                              uint32_t *wcount, uint32_t *wtab) {
+                                              uint32_t *wcount, uint32_t *wtab,
+                                              typename Traits<T>::K *rep) {
   // The histogram's atomics return nothing; lanes of a warp adding to one
   // counter cost no more than lanes adding to different ones, so the warp
   // aggregation that compaction uses (h.heavy) only slows this pass down
   // (measured at 2^26: two-valued, constant and sorted inputs 74 -> 55 us).
-  if (h.dup)
+  // rep: single-key tracking (and swizzled positions), see k_hist.
+  if (rep)
     hist_body<T, UNROLL, INGEST, SPEC, true>(x, n, hist, lut, h.base, h.shift, copy_to, cr,
-                                             wcount, wtab);
+                                             wcount, wtab, rep);
   else
     hist_body<T, UNROLL, INGEST, SPEC, false>(x, n, hist, lut, h.base, h.shift, copy_to, cr,
-                                              wcount, wtab);
+                                              wcount, wtab, nullptr);
 }
 
 // copy_to == nullptr: x is the device vector.  Otherwise x is a mapped host
@@ -1151,14 +1211,19 @@ __device__ __forceinline__ void hist_dispatch(const T *__restrict__ x, uint64_t 
 // buckets, warp w of CTA c lists its candidates in pool chunks and leaves its
 // count in cand_cnt[c * kCandWarps + w] and its chunk table in
 // cand_tab[(c * kCandWarps + w) * kCandChunksPerWarp ...); cand_next counts
-// the chunks handed out (zero on entry).
+// the chunks handed out (zero on entry).  reps (nullptr: none): when the
+// table's keys repeat often and it has at most dup_nb_cap(nb_max) buckets, the
+// CTA also tracks each bucket's key (the first dup_nb_cap counts of the shared
+// histogram are followed by as many keys) and writes its row of keys to
+// reps[c * nb_max ...), with kMixed in the row's count where a bucket held
+// more than one key.
 template <class T, int UNROLL>
 __global__ void __launch_bounds__(1024, 1)
     k_hist(const T *__restrict__ x, uint64_t n, const LutHeader<typename Traits<T>::K> *hdr,
            const uint32_t *__restrict__ lut_g, uint32_t *__restrict__ partials, uint32_t nb_max,
            const Ctrl *ctrl, T *__restrict__ copy_to, typename Traits<T>::K *__restrict__ cand,
            uint32_t *__restrict__ cand_cnt, uint32_t *__restrict__ cand_tab,
-           uint32_t *cand_next) {
+           uint32_t *cand_next, typename Traits<T>::K *__restrict__ reps) {
   pdl_start();
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
@@ -1169,8 +1234,14 @@ __global__ void __launch_bounds__(1024, 1)
   if (ctrl->status & ST_FATAL) return;
   const LutHeader<K> h = *hdr;
   for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
+  const uint32_t dcap = dup_nb_cap<K>(nb_max);
+  const bool track = reps != nullptr && h.dup && dcap != 0 && h.nb <= dcap;
+  K *rep = track ? reinterpret_cast<K *>(hist + dcap) : nullptr;
   const uint32_t span = min(bank_span(h.nb), nb_max);
-  for (uint32_t b = threadIdx.x; b < span; b += blockDim.x) hist[b] = 0;
+  for (uint32_t b = threadIdx.x; b < span; b += blockDim.x) {
+    hist[b] = 0;
+    if (track) rep[b] = KeyMax<K>::v;
+  }
   __syncthreads();
   const bool spec = cand != nullptr && h.spec != 0;
   const uint32_t warp = threadIdx.x >> 5;
@@ -1185,19 +1256,22 @@ __global__ void __launch_bounds__(1024, 1)
   uint32_t *wc = s_wcnt + warp, *wt = s_tab + warp * kCandChunksPerWarp;
   if (copy_to) {
     if (spec)
-      hist_dispatch<T, UNROLL, true, true>(x, n, hist, lut, h, copy_to, cr, wc, wt);
+      hist_dispatch<T, UNROLL, true, true>(x, n, hist, lut, h, copy_to, cr, wc, wt, rep);
     else
-      hist_dispatch<T, UNROLL, true, false>(x, n, hist, lut, h, copy_to, cr, wc, wt);
+      hist_dispatch<T, UNROLL, true, false>(x, n, hist, lut, h, copy_to, cr, wc, wt, rep);
   } else {
     if (spec)
-      hist_dispatch<T, UNROLL, false, true>(x, n, hist, lut, h, nullptr, cr, wc, wt);
+      hist_dispatch<T, UNROLL, false, true>(x, n, hist, lut, h, nullptr, cr, wc, wt, rep);
     else
-      hist_dispatch<T, UNROLL, false, false>(x, n, hist, lut, h, nullptr, cr, wc, wt);
+      hist_dispatch<T, UNROLL, false, false>(x, n, hist, lut, h, nullptr, cr, wc, wt, rep);
   }
   __syncthreads();
   uint32_t *row = partials + (uint64_t)blockIdx.x * nb_max;
-  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x)
-    row[b] = hist[h.dup ? bank_swz(b) : b];
+  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) {
+    const uint32_t i = track ? bank_swz(b) : b;
+    row[b] = hist[i];
+    if (track) reps[(uint64_t)blockIdx.x * nb_max + b] = rep[i];
+  }
   if (spec) {
     if (threadIdx.x < kCandWarps)
       cand_cnt[(uint64_t)blockIdx.x * kCandWarps + threadIdx.x] = s_wcnt[threadIdx.x];
@@ -1219,24 +1293,30 @@ constexpr int kScanThreads = 256;
 constexpr int kScanTile = 64;  // buckets per CTA
 
 // 16 lanes read a row's 64 buckets of the tile as 16-byte vectors, and the
-// CTA's 16 groups of 16 lanes split the rows between them (at most 12 rows per
-// thread at once: one round of loads for 152 rows).  The rows are read once;
+// CTA's 16 groups of 16 lanes split the rows between them (8 rows per thread
+// at once: two rounds of loads for 152 rows; a tracking table reads the rows
+// again for the buckets' keys).  The rows are read once;
 // compaction later takes each CTA's share of a bucket's segment from its own
 // row.
 template <class K>
-__global__ void __launch_bounds__(kScanThreads)
+__global__ void __launch_bounds__(kScanThreads, 4)
     k_colsum(const uint32_t *__restrict__ partials, uint32_t rows, uint32_t nb_max,
              const LutHeader<K> *hdr, uint32_t *__restrict__ bpre, uint32_t *__restrict__ ttot,
-             const Ctrl *ctrl) {
+             const Ctrl *ctrl, const K *__restrict__ reps, uint32_t *__restrict__ bsingle,
+             K *__restrict__ bkey) {
   pdl_start();
   constexpr uint32_t kVecs = kScanTile / 4;              // 16-byte vectors per tile row
   constexpr uint32_t kGroups = kScanThreads / kVecs;     // row groups
-  constexpr uint32_t kBatch = 12;                        // loads in flight per thread
+  constexpr uint32_t kBatch = 8;                         // loads in flight per thread
   __shared__ uint32_t gsum[kGroups][kScanTile];
   __shared__ uint32_t s_w2[2];
+  __shared__ uint8_t gstate[kGroups][kScanTile];  // single-key tracking: 0 none, 1 one key, 2 more
+  __shared__ K gkey[kGroups][kScanTile];
   if (ctrl->status & ST_FATAL) return;
   const uint32_t nb = hdr->nb;
   if ((uint64_t)blockIdx.x * kScanTile >= nb) return;
+  const uint32_t dcap = dup_nb_cap<K>(nb_max);
+  const bool track = reps != nullptr && hdr->dup && dcap != 0 && nb <= dcap;
   // thread t sums buckets 4 (t % kVecs) .. + 3 of the tile over row group
   // t / kVecs: a row's 64 buckets are one 256-byte span read by 16 lanes
   const uint32_t v = threadIdx.x % kVecs, grp = threadIdx.x / kVecs;
@@ -1254,10 +1334,36 @@ __global__ void __launch_bounds__(kScanThreads)
         e[q] = r + q < r1 ? __ldcg(p + (uint64_t)(r + q) * row4) : make_uint4(0, 0, 0, 0);
 #pragma unroll
       for (uint32_t q = 0; q < kBatch; ++q) {
-        gs.x += e[q].x;
-        gs.y += e[q].y;
-        gs.z += e[q].z;
-        gs.w += e[q].w;
+        gs.x += e[q].x & ~kMixed;
+        gs.y += e[q].y & ~kMixed;
+        gs.z += e[q].z & ~kMixed;
+        gs.w += e[q].w & ~kMixed;
+      }
+    }
+  }
+  // single-key tracking of the four buckets (a second pass over the rows, in
+  // tracking tables only): per row with keys in a bucket, its key or "more
+  // than one"
+  uint32_t st[4] = {0, 0, 0, 0};  // 0 none, 1 one key (key), 2 more
+  K key[4] = {0, 0, 0, 0};
+  if (track && b0 < nb) {
+    for (uint32_t r = r0; r < r1; ++r) {
+      const uint4 e = __ldcg(p + (uint64_t)r * row4);
+      const uint32_t c4[4] = {e.x, e.y, e.z, e.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (!(c4[j] & ~kMixed)) continue;
+        if (c4[j] & kMixed) {
+          st[j] = 2;
+        } else if (st[j] != 2) {
+          const K rk = __ldcg(reps + (uint64_t)r * nb_max + b0 + j);
+          if (st[j] == 0) {
+            st[j] = 1;
+            key[j] = rk;
+          } else if (rk != key[j]) {
+            st[j] = 2;
+          }
+        }
       }
     }
   }
@@ -1266,6 +1372,13 @@ __global__ void __launch_bounds__(kScanThreads)
   gsum[grp][4 * v + 1] = b0 + 1 < nb ? gs.y : 0u;
   gsum[grp][4 * v + 2] = b0 + 2 < nb ? gs.z : 0u;
   gsum[grp][4 * v + 3] = b0 + 3 < nb ? gs.w : 0u;
+  if (track) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      gstate[grp][4 * v + j] = (uint8_t)st[j];
+      gkey[grp][4 * v + j] = key[j];
+    }
+  }
   __syncthreads();
   // the tile's kScanTile buckets (two warps) -> their exclusive prefix inside
   // the tile, and the tile's total
@@ -1282,6 +1395,22 @@ __global__ void __launch_bounds__(kScanThreads)
     const uint32_t b = blockIdx.x * kScanTile + col;
     if (b < nb) bpre[b] = incl - c + (col >= 32 ? s_w2[0] : 0u);
     if (col == 0) ttot[blockIdx.x] = s_w2[0] + s_w2[1];
+    if (track && b < nb) {
+      // one key in the whole vector: every row group saw none or the same one
+      uint32_t s1 = 0;
+      K k1 = 0;
+#pragma unroll
+      for (uint32_t g = 0; g < kGroups; ++g) {
+        const uint32_t sg = gstate[g][col];
+        if (sg == 2 || (sg == 1 && s1 == 1 && gkey[g][col] != k1)) s1 = 2;
+        else if (sg == 1 && s1 == 0) {
+          s1 = 1;
+          k1 = gkey[g][col];
+        }
+      }
+      bsingle[b] = s1 == 1 ? 1u : 0u;
+      bkey[b] = k1;
+    }
   }
 }
 static_assert(kScanTile == 64, "k_colsum's tile prefix covers two warps");
@@ -1562,7 +1691,8 @@ __global__ void __launch_bounds__(1024, 1)
            typename Traits<InT>::K *__restrict__ seg_lo,
            typename Traits<InT>::K *__restrict__ seg_hi, uint32_t *__restrict__ req_bucket,
            uint32_t *__restrict__ req_local, Req *__restrict__ klist, uint64_t surv_cap,
-           Premap pm) {
+           Premap pm, const uint32_t *__restrict__ bsingle = nullptr,
+           const typename Traits<InT>::K *__restrict__ bkey = nullptr) {
   // The requests are complete before the call's first kernel (uploaded, made
   // by a kernel the plainly launched sample kernel waits for, or left by an
   // earlier call): with at most one per thread, each thread loads its own
@@ -1722,6 +1852,8 @@ __global__ void __launch_bounds__(1024, 1)
   const uint32_t sper = (tot_slots + nt - 1) / nt;
   const uint32_t s0 = min(tot_slots, tid * sper), s1 = min(tot_slots, s0 + sper);
   uint64_t my_surv = 0;
+  const uint32_t dcap = dup_nb_cap<K>(nb_max);
+  const bool dtrack = bsingle != nullptr && bkey != nullptr && h.dup && dcap != 0 && nb <= dcap;
   for (uint32_t q = s0; q < s1; ++q) {
     const uint32_t b = segb_smem ? s_segb[q] : __ldcg(seg_bucket + q);
     const K klo = bucket_lo<K>(b, h.base, h.shift, lut);
@@ -1730,10 +1862,14 @@ __global__ void __launch_bounds__(1024, 1)
     // top entry's bucket can wrap past the key width, and then bucket b runs
     // up to the largest key
     const bool single = (knext > klo) ? (knext - klo == K(1)) : (klo == KeyMax<K>::v);
-    const uint32_t cb = single ? 0u : (uint32_t)((b + 1 < nb ? excl[b + 1] : n) - excl[b]);
+    // a wider bucket that the histogram pass saw holding one key (k_colsum)
+    const bool one = !single && dtrack && __ldcg(bsingle + b) != 0u;
+    const uint32_t cb =
+        (single || one) ? 0u : (uint32_t)((b + 1 < nb ? excl[b + 1] : n) - excl[b]);
+    const K flat_key = one ? __ldcg(bkey + b) : klo;
     seg_size[q] = cb;  // 0 marks a flat slot
-    seg_lo[q] = klo;
-    seg_hi[q] = single ? klo : (knext > klo ? knext - K(1) : KeyMax<K>::v);
+    seg_lo[q] = flat_key;
+    seg_hi[q] = (single || one) ? flat_key : (knext > klo ? knext - K(1) : KeyMax<K>::v);
     kcnt[q] = pm.bits ? __ldcg(pm.bcount + b) : 0u;  // premapped: the bucket's request count
     kcur[q] = 0;
     fill[q] = 0;
@@ -2009,7 +2145,7 @@ __global__ void __launch_bounds__(1024, 1)
     const uint32_t sz = seg_size[s];
     if (sz == 0) continue;
     const uint32_t b = seg_bucket[s];
-    const uint32_t cnt = row[b];
+    const uint32_t cnt = row[b] & ~kMixed;
     const uint32_t pre = cnt ? atomicAdd(fill + s, cnt) : 0u;
     const uint32_t at = (uint32_t)(seg_off[s] + pre);
     cursor[b] = at;
@@ -2065,22 +2201,6 @@ template <class K>
 __host__ __device__ constexpr size_t finish_smem_for(uint32_t bcap) {
   return 5 * kFinBins * sizeof(uint32_t) + (size_t)bcap * sizeof(K) * 3 / 2 +
          2 * kFinBins * sizeof(K);
-}
-
-__device__ __forceinline__ uint32_t atomic_cas_key(uint32_t *p, uint32_t cmp, uint32_t v) {
-  return atomicCAS(p, cmp, v);
-}
-__device__ __forceinline__ uint64_t atomic_cas_key(uint64_t *p, uint64_t cmp, uint64_t v) {
-  return atomicCAS(reinterpret_cast<unsigned long long *>(p), (unsigned long long)cmp,
-                   (unsigned long long)v);
-}
-__device__ __forceinline__ void atomic_min_key(uint32_t *p, uint32_t v) { atomicMin(p, v); }
-__device__ __forceinline__ void atomic_max_key(uint32_t *p, uint32_t v) { atomicMax(p, v); }
-__device__ __forceinline__ void atomic_min_key(uint64_t *p, uint64_t v) {
-  atomicMin(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
-}
-__device__ __forceinline__ void atomic_max_key(uint64_t *p, uint64_t v) {
-  atomicMax(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
 }
 
 template <class K>

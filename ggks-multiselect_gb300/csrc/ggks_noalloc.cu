@@ -167,9 +167,11 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kNaNbMax * 4);
     set_smem_max<k_hist<float, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
     k_hist<float, UNROLL><<<G, 1024, smem, s>>>(d_vec, n, hdr, lut, partials, kNaNbMax, ctrl,
-                                                nullptr, nullptr, nullptr, nullptr, nullptr);
+                                                nullptr, nullptr, nullptr, nullptr, nullptr,
+                                                nullptr);
   }
-  k_colsum<K><<<col_tiles, kScanThreads, 0, s>>>(partials, G, kNaNbMax, hdr, bpre, ttot, ctrl);
+  k_colsum<K><<<col_tiles, kScanThreads, 0, s>>>(partials, G, kNaNbMax, hdr, bpre, ttot, ctrl,
+                                                  nullptr, nullptr, nullptr);
   {
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kNaNbMax * 5);
     set_smem_max<k_plan<float, float>>(kPlanSmemMax);

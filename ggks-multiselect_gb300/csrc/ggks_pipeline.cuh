@@ -51,7 +51,8 @@ struct Plan {
   size_t out = 0, ctrl = 0, reqs = 0, hdr = 0, lut = 0, samples = 0, partials = 0,
          bpre = 0, ttot = 0, seg_bucket = 0, seg_off = 0, seg_size = 0, kstart = 0, kcnt = 0, fill = 0,
          kcur = 0, seg_lo = 0, seg_hi = 0, deferred = 0, req_bucket = 0, req_local = 0, klist = 0,
-         pm_bits = 0, pm_bcount = 0, pm_bslot = 0, cand_cnt = 0, cand_tab = 0, total = 0;
+         pm_bits = 0, pm_bcount = 0, pm_bslot = 0, cand_cnt = 0, cand_tab = 0, reps = 0,
+         bsingle = 0, bkey = 0, total = 0;
   // speculative compaction: the candidate pool is the survivor buffer from
   // surv_half on, cand_chunks chunks of kCandChunk keys
   uint64_t surv_half = 0;
@@ -145,6 +146,11 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   arr(p.pm_bslot, p.nb_max, 4);
   arr(p.cand_cnt, (size_t)p.G * kCandWarps, 4);
   arr(p.cand_tab, (size_t)p.G * kCandWarps * kCandChunksPerWarp, 4);
+  // single-key tracking of tables whose keys repeat often: each CTA's key per
+  // bucket, and per bucket whether the vector holds one key there and which
+  arr(p.reps, (size_t)p.G * p.nb_max, sizeof(K));
+  arr(p.bsingle, p.nb_max, 4);
+  arr(p.bkey, p.nb_max, sizeof(K));
   p.total = o;
   return p;
 }
@@ -285,6 +291,9 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   K *cand = surv + p.surv_half;
   uint32_t *cand_cnt = reinterpret_cast<uint32_t *>(A + p.cand_cnt);
   uint32_t *cand_tab = reinterpret_cast<uint32_t *>(A + p.cand_tab);
+  K *reps = reinterpret_cast<K *>(A + p.reps);
+  uint32_t *bsingle = reinterpret_cast<uint32_t *>(A + p.bsingle);
+  K *bkey = reinterpret_cast<K *>(A + p.bkey);
   OutT *d_out = d_out_user ? d_out_user : reinterpret_cast<OutT *>(A + p.out);
   const bool out_in_arena = d_out_user == nullptr;
 
@@ -345,14 +354,14 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     // with a mapped host vector, this pass also writes the device copy d_in
     L(launch(p.unroll8 ? k_hist<InT, 8> : k_hist<InT, 4>, p.G, 1024, smem, s, ingest ? ingest : d_in, n, hdr, lut, partials,
              p.nb_max, ctrl, ingest ? const_cast<InT *>(d_in) : nullptr, cand, cand_cnt, cand_tab,
-             &ctrl->cand_next));
+             &ctrl->cand_next, reps));
     ran[GGKS_PASS_HIST] = true;
   }
   // ---- (d) reduce + decoupled look-back scan
   {
     PassTimer t(ctx, s, GGKS_PASS_SCAN);
     L(launch(k_colsum<K>, p.scan_tiles, kScanThreads, 0, s, partials, p.G, p.nb_max, hdr, bpre,
-             ttot, ctrl));
+             ttot, ctrl, reps, bsingle, bkey));
     ran[GGKS_PASS_SCAN] = true;
   }
   // ---- (e) plan
@@ -381,7 +390,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     }
     L(launch(k_plan<InT, OutT>, 1, 1024, smem, s, hdr, lut, bpre, ttot, n, rq, num_req, p.nb_max,
              ctrl, seg_bucket, seg_off, seg_size, kstart, kcnt, kcur, fill, seg_lo, seg_hi,
-             req_bucket, req_local, klist, p.surv_cap, pm));
+             req_bucket, req_local, klist, p.surv_cap, pm, bsingle, bkey));
     if (premap) {
       L(launch(k_reqplace, (num_req + 1023) / 1024, 1024, 0, s, ctrl, rq, num_req, req_bucket,
                req_local, pm_bslot, kstart, kcur, klist));

@@ -160,6 +160,34 @@ def test_repeated_calls_one_context(g, orc):
     ctx.close()
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_single_key_buckets_tracked(g, orc, dtype):
+    """Integer-valued floats in [0, 256): every value's bucket spans many keys
+    but holds one.  The histogram pass tracks each bucket's key, so every
+    requested bucket is answered from its key and nothing is compacted.  A
+    second key 5 ulps from one value (inside the same bucket) must be seen as
+    a second key, and that bucket compacted and selected as usual."""
+    import ggks_problems as gp
+    n = 1 << 22 if dtype == np.float32 else 1 << 21
+    r = np.random.default_rng(17)
+    x = r.integers(0, 256, n).astype(dtype)
+    ks = gp.k_distinct(n, 1001, 5)
+    d = DeviceArray(x)
+    ctx = g.Context(0)
+    assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks, ctx=ctx), orc.multiselect(x, ks, 8),
+                "integer valued")
+    assert ctx.stats()["survivors"] == 0
+    y = x.copy()
+    pick = np.nonzero(y == 200)[0][::3]
+    y[pick] = np.nextafter(np.nextafter(np.nextafter(np.nextafter(np.nextafter(
+        y[pick], dtype(300)), dtype(300)), dtype(300)), dtype(300)), dtype(300))
+    d = DeviceArray(y)
+    ctx.reset_stats()
+    assert_same(g.multiselect_ptr(d.ptr, n, y.dtype, ks, ctx=ctx), orc.multiselect(y, ks, 8),
+                "integer valued, one bucket with two keys")
+    ctx.close()
+
+
 def test_fresh_context_while_default_stream_busy(g, orc):
     """A context's workspace is cleared when it is allocated.  The clearing
     must be ordered on the context's own (non-blocking) stream: issued to the
