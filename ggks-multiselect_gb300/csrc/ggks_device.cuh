@@ -983,13 +983,12 @@ __device__ __forceinline__ void atomic_max_key(uint64_t *p, uint64_t v) {
   atomicMax(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
 }
 
-// Shared-memory position of bucket b in the histogram of a table whose keys
-// repeat often (LutHeader::dup): the low five bits XOR the next five (a
-// permutation inside every block of 1024 buckets), so that buckets at
-// power-of-two strides -- integer-valued floats put theirs 512 apart -- do not
-// all fall into one bank (2^26 floats in [0, 256): 232 -> 79 us).  Other
-// tables keep plain positions: the two operations per key cost the histogram
-// of a constant or two-valued vector 10 %.
+// Shared-memory position of bucket b in the histogram of a table that tracks
+// single-key buckets (its keys repeat often, LutHeader::dup): the low five
+// bits XOR the next five (a permutation inside every block of 1024 buckets),
+// so that buckets at power-of-two strides -- integer-valued floats put theirs
+// 512 apart -- do not all fall into one bank (2^26 floats in [0, 256), counts
+// alone: 232 -> 79 us).  Other tables keep plain positions.
 __device__ __forceinline__ uint32_t bank_swz(uint32_t b) { return b ^ ((b >> 5) & 31u); }
 // buckets [0, nb) occupy positions [0, bank_span(nb)) once swizzled
 __device__ __forceinline__ uint32_t bank_span(uint32_t nb) { return (nb + 1023u) & ~1023u; }
