@@ -534,7 +534,10 @@ def run_batched(torch, ggks, gp, dev, sptr, count=4096):
     }
 
 
-SERVE_RATES = (1000, 5000, 20000, 50000)
+# 1k-50k requests/s is the serving configuration's range.  At 50k the trace
+# itself caps the served rate near 48k, so the ratio there is bounded by 50k over
+# the sequential rate; 100k, above the range, shows the server's capacity.
+SERVE_RATES = (1000, 5000, 20000, 50000, 100000)
 
 
 def run_served(torch, ggks, gp, dev, sptr, per_rate=4000):
