@@ -5,8 +5,10 @@
 Workload (one "step"): one exact multiselect of a resident 2^28-element float32
 vector drawn from normal(0,1) (seed 1) with 1001 distinct k's drawn uniformly
 from [1, n] -- the large single-multiselect configuration.  The other inputs of
-that configuration (Cauchy, half-normal, uint32, float64) are timed after the
-headline and reported under "variants".
+that configuration (Cauchy, half-normal, uint32, float64) and the top-k
+configuration (2^26 float32 uniform, uint32 over 2^16 values and an ascending
+float32 copy; K = 32, 1024, 65536) are timed after the headline and reported
+under "variants".
 
 Metric: input GB/s per multiselect = n * sizeof(T) / time of one wrapper call
 (k upload, all passes, result download, synchronisation).  "e2e" is the same
@@ -17,6 +19,10 @@ memory, so the host-to-device copy is inside every step.
 lengths in [2^10, 2^22] with 1-64 k's each -- selected by one batched call (one
 persistent launch), against 4096 sequential ggks_multiselect_f32 calls on the
 same vectors (requests/s, bit-exact comparison).
+
+"served": Poisson request streams at 1k-50k requests/s (and 100k, above that
+range, for the server's capacity) through a ggks_server against sequential
+plain calls (requests/s, p50/p99 latency, bit-exact comparison).
 
 Under torchrun (N > 1) every rank runs an independent replica on its own GPU
 (the path does not shard: replicas only); value = all ranks' bytes / max time.
