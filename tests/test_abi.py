@@ -172,3 +172,36 @@ def test_select_invalid_arguments_rejected_without_device(lib, sfx, dt):
     assert f(fake, 0, 1, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
     assert f(fake, 10, 0, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
     assert f(fake, 10, 11, out.ctypes.data, ctypes.byref(o)) == ggks.INVALID_ARG
+
+
+def test_python_structs_match_the_header(tmp_path):
+    """The ctypes mirrors in ggks.py have the sizes and field offsets of the
+    structs include/ggks.h declares (a C program compiled against the header
+    prints them; nothing is called)."""
+    import subprocess
+
+    import ggks
+    pairs = [("ggks_opts", ggks.Opts), ("ggks_stats", ggks.Stats),
+             ("ggks_server_config", ggks.ServerConfig), ("ggks_request", ggks.Request),
+             ("ggks_server_stats", ggks.ServerStats)]
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "ggks.h"', "int main(void) {"]
+    for cname, cls in pairs:
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c11", str(src), "-I", os.path.join(ROOT, "include"), "-o",
+                        str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n"):
+        if line:
+            name, field, val = line.split()
+            got[(name, field)] = int(val)
+    for cname, cls in pairs:
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
