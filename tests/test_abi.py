@@ -205,3 +205,62 @@ def test_python_structs_match_the_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(cls), cname
         for f, _ in cls._fields_:
             assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
+
+
+def test_rank_windows_host_logic(tmp_path):
+    """The host's rank windows for speculative compaction (set_windows in the
+    pipeline header), built into a host program with nvcc and run without a
+    device: one window over all ranks, two split at the widest gap for up to
+    64 requests, none when they span more than n / 16 ranks."""
+    import shutil
+    import subprocess
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    csrc = os.path.join(ROOT, "ggks-multiselect_gb300", "csrc")
+    src = tmp_path / "windows.cu"
+    src.write_text(r"""
+#include <cstdio>
+#include "ggks_pipeline.cuh"
+using namespace ggks;
+static void run(const char *name, const uint32_t *ranks, uint32_t m, uint64_t n) {
+  Ctrl c = {};
+  Req r[128];
+  for (uint32_t i = 0; i < m; ++i) { r[i].rank = ranks[i]; r[i].out = i; }
+  set_windows(&c, r, m, n);
+  printf("%s %u", name, c.spec_nwin);
+  for (uint32_t w = 0; w < c.spec_nwin; ++w)
+    printf(" %llu %llu", (unsigned long long)c.spec_lo[w], (unsigned long long)c.spec_hi[w]);
+  printf("\n");
+}
+int main() {
+  const uint64_t n = 1 << 20;
+  const uint32_t one[] = {5000};
+  const uint32_t ends[] = {3, 1, 2, 1048575, 1048570, 0};
+  const uint32_t close[] = {700000, 700010, 700005};
+  const uint32_t spread[] = {0, 524288, 1048575};
+  uint32_t many[100];
+  for (int i = 0; i < 100; ++i) many[i] = 900000 + 7 * i;
+  run("one", one, 1, n);
+  run("ends", ends, 6, n);
+  run("close", close, 3, n);
+  run("spread", spread, 3, n);
+  run("many", many, 100, n);
+  return 0;
+}
+""")
+    exe = tmp_path / "windows"
+    r = subprocess.run([nvcc, "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a",
+                        "-I", csrc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                               check=True).stdout.splitlines():
+        name, *vals = line.split()
+        out[name] = [int(v) for v in vals]
+    assert out["one"] == [1, 5000, 5000]
+    assert out["ends"] == [2, 0, 3, 1048570, 1048575]      # split at the widest gap
+    assert out["close"] == [2, 700000, 700000, 700005, 700010]  # equal gaps: the first
+    assert out["spread"] == [0]                              # spans more than n / 16
+    assert out["many"] == [1, 900000, 900000 + 7 * 99]      # > 64 requests: one window
