@@ -85,12 +85,29 @@ def measured_peak():
         return PEAK_FALLBACK_GBS, "fallback"
 
 
-def workload(log2n, seed=1):
+def workload(log2n):
+    """The headline input: the large configuration's float32 normal vector
+    (seed 1) with its 1001 distinct k's (seed 101)."""
     import ggks_problems as gp
+    return gp.config_l("f32_normal", log2n)
+
+
+def bench_config(log2n, ws):
+    """The workload's description, printed identically by both arms."""
     n = 1 << log2n
-    x = gp.normal_f32(n, seed)
-    k = gp.k_distinct(n, NUM_K, 100 + seed)
-    return x, k
+    return {"workload": f"multiselect n=2^{log2n} f32 normal(0,1) seed 1, "
+                        f"{NUM_K} distinct k's uniform in [1,n] (seed 101)",
+            "n": n, "num_k": NUM_K, "elem": "float32 (ordered as u32 keys)",
+            "parallelism": "replicas" if ws > 1 else "single GPU",
+            "l2": (f"input ({n * 4 >> 20} MiB) larger than L2 (129 MB); no flush needed"
+                   if n * 4 > 129 * 10**6 else
+                   f"input ({n * 4 >> 20} MiB) smaller than L2 (129 MB): not flushed")}
+
+
+def same_bits(a, b):
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    return a.dtype == b.dtype and a.shape == b.shape and bool(
+        np.array_equal(a.view(np.uint8), b.view(np.uint8)))
 
 
 # ---------------------------------------------------------------------------
@@ -206,9 +223,7 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(t * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"multiselect n=2^{args.log2n} f32 normal(0,1) seed 1, "
-                               f"{NUM_K} distinct k's", "n": int(x.size), "num_k": NUM_K,
-                   "parallelism": "replicas", "l2": "n/a (CPU)"},
+        "config": bench_config(args.log2n, ws),
         "cpu_baseline": {"value": round(gbs, 4), "unit": "GB/s", "cores": threads, "kind": "port",
                          "sample": f"full workload per step: sort-and-choose of all {x.size} "
                                    f"elements, {threads} threads (parallel LSD radix sort of keys)"},
@@ -223,19 +238,21 @@ def run_reference(args):
 # our arm
 # ---------------------------------------------------------------------------
 def cpu_baseline(x, k):
-    """Single-threaded sort-and-choose on a bounded sample of the workload."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    oracle.build()
+    """Single-threaded sort-and-choose with std::sort (the reference's own
+    oracle, multiselectTimingFunctions.cu:51-95, on the host) on a bounded
+    sample of the workload: the first 2^26 elements with the k list clipped to
+    that length."""
+    orc = oracle_mod()
     m = 1 << 26
     xs = x[:m]
     ks = np.clip(k, 1, m).astype(np.uint32)
     t0 = time.perf_counter()
-    oracle.multiselect(xs, ks, threads=1)
+    orc.multiselect_stdsort(xs, ks)
     dt = time.perf_counter() - t0
     return {"value": round(xs.nbytes / dt / 1e9, 4), "unit": "GB/s", "cores": 1, "kind": "port",
-            "sample": f"first 2^26 of the 2^28 elements (256 MiB), {ks.size} k's, one "
-                      f"single-threaded sort-and-choose ({dt:.2f} s)"}
+            "sample": f"first 2^26 of the 2^28 elements (256 MiB), {ks.size} k's clipped to "
+                      f"[1, 2^26]: one single-threaded std::sort of the keys, then index "
+                      f"({dt:.2f} s)"}
 
 
 def timed_steps(fn, steps, warmup, stream, torch, after_warmup=None):
@@ -281,9 +298,6 @@ def run_ggks(args):
         ggks.multiselect_ptr(d_x.data_ptr(), n, np.float32, k, ctx=ctx, stream=sptr, out=out)
 
     sampler = ClockSampler(local).start()
-    # correctness of the timed path on this input: checked once, bit-exact,
-    # against the sort of a 2^26 slice is too weak; the full-size check lives in
-    # the gpu tests.  Here: ranks of the answers by counting on the device.
     if ws > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -310,6 +324,7 @@ def run_ggks(args):
                              after_warmup=ctx.reset_stats)
     st = ctx.stats()
     ctx.set_profiling(False)
+    timed_out = out.copy()  # the last timed call's answers, checked below
     gpu_launches = int(st["launches"])
     stream_ms = {dom: st["pass_ms"][dom] / max(1, st["pass_launches"][dom])}
     clocks = sampler.summary(t0, t1)
@@ -346,10 +361,14 @@ def run_ggks(args):
         dist.all_reduce(etmax, op=dist.ReduceOp.MAX)
     e2e_val = ws * n * 4 / (float(etmax.item()) * 1e-3) / 1e9
     sampler.stop()
+    # the timed calls' answers against sort-and-choose (outside every timed
+    # region): the headline on every rank, the rest on rank 0 below
+    want = oracle_mod().multiselect(x, k, threads=os.cpu_count() or 1)
+    parity = {"headline": same_bits(timed_out, want), "headline_e2e": same_bits(out, want)}
 
     variants = {}
     if not args.no_variants and rank == 0:
-        variants = run_variants(torch, ggks, gp, ctx, stream, sptr, dev, args.log2n)
+        variants = run_variants(torch, ggks, gp, ctx, stream, sptr, dev, args.log2n, parity)
     batched = served = None
     if not args.no_batched and rank == 0:
         batched = run_batched(torch, ggks, gp, dev, sptr)
@@ -363,21 +382,19 @@ def run_ggks(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
             "data": "synthetic (numpy PCG64)",
-            "config": {"workload": f"multiselect n=2^{args.log2n} f32 normal(0,1) seed 1, "
-                                   f"{NUM_K} distinct k's uniform in [1,n]",
-                       "n": n, "num_k": NUM_K, "elem": "float32 (ordered as u32 keys)",
-                       "parallelism": "replicas" if ws > 1 else "single GPU",
-                       "l2": (f"input ({n * 4 >> 20} MiB) larger than L2 (129 MB); no flush needed"
-                              if n * 4 > 129 * 10**6 else
-                              f"input ({n * 4 >> 20} MiB) smaller than L2 (129 MB): not flushed")},
+            "config": bench_config(args.log2n, ws),
             "elements_per_s": round(ws * n / (ms_max * 1e-3), 1),
             "roofline": roofline,
             "pass_ms": {p: round(v, 4) for p, v in pass_ms.items()},
+            "survivors_per_call": int(st["survivors"] // max(1, st["calls"])),
+            "recursions_per_call": round(st["recursions"] / max(1, st["calls"]), 3),
             "e2e": {"value": round(e2e_val, 2), "unit": "GB/s",
                     "h2d_bytes_per_step": n * 4 + k.size * 4, "d2h_bytes_per_step": k.size * 4,
                     "entry": "ggks_multiselect_host_f32 (pinned host vector)"},
             "gpu_launches": gpu_launches,
             "clocks": clocks,
+            "parity": all(parity.values()),
+            "parity_checked": {kk: bool(v) for kk, v in parity.items()},
         }
         if variants:
             line["variants"] = variants
@@ -395,17 +412,44 @@ def run_ggks(args):
     return 0
 
 
-def run_variants(torch, ggks, gp, ctx, stream, sptr, dev, log2n):
-    """The other inputs of the large configuration, timed the same way."""
+def oracle_mod():
+    """The CPU checker (sort-and-choose), used outside every timed region."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    return oracle
+
+
+def timed_calls_flushed(fn, steps, warmup, stream, torch, dev):
+    """Per-call device time of a synchronous call on a small input: before
+    each call a 256 MiB write evicts the input from L2 (129 MB); CUDA events
+    bracket only the call.  Returns the mean ms per call."""
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)
+    for _ in range(warmup):
+        fn()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for e0, e1 in ev:
+            flush.zero_()
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+    torch.cuda.synchronize()
+    return sum(e0.elapsed_time(e1) for e0, e1 in ev) / steps
+
+
+def run_variants(torch, ggks, gp, ctx, stream, sptr, dev, log2n, parity):
+    """The other inputs of the large configuration, the top-k configuration
+    and the plain configuration, timed the same way; each timed call's answers
+    are checked against sort-and-choose outside the timed regions."""
+    orc = oracle_mod()
+    thr = os.cpu_count() or 1
     res = {}
-    specs = [("f32_cauchy", "f32", "cauchy", log2n, 2), ("f32_half_normal", "f32", "half_normal",
-                                                         log2n, 3),
-             ("u32_uniform", "u32", "uniform", log2n, 4),
-             ("f64_uniform_pm1e6", "f64", "uniform_pm1e6", log2n - 1, 5)]
-    for name, dt, dist_name, lg, seed in specs:
-        n = 1 << lg
-        x = gp.generate(dt, dist_name, n, seed)
-        k = gp.k_distinct(n, NUM_K, 200 + seed)
+    for name, dt, dist_name, lg, seed in gp.L_INPUTS[1:]:
+        lg = lg - (N_LOG2 - log2n)
+        x, k = gp.config_l(name, lg)
+        n = x.size
         carrier = x.view(np.int32) if dt == "u32" else x
         d = torch.from_numpy(carrier).to(dev)
         out = np.empty(k.size, dtype=x.dtype)
@@ -414,51 +458,63 @@ def run_variants(torch, ggks, gp, ctx, stream, sptr, dev, log2n):
             ggks.multiselect_ptr(d.data_ptr(), n, x.dtype, k, ctx=ctx, stream=sptr, out=out)
 
         ms, _, _ = timed_steps(step, 10, 3, stream, torch)
+        parity[name] = same_bits(out, orc.multiselect(x, k, threads=thr))
         res[name] = {"n": n, "ms": round(ms, 4), "GB/s": round(x.nbytes / (ms * 1e-3) / 1e9, 1)}
         del d
-    # top-k configuration, K = 65536 on 2^26 f32 uniform
-    n = 1 << 26
-    x = gp.uniform_f32(n, 0)
-    d = torch.from_numpy(x).to(dev)
-    out = np.empty(65536, dtype=np.float32)
-
-    def tk():
-        ggks.topk_ptr(d.data_ptr(), n, np.float32, 65536, ctx=ctx, stream=sptr, out=out)
-
-    ms, _, _ = timed_steps(tk, 10, 3, stream, torch)
-    ctx.set_profiling(True)
-    ctx.reset_stats()
-    for _ in range(5):
-        tk()
-    torch.cuda.synchronize()
-    st = ctx.stats()
-    ctx.set_profiling(False)
-    res["topk_f32_2^26_K65536"] = {
-        "n": n, "ms": round(ms, 4), "GB/s": round(x.nbytes / (ms * 1e-3) / 1e9, 1),
-        "pass_ms": {p: round(st["pass_ms"][p] / max(1, st["pass_launches"][p]), 4)
-                    for p in ggks.PASS_NAMES},
-        "recursions": st["recursions"], "survivors": st["survivors"] // 5}
-    # the rest of the top-k configuration: K in {32, 1024, 65536} on 2^26 float32
-    # uniform, uint32 uniform over [0, 2^16) and the ascending float32 copy (ms per call)
-    u16 = gp.uniform_u32(n, 1, 1 << 16)
-    inputs = [("f32_uniform", d, np.float32),
-              ("u32_uniform16", torch.from_numpy(u16.view(np.int32)).to(dev), np.uint32),
-              ("f32_sorted", torch.sort(d)[0], np.float32)]
+    # top-k configuration: K in {32, 1024, 65536} on 2^26 float32 uniform,
+    # uint32 uniform over [0, 2^16) and the ascending float32 copy (ms per call)
+    n = 1 << gp.T_LOG2N
     grid = {}
-    for name, dt, npdt in inputs:
+    detail = None
+    for name in gp.T_INPUTS:
+        x = gp.config_t(name)
+        carrier = x.view(np.int32) if x.dtype == np.uint32 else x
+        d = torch.from_numpy(carrier).to(dev)
+        want = orc.topk(x, max(gp.T_KS), threads=thr)
         row = {}
-        for K in (32, 1024, 65536):
-            o = np.empty(K, dtype=npdt)
+        for K in gp.T_KS:
+            o = np.empty(K, dtype=x.dtype)
 
             def tkk():
-                ggks.topk_ptr(dt.data_ptr(), n, npdt, K, ctx=ctx, stream=sptr, out=o)
+                ggks.topk_ptr(d.data_ptr(), n, x.dtype, K, ctx=ctx, stream=sptr, out=o)
 
             ms, _, _ = timed_steps(tkk, 10, 3, stream, torch)
+            parity[f"topk_{name}_K{K}"] = same_bits(o, want[:K])
             row[str(K)] = round(ms, 4)
         grid[name] = row
-        if dt is not d:
-            del dt
+        if name == "f32_uniform":
+            # per-pass device times of the K = 65536 call (events around every pass)
+            ctx.set_profiling(True)
+            ctx.reset_stats()
+            o = np.empty(65536, dtype=x.dtype)
+            for _ in range(5):
+                ggks.topk_ptr(d.data_ptr(), n, x.dtype, 65536, ctx=ctx, stream=sptr, out=o)
+            torch.cuda.synchronize()
+            st = ctx.stats()
+            ctx.set_profiling(False)
+            detail = {"n": n, "ms": row["65536"],
+                      "GB/s": round(x.nbytes / (row["65536"] * 1e-3) / 1e9, 1),
+                      "pass_ms": {p: round(st["pass_ms"][p] / max(1, st["pass_launches"][p]), 4)
+                                  for p in ggks.PASS_NAMES},
+                      "recursions": st["recursions"], "survivors": st["survivors"] // 5}
+        del d
+    res["topk_f32_2^26_K65536"] = detail
     res["topk_grid_2^26_ms"] = grid
+    # plain configuration: 2^20 float32 uniform (seed 0), 101 k's on the p grid;
+    # the 4 MiB input fits L2, so L2 is flushed before every timed call
+    x, k = gp.config_p()
+    d = torch.from_numpy(x).to(dev)
+    out = np.empty(k.size, dtype=x.dtype)
+
+    def pstep():
+        ggks.multiselect_ptr(d.data_ptr(), x.size, x.dtype, k, ctx=ctx, stream=sptr, out=out)
+
+    ms = timed_calls_flushed(pstep, 50, 5, stream, torch, dev)
+    parity["plain_P"] = same_bits(out, orc.multiselect(x, k, threads=thr))
+    res["plain_P_2^20_101k"] = {"n": x.size, "num_k": int(k.size), "us": round(ms * 1e3, 2),
+                                "GB/s": round(x.nbytes / (ms * 1e-3) / 1e9, 1),
+                                "l2": "flushed before every call (256 MiB write, not timed)"}
+    del d
     return res
 
 
@@ -638,6 +694,12 @@ def run_served(torch, ggks, gp, dev, sptr, per_rate=4000):
                        "p50_ms": pct(srv_lat, 50), "p99_ms": pct(srv_lat, 99),
                        "GB/s": round(in_bytes / srv_span / 1e9, 1),
                        "batches": sst["batches"], "launches": sst["launches"],
+                       "concurrent_launches": sst["concurrent_launches"],
+                       "hbm_waits": sst["hbm_waits"], "single_calls": sst["single_calls"],
+                       "recursions": sst["recursions"],
+                       "batch_phase_ms": {p: round(v, 2) for p, v in sst["batch_phase_ms"].items()},
+                       "kernel_ms": round(sst["kernel_ms"], 2),
+                       "lane_group_ms": round(sst["group_ms"], 2),
                        "mean_batch": round(sst["batched_requests"] / max(1, sst["batches"]), 2)},
             "sequential_plain": {"req_per_s": round(len(trace) / seq_span, 1),
                                  "p50_ms": pct(seq_lat, 50), "p99_ms": pct(seq_lat, 99)},

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -40,17 +41,25 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
 
   // co-resident grid: every CTA the SMs hold at once
   const int smem = batch_smem_bytes<T>();
-  static int blocks_per_sm = -1;  // per instantiation; one GPU model per process
+  // the kernel's attributes belong to it as loaded on one device: set up once
+  // per device (per instantiation), the resulting occupancy remembered + 1
+  static std::atomic<int> bps_plus1[kMaxDevices];  // static storage: starts at zero
+  const bool tracked = ctx.device >= 0 && ctx.device < kMaxDevices;
+  int blocks_per_sm = tracked ? bps_plus1[ctx.device].load(std::memory_order_acquire) - 1 : -1;
   if (blocks_per_sm < 0) {
-    cudaFuncSetAttribute((const void *)k_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t ae = cudaFuncSetAttribute((const void *)k_batch<T>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     // two CTAs of about 100 KB each per SM: ask for the largest shared-memory carveout
-    cudaFuncSetAttribute((const void *)k_batch<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                         100);
+    if (ae == cudaSuccess)
+      ae = cudaFuncSetAttribute((const void *)k_batch<T>,
+                                cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (ae != cudaSuccess) return from_cuda(ae);
     int b = 0;
     const cudaError_t oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<T>, kBThreads,
                                                                            smem);
     if (oe != cudaSuccess) return from_cuda(oe);
     blocks_per_sm = b;
+    if (tracked) bps_plus1[ctx.device].store(b + 1, std::memory_order_release);
   }
   if (blocks_per_sm < 1) return GGKS_UNSUPPORTED;
   const uint32_t max_grid = (uint32_t)blocks_per_sm * (uint32_t)ctx.sm_count;
@@ -216,8 +225,7 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   // every CTA the SMs hold at once, or fewer when the batch has less work
   // (each grid barrier waits for every CTA)
   const uint32_t work = std::max(std::max(num_tiles, P), R / 8);
-  const uint32_t grid = std::max(1u, std::min(max_grid, work));
-  ctx.stats.batch_grid = grid;
+  const uint32_t grid_want = std::max(1u, std::min(max_grid, work));
 
   float ms_total = 0.f;
   // the results come back with the control block (one synchronisation); a
@@ -232,20 +240,34 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
       if (r == cudaSuccess) r = cudaEventCreate(&ctx.bev1);
       if (r != cudaSuccess) return r;
     }
+    // a share of the co-resident CTAs when other batches may run at once,
+    // held until this launch has finished
+    uint32_t grid = grid_want, units = 0;
+    if (ctx.grid_budget) grid = ctx.grid_budget->acquire(grid_want, max_grid, &units);
+    struct Share {
+      GridBudget *b;
+      uint32_t u;
+      ~Share() {
+        if (b) b->release(u);
+      }
+    } share{ctx.grid_budget, units};
+    ctx.stats.batch_grid = grid;
     cudaEventRecord(ctx.bev0, s);
     cudaError_t r = cudaLaunchCooperativeKernel((const void *)k_batch<T>, dim3(grid), dim3(kBThreads),
                                                 args, (size_t)smem, s);
     cudaEventRecord(ctx.bev1, s);
     ctx.stats.launches++;
-    if (r != cudaSuccess) return r;
-    r = cudaMemcpyAsync(h_ctrl, ctrl, sizeof(BCtrl), cudaMemcpyDeviceToHost, s);
-    if (r != cudaSuccess) return r;
-    if (h_out) {
-      r = cudaMemcpyAsync(h_res, d_out, out_bytes, cudaMemcpyDeviceToHost, s);
-      if (r != cudaSuccess) return r;
-      res_fresh = true;
+    if (r != cudaSuccess) {
+      cudaStreamSynchronize(s);  // nothing of this launch may run once its share is returned
+      return r;
     }
-    r = cudaStreamSynchronize(s);
+    r = cudaMemcpyAsync(h_ctrl, ctrl, sizeof(BCtrl), cudaMemcpyDeviceToHost, s);
+    if (r == cudaSuccess && h_out) {
+      r = cudaMemcpyAsync(h_res, d_out, out_bytes, cudaMemcpyDeviceToHost, s);
+      res_fresh = r == cudaSuccess;
+    }
+    const cudaError_t rs = cudaStreamSynchronize(s);
+    if (r == cudaSuccess) r = rs;
     float ms = 0.f;
     if (r == cudaSuccess && cudaEventElapsedTime(&ms, ctx.bev0, ctx.bev1) == cudaSuccess)
       ms_total += ms;

@@ -65,7 +65,19 @@ constexpr int kLutIdxBits = 12;
 constexpr uint32_t kLutIdx = 1u << kLutIdxBits;  // slices over the sample span
 constexpr uint32_t kLutEntries = kLutIdx + 1;    // + one for keys above the span
 constexpr uint32_t kLutPadded = (kLutEntries + 3) & ~3u;  // 16-byte multiple
-constexpr int kMaxSubBits = 12;                  // at most 2^12 buckets per slice
+// at most 2^15 buckets per slice, and 2^(24 - slice bits) so that a packed
+// table entry's first-bucket offset fits its signed 25-bit field
+constexpr int kMaxSubBits = 15;
+// The single-vector path's table: 2^9 slices.  Its streaming passes keep the
+// table in shared memory once per bank -- entry j of copy l at word 32 j + l,
+// read by lane l only -- so that a warp's 32 lookups take one wavefront
+// whatever slices its keys fall in (one shared copy costs about three: the
+// lanes' distinct entries pile up in a few banks).  2^9 slices keep the 32
+// copies at 64 KB beside the 128 KB histogram.  The sample is still binned in
+// 2^12 fine slices, which place the speculative windows (see build_lut_cta).
+constexpr int kSvBits = 9;
+constexpr uint32_t kSvSlices = 1u << kSvBits;
+constexpr uint32_t kRepWords = (kSvSlices + 1) * 32;  // 32 copies of the 2^9 + 1 entries
 constexpr uint32_t kMaxNb = 32768;  // buckets of one vector: shared-memory histogram limit (u32)
 constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
 constexpr uint32_t kInactive = 0x80000000u;  // compaction cursor of an inactive bucket
@@ -387,7 +399,8 @@ __device__ __forceinline__ uint32_t hash32(uint32_t a) {
 // ---------------------------------------------------------------------------
 // lut[j] = (C_j << 7) | rs_j.  For slice j with first bucket B_j cut into 2^b_j
 // sub-buckets: rs_j = shift - b_j and C_j = B_j - (j << b_j), a signed 25-bit
-// value (|j << b_j| < 2^24 because j < 2^12 and b_j <= 12).  Then
+// value (|j << b_j| < 2^24 because a table of 2^s slices has j < 2^s and
+// b_j <= 24 - s).  Then
 //   bucket = C_j + ((key - base) >> rs_j),
 // since (key - base) >> rs_j = (j << b_j) + sub-bucket on slice j.  Empty
 // slices of one run share a bucket (b = 0); the top entry (keys above the
@@ -409,6 +422,26 @@ __device__ __forceinline__ uint32_t bucket_of(K key, K base, uint32_t shift, con
   const uint32_t e = lut[j];
   const uint32_t b = (uint32_t)((int32_t)e >> 7) + shr_clamp(d, e & 127u);
   return key < base ? 0u : b;
+}
+
+// bucket_of on the single-vector table (kSvSlices slices) replicated once per
+// bank in shared memory: lane_lut = table + (lane index), entry j at
+// lane_lut[32 j], so the lanes of a warp never share a bank.
+template <class K>
+__device__ __forceinline__ uint32_t bucket_of_rep(K key, K base, uint32_t shift,
+                                                  const uint32_t *lane_lut) {
+  const K d = key - base;  // wraps for key < base; that result is discarded
+  const K idx = d >> shift;
+  const uint32_t j = idx < (K)kSvSlices ? (uint32_t)idx : kSvSlices;
+  const uint32_t e = lane_lut[j << 5];
+  const uint32_t b = (uint32_t)((int32_t)e >> 7) + shr_clamp(d, e & 127u);
+  return key < base ? 0u : b;
+}
+
+// Copies the single-vector table (kSvSlices + 1 entries, global) into shared
+// memory once per bank (kRepWords words); the caller synchronises.
+__device__ __forceinline__ void load_rep_table(uint32_t *rep, const uint32_t *__restrict__ lut_g) {
+  for (uint32_t i = threadIdx.x; i < kRepWords; i += blockDim.x) rep[i] = __ldg(lut_g + (i >> 5));
 }
 
 __device__ __forceinline__ uint32_t lut_pack(int32_t C, uint32_t rs) {
@@ -508,8 +541,8 @@ __device__ __forceinline__ V block_reduce(V v, Op op, V *sh /* >= 32 */) {
 // finish counts the samples per slice and builds the table.
 //
 // Allocation: a slice with c samples gets 2^b sub-buckets,
-// b = clamp(ceil(log2 c) - t, 0, min(shift, 20)), and empty slices merge into
-// one bucket per run.  The smallest threshold t whose bucket total fits nb_max
+// b = clamp(ceil(log2 c) - t, 0, min(shift, 15, 24 - slice bits)), and empty
+// slices merge into one bucket per run.  The smallest threshold t whose bucket total fits nb_max
 // is found from a histogram of ceil(log2 c) over the slices, so each candidate
 // t costs a 33-term sum on one thread.
 // Builds the splitter table of one problem from its S sampled keys (kmin /
@@ -518,11 +551,24 @@ __device__ __forceinline__ V block_reduce(V v, Op op, V *sh /* >= 32 */) {
 // makes every threshold feasible), and thread 0 writes the header.  The
 // samples are in shared memory (SMEM) or in global memory written by other
 // CTAs (read past L1).
+//
+// pre_cnt (global, kLutIdx words): the samples already binned in 2^12 fine
+// slices of the span ((key - kmin) >> fine shift, fine shift = bit length of
+// the span - 12, at least 0); every slice is a run of 2^fold fine slices.
+// With pre_cnt a slice's sub-buckets follow its peak density -- its largest
+// fine count times 2^fold, in place of its count -- so that a slice whose
+// keys crowd into part of its range (the slice holding the sampled maximum,
+// whose keys stop there; a steep stretch of a distribution) gets buckets as
+// narrow as its densest part needs.
+// fine (shared, kLutIdx words, with pre_cnt only): lent by the caller to keep
+// the fine counts, which place the speculative windows (sp) at fine-slice
+// precision; without it no window is computed.
 template <class K, int SPT, bool SMEM>
 __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint32_t nb_max,
                               uint32_t *lut, LutHeader<K> *hdr, int nsl_bits = kLutIdxBits,
                               uint32_t *pre_cnt = nullptr, int64_t pre_same_key = -1,
-                              const SpecArgs *sp = nullptr, uint32_t dup_cap = 0) {
+                              const SpecArgs *sp = nullptr, uint32_t dup_cap = 0,
+                              uint32_t *fine = nullptr) {
   __shared__ uint32_t cnt[kLutIdx];
   __shared__ uint32_t lch[36];  // [0, 33): slices by ceil(log2 c); [34]: empty-run starts
   __shared__ uint32_t red32[33];
@@ -540,12 +586,17 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
     nb_max = dup_cap;
   const int bl = bitlen<K>(kmax - kmin);
   const uint32_t shift = bl > nsl_bits ? (uint32_t)(bl - nsl_bits) : 0u;
-  const int bcap = (int)(shift < (uint32_t)kMaxSubBits ? shift : (uint32_t)kMaxSubBits);
+  const uint32_t fsh = bl > kLutIdxBits ? (uint32_t)(bl - kLutIdxBits) : 0u;  // fine slices
+  const uint32_t fold = shift - fsh;  // a slice is 2^fold fine slices
+  int bcap = (int)(shift < (uint32_t)kMaxSubBits ? shift : (uint32_t)kMaxSubBits);
+  if (bcap > 24 - nsl_bits) bcap = 24 - nsl_bits;
 
-  // --- sample counts per slice: counted by the caller (pre_cnt, global, left
-  // zero here for the next call), or from the samples
+  // --- sample counts per slice: counted by the caller in fine slices
+  // (pre_cnt, global, left zero here for the next call), or from the samples
   if (tid < 36) lch[tid] = 0;
   if (pre_cnt) {
+    for (uint32_t j = tid; j < nsl; j += blockDim.x) cnt[j] = 0;
+    __syncthreads();
     for (uint32_t j0 = tid; j0 < kLutIdx; j0 += 4 * blockDim.x) {
       uint32_t c4[4];
 #pragma unroll
@@ -557,7 +608,8 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
       for (int u = 0; u < 4; ++u) {
         const uint32_t j = j0 + u * blockDim.x;
         if (j < kLutIdx) {
-          cnt[j] = c4[u];
+          if (fine) fine[j] = c4[u];
+          if (c4[u] && (j >> fold) < nsl) atomicMax(&cnt[j >> fold], c4[u] << fold);
           pre_cnt[j] = 0;
         }
       }
@@ -674,10 +726,10 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
   // prediction only decides what the histogram pass keeps: compaction checks
   // that every segment's bucket was kept before it reads the candidates.
   __shared__ uint32_t s_sp[8];  // per window: first bucket, last bucket, first / end sample rank
-  const bool spec_on = sp != nullptr && sp->cand_cap != 0 && sp->ctrl->spec_nwin != 0;
+  const bool spec_on = sp != nullptr && sp->cand_cap != 0 && sp->ctrl->spec_nwin != 0 &&
+                       pre_cnt != nullptr && fine != nullptr;
   uint32_t wa[2] = {0, 0}, wb[2] = {0, 0}, nwin = 0;
   bool wlo_open[2] = {false, false}, whi_open[2] = {false, false};
-  uint32_t cpre = 0;
   if (spec_on) {
     nwin = sp->ctrl->spec_nwin < 2u ? sp->ctrl->spec_nwin : 2u;
     // single precision (float64 is slow on this part; sample ranks need
@@ -695,13 +747,8 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
       wa[w] = wlo_open[w] ? 0u : (a >= dS - 1.0f ? S - 1u : (uint32_t)a);
       wb[w] = whi_open[w] ? S - 1u : (uint32_t)b;
     }
-    // defaults (replaced below; no slice left unmatched): every bucket, every sample
+    // defaults (replaced below; no fine slice left unmatched): every bucket, every sample
     if (tid < 8) s_sp[tid] = (tid & 3) == 1 ? 0xFFFFFFFEu : ((tid & 3) == 3 ? S : 0u);
-    uint32_t csum = 0;
-#pragma unroll
-    for (int q = 0; q < SPT; ++q) csum += c[q];
-    uint32_t ctot;
-    cpre = block_incl_scan(csum, &ctot, red32) - csum;
   }
   // the table also goes to cnt[] (its counts are no longer read) for the
   // collision estimate below
@@ -714,22 +761,6 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
     } else if (c[q]) {
       const int b = bits_of(q);
       e = lut_pack((int32_t)run - (int32_t)(j << b), shift - (uint32_t)b);
-      if (spec_on) {
-        // the slices with samples split the sample ranks [0, S) in order
-#pragma unroll
-        for (uint32_t w = 0; w < 2; ++w) {
-          if (w >= nwin) break;
-          if (cpre <= wa[w] && wa[w] < cpre + c[q]) {
-            s_sp[4 * w + 0] = run;
-            s_sp[4 * w + 2] = cpre;
-          }
-          if (cpre <= wb[w] && wb[w] < cpre + c[q]) {
-            s_sp[4 * w + 1] = run + my[q] - 1u;
-            s_sp[4 * w + 3] = cpre + c[q];
-          }
-        }
-        cpre += c[q];
-      }
     } else {
       // one bucket per run of empty slices
       e = lut_pack((int32_t)(prev_nonempty[q] ? run : run - 1u) - (int32_t)j, shift);
@@ -758,6 +789,43 @@ __device__ void build_lut_cta(const K *samples, uint32_t S, K kmin, K kmax, uint
     const uint32_t e = j == nsl ? top : cnt[j];
     return (uint32_t)((int32_t)e >> 7) + shr_clamp(d, e & 127u);
   };
+  if (spec_on) {
+    // The fine slices split the sample ranks [0, S) in order: the fine slice
+    // holding a window's first (last) sample rank gives the window's first
+    // (last) bucket, that of the fine slice's first (last) key.  Each thread
+    // takes kLutIdx / blockDim.x consecutive fine slices (at most 4).
+    const uint32_t per = kLutIdx / blockDim.x;
+    uint32_t fc[4], fsum = 0;
+#pragma unroll
+    for (uint32_t q = 0; q < 4; ++q) {
+      fc[q] = q < per ? fine[per * tid + q] : 0u;
+      fsum += fc[q];
+    }
+    uint32_t ftot;
+    uint32_t fpre = block_incl_scan(fsum, &ftot, red32) - fsum;
+    const K span = kmax - kmin;
+#pragma unroll
+    for (uint32_t q = 0; q < 4; ++q) {
+      if (q >= per || fc[q] == 0) continue;
+      const uint32_t jf = per * tid + q;
+#pragma unroll
+      for (uint32_t w = 0; w < 2; ++w) {
+        if (w >= nwin) break;
+        if (fpre <= wa[w] && wa[w] < fpre + fc[q]) {
+          s_sp[4 * w + 0] = bucket(kmin + ((K)jf << fsh));
+          s_sp[4 * w + 2] = fpre;
+        }
+        if (fpre <= wb[w] && wb[w] < fpre + fc[q]) {
+          K dend = ((K)(jf + 1u) << fsh) - K(1);
+          dend = dend < span ? dend : span;
+          s_sp[4 * w + 1] = bucket(kmin + dend);
+          s_sp[4 * w + 3] = fpre + fc[q];
+        }
+      }
+      fpre += fc[q];
+    }
+    __syncthreads();
+  }
   auto ld = [&](uint32_t i) -> K { return SMEM ? samples[i] : __ldcg(samples + i); };
   // four pairs of each kind per thread and step, all loads issued first (the
   // far-apart pairs only when the caller has not counted them)
@@ -932,9 +1000,12 @@ __global__ void __launch_bounds__(1024) k_lut(const K *__restrict__ samples, uin
   __syncthreads();
   if (!s_last) return;
 
+  // the table has kSvSlices slices; the fine counts (this CTA's ccnt is free
+  // now) place the speculative windows
+  __syncthreads();
   const SpecArgs sa{ctrl, n, cand_cap, G};
-  build_lut_cta<K, 4, false>(samples, S, kmin, kmax, nb_max, lut, hdr, kLutIdxBits, slice_cnt,
-                             (int64_t)__ldcg(&ctrl->same_key), &sa, dup_nb_cap<K>(nb_max));
+  build_lut_cta<K, 4, false>(samples, S, kmin, kmax, nb_max, lut, hdr, kSvBits, slice_cnt,
+                             (int64_t)__ldcg(&ctrl->same_key), &sa, dup_nb_cap<K>(nb_max), ccnt);
   if (tid == 0) {
     ctrl->nb = hdr->nb;
     ctrl->spec_on = hdr->spec != 0 ? 1u : 0u;
@@ -1085,7 +1156,8 @@ __device__ __forceinline__ void cand_put_warp(const CandPool<K> &cp, K k, bool k
 // single-key tracking in rep (track_key).
 template <class T, int UNROLL, bool INGEST, bool SPEC, bool SWZ>
 __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, uint32_t *hist,
-                                          const uint32_t *lut, typename Traits<T>::K base,
+                                          const uint32_t *lut /* lane's table */,
+                                          typename Traits<T>::K base,
                                           uint32_t shift, T *__restrict__ copy_to,
                                           const CandPool<typename Traits<T>::K> &cr,
                                           uint32_t *wcount, uint32_t *wtab,
@@ -1121,7 +1193,7 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
       bool any = false;
 #pragma unroll
       for (int e = 0; e < PV; ++e) {
-        b[e] = bucket_of<K>(k[e], base, shift, lut);
+        b[e] = bucket_of_rep<K>(k[e], base, shift, lut);
         const uint32_t i = SWZ ? bank_swz(b[e]) : b[e];
         atomicAdd(&hist[i], 1u);
         if (SWZ) track_key<K>(hist, rep, i, k[e]);
@@ -1150,7 +1222,7 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
       vec_keys<T>(vv, k);
 #pragma unroll
       for (int e = 0; e < PV; ++e) {
-        const uint32_t b = valid ? bucket_of<K>(k[e], base, shift, lut) : 0u;
+        const uint32_t b = valid ? bucket_of_rep<K>(k[e], base, shift, lut) : 0u;
         if (valid) {
           const uint32_t i = SWZ ? bank_swz(b) : b;
           atomicAdd(&hist[i], 1u);
@@ -1169,7 +1241,7 @@ __device__ __forceinline__ void hist_body(const T *__restrict__ x, uint64_t n, u
           const T v = x[e];
           if (INGEST) copy_to[e] = v;
           k = Traits<T>::key(v);
-          b = bucket_of<K>(k, base, shift, lut);
+          b = bucket_of_rep<K>(k, base, shift, lut);
           const uint32_t i = SWZ ? bank_swz(b) : b;
           atomicAdd(&hist[i], 1u);
           if (SWZ) track_key<K>(hist, rep, i, k);
@@ -1226,13 +1298,14 @@ __global__ void __launch_bounds__(1024, 1)
   pdl_start();
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
-  uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
-  uint32_t *hist = (lut + kLutPadded);
+  uint32_t *rep_lut = reinterpret_cast<uint32_t *>(smem_raw);  // one copy per bank
+  uint32_t *hist = (rep_lut + kRepWords);
+  const uint32_t *lut = rep_lut + (threadIdx.x & 31);  // this lane's copy
   __shared__ uint32_t s_wcnt[kCandWarps];
   __shared__ uint32_t s_tab[kCandWarps * kCandChunksPerWarp];
   if (ctrl->status & ST_FATAL) return;
   const LutHeader<K> h = *hdr;
-  for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
+  load_rep_table(rep_lut, lut_g);
   const uint32_t dcap = dup_nb_cap<K>(nb_max);
   const bool track = reps != nullptr && h.dup && dcap != 0 && h.nb <= dcap;
   K *rep = track ? reinterpret_cast<K *>(hist + dcap) : nullptr;
@@ -1855,8 +1928,8 @@ __global__ void __launch_bounds__(1024, 1)
   const bool dtrack = bsingle != nullptr && bkey != nullptr && h.dup && dcap != 0 && nb <= dcap;
   for (uint32_t q = s0; q < s1; ++q) {
     const uint32_t b = segb_smem ? s_segb[q] : __ldcg(seg_bucket + q);
-    const K klo = bucket_lo<K>(b, h.base, h.shift, lut);
-    const K knext = (b + 1 < nb) ? bucket_lo<K>(b + 1, h.base, h.shift, lut) : K(0);
+    const K klo = bucket_lo<K>(b, h.base, h.shift, lut, kSvSlices);
+    const K knext = (b + 1 < nb) ? bucket_lo<K>(b + 1, h.base, h.shift, lut, kSvSlices) : K(0);
     // single key iff the next bucket starts one key later; the start of the
     // top entry's bucket can wrap past the key width, and then bucket b runs
     // up to the largest key
@@ -2005,9 +2078,10 @@ __global__ void __launch_bounds__(1024, 1)
 // (match.any) and take consecutive positions.
 template <class T, bool HEAVY>
 __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Traits<T>::K base,
-                                            uint32_t shift, const uint32_t *lut, uint32_t *cursor,
+                                            uint32_t shift, const uint32_t *lut /* lane's table */,
+                                            uint32_t *cursor,
                                             typename Traits<T>::K *__restrict__ surv, uint32_t cap) {
-  const uint32_t b = bucket_of(k, base, shift, lut);
+  const uint32_t b = bucket_of_rep(k, base, shift, lut);
   uint32_t pos;
   if (HEAVY) {
     const uint32_t peers = __match_any_sync(0xffffffffu, b);
@@ -2024,11 +2098,66 @@ __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Tr
   st_global_if(surv + pos, k, pos < cap);
 }
 
-template <class T, int UNROLL, bool HEAVY>
-__device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n, uint32_t *cursor,
-                                             const uint32_t *lut, typename Traits<T>::K base,
-                                             uint32_t shift, typename Traits<T>::K *__restrict__ surv,
-                                             uint32_t cap) {
+// Filtered compaction (the default for up to kCompactRanks slots): shared
+// memory holds the active buckets' bitmap once per bank -- word w of lane l's
+// copy at bm[32 w + l], so a warp's 32 bitmap reads take one wavefront -- the
+// active buckets before each word (prefix), and one cursor per active bucket
+// in bucket order (rank).  An element of an inactive bucket (most of them)
+// costs a table lookup and a bitmap read, both without bank conflicts; only
+// the elements of active buckets take a cursor atomic.  (The plain mode's
+// shared atomic on every element's bucket costs about four wavefronts per
+// warp: random lanes pile up in a few banks.)
+constexpr uint32_t kCompactRanks = 4096;
+struct ActiveSet {
+  const uint32_t *bm_lane;  // bm + lane: this lane's copy
+  const uint32_t *prefix;   // active buckets before word w
+  uint32_t *cursor;         // by rank
+};
+// predicated shared-memory atomic add of 1 (a lane with pred false issues no
+// access and keeps *old); no branch, so the keys of a vector stay in flight
+// together
+__device__ __forceinline__ void atom_add1_if(uint32_t *p, bool pred, uint32_t &old) {
+  asm volatile(
+      "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %2, 0;\n\t@q atom.shared.add.u32 %0, [%1], 1;\n\t}"
+      : "+r"(old)
+      : "r"(smem_addr(p)), "r"((uint32_t)pred)
+      : "memory");
+}
+
+// The PV keys of one vector: lookups and bitmap reads for all of them first,
+// then the (rare) cursor updates and stores, predicated rather than branched.
+template <class K, int PV>
+__device__ __forceinline__ void compact_filtered(const K (&kk)[PV], K base, uint32_t shift,
+                                                 const uint32_t *lut /* lane's table */,
+                                                 const ActiveSet &as, K *__restrict__ surv,
+                                                 uint32_t cap) {
+  uint32_t w[PV], below[PV];
+  bool act[PV];
+#pragma unroll
+  for (int e = 0; e < PV; ++e) {
+    const uint32_t b = bucket_of_rep(kk[e], base, shift, lut);
+    w[e] = b >> 5;
+    const uint32_t word = as.bm_lane[w[e] << 5];
+    act[e] = (word >> (b & 31u)) & 1u;
+    below[e] = __popc(word & ((1u << (b & 31u)) - 1u));
+  }
+  uint32_t r[PV];
+#pragma unroll
+  for (int e = 0; e < PV; ++e) r[e] = (act[e] ? as.prefix[w[e]] : 0u) + below[e];
+#pragma unroll
+  for (int e = 0; e < PV; ++e) {
+    uint32_t pos = 0xFFFFFFFFu;
+    atom_add1_if(as.cursor + r[e], act[e], pos);
+    st_global_if(surv + pos, kk[e], act[e] && pos < cap);
+  }
+}
+
+// Streams the CTA's tiles (and, in the owner CTA, the leftover vectors and
+// the scalar head / tail) through onev(keys of one vector, in_tiles) and
+// one(key) for the scalar head and tail.
+template <class T, int UNROLL, class FV, class F>
+__device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n, FV &&onev,
+                                             F &&one) {
   using K = typename Traits<T>::K;
   using V = typename Traits<T>::Vec;
   constexpr int PV = Traits<T>::kPerVec;
@@ -2050,9 +2179,7 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
     for (int u = 0; u < UNROLL; ++u) {
       K kk[PV];
       vec_keys<T>(v[u], kk);
-#pragma unroll
-      for (int e = 0; e < PV; ++e)
-        compact_one<T, HEAVY>(kk[e], base, shift, lut, cursor, surv, cap);
+      onev(kk, true);
     }
   }
   const uint32_t owner = (uint32_t)(ntiles % gridDim.x);
@@ -2061,15 +2188,18 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
       V vv = ldg_stream(xv + vi);
       K kk[PV];
       vec_keys<T>(vv, kk);
-#pragma unroll
-      for (int e = 0; e < PV; ++e)
-        compact_one<T, false>(kk[e], base, shift, lut, cursor, surv, cap);
+      onev(kk, false);
     }
-    for (uint64_t e = threadIdx.x; e < sp.head; e += blockDim.x)
-      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, cap);
-    for (uint64_t e = sp.tail0 + threadIdx.x; e < n; e += blockDim.x)
-      compact_one<T, false>(Traits<T>::key(x[e]), base, shift, lut, cursor, surv, cap);
+    for (uint64_t e = threadIdx.x; e < sp.head; e += blockDim.x) one(Traits<T>::key(x[e]));
+    for (uint64_t e = sp.tail0 + threadIdx.x; e < n; e += blockDim.x) one(Traits<T>::key(x[e]));
   }
+}
+
+// dynamic shared memory of k_compact: the table once per bank, then either
+// one cursor per bucket (plain and heavy modes) or the filtered mode's bitmap
+// copies (nb_max words), word prefixes (nb_max / 32) and rank cursors
+__host__ __device__ constexpr size_t compact_smem_bytes(uint32_t nb_max) {
+  return (size_t)(kRepWords + nb_max + nb_max / 32 + kCompactRanks) * sizeof(uint32_t);
 }
 
 // Grid and tile assignment must equal k_hist's (same G, same owner of the
@@ -2079,7 +2209,11 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
 // never matters) and leaves the share's end in its row of the per-CTA counts
 // for the check at the end.  A call that overflows the survivor buffer stops
 // here before touching the rows or the counters, so its re-run finds both as
-// the plan left them.
+// the plan left them.  nb_max is a multiple of 32.
+//
+// Modes: filtered (see compact_filtered) for up to kCompactRanks slots;
+// otherwise one cursor per bucket, with heavy mode's warp-aggregated updates
+// when lanes often share a bucket.
 //
 // Speculative compaction: when the histogram pass kept candidates (cand not
 // null, the table's spec on) and every segment's bucket is a kept one, CTA c's
@@ -2100,10 +2234,16 @@ __global__ void __launch_bounds__(1024, 1)
   pdl_start();
   using K = typename Traits<T>::K;
   extern __shared__ uint4 smem_raw[];
-  uint32_t *lut = reinterpret_cast<uint32_t *>(smem_raw);
-  uint32_t *cursor = (lut + kLutPadded);
+  uint32_t *rep_lut = reinterpret_cast<uint32_t *>(smem_raw);  // one copy per bank
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t *lut = rep_lut + lane;  // this lane's copy
+  uint32_t *cursor = rep_lut + kRepWords;  // plain / heavy: per bucket
+  uint32_t *bm = rep_lut + kRepWords;      // filtered: bitmap copies
+  uint32_t *prefix = bm + nb_max;
+  uint32_t *rcur = prefix + nb_max / 32;
   __shared__ bool s_bad;
   __shared__ bool s_spec_miss;
+  __shared__ uint32_t s_scan[33];
   __shared__ uint32_t s_wcnt[kCandWarps];
   __shared__ uint32_t s_tab[kCandWarps * kCandChunksPerWarp];
   // nothing to compact when every slot is a single-key one (answered by the
@@ -2111,10 +2251,16 @@ __global__ void __launch_bounds__(1024, 1)
   if ((ctrl->status & (ST_FATAL | ST_OVERFLOW)) || ctrl->total_surv == 0) return;
   const LutHeader<K> h = *hdr;
   const uint32_t c = blockIdx.x;
-  for (uint32_t j = threadIdx.x; j < kLutEntries; j += blockDim.x) lut[j] = lut_g[j];
+  load_rep_table(rep_lut, lut_g);
   const uint32_t num_slots = ctrl->num_slots;
   const bool spec = cand != nullptr && h.spec != 0;
-  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) cursor[b] = kInactive;
+  const bool filtered = !h.heavy && num_slots <= kCompactRanks;
+  const uint32_t nbw = (h.nb + 31) / 32;  // bitmap words (<= 1024)
+  if (filtered) {
+    for (uint32_t i = threadIdx.x; i < nbw * 32; i += blockDim.x) bm[i] = 0;
+  } else {
+    for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) cursor[b] = kInactive;
+  }
   if (threadIdx.x == 0) {
     s_bad = false;
     s_spec_miss = false;
@@ -2138,8 +2284,28 @@ __global__ void __launch_bounds__(1024, 1)
       }
     }
   }
+  if (filtered) {
+    // the active buckets (segments with survivors) in copy 0, then in every
+    // lane's copy, and the number of active buckets before each word
+    for (uint32_t s = threadIdx.x; s < num_slots; s += blockDim.x) {
+      if (seg_size[s] == 0) continue;
+      const uint32_t b = seg_bucket[s];
+      atomicOr(&bm[(b >> 5) << 5], 1u << (b & 31u));
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < nbw * 32; i += blockDim.x)
+      if (i & 31u) bm[i] = bm[i & ~31u];
+    const uint32_t pc = threadIdx.x < nbw ? (uint32_t)__popc(bm[threadIdx.x << 5]) : 0u;
+    uint32_t tot;
+    const uint32_t excl = block_incl_scan(pc, &tot, s_scan) - pc;
+    if (threadIdx.x < nbw) prefix[threadIdx.x] = excl;
+    __syncthreads();
+  }
   // flat slots (seg_size 0: a single-key bucket) are answered without survivors
   uint32_t *row = rows + (uint64_t)c * nb_max;
+  auto rank_of = [&](uint32_t b) {
+    return prefix[b >> 5] + (uint32_t)__popc(bm[(b >> 5) << 5] & ((1u << (b & 31u)) - 1u));
+  };
   for (uint32_t s = threadIdx.x; s < num_slots; s += blockDim.x) {
     const uint32_t sz = seg_size[s];
     if (sz == 0) continue;
@@ -2147,33 +2313,71 @@ __global__ void __launch_bounds__(1024, 1)
     const uint32_t cnt = row[b] & ~kMixed;
     const uint32_t pre = cnt ? atomicAdd(fill + s, cnt) : 0u;
     const uint32_t at = (uint32_t)(seg_off[s] + pre);
-    cursor[b] = at;
+    if (filtered)
+      rcur[rank_of(b)] = at;
+    else
+      cursor[b] = at;
     row[b] = at + cnt;
     if (spec && !in_spec(h, b)) s_spec_miss = true;
   }
   __syncthreads();
   const uint32_t cap = (uint32_t)(surv_cap < (uint64_t)kInactive ? surv_cap : kInactive);
+  const ActiveSet as{bm + lane, prefix, rcur};
   if (spec && !s_spec_miss && ctrl->total_surv <= surv_half) {
     // warp w reads the candidates of the histogram pass's warp w
     const uint32_t w = threadIdx.x >> 5;
     const uint32_t *wt = s_tab + w * kCandChunksPerWarp;
     const uint32_t cw = s_wcnt[w];
     const uint32_t cap_lo = (uint32_t)(surv_half < (uint64_t)cap ? surv_half : cap);
-    for (uint32_t i = threadIdx.x & 31; i < cw; i += 32)
-      compact_one<T, false>(cand[(uint64_t)wt[i / kCandChunk] * kCandChunk + i % kCandChunk],
-                            h.base, h.shift, lut, cursor, surv, cap_lo);
+    for (uint32_t i = lane; i < cw; i += 32) {
+      const K k[1] = {cand[(uint64_t)wt[i / kCandChunk] * kCandChunk + i % kCandChunk]};
+      if (filtered)
+        compact_filtered<K, 1>(k, h.base, h.shift, lut, as, surv, cap_lo);
+      else
+        compact_one<T, false>(k[0], h.base, h.shift, lut, cursor, surv, cap_lo);
+    }
     if (threadIdx.x == 0) atomicAdd(&ctrl->spec_ctas, 1u);
+  } else if (filtered) {
+    constexpr int PV = Traits<T>::kPerVec;
+    compact_body<T, UNROLL>(
+        x, n,
+        [&](const K(&kk)[PV], bool) { compact_filtered<K, PV>(kk, h.base, h.shift, lut, as, surv, cap); },
+        [&](K k) {
+          const K k1[1] = {k};
+          compact_filtered<K, 1>(k1, h.base, h.shift, lut, as, surv, cap);
+        });
   } else if (h.heavy) {
-    compact_body<T, UNROLL, true>(x, n, cursor, lut, h.base, h.shift, surv, cap);
+    constexpr int PV = Traits<T>::kPerVec;
+    compact_body<T, UNROLL>(
+        x, n,
+        [&](const K(&kk)[PV], bool in_tiles) {
+#pragma unroll
+          for (int e = 0; e < PV; ++e) {
+            if (in_tiles)
+              compact_one<T, true>(kk[e], h.base, h.shift, lut, cursor, surv, cap);
+            else
+              compact_one<T, false>(kk[e], h.base, h.shift, lut, cursor, surv, cap);
+          }
+        },
+        [&](K k) { compact_one<T, false>(k, h.base, h.shift, lut, cursor, surv, cap); });
   } else {
-    compact_body<T, UNROLL, false>(x, n, cursor, lut, h.base, h.shift, surv, cap);
+    constexpr int PV = Traits<T>::kPerVec;
+    compact_body<T, UNROLL>(
+        x, n,
+        [&](const K(&kk)[PV], bool) {
+#pragma unroll
+          for (int e = 0; e < PV; ++e)
+            compact_one<T, false>(kk[e], h.base, h.shift, lut, cursor, surv, cap);
+        },
+        [&](K k) { compact_one<T, false>(k, h.base, h.shift, lut, cursor, surv, cap); });
   }
   __syncthreads();
   // every cursor must have reached the end of the CTA's share; anything else
   // means the input changed between the two passes
   for (uint32_t s = threadIdx.x; s < num_slots; s += blockDim.x) {
     if (seg_size[s] == 0) continue;
-    if (cursor[seg_bucket[s]] != row[seg_bucket[s]]) s_bad = true;
+    const uint32_t b = seg_bucket[s];
+    if ((filtered ? rcur[rank_of(b)] : cursor[b]) != row[b]) s_bad = true;
   }
   __syncthreads();
   if (threadIdx.x == 0 && s_bad) atomicOr(&ctrl->status, ST_INTERNAL);
@@ -2187,8 +2391,9 @@ __global__ void __launch_bounds__(1024, 1)
 // histogram of up to 1024 bins over the top bits of (key - min), and a gather of only
 // the bins that hold requested ranks into shared memory.  Each gathered bin is
 // sorted (a warp bitonic network for bins of <= 32 keys, a CTA bitonic sort for
-// larger ones) and every request reads its rank.  Segments whose needed bins
-// exceed the shared-memory buffer are listed for a recursive re-selection.
+// larger ones) and every request reads its rank; needed bins beyond the
+// shared-memory buffer take further rounds.  Segments with a needed bin larger
+// than the sorting scratch are listed for a recursive re-selection.
 constexpr int kFinBins = 1024;
 constexpr int kFinBinBits = 10;
 constexpr int kFinThreads = 256;
@@ -2256,8 +2461,11 @@ __device__ __forceinline__ uint32_t bin_of_rank(const uint32_t *start, uint32_t 
 // requests rq[] hold local ranks and output positions.  Called by a whole CTA
 // (a multiple of kFinThreads threads); smem is finish_smem_for<K>(bcap) bytes:
 // 5 * kFinBins u32, the gather buffer (bcap keys), the scratch (bcap / 2
-// keys), per-bin minima and maxima (kFinBins keys each).  Returns false when
-// the needed bins do not fit: the slot needs a recursive re-selection.
+// keys), per-bin minima and maxima (kFinBins keys each).  Needed bins that
+// together exceed the gather buffer are gathered, sorted and answered in up
+// to kFinMaxRounds rounds; returns false when a single needed bin exceeds the
+// scratch or more rounds would be needed: the slot needs a recursive
+// re-selection.
 // 16-byte vectors of survivor keys, read past L1 (the survivors may have been
 // written earlier in the same kernel)
 template <class K>
@@ -2279,6 +2487,7 @@ struct KeyVec<uint64_t> {
   static __device__ __forceinline__ uint64_t key(const V &v, int e) { return e == 0 ? v.x : v.y; }
 };
 constexpr uint32_t kSpecBins = 24;  // bins kept either side of a request's predicted bin
+constexpr uint32_t kFinMaxRounds = 4;  // gather rounds of a slot (more: recursive re-selection)
 constexpr int kFinVecs = 2;  // vectors per thread and chunk in k_finish (63 registers)
 
 template <class K, class OutT, int VECS = kFinVecs>
@@ -2298,7 +2507,7 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
   __shared__ K redk[33];
   __shared__ uint32_t red32[33];
   __shared__ uint32_t big[kMaxBig];
-  __shared__ uint32_t s_nbig, s_nsmall, s_maxneed, s_v, s_spec, s_wlo, s_wsp;
+  __shared__ uint32_t s_nbig, s_nsmall, s_maxneed, s_v, s_spec, s_wlo, s_wsp, s_end;
   __shared__ uint32_t s_wn[32];  // speculative gather: keys kept per warp
   constexpr uint32_t PER = kFinBins / kFinThreads;  // bins per thread (at most)
   const uint32_t tcap = bcap / 2;                   // scratch T holds one bin of <= tcap keys
@@ -2538,61 +2747,94 @@ __device__ bool finish_slot(const K *__restrict__ src, uint32_t size, K lo, K hi
     __syncthreads();
     return true;
   }
-  if (!fits) {  // the needed bins do not fit: the caller re-selects this slot
+  // a needed bin that does not fit, or so many needed keys that the rounds
+  // would read the segment more than kFinMaxRounds times: the caller
+  // re-selects this slot on its keys
+  if (s_maxneed > tcap || V > kFinMaxRounds * bcap) {
     __syncthreads();
     return false;
   }
+  (void)fits;
 
-  // ---- gather the needed bins
-  {
-    auto put = [&](K k) {
-      const uint32_t bb = min((uint32_t)((k - mn) >> sh), nbins - 1u);
-      const uint32_t g = gofs[bb];
-      if (g < kFlatBin) B[g + atomicAdd(&cur[bb], 1u)] = k;
-    };
-    if (s_spec) {
-      const uint32_t wcap = tcap / nwarps;
-      for (uint32_t w = 0; w < nwarps; ++w)
-        for (uint32_t i = tid; i < s_wn[w]; i += blockDim.x) put(T[w * wcap + i]);
-    } else {
-      each_key(put);
-    }
-  }
-  __syncthreads();
-
-  // ---- sort each needed bin: a warp per bin of 2..32 keys
+  // ---- gather, sort and answer the needed bins in rounds of at most bcap
+  // keys, in bin order (one round when they all fit; every further round
+  // reads the segment again -- a slot whose ranks are all requested, as a
+  // top-k's are, holds more keys than one round)
   const uint32_t nsmall = s_nsmall;
-  for (uint32_t q = warp; q < nsmall; q += nwarps) {
-    const uint32_t bb = small[q];
-    const uint32_t g = gofs[bb], c = hist[bb];
-    K v = lane < c ? B[g + lane] : KeyMax<K>::v;
-    v = warp_bitonic32(v);
-    if (lane < c) B[g + lane] = v;
-  }
-  // larger bins: the whole CTA, one at a time
   const uint32_t nbig = s_nbig;
-  for (uint32_t q = 0; q < (nbig <= (uint32_t)kMaxBig ? nbig : nbins); ++q) {
-    const uint32_t bb = nbig <= (uint32_t)kMaxBig ? big[q] : q;
-    const uint32_t g = gofs[bb], c = hist[bb];
-    if (g >= kFlatBin || c <= 32) continue;
-    uint32_t P = 64;
-    while (P < c) P <<= 1;
+  uint32_t base = 0;
+  do {
+    uint32_t end = V;
+    if (V - base > bcap) {
+      // the round ends at the last needed bin that ends within bcap keys (the
+      // first bin from base fits: no needed bin exceeds tcap < bcap)
+      if (tid == 0) s_end = base;
+      __syncthreads();
+      for (uint32_t bb = tid; bb < nbins; bb += blockDim.x) {
+        const uint32_t g = gofs[bb];
+        if (g >= kFlatBin) continue;
+        const uint32_t e = g + hist[bb];
+        if (g >= base && e <= base + bcap) atomicMax(&s_end, e);
+      }
+      __syncthreads();
+      end = s_end;
+    }
+    auto in_round = [&](uint32_t g) { return g >= base && g < end; };
+    // gather this round's bins
+    {
+      auto put = [&](K k) {
+        const uint32_t bb = min((uint32_t)((k - mn) >> sh), nbins - 1u);
+        const uint32_t g = gofs[bb];
+        if (in_round(g)) B[g - base + atomicAdd(&cur[bb], 1u)] = k;
+      };
+      if (s_spec) {
+        const uint32_t wcap = tcap / nwarps;
+        for (uint32_t w = 0; w < nwarps; ++w)
+          for (uint32_t i = tid; i < s_wn[w]; i += blockDim.x) put(T[w * wcap + i]);
+      } else {
+        each_key(put);
+      }
+    }
     __syncthreads();
-    for (uint32_t i = tid; i < P; i += blockDim.x) T[i] = i < c ? B[g + i] : KeyMax<K>::v;
-    __syncthreads();
-    bitonic_sort_smem(T, P);
-    for (uint32_t i = tid; i < c; i += blockDim.x) B[g + i] = T[i];
-  }
-  __syncthreads();
 
-  // ---- answer
-  for (uint32_t j = tid; j < m; j += blockDim.x) {
-    const Req e = req_at(j);
-    const uint32_t bb = bin_of_rank(start, nbins, e.rank);
-    const uint32_t g = gofs[bb];
-    out[e.out] = Traits<OutT>::value(g == kFlatBin ? bmin[bb] : B[g + (e.rank - start[bb])]);
-  }
-  __syncthreads();
+    // sort each needed bin: a warp per bin of 2..32 keys
+    for (uint32_t q = warp; q < nsmall; q += nwarps) {
+      const uint32_t bb = small[q];
+      const uint32_t g = gofs[bb], c = hist[bb];
+      if (!in_round(g)) continue;
+      K v = lane < c ? B[g - base + lane] : KeyMax<K>::v;
+      v = warp_bitonic32(v);
+      if (lane < c) B[g - base + lane] = v;
+    }
+    // larger bins: the whole CTA, one at a time
+    for (uint32_t q = 0; q < (nbig <= (uint32_t)kMaxBig ? nbig : nbins); ++q) {
+      const uint32_t bb = nbig <= (uint32_t)kMaxBig ? big[q] : q;
+      const uint32_t g = gofs[bb], c = hist[bb];
+      if (!in_round(g) || c <= 32) continue;
+      uint32_t P = 64;
+      while (P < c) P <<= 1;
+      __syncthreads();
+      for (uint32_t i = tid; i < P; i += blockDim.x) T[i] = i < c ? B[g - base + i] : KeyMax<K>::v;
+      __syncthreads();
+      bitonic_sort_smem(T, P);
+      for (uint32_t i = tid; i < c; i += blockDim.x) B[g - base + i] = T[i];
+    }
+    __syncthreads();
+
+    // answer the requests whose bins this round holds (one-key bins: once)
+    for (uint32_t j = tid; j < m; j += blockDim.x) {
+      const Req e = req_at(j);
+      const uint32_t bb = bin_of_rank(start, nbins, e.rank);
+      const uint32_t g = gofs[bb];
+      if (g == kFlatBin) {
+        if (base == 0) out[e.out] = Traits<OutT>::value(bmin[bb]);
+      } else if (in_round(g)) {
+        out[e.out] = Traits<OutT>::value(B[g - base + (e.rank - start[bb])]);
+      }
+    }
+    __syncthreads();
+    base = end;
+  } while (base < V);
   return true;
 }
 

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <condition_variable>
 #include <cstddef>
 #include <cstdint>
 #include <map>
@@ -14,11 +16,58 @@
 
 namespace ggks {
 
+// devices whose per-device launch settings (shared-memory limits, occupancy)
+// are remembered; a larger device index is set up again on every call
+constexpr int kMaxDevices = 64;
+
 // Tunables of the batched path: bucket budget of a problem is about n / div
 // buckets; tiles of the (problem, tile) queue hold `tile` elements.
 struct BatchTune {
   uint32_t div = 256;
   uint32_t tile = 1u << 18;
+};
+
+// Co-resident CTAs of one device, shared by batched launches that may be in
+// flight at the same time (the server's lanes).  A persistent launch waits on
+// grid barriers for all of its CTAs, so the grids in flight together must fit
+// on the device at once: a launch takes its share before it starts and gives
+// it back once it has finished.  Shares are counted in kUnits per device,
+// each kernel's grid measured against the CTAs it alone can keep resident.
+struct GridBudget {
+  static constexpr uint32_t kUnits = 1024;
+  std::mutex mu;
+  std::condition_variable cv;
+  uint32_t free_units = kUnits;
+  uint32_t floor_units = kUnits;  // a launch waits until this much is free (or all it wants)
+  uint32_t active = 0;            // launches holding a share
+  uint64_t concurrent = 0;        // launches started while another held a share
+  // Grid (<= want, >= 1) for a launch of a kernel that keeps max_grid CTAs
+  // resident on the device; *units receives the share taken.
+  uint32_t acquire(uint32_t want, uint32_t max_grid, uint32_t *units) {
+    auto need = [&](uint32_t g) {
+      return (uint32_t)(((uint64_t)g * kUnits + max_grid - 1) / max_grid);
+    };
+    const uint32_t floor_grid =
+        (uint32_t)std::max<uint64_t>(1, (uint64_t)max_grid * floor_units / kUnits);
+    const uint32_t first = std::min(want, floor_grid);
+    std::unique_lock<std::mutex> lk(mu);
+    cv.wait(lk, [&] { return free_units >= need(first); });
+    uint32_t g = (uint32_t)std::min<uint64_t>(want, (uint64_t)free_units * max_grid / kUnits);
+    g = std::max(g, first);
+    *units = need(g);
+    free_units -= *units;
+    if (active > 0) ++concurrent;
+    ++active;
+    return g;
+  }
+  void release(uint32_t units) {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      free_units += units;
+      --active;
+    }
+    cv.notify_all();
+  }
 };
 
 // A context owns one device, one stream, a device arena (per-call scratch), a
@@ -54,6 +103,7 @@ struct Context {
   std::map<uint64_t, BatchTune> tuned;
   BatchTune last_tune;
   BatchTune pinned_tune{0, 0};  // div != 0: used for every batch (no autotuning)
+  GridBudget *grid_budget = nullptr;  // shared with other contexts' batched launches, if set
 
   ggks_stats stats{};
   uint32_t profiling = 0;  // bit i: time pass i with CUDA events

@@ -1,12 +1,12 @@
 // ggks_noalloc.cu -- a float32 multiselect that allocates no memory.
 //
-// Who needs it: callers that cannot allocate device memory at the point of
-// the call -- code that runs while a CUDA graph is being captured (where a
-// cudaMalloc would break or serialise the capture), engines whose memory is
-// owned by another allocator that must account for every byte, and latency-
-// critical paths that may not block on the allocator.  The regular entry
-// points grow a per-context workspace and pinned staging with cudaMalloc /
-// cudaHostAlloc; this one does not.
+// Who needs it: callers that may not allocate device memory when they
+// select -- an engine or framework whose device memory all belongs to its own
+// allocator, which budgets every byte (a cudaMalloc behind its back can
+// exhaust the device or break that accounting), and latency-bound loops where
+// an allocation would stall on the driver.  The regular entry points grow a
+// per-context workspace and pinned staging with cudaMalloc / cudaHostAlloc;
+// this one does not.
 //
 // How: all scratch lives in one file-scope __device__ array of fixed size
 // (kNaScratchBytes, about 11 MB), which every GPU that loads this library
@@ -17,10 +17,13 @@
 //
 // The array's name is only a host-side stand-in for the device symbol; its
 // device address comes from cudaGetSymbolAddress, called once per device with
-// that device current on the first call there (so the first call on a device
-// must come before any stream capture).  Every call shares the one array:
-// calls whose work overlaps on the GPU (different streams, or several host
-// threads) race and must be serialised by the caller.
+// that device current on the first call there, which also sets the kernels'
+// shared-memory limits on that device (so the first call on a device must
+// come before any stream capture).  Every call shares the one array, which
+// keeps the last call's contents; each call clears the control block and the
+// slice counts, the only parts that must start at zero.  Calls whose work
+// overlaps on the GPU (different streams, or several host threads) race and
+// must be serialised by the caller.
 #include <mutex>
 
 #include "ggks_pipeline.cuh"
@@ -155,6 +158,14 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
   const uint32_t fg = 5u * (uint32_t)sms;
   const uint32_t fin_grid = num_k < fg ? num_k : fg;
 
+  // the kernels' shared-memory limits on this device (set on its first call)
+  e = set_smem_max<k_hist<float, UNROLL>>((int)(kRepWords * sizeof(uint32_t) + (size_t)kMaxNb * 4));
+  if (e == cudaSuccess) e = set_smem_max<k_plan<float, float>>(kPlanSmemMax);
+  if (e == cudaSuccess)
+    e = set_smem_max<k_compact<float, UNROLL>>((int)compact_smem_bytes(kMaxNb));
+  if (e == cudaSuccess) e = set_smem_max<k_finish<K, float>>(finish_smem_bytes<float>());
+  if (e != cudaSuccess) return from_cuda(e);
+
   // the control block and the slice counts start at zero
   e = cudaMemsetAsync(A + kNaCtrl, 0, kNaSliceCnt + kSliceCntBytes, s);
   if (e != cudaSuccess) return from_cuda(e);
@@ -164,8 +175,7 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
                                                reinterpret_cast<uint32_t *>(A + kNaSliceCnt), n,
                                                0u, G);
   {
-    const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kNaNbMax * 4);
-    set_smem_max<k_hist<float, UNROLL>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
+    const int smem = (int)(kRepWords * sizeof(uint32_t) + (size_t)kNaNbMax * 4);
     k_hist<float, UNROLL><<<G, 1024, smem, s>>>(d_vec, n, hdr, lut, partials, kNaNbMax, ctrl,
                                                 nullptr, nullptr, nullptr, nullptr, nullptr,
                                                 nullptr);
@@ -174,23 +184,19 @@ extern "C" int ggks_multiselect_noalloc_f32(const float *d_vec, uint64_t n, cons
                                                   nullptr, nullptr, nullptr);
   {
     const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kNaNbMax * 5);
-    set_smem_max<k_plan<float, float>>(kPlanSmemMax);
     k_plan<float, float><<<1, 1024, smem, s>>>(hdr, lut, bpre, ttot, n, reqs, num_k, kNaNbMax,
                                                 ctrl, seg_bucket, seg_off,
                                                 seg_size, kstart, kcnt, kcur, fill, seg_lo, seg_hi,
                                                 req_bucket, req_local, klist, n, Premap{});
   }
   {
-    const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)kNaNbMax * 4);
-    set_smem_max<k_compact<float, UNROLL>>(
-        (int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
+    const int smem = (int)compact_smem_bytes(kNaNbMax);
     k_compact<float, UNROLL><<<G, 1024, smem, s>>>(d_vec, n, hdr, lut, seg_bucket, seg_off,
                                                    seg_size, partials, fill, kNaNbMax, surv, n,
                                                    ctrl, nullptr, nullptr, nullptr, 0);
   }
   {
     const int smem = finish_smem_bytes<float>();
-    set_smem_max<k_finish<K, float>>(smem);
     k_finish<K, float><<<fin_grid, kFinThreads, smem, s>>>(surv, ctrl, seg_off, seg_size, seg_lo,
                                                           seg_hi, kstart, kcnt, klist, deferred,
                                                           cap_keys, d_out);

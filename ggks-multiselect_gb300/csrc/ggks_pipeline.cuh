@@ -4,6 +4,7 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -155,15 +156,25 @@ static Plan make_plan(const Context &ctx, uint64_t n, uint32_t num_req) {
   return p;
 }
 
-// Raise a kernel's dynamic shared-memory limit once per process (thread-safe
-// static initialisation; one GPU per process).
+// Raise a kernel's dynamic shared-memory limit on the current device.  The
+// attribute belongs to the kernel as loaded on one device, so it is set once
+// per device (the largest value asked for so far is remembered per device);
+// the result of the setting is returned for the caller to check.
 template <auto F>
-static void set_smem_max(int bytes) {
-  static const bool done = [bytes]() {
-    cudaFuncSetAttribute((const void *)F, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    return true;
-  }();
-  (void)done;
+static cudaError_t set_smem_max(int bytes) {
+  static std::atomic<int> set_to[kMaxDevices];  // static storage: starts at zero
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const bool tracked = dev >= 0 && dev < kMaxDevices;
+  if (tracked && set_to[dev].load(std::memory_order_acquire) >= bytes) return cudaSuccess;
+  e = cudaFuncSetAttribute((const void *)F, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess && tracked) {
+    int cur = set_to[dev].load(std::memory_order_acquire);
+    while (cur < bytes && !set_to[dev].compare_exchange_weak(cur, bytes)) {
+    }
+  }
+  return e;
 }
 
 // Launches a pipeline kernel with programmatic stream serialization: it may be
@@ -347,9 +358,9 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   }
   // ---- (c) histogram
   {
-    const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 4);
-    set_smem_max<k_hist<InT, 8>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
-    set_smem_max<k_hist<InT, 4>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
+    const int smem = (int)(kRepWords * sizeof(uint32_t) + (size_t)p.nb_max * 4);
+    L(set_smem_max<k_hist<InT, 8>>((int)(kRepWords * sizeof(uint32_t) + (size_t)kMaxNb * 4)));
+    L(set_smem_max<k_hist<InT, 4>>((int)(kRepWords * sizeof(uint32_t) + (size_t)kMaxNb * 4)));
     PassTimer t(ctx, s, GGKS_PASS_HIST);
     // with a mapped host vector, this pass also writes the device copy d_in
     L(launch(p.unroll8 ? k_hist<InT, 8> : k_hist<InT, 4>, p.G, 1024, smem, s, ingest ? ingest : d_in, n, hdr, lut, partials,
@@ -369,7 +380,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     // per-slot request counters in shared memory unless the requests are premapped
     const int smem = (int)(align_up(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 5, 16) +
                            (num_req < kPremapMin ? kPlanSlotBytes : 0));
-    set_smem_max<k_plan<InT, OutT>>(kPlanSmemMax);
+    L(set_smem_max<k_plan<InT, OutT>>(kPlanSmemMax));
     PassTimer t(ctx, s, GGKS_PASS_PLAN);
     Premap pm;
     const bool premap = num_req >= kPremapMin;
@@ -381,7 +392,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
       // many CTAs (k_reqplace); the plan CTA only numbers the slots
       e = cudaMemsetAsync(pm_bits, 0, (size_t)p.nb_max / 8 + (size_t)p.nb_max * 4, s);
       if (e != cudaSuccess) return from_cuda(e);
-      set_smem_max<k_reqmap>((int)(kMaxNb * 4));
+      L(set_smem_max<k_reqmap>((int)(kMaxNb * 4)));
       L(launch(k_reqmap, (num_req + kReqmapPerCta - 1) / kReqmapPerCta, 1024, p.nb_max * 4, s,
                bpre, ttot, ctrl, rq, num_req, req_bucket, req_local, pm_bits, pm_bcount));
       pm.bits = pm_bits;
@@ -402,9 +413,9 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
   const K *cand_live = cand;  // no candidates once the survivor buffer is replaced
   auto launch_tail = [&]() {
     {
-      const int smem = (int)(kLutPadded * sizeof(uint32_t) + (size_t)p.nb_max * 4);
-      set_smem_max<k_compact<InT, 8>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
-      set_smem_max<k_compact<InT, 4>>((int)(kLutPadded * sizeof(uint32_t) + (size_t)kMaxNb * 4));
+      const int smem = (int)compact_smem_bytes(p.nb_max);
+      L(set_smem_max<k_compact<InT, 8>>((int)compact_smem_bytes(kMaxNb)));
+      L(set_smem_max<k_compact<InT, 4>>((int)compact_smem_bytes(kMaxNb)));
       PassTimer t(ctx, s, GGKS_PASS_COMPACT);
       L(launch(p.unroll8 ? k_compact<InT, 8> : k_compact<InT, 4>, p.G, 1024, smem, s, d_in, n, hdr, lut, seg_bucket, seg_off,
                seg_size, partials, fill, p.nb_max, surv, surv_cap, ctrl, cand_live, cand_cnt,
@@ -413,7 +424,7 @@ int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint
     }
     {
       const int smem = finish_smem_bytes<InT>();
-      set_smem_max<k_finish<K, OutT>>(smem);
+      L(set_smem_max<k_finish<K, OutT>>(smem));
       PassTimer t(ctx, s, GGKS_PASS_FINISH);
       L(launch(k_finish<K, OutT>, p.fin_grid, kFinThreads, smem, s, surv, ctrl, seg_off, seg_size,
                seg_lo, seg_hi, kstart, kcnt, klist, deferred, p.cap_keys, d_out));

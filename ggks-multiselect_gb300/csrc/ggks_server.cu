@@ -2,26 +2,33 @@
 // sizes and element types arrive at any time and are coalesced into batched
 // launches (continuous batching).
 //
-// Two host threads per server:
+// Host threads per server:
 //   admission  takes submitted requests in arrival order while their device
-//              bytes fit the HBM cap (uploaded vector + bucket-state estimate),
-//              copies host vectors to the device on a copy stream, and hands
-//              requests whose data is on the device to the executor;
-//   executor   takes every device-ready request (up to max_batch), runs one
-//              batched selection per element type (select_batch: one
-//              persistent launch each; a type with a single request takes the
-//              single-vector pipeline, whose latency is lower), scatters the
-//              results to the callers' buffers, releases the requests' device
-//              bytes.
-// Requests that arrive while a batch is on the GPU are admitted and uploaded
-// meanwhile (the copy stream overlaps the compute stream) and join the next
-// batch.  Batches run one after another on the compute stream, so no two
-// cooperative launches are ever in flight together.
+//              bytes (uploaded vector + bucket-state estimate) fit the
+//              admission budget -- the HBM cap, and the device's free memory
+//              less a reserve -- copies host vectors to the device on a copy
+//              stream, and hands requests whose data is on the device to the
+//              lanes;
+//   lanes      (2 by default) each take every device-ready request (up to
+//              max_batch), run one batched selection per element type
+//              (select_batch: one persistent launch each; a type with a
+//              single request takes the single-vector pipeline, whose latency
+//              is lower), scatter the results to the callers' buffers and
+//              release the requests' device bytes.  Each lane has its own
+//              context (stream and workspace), so one lane plans and uploads
+//              its batch while another's runs, and their launches run on the
+//              device together: the persistent grids take shares of the
+//              co-resident CTAs (GridBudget), so every grid in flight is
+//              resident at once.
+// Requests that arrive while batches are on the GPU are admitted and uploaded
+// meanwhile and join the next batch.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <unordered_map>
@@ -49,11 +56,21 @@ struct SReq {
   bool done = false;
 };
 
+struct Lane {
+  Context ctx;
+  std::thread thr;
+};
+
+constexpr uint64_t kDefaultReserve = 1ull << 30;
+constexpr uint32_t kMaxLanes = 8;
+
 struct Server {
   int device = 0;
-  uint64_t cap = 0, used = 0;
+  uint64_t cap = 0, used = 0, reserve = kDefaultReserve;
   uint32_t max_batch = 0;
-  Context ctx;
+  std::vector<std::unique_ptr<Lane>> lanes;
+  GridBudget budget;
+  std::atomic<uint32_t> groups_running{0};
   cudaStream_t copy_stream = nullptr;
   std::mutex mu;
   std::condition_variable cv_admit, cv_exec, cv_done;
@@ -63,7 +80,7 @@ struct Server {
   std::unordered_map<uint64_t, SReq *> live;
   uint64_t next_ticket = 1;
   bool stopping = false;
-  std::thread admit_thr, exec_thr;
+  std::thread admit_thr;
   ggks_server_stats st{};
 };
 
@@ -76,18 +93,57 @@ static uint64_t charge_of(const SReq &r) {
   return (r.host ? vb : 0) + 65536 + vb / 16 + (uint64_t)r.k.size() * 64;
 }
 
+// Admission budget: the cap, and no more than the device's free memory
+// (less the reserve) on top of the bytes already admitted.
+static uint64_t admit_budget(Server *S) {
+  size_t fr = 0, tot = 0;
+  uint64_t hbm = S->cap;
+  if (cudaMemGetInfo(&fr, &tot) == cudaSuccess)
+    hbm = S->used + (fr > S->reserve ? (uint64_t)fr - S->reserve : 0ull);
+  const uint64_t b = std::min(S->cap, hbm);
+  S->st.admit_budget_bytes = b;
+  return b;
+}
+
 static void admit_loop(Server *S) {
   cudaSetDevice(S->device);
   std::unique_lock<std::mutex> lk(S->mu);
+  bool held = false;       // the head waits for device memory ...
+  uint64_t used_at_hold = 0;  // ... since the admitted bytes were this much
   for (;;) {
+    // a held head is tried again once admitted bytes have been released
     S->cv_admit.wait(lk, [&] {
       return S->stopping || !S->uploading.empty() ||
-             (!S->pending.empty() && S->used + S->pending.front()->bytes <= S->cap);
+             (!S->pending.empty() && S->used + S->pending.front()->bytes <= S->cap &&
+              (!held || S->used < used_at_hold));
     });
     if (S->stopping && S->pending.empty() && S->uploading.empty()) return;
-    // admit in arrival order while the cap allows
+    // admit in arrival order while the cap and the free memory allow; the
+    // budget is taken once per round (cudaMemGetInfo), again when the head
+    // does not fit it
+    uint64_t budget = admit_budget(S);
+    held = false;
     while (!S->pending.empty() && S->used + S->pending.front()->bytes <= S->cap) {
       SReq *r = S->pending.front();
+      if (S->used + r->bytes > budget) {
+        budget = admit_budget(S);
+        if (S->used + r->bytes > budget) {
+          if (S->used == 0 && S->uploading.empty()) {
+            // nothing admitted will free memory: it cannot fit
+            S->pending.pop_front();
+            r->status = GGKS_OOM;
+            r->t_done = Clock::now();
+            r->done = true;
+            S->st.completed++;
+            S->cv_done.notify_all();
+            continue;
+          }
+          S->st.hbm_waits++;
+          held = true;  // retried when an admitted request completes
+          used_at_hold = S->used;
+          break;
+        }
+      }
       S->pending.pop_front();
       S->used += r->bytes;
       S->st.peak_bytes = std::max(S->st.peak_bytes, S->used);
@@ -123,17 +179,21 @@ static void admit_loop(Server *S) {
 }
 
 template <class T>
-static void run_group(Server *S, std::vector<SReq *> &g) {
+static void run_group(Server *S, Context &ctx, std::vector<SReq *> &g) {
   if (g.size() == 1) {
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->st.single_calls++;
+    }
     // a lone request: the single-vector pipeline has the lower latency
     SReq *r = g[0];
     const T *vec = static_cast<const T *>(r->host ? r->dvec : r->vec);
     ReqSource src;
     src.h_k = r->k.data();
     const T *res = nullptr;
-    std::lock_guard<std::mutex> lk(S->ctx.mu);
-    r->status = select<T, T>(S->ctx, vec, r->n, src, (uint32_t)r->k.size(), nullptr, &res,
-                             S->ctx.stream, nullptr);
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    r->status = select<T, T>(ctx, vec, r->n, src, (uint32_t)r->k.size(), nullptr, &res,
+                             ctx.stream, nullptr);
     if (r->status == GGKS_OK) std::memcpy(r->out, res, r->k.size() * sizeof(T));
     return;
   }
@@ -153,9 +213,14 @@ static void run_group(Server *S, std::vector<SReq *> &g) {
   in.num_problems = (uint32_t)g.size();
   in.k_off = off.data();
   in.k = ks.data();
-  std::lock_guard<std::mutex> lk(S->ctx.mu);
-  const BatchTune tune = S->ctx.pinned_tune.div ? S->ctx.pinned_tune : BatchTune{};
-  const int st = select_batch<T>(S->ctx, in, nullptr, out.data(), S->ctx.stream, tune, nullptr);
+  std::lock_guard<std::mutex> lk(ctx.mu);
+  const BatchTune tune = ctx.pinned_tune.div ? ctx.pinned_tune : BatchTune{};
+  float kms = 0.f;
+  const int st = select_batch<T>(ctx, in, nullptr, out.data(), ctx.stream, tune, &kms);
+  {
+    std::lock_guard<std::mutex> lk2(S->mu);
+    S->st.kernel_ms += kms;
+  }
   for (size_t i = 0; i < g.size(); ++i) {
     if (st != GGKS_OK) {
       g[i]->status = st;
@@ -167,10 +232,10 @@ static void run_group(Server *S, std::vector<SReq *> &g) {
 
 // marks a finished group done: frees its uploads, releases its bytes and
 // wakes its waiters and the admission thread
-static void complete(Server *S, std::vector<SReq *> &g, bool launched) {
+static void complete(Server *S, cudaStream_t stream, std::vector<SReq *> &g, bool launched) {
   for (SReq *r : g)
-    if (r->dvec) cudaFreeAsync(r->dvec, S->ctx.stream);
-  cudaStreamSynchronize(S->ctx.stream);
+    if (r->dvec) cudaFreeAsync(r->dvec, stream);
+  cudaStreamSynchronize(stream);
   const auto now = Clock::now();
   std::lock_guard<std::mutex> lk(S->mu);
   for (SReq *r : g) {
@@ -187,7 +252,23 @@ static void complete(Server *S, std::vector<SReq *> &g, bool launched) {
   S->cv_admit.notify_one();
 }
 
-static void exec_loop(Server *S) {
+// runs one element type's group on a lane; counts it as concurrent when
+// another lane's group is on the device at the same time
+template <class T>
+static void run_counted(Server *S, Lane &L, std::vector<SReq *> &g) {
+  const auto t0 = Clock::now();
+  if (S->groups_running.fetch_add(1) > 0) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->st.concurrent_launches++;
+  }
+  run_group<T>(S, L.ctx, g);
+  S->groups_running.fetch_sub(1);
+  complete(S, L.ctx.stream, g, true);
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->st.group_ms += std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
+
+static void lane_loop(Server *S, Lane *L) {
   cudaSetDevice(S->device);
   std::vector<SReq *> batch;
   for (;;) {
@@ -197,7 +278,10 @@ static void exec_loop(Server *S) {
         return !S->ready.empty() ||
                (S->stopping && S->pending.empty() && S->uploading.empty());
       });
-      if (S->ready.empty()) return;
+      if (S->ready.empty()) {
+        S->cv_exec.notify_all();  // the other lanes stop too
+        return;
+      }
       batch.clear();
       while (!S->ready.empty() && (S->max_batch == 0 || batch.size() < S->max_batch)) {
         batch.push_back(S->ready.front());
@@ -209,19 +293,10 @@ static void exec_loop(Server *S) {
     }
     std::vector<SReq *> g[3], failed;
     for (SReq *r : batch) (r->status == GGKS_OK ? g[r->dtype] : failed).push_back(r);
-    if (!failed.empty()) complete(S, failed, false);
-    if (!g[GGKS_DTYPE_F32].empty()) {
-      run_group<float>(S, g[GGKS_DTYPE_F32]);
-      complete(S, g[GGKS_DTYPE_F32], true);
-    }
-    if (!g[GGKS_DTYPE_U32].empty()) {
-      run_group<uint32_t>(S, g[GGKS_DTYPE_U32]);
-      complete(S, g[GGKS_DTYPE_U32], true);
-    }
-    if (!g[GGKS_DTYPE_F64].empty()) {
-      run_group<double>(S, g[GGKS_DTYPE_F64]);
-      complete(S, g[GGKS_DTYPE_F64], true);
-    }
+    if (!failed.empty()) complete(S, L->ctx.stream, failed, false);
+    if (!g[GGKS_DTYPE_F32].empty()) run_counted<float>(S, *L, g[GGKS_DTYPE_F32]);
+    if (!g[GGKS_DTYPE_U32].empty()) run_counted<uint32_t>(S, *L, g[GGKS_DTYPE_U32]);
+    if (!g[GGKS_DTYPE_F64].empty()) run_counted<double>(S, *L, g[GGKS_DTYPE_F64]);
   }
 }
 
@@ -232,12 +307,18 @@ using namespace ggks;
 extern "C" {
 
 int ggks_server_create(const ggks_server_config *cfg, ggks_server **out) {
-  if (!cfg || !out || cfg->hbm_cap_bytes == 0) return GGKS_INVALID_ARG;
+  if (!cfg || !out || cfg->hbm_cap_bytes == 0 || cfg->lanes > kMaxLanes) return GGKS_INVALID_ARG;
   *out = nullptr;
   Server *S = new Server();
+  const uint32_t nl = cfg->lanes ? cfg->lanes : 2u;
   int cur = -1;
   cudaGetDevice(&cur);
-  int st = context_init(S->ctx, cfg->device);
+  int st = GGKS_OK;
+  for (uint32_t i = 0; i < nl && st == GGKS_OK; ++i) {
+    S->lanes.emplace_back(new Lane());
+    st = context_init(S->lanes.back()->ctx, cfg->device);
+    S->lanes.back()->ctx.grid_budget = &S->budget;
+  }
   if (st == GGKS_OK &&
       cudaStreamCreateWithFlags(&S->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
     st = GGKS_CUDA_ERROR;
@@ -248,9 +329,12 @@ int ggks_server_create(const ggks_server_config *cfg, ggks_server **out) {
   }
   S->device = cfg->device;
   S->cap = cfg->hbm_cap_bytes;
+  S->reserve = cfg->hbm_reserve_bytes ? cfg->hbm_reserve_bytes : kDefaultReserve;
   S->max_batch = cfg->max_batch;
+  // a launch waits for an even share of the device (or all it wants)
+  S->budget.floor_units = GridBudget::kUnits / nl;
   S->admit_thr = std::thread(admit_loop, S);
-  S->exec_thr = std::thread(exec_loop, S);
+  for (auto &L : S->lanes) L->thr = std::thread(lane_loop, S, L.get());
   *out = reinterpret_cast<ggks_server *>(S);
   return GGKS_OK;
 }
@@ -269,7 +353,7 @@ int ggks_server_destroy(ggks_server *srv) {
     std::lock_guard<std::mutex> lk(S->mu);
   }
   S->cv_exec.notify_all();
-  S->exec_thr.join();
+  for (auto &L : S->lanes) L->thr.join();
   for (auto &kv : S->live) delete kv.second;
   int cur = -1;
   cudaGetDevice(&cur);
@@ -341,16 +425,33 @@ int ggks_server_wait(ggks_server *srv, uint64_t ticket, double *latency_ms) {
 int ggks_server_get_stats(ggks_server *srv, ggks_server_stats *out) {
   if (!srv || !out) return GGKS_INVALID_ARG;
   Server *S = reinterpret_cast<Server *>(srv);
-  std::lock_guard<std::mutex> lk(S->mu);
-  *out = S->st;
-  out->in_flight_bytes = S->used;
+  ggks_server_stats st;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    st = S->st;
+    st.in_flight_bytes = S->used;
+  }
+  // the lanes' batched phases and recursions, read under each lane's lock
+  st.recursions = 0;
+  for (int ph = 0; ph < GGKS_NUM_BATCH_PHASES; ++ph) st.batch_phase_ms[ph] = 0.0;
+  for (auto &L : S->lanes) {
+    std::lock_guard<std::mutex> lk(L->ctx.mu);
+    st.recursions += L->ctx.stats.recursions;
+    for (int ph = 0; ph < GGKS_NUM_BATCH_PHASES; ++ph)
+      st.batch_phase_ms[ph] += L->ctx.stats.batch_phase_ms[ph];
+  }
+  *out = st;
   return GGKS_OK;
 }
 
 int ggks_server_set_tuning(ggks_server *srv, uint32_t div, uint32_t tile) {
   if (!srv) return GGKS_INVALID_ARG;
   Server *S = reinterpret_cast<Server *>(srv);
-  return ggks_batch_set_tuning(reinterpret_cast<ggks_context *>(&S->ctx), div, tile);
+  for (auto &L : S->lanes) {
+    const int st = ggks_batch_set_tuning(reinterpret_cast<ggks_context *>(&L->ctx), div, tile);
+    if (st != GGKS_OK) return st;
+  }
+  return GGKS_OK;
 }
 
 }  // extern "C"

@@ -75,7 +75,8 @@ REQ_HOST_VECTOR = 2
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("max_batch", ctypes.c_uint32),
-                ("hbm_cap_bytes", ctypes.c_uint64)]
+                ("hbm_cap_bytes", ctypes.c_uint64), ("hbm_reserve_bytes", ctypes.c_uint64),
+                ("lanes", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class Request(ctypes.Structure):
@@ -87,10 +88,17 @@ class Request(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [(f, ctypes.c_uint64) for f in (
         "submitted", "completed", "batches", "batched_requests", "max_batch_seen", "launches",
-        "uploads", "upload_bytes", "peak_bytes", "in_flight_bytes")]
+        "uploads", "upload_bytes", "peak_bytes", "in_flight_bytes", "concurrent_launches",
+        "hbm_waits", "admit_budget_bytes", "single_calls", "recursions")] + [
+        ("batch_phase_ms", ctypes.c_double * NUM_BATCH_PHASES), ("kernel_ms", ctypes.c_double),
+        ("group_ms", ctypes.c_double)]
 
     def as_dict(self):
-        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+        d = {f: int(getattr(self, f)) for f, t in self._fields_ if t is ctypes.c_uint64}
+        d["batch_phase_ms"] = dict(zip(BATCH_PHASE_NAMES, list(self.batch_phase_ms)))
+        d["kernel_ms"] = float(self.kernel_ms)
+        d["group_ms"] = float(self.group_ms)
+        return d
 
 
 # every symbol declared in include/ggks.h
@@ -452,8 +460,10 @@ class Server:
     """A ggks_server: requests submitted from any thread are admitted under an
     HBM cap and coalesced into batched launches (continuous batching)."""
 
-    def __init__(self, device=0, hbm_cap_bytes=64 << 30, max_batch=0):
-        cfg = ServerConfig(int(device), int(max_batch), int(hbm_cap_bytes))
+    def __init__(self, device=0, hbm_cap_bytes=64 << 30, max_batch=0, hbm_reserve_bytes=0,
+                 lanes=0):
+        cfg = ServerConfig(int(device), int(max_batch), int(hbm_cap_bytes),
+                           int(hbm_reserve_bytes), int(lanes), 0)
         h = ctypes.c_void_p()
         _check(lib().ggks_server_create(ctypes.byref(cfg), ctypes.byref(h)), "server_create")
         self.handle = h

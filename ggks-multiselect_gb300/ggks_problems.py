@@ -237,6 +237,55 @@ def k_sectioned(n, count, seed):
 
 
 # ---------------------------------------------------------------------------
+# the single-vector configurations, as seeded inputs (the benchmark times them;
+# the full-size parity tests check the same inputs)
+# ---------------------------------------------------------------------------
+# plain: 2^20 float32 uniform [0, 1), seed 0, 101 k's on the p grid
+P_LOG2N = 20
+# large: 1001 distinct k's uniform in [1, n] (seed 100 + the input's seed)
+L_NUM_K = 1001
+L_INPUTS = (  # (name, dtype, distribution, log2 n, seed)
+    ("f32_normal", "f32", "normal", 28, 1),
+    ("f32_cauchy", "f32", "cauchy", 28, 2),
+    ("f32_half_normal", "f32", "half_normal", 28, 3),
+    ("u32_uniform", "u32", "uniform", 28, 4),
+    ("f64_uniform_pm1e6", "f64", "uniform_pm1e6", 27, 5),
+)
+# top-k: 2^26 elements, K in T_KS; the ascending input is the sorted float32 one
+T_LOG2N = 26
+T_KS = (32, 1024, 65536)
+T_INPUTS = ("f32_uniform", "u32_uniform16", "f32_sorted")
+
+
+def config_p():
+    """The plain configuration: (vector, k list)."""
+    n = 1 << P_LOG2N
+    return uniform_f32(n, 0), k_pgrid(n, 101)
+
+
+def config_l(name, log2n=None):
+    """One input of the large configuration: (vector, k list); log2n
+    overrides the size (smaller runs of the same recipe)."""
+    for nm, dt, dist, lg, seed in L_INPUTS:
+        if nm == name:
+            n = 1 << (lg if log2n is None else log2n)
+            return generate(dt, dist, n, seed), k_distinct(n, L_NUM_K, 100 + seed)
+    raise KeyError(name)
+
+
+def config_t(name, log2n=T_LOG2N):
+    """One input of the top-k configuration."""
+    n = 1 << log2n
+    if name == "f32_uniform":
+        return uniform_f32(n, 0)
+    if name == "u32_uniform16":
+        return uniform_u32(n, 1, 1 << 16)
+    if name == "f32_sorted":
+        return np.sort(uniform_f32(n, 0))
+    raise KeyError(name)
+
+
+# ---------------------------------------------------------------------------
 # batched workload: many independent vectors of uneven lengths
 # ---------------------------------------------------------------------------
 BATCH_DISTS = ("uniform", "normal", "cauchy", "uint_valued")

@@ -130,12 +130,13 @@ int ggks_select_u32(const uint32_t *d_vec, uint64_t n, uint32_t k, uint32_t *out
 /* ------------------------------------------------------------------------ */
 
 /* No counterpart in the reference.  A float32 multiselect for callers that
- * cannot allocate memory when they call it: code running while a CUDA graph is
- * captured, engines whose device memory belongs to another allocator, and
- * latency-critical paths that may not block on an allocator.  It calls no
- * cudaMalloc, cudaFree, cudaHostAlloc or other allocating routine; its scratch
- * is one fixed device array (about 11 MB) that every GPU loading this library
- * holds until the process exits.
+ * may not allocate memory when they select: an engine or framework whose
+ * device memory all belongs to its own allocator, which budgets every byte (an
+ * allocation behind its back can exhaust the device or break its accounting),
+ * and latency-bound loops where an allocation would stall on the driver.  It
+ * calls no cudaMalloc, cudaFree, cudaHostAlloc or other allocating routine; its
+ * scratch is one fixed device array (about 11 MB) that every GPU loading this
+ * library holds until the process exits.
  *   d_vec: device vector of n floats; d_k: device array of num_k k's (k-th
  *   largest, 1-based); d_out: device array of num_k results in k order;
  *   stream: a cudaStream_t (NULL: the legacy default stream).  The call
@@ -143,8 +144,11 @@ int ggks_select_u32(const uint32_t *d_vec, uint64_t n, uint32_t k, uint32_t *out
  * Limits: 1 <= n <= GGKS_NOALLOC_MAX_N and 1 <= num_k <= GGKS_NOALLOC_MAX_K,
  * else GGKS_INVALID_ARG (also for a k outside [1, n]); an input whose buckets
  * would need a recursive re-selection (heavy, nearly equal duplicates) returns
- * GGKS_UNSUPPORTED.  The first call on a device looks up the scratch's device
- * address; make it before capturing a stream.  All calls share the scratch:
+ * GGKS_UNSUPPORTED (d_out may then hold partial results; nothing past its
+ * num_k entries is written).  The first call on a device looks up the
+ * scratch's device address and sets the kernels' shared-memory limits there;
+ * make it before any stream capture.  All calls share the scratch, which
+ * keeps the last call's contents (each call clears what must start at zero):
  * calls that overlap on the GPU race and must be serialised by the caller. */
 #define GGKS_NOALLOC_MAX_N (1ull << 21)
 #define GGKS_NOALLOC_MAX_K 2048u
@@ -204,6 +208,11 @@ int ggks_batch_last_tuning(ggks_context *ctx, uint32_t *div, uint32_t *tile);
  * instead of the autotuner's choice; div = 0 unpins. */
 int ggks_batch_set_tuning(ggks_context *ctx, uint32_t div, uint32_t tile);
 
+/* passes of a single-vector call and phases of a batched launch, as counted
+ * by the statistics below */
+#define GGKS_NUM_PASSES 6
+#define GGKS_NUM_BATCH_PHASES 5
+
 /* ------------------------------------------------------------------------ */
 /* Serving loop                                                              */
 /* ------------------------------------------------------------------------ */
@@ -214,19 +223,29 @@ int ggks_batch_set_tuning(ggks_context *ctx, uint32_t div, uint32_t tile);
  * time, from any thread, and coalesces them into batched launches:
  *   - admission: requests are taken in arrival order while the device bytes
  *     of the admitted ones (uploaded vector + bucket-state estimate) stay
- *     within hbm_cap_bytes; a host vector is copied to the device then, on a
- *     copy stream that overlaps the running batch;
- *   - execution: every request whose data is on the device (at most max_batch,
- *     0 = no limit) joins the next batch; one persistent launch per element
- *     type present.  Requests arriving meanwhile join the batch after it.
+ *     within the admission budget, min(hbm_cap_bytes, the device's free
+ *     memory - hbm_reserve_bytes + the bytes already admitted); a request
+ *     that does not fit waits for earlier ones to finish (GGKS_OOM if nothing
+ *     is admitted and it still does not fit).  A host vector is copied to the
+ *     device then, on a copy stream that overlaps the running batches;
+ *   - execution: `lanes` executors (each with its own stream and workspace)
+ *     each take the requests whose data is on the device (at most max_batch,
+ *     0 = no limit) and run them as one persistent launch per element type
+ *     present.  Batches of different lanes are planned, uploaded and run on
+ *     the device at the same time; their persistent grids share the device's
+ *     co-resident CTAs, so that every grid is resident at once.  Requests
+ *     arriving meanwhile join the next batch.
  * Each result equals the result of the single-vector entry point on the same
  * vector and k's, bit for bit. */
 typedef struct ggks_server ggks_server;
 
 typedef struct ggks_server_config {
   int device;
-  uint32_t max_batch;     /* requests per batch at most; 0 = no limit */
-  uint64_t hbm_cap_bytes; /* admission cap on the admitted requests' device bytes */
+  uint32_t max_batch;         /* requests per batch at most; 0 = no limit */
+  uint64_t hbm_cap_bytes;     /* admission cap on the admitted requests' device bytes */
+  uint64_t hbm_reserve_bytes; /* device memory admission leaves free; 0 = 1 GiB */
+  uint32_t lanes;             /* batches in flight at once, 1..8; 0 = 2 */
+  uint32_t reserved;
 } ggks_server_config;
 
 #define GGKS_DTYPE_F32 0
@@ -255,6 +274,14 @@ typedef struct ggks_server_stats {
   uint64_t uploads, upload_bytes; /* host vectors copied at admission */
   uint64_t peak_bytes;       /* largest admitted device bytes */
   uint64_t in_flight_bytes;  /* admitted device bytes now */
+  uint64_t concurrent_launches; /* launches started while another lane's batch ran */
+  uint64_t hbm_waits;        /* admissions held back by the device's free memory */
+  uint64_t admit_budget_bytes; /* the admission budget at the last admission */
+  uint64_t single_calls;     /* lone requests of a type run on the single-vector pipeline */
+  uint64_t recursions;       /* oversized segments re-selected, all lanes */
+  double batch_phase_ms[GGKS_NUM_BATCH_PHASES]; /* device time per batch phase, all lanes */
+  double kernel_ms;          /* device time of the batched launches, all lanes */
+  double group_ms;           /* lane wall time per element-type group (plan, run, results) */
 } ggks_server_stats;
 
 int ggks_server_create(const ggks_server_config *cfg, ggks_server **out);
@@ -281,9 +308,9 @@ int ggks_server_set_tuning(ggks_server *srv, uint32_t div, uint32_t tile);
 int ggks_context_create(int device, ggks_context **out);
 int ggks_context_destroy(ggks_context *ctx);
 
-/* Per-pass statistics of a context, accumulated since the last reset. */
-#define GGKS_NUM_PASSES 6
-#define GGKS_NUM_BATCH_PHASES 5
+/* Per-pass statistics of a context, accumulated since the last reset
+ * (GGKS_NUM_PASSES and GGKS_NUM_BATCH_PHASES are defined with the batched
+ * entry points). */
 typedef struct ggks_stats {
   uint64_t calls;                     /* selection calls completed */
   uint64_t launches;                  /* kernels launched by this library */

@@ -27,10 +27,12 @@
  * compares with the native operator<, which leaves those cases unordered; for
  * all other inputs the two orders are identical.
  *
- * Parity pin: the reference ships no golden vectors for this path and its
- * path only runs on a GPU; the oracle is pinned by closed-form known-answer
+ * Parity unpinned: the reference ships no golden vectors for this path, and
+ * its path (CUDA kernels and Thrust on the device, sort-and-choose included)
+ * runs only on a GPU, so no output of the reference itself stands behind this
+ * restatement.  It is checked instead against closed-form known-answer
  * vectors built from the reference's deterministic generators
- * (generateProblems.cu) and by an independent sort (numpy) in the tests.
+ * (generateProblems.cu) and against an independent sort (numpy) in the tests.
  */
 #ifndef GGKS_ORACLE_H_
 #define GGKS_ORACLE_H_
@@ -77,6 +79,16 @@ int ggks_oracle_bucket_multiselect_f64(const double *vec, uint32_t n, const uint
                                        uint32_t num_k, double *out, uint64_t seed);
 int ggks_oracle_bucket_multiselect_u32(const uint32_t *vec, uint32_t n, const uint32_t *k,
                                        uint32_t num_k, uint32_t *out, uint64_t seed);
+
+/* Sort-and-choose multiselect on one thread with the C++ standard library's
+ * std::sort of the keys (ggks_oracle_stdsort.cpp): the benchmark's CPU
+ * baseline.  Same k convention and output as ggks_oracle_multiselect_*. */
+int ggks_oracle_multiselect_stdsort_f32(const float *vec, uint64_t n, const uint32_t *k,
+                                        uint32_t num_k, float *out);
+int ggks_oracle_multiselect_stdsort_f64(const double *vec, uint64_t n, const uint32_t *k,
+                                        uint32_t num_k, double *out);
+int ggks_oracle_multiselect_stdsort_u32(const uint32_t *vec, uint64_t n, const uint32_t *k,
+                                        uint32_t num_k, uint32_t *out);
 
 /* Ascending sort of keys (LSD radix); exposed for tests of the oracle. */
 int ggks_oracle_sort_keys_u32(uint32_t *keys, uint64_t n, int threads);

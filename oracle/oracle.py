@@ -17,6 +17,8 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libggks_oracle.so")
 SRC_PATH = os.path.join(_HERE, "ggks_oracle.c")
+SRC_CPP = os.path.join(_HERE, "ggks_oracle_stdsort.cpp")
+HDR_PATH = os.path.join(_HERE, "ggks_oracle.h")
 
 _lib = None
 
@@ -25,13 +27,21 @@ _SUFFIX = {np.dtype(np.float32): "f32", np.dtype(np.float64): "f64",
 
 
 def build(force=False):
-    """Compile the oracle with gcc into oracle/libggks_oracle.so."""
+    """Compile the oracle (gcc for the C restatement, g++ for the std::sort
+    baseline) into oracle/libggks_oracle.so."""
+    srcs = (SRC_PATH, SRC_CPP, HDR_PATH)
     if (not force and os.path.exists(LIB_PATH)
-            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC_PATH)):
+            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(p) for p in srcs)):
         return LIB_PATH
-    cmd = ["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-pthread",
-           SRC_PATH, "-o", LIB_PATH, "-lm"]
-    subprocess.run(cmd, check=True)
+    tmp = LIB_PATH + f".{os.getpid()}"
+    o_c, o_cpp = tmp + ".c.o", tmp + ".cpp.o"
+    subprocess.run(["gcc", "-O3", "-std=c11", "-fPIC", "-pthread", "-c", SRC_PATH, "-o", o_c],
+                   check=True)
+    subprocess.run(["g++", "-O3", "-std=c++17", "-fPIC", "-c", SRC_CPP, "-o", o_cpp], check=True)
+    subprocess.run(["g++", "-shared", "-pthread", o_c, o_cpp, "-o", tmp, "-lm"], check=True)
+    os.replace(tmp, LIB_PATH)  # atomic: concurrent builders never see a partial file
+    for f in (o_c, o_cpp):
+        os.remove(f)
     return LIB_PATH
 
 
@@ -50,6 +60,9 @@ def lib():
             f.restype = ctypes.c_int
             f = getattr(L, "ggks_oracle_bucket_multiselect_" + sfx)
             f.argtypes = [P, ctypes.c_uint32, P, ctypes.c_uint32, P, ctypes.c_uint64]
+            f.restype = ctypes.c_int
+            f = getattr(L, "ggks_oracle_multiselect_stdsort_" + sfx)
+            f.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32, P]
             f.restype = ctypes.c_int
         for sfx in ("u32", "u64"):
             f = getattr(L, "ggks_oracle_sort_keys_" + sfx)
@@ -77,6 +90,19 @@ def multiselect(vec, k, threads=1):
     rc = getattr(lib(), "ggks_oracle_multiselect_" + sfx)(
         _ptr(vec), vec.size, _ptr(k), k.size, _ptr(out), int(threads))
     _check(rc, "multiselect")
+    return out
+
+
+def multiselect_stdsort(vec, k):
+    """Sort-and-choose multiselect with one thread's std::sort (the CPU
+    baseline of the benchmark)."""
+    vec = np.ascontiguousarray(vec)
+    k = np.ascontiguousarray(k, dtype=np.uint32)
+    out = np.empty(len(k), dtype=vec.dtype)
+    sfx = _SUFFIX[vec.dtype]
+    rc = getattr(lib(), "ggks_oracle_multiselect_stdsort_" + sfx)(
+        _ptr(vec), vec.size, _ptr(k), k.size, _ptr(out))
+    _check(rc, "multiselect_stdsort")
     return out
 
 

@@ -44,12 +44,27 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_binary_is_sm103a(lib):
+    """The built library's fat binary holds device code for sm_103a only: the
+    CUDA toolkit's listing of its embedded ELF images names one per
+    translation unit, every one for sm_103a, and no PTX for a JIT to fall
+    back on."""
+    import shutil
+    import subprocess
+
     import ggks
-    # the fat binary carries sm_103a code (checked through nvcc's own listing
-    # tool would need a GPU-free dump; the build flags are asserted instead)
-    import ggks_build
-    assert "arch=compute_103a,code=sm_103a" in ggks_build.ARCH
-    assert os.path.getsize(ggks.LIB_PATH) > 100_000
+    tool = shutil.which("cuobjdump") or os.path.join(
+        os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "cuobjdump")
+    if not os.path.exists(tool):
+        pytest.skip("cuobjdump not installed")
+    r = subprocess.run([tool, "--list-elf", ggks.LIB_PATH], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    names = re.findall(r"ELF file\s+\d+:\s+(\S+)", r.stdout)
+    units = {os.path.basename(p)[:-3] for p in
+             __import__("glob").glob(os.path.join(ROOT, "ggks-multiselect_gb300", "csrc", "*.cu"))}
+    assert names and all(n.endswith(".sm_103a.cubin") for n in names), names
+    assert units <= {n.split(".")[0] for n in names}, (units, names)
+    r = subprocess.run([tool, "--list-ptx", ggks.LIB_PATH], capture_output=True, text=True)
+    assert not re.search(r"PTX file\s+\d+:", r.stdout + r.stderr), r.stdout
 
 
 def test_status_strings(lib):

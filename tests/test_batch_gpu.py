@@ -172,17 +172,17 @@ def test_batch_survivor_overflow_and_single_key_bins(g, orc):
 
 
 def test_batch_deferred_segments_recurse(g, orc):
-    """float64: 30% of the vector is a dense cluster of distinct keys just
-    above 1.0 (within 2^22 keys), the rest a narrow normal around it plus a few
-    huge values, so the buckets around 1.0 are about 2^40 keys wide: the
-    cluster's bin holds hundreds of thousands of distinct keys and exceeds the
-    finisher's shared memory.  The slot is selected again on its keys
-    (recursive level)."""
+    """float64: 30% of the vector is two neighbouring keys (1.0 and the next
+    double), the rest a narrow normal around them plus a few huge values, so
+    the buckets around 1.0 are about 2^40 keys wide: the finisher's bin holding
+    the two keys holds some 600 000 of them (even over the segment's actual
+    key range) and exceeds its shared memory.  The slot is selected again on
+    its keys (recursive level)."""
     r = np.random.default_rng(3)
     n = 1 << 21
     x = 1.0 + r.standard_normal(n) * 1e-3
     m = (3 * n) // 10
-    x[:m] = 1.0 + r.integers(0, 1 << 20, m) * 2.0 ** -50
+    x[:m] = np.where(r.random(m) < 0.5, 1.0, np.nextafter(1.0, 2.0))
     x[-16:] = np.array([1e300, -1e300] * 8)
     r.shuffle(x)
     ctx = g.Context(0)

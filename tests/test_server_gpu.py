@@ -1,7 +1,9 @@
 """GPU tests of the serving loop (ggks_server_*): requests of mixed sizes,
-element types and kinds are admitted under an HBM cap and coalesced into
-batched launches; each result must equal, bit for bit, the single-vector
-entry point on the same vector and k's (the result "alone")."""
+element types and kinds are admitted under an HBM cap and the device's free
+memory and coalesced into batched launches on several lanes; each result must
+equal, bit for bit, the single-vector entry point on the same vector and k's
+(the result "alone") and the oracle (sort-and-choose)."""
+import os
 import threading
 
 import numpy as np
@@ -20,6 +22,18 @@ def g():
     import ggks
     ggks.lib()
     return ggks
+
+
+@pytest.fixture(scope="module")
+def orc():
+    import oracle
+    oracle.build()
+    return oracle
+
+
+def _oracle(orc, x, kind, arg):
+    thr = os.cpu_count() or 1
+    return orc.multiselect(x, arg, thr) if kind == "ms" else orc.topk(x, arg, thr)
 
 
 def _mixed_requests(seed, count, max_log2=22):
@@ -51,10 +65,12 @@ def _alone(g, d, x, kind, arg):
     return g.topk_ptr(d.ptr, x.size, x.dtype, arg)
 
 
-def test_server_results_same_alone_and_in_mix(g):
+def test_server_results_same_alone_and_in_mix(g, orc):
     reqs = _mixed_requests(1, 80)
     devs = [DeviceArray(x) for x, _, _ in reqs]
     alone = [_alone(g, d, x, kind, arg) for d, (x, kind, arg) in zip(devs, reqs)]
+    for i, (x, kind, arg) in enumerate(reqs):
+        assert_same(alone[i], _oracle(orc, x, kind, arg), f"alone vs oracle {i}")
     srv = g.Server(0, hbm_cap_bytes=64 << 30)
     tickets = []
     for d, (x, kind, arg) in zip(devs, reqs):
@@ -74,7 +90,7 @@ def test_server_results_same_alone_and_in_mix(g):
     assert st["max_batch_seen"] > 1
 
 
-def test_server_host_vectors_under_a_small_cap(g):
+def test_server_host_vectors_under_a_small_cap(g, orc):
     """Host vectors are uploaded at admission; the admitted bytes never exceed
     the cap, so requests wait for earlier ones to finish."""
     import ggks_problems as gp
@@ -89,15 +105,16 @@ def test_server_host_vectors_under_a_small_cap(g):
     for i, (x, k) in enumerate(zip(xs, ks)):
         d = DeviceArray(x)
         assert_same(res[i], g.multiselect_ptr(d.ptr, x.size, x.dtype, k), f"host request {i}")
+        assert_same(res[i], orc.multiselect(x, k, 8), f"host request {i} vs oracle")
     assert st["uploads"] == len(xs)
     assert 0 < st["peak_bytes"] <= cap
     assert st["in_flight_bytes"] == 0
 
 
-def test_server_concurrent_submitters(g):
+def test_server_concurrent_submitters(g, orc):
     reqs = _mixed_requests(2, 64, max_log2=20)
     devs = [DeviceArray(x) for x, _, _ in reqs]
-    alone = [_alone(g, d, x, kind, arg) for d, (x, kind, arg) in zip(devs, reqs)]
+    alone = [_oracle(orc, x, kind, arg) for x, kind, arg in reqs]
     srv = g.Server(0, hbm_cap_bytes=8 << 30, max_batch=16)
     results = [None] * len(reqs)
 
@@ -119,6 +136,62 @@ def test_server_concurrent_submitters(g):
         assert_same(results[i], alone[i], f"concurrent request {i}")
     assert st["completed"] == len(reqs)
     assert st["max_batch_seen"] <= 16
+
+
+def test_server_lanes_overlap(g, orc):
+    """With two lanes and small batches under load, one lane's batch is on the
+    device while another lane plans and launches its own: the server counts
+    launches that started while another lane's batch ran.  Every result
+    equals the oracle's."""
+    reqs = _mixed_requests(5, 160, max_log2=21)
+    devs = [DeviceArray(x) for x, _, _ in reqs]
+    srv = g.Server(0, hbm_cap_bytes=16 << 30, max_batch=6, lanes=2)
+    tickets = [srv.submit(d.ptr, x.size, x.dtype, k=arg if kind == "ms" else None,
+                          K=arg if kind == "topk" else None)
+               for d, (x, kind, arg) in zip(devs, reqs)]
+    res = [srv.wait(t)[0] for t in tickets]
+    st = srv.stats()
+    srv.close()
+    for i, (x, kind, arg) in enumerate(reqs):
+        assert_same(res[i], _oracle(orc, x, kind, arg), f"lanes request {i}")
+    assert st["completed"] == len(reqs)
+    assert st["batches"] >= len(reqs) // 6
+    assert st["concurrent_launches"] > 0
+
+
+def test_server_admission_by_free_device_memory(g, orc):
+    """The admission budget follows the device's free memory: with a reserve
+    that leaves only 512 MB of it to the server, 16 host-vector requests of
+    64 MB wait for earlier ones to finish (hbm_waits) although the
+    cap would admit them all, and every result is exact.  A request that could
+    never fit -- the reserve larger than the free memory, nothing admitted --
+    fails with GGKS_OOM instead of waiting forever."""
+    import torch
+
+    import ggks_problems as gp
+    xs = [gp.generate("f32", "uniform", 1 << 24, seed=40 + i) for i in range(16)]
+    ks = [gp.k_distinct(x.size, 64, i) for i, x in enumerate(xs)]
+    torch.cuda.synchronize()
+    free = torch.cuda.mem_get_info()[0]
+    srv = g.Server(0, hbm_cap_bytes=64 << 30, hbm_reserve_bytes=free - (512 << 20))
+    tickets = [srv.submit(x.ctypes.data, x.size, x.dtype, k=k, host=True) for x, k in zip(xs, ks)]
+    res = [srv.wait(t)[0] for t in tickets]
+    st = srv.stats()
+    srv.close()
+    for i, (x, k) in enumerate(zip(xs, ks)):
+        assert_same(res[i], orc.multiselect(x, k, 8), f"budget request {i}")
+    assert st["hbm_waits"] > 0
+    assert st["peak_bytes"] <= 512 << 20
+    assert 0 < st["admit_budget_bytes"] < 64 << 30
+    assert st["in_flight_bytes"] == 0
+    torch.cuda.synchronize()
+    free = torch.cuda.mem_get_info()[0]
+    srv = g.Server(0, hbm_cap_bytes=64 << 30, hbm_reserve_bytes=free + (1 << 30))
+    t = srv.submit(xs[0].ctypes.data, xs[0].size, xs[0].dtype, k=ks[0], host=True)
+    with pytest.raises(g.GgksError) as e:
+        srv.wait(t)
+    assert e.value.status == g.OOM
+    srv.close()
 
 
 def test_server_rejections(g):
