@@ -324,6 +324,7 @@ static int api_topk(const T *vec, uint64_t n, uint32_t K, T *out, const ggks_opt
   const bool out_dev = opts && (opts->flags & GGKS_FLAG_OUT_DEVICE);
   ReqSource src;
   src.topk = true;
+  src.topk_pipeline = opts && (opts->flags & GGKS_FLAG_TOPK_PIPELINE);
   const T *hres = nullptr;
   st = select<T, T>(*ctx, d_in, n, src, K, out_dev ? out : nullptr, out_dev ? nullptr : &hres, s,
                    ingest);

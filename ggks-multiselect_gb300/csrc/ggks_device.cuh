@@ -165,6 +165,7 @@ enum : uint32_t {
   ST_TIMEOUT = 4u,   // a bounded wait gave up
   ST_INTERNAL = 8u,  // a consistency check failed (counts do not add up to n)
   ST_BAD_K = 16u,    // a k outside [1, n] (device-side k lists)
+  ST_TOPK_MISS = 32u,  // the threshold top-k's candidates fell short: run the pipeline
 };
 constexpr uint32_t ST_FATAL = ST_TIMEOUT | ST_INTERNAL;
 
@@ -2098,60 +2099,6 @@ __device__ __forceinline__ void compact_one(typename Traits<T>::K k, typename Tr
   st_global_if(surv + pos, k, pos < cap);
 }
 
-// Filtered compaction (the default for up to kCompactRanks slots): shared
-// memory holds the active buckets' bitmap once per bank -- word w of lane l's
-// copy at bm[32 w + l], so a warp's 32 bitmap reads take one wavefront -- the
-// active buckets before each word (prefix), and one cursor per active bucket
-// in bucket order (rank).  An element of an inactive bucket (most of them)
-// costs a table lookup and a bitmap read, both without bank conflicts; only
-// the elements of active buckets take a cursor atomic.  (The plain mode's
-// shared atomic on every element's bucket costs about four wavefronts per
-// warp: random lanes pile up in a few banks.)
-constexpr uint32_t kCompactRanks = 4096;
-struct ActiveSet {
-  const uint32_t *bm_lane;  // bm + lane: this lane's copy
-  const uint32_t *prefix;   // active buckets before word w
-  uint32_t *cursor;         // by rank
-};
-// predicated shared-memory atomic add of 1 (a lane with pred false issues no
-// access and keeps *old); no branch, so the keys of a vector stay in flight
-// together
-__device__ __forceinline__ void atom_add1_if(uint32_t *p, bool pred, uint32_t &old) {
-  asm volatile(
-      "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %2, 0;\n\t@q atom.shared.add.u32 %0, [%1], 1;\n\t}"
-      : "+r"(old)
-      : "r"(smem_addr(p)), "r"((uint32_t)pred)
-      : "memory");
-}
-
-// The PV keys of one vector: lookups and bitmap reads for all of them first,
-// then the (rare) cursor updates and stores, predicated rather than branched.
-template <class K, int PV>
-__device__ __forceinline__ void compact_filtered(const K (&kk)[PV], K base, uint32_t shift,
-                                                 const uint32_t *lut /* lane's table */,
-                                                 const ActiveSet &as, K *__restrict__ surv,
-                                                 uint32_t cap) {
-  uint32_t w[PV], below[PV];
-  bool act[PV];
-#pragma unroll
-  for (int e = 0; e < PV; ++e) {
-    const uint32_t b = bucket_of_rep(kk[e], base, shift, lut);
-    w[e] = b >> 5;
-    const uint32_t word = as.bm_lane[w[e] << 5];
-    act[e] = (word >> (b & 31u)) & 1u;
-    below[e] = __popc(word & ((1u << (b & 31u)) - 1u));
-  }
-  uint32_t r[PV];
-#pragma unroll
-  for (int e = 0; e < PV; ++e) r[e] = (act[e] ? as.prefix[w[e]] : 0u) + below[e];
-#pragma unroll
-  for (int e = 0; e < PV; ++e) {
-    uint32_t pos = 0xFFFFFFFFu;
-    atom_add1_if(as.cursor + r[e], act[e], pos);
-    st_global_if(surv + pos, kk[e], act[e] && pos < cap);
-  }
-}
-
 // Streams the CTA's tiles (and, in the owner CTA, the leftover vectors and
 // the scalar head / tail) through onev(keys of one vector, in_tiles) and
 // one(key) for the scalar head and tail.
@@ -2195,11 +2142,10 @@ __device__ __forceinline__ void compact_body(const T *__restrict__ x, uint64_t n
   }
 }
 
-// dynamic shared memory of k_compact: the table once per bank, then either
-// one cursor per bucket (plain and heavy modes) or the filtered mode's bitmap
-// copies (nb_max words), word prefixes (nb_max / 32) and rank cursors
+// dynamic shared memory of k_compact: the table once per bank, then one
+// cursor per bucket
 __host__ __device__ constexpr size_t compact_smem_bytes(uint32_t nb_max) {
-  return (size_t)(kRepWords + nb_max + nb_max / 32 + kCompactRanks) * sizeof(uint32_t);
+  return (size_t)(kRepWords + nb_max) * sizeof(uint32_t);
 }
 
 // Grid and tile assignment must equal k_hist's (same G, same owner of the
@@ -2209,11 +2155,15 @@ __host__ __device__ constexpr size_t compact_smem_bytes(uint32_t nb_max) {
 // never matters) and leaves the share's end in its row of the per-CTA counts
 // for the check at the end.  A call that overflows the survivor buffer stops
 // here before touching the rows or the counters, so its re-run finds both as
-// the plan left them.  nb_max is a multiple of 32.
+// the plan left them.  In heavy mode (lanes of a warp often share a bucket)
+// the cursor updates are warp-aggregated.
 //
-// Modes: filtered (see compact_filtered) for up to kCompactRanks slots;
-// otherwise one cursor per bucket, with heavy mode's warp-aggregated updates
-// when lanes often share a bucket.
+// A filtered variant was measured and not kept: the active buckets' bitmap
+// held once per bank, so that only elements of active buckets take a cursor
+// atomic, cut the shared-memory wavefronts per warp of 32 keys from 5.3 to
+// 4.5 (atomics 4.0 -> 0.9), but the bitmap read, rank and predicated update
+// doubled the instructions per key (18.5 -> 40), and the pass became issue
+// bound: 2^27 keys took 194 us against 129 us.
 //
 // Speculative compaction: when the histogram pass kept candidates (cand not
 // null, the table's spec on) and every segment's bucket is a kept one, CTA c's
@@ -2237,13 +2187,9 @@ __global__ void __launch_bounds__(1024, 1)
   uint32_t *rep_lut = reinterpret_cast<uint32_t *>(smem_raw);  // one copy per bank
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t *lut = rep_lut + lane;  // this lane's copy
-  uint32_t *cursor = rep_lut + kRepWords;  // plain / heavy: per bucket
-  uint32_t *bm = rep_lut + kRepWords;      // filtered: bitmap copies
-  uint32_t *prefix = bm + nb_max;
-  uint32_t *rcur = prefix + nb_max / 32;
+  uint32_t *cursor = rep_lut + kRepWords;  // per bucket
   __shared__ bool s_bad;
   __shared__ bool s_spec_miss;
-  __shared__ uint32_t s_scan[33];
   __shared__ uint32_t s_wcnt[kCandWarps];
   __shared__ uint32_t s_tab[kCandWarps * kCandChunksPerWarp];
   // nothing to compact when every slot is a single-key one (answered by the
@@ -2254,13 +2200,7 @@ __global__ void __launch_bounds__(1024, 1)
   load_rep_table(rep_lut, lut_g);
   const uint32_t num_slots = ctrl->num_slots;
   const bool spec = cand != nullptr && h.spec != 0;
-  const bool filtered = !h.heavy && num_slots <= kCompactRanks;
-  const uint32_t nbw = (h.nb + 31) / 32;  // bitmap words (<= 1024)
-  if (filtered) {
-    for (uint32_t i = threadIdx.x; i < nbw * 32; i += blockDim.x) bm[i] = 0;
-  } else {
-    for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) cursor[b] = kInactive;
-  }
+  for (uint32_t b = threadIdx.x; b < h.nb; b += blockDim.x) cursor[b] = kInactive;
   if (threadIdx.x == 0) {
     s_bad = false;
     s_spec_miss = false;
@@ -2284,28 +2224,8 @@ __global__ void __launch_bounds__(1024, 1)
       }
     }
   }
-  if (filtered) {
-    // the active buckets (segments with survivors) in copy 0, then in every
-    // lane's copy, and the number of active buckets before each word
-    for (uint32_t s = threadIdx.x; s < num_slots; s += blockDim.x) {
-      if (seg_size[s] == 0) continue;
-      const uint32_t b = seg_bucket[s];
-      atomicOr(&bm[(b >> 5) << 5], 1u << (b & 31u));
-    }
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < nbw * 32; i += blockDim.x)
-      if (i & 31u) bm[i] = bm[i & ~31u];
-    const uint32_t pc = threadIdx.x < nbw ? (uint32_t)__popc(bm[threadIdx.x << 5]) : 0u;
-    uint32_t tot;
-    const uint32_t excl = block_incl_scan(pc, &tot, s_scan) - pc;
-    if (threadIdx.x < nbw) prefix[threadIdx.x] = excl;
-    __syncthreads();
-  }
   // flat slots (seg_size 0: a single-key bucket) are answered without survivors
   uint32_t *row = rows + (uint64_t)c * nb_max;
-  auto rank_of = [&](uint32_t b) {
-    return prefix[b >> 5] + (uint32_t)__popc(bm[(b >> 5) << 5] & ((1u << (b & 31u)) - 1u));
-  };
   for (uint32_t s = threadIdx.x; s < num_slots; s += blockDim.x) {
     const uint32_t sz = seg_size[s];
     if (sz == 0) continue;
@@ -2313,39 +2233,22 @@ __global__ void __launch_bounds__(1024, 1)
     const uint32_t cnt = row[b] & ~kMixed;
     const uint32_t pre = cnt ? atomicAdd(fill + s, cnt) : 0u;
     const uint32_t at = (uint32_t)(seg_off[s] + pre);
-    if (filtered)
-      rcur[rank_of(b)] = at;
-    else
-      cursor[b] = at;
+    cursor[b] = at;
     row[b] = at + cnt;
     if (spec && !in_spec(h, b)) s_spec_miss = true;
   }
   __syncthreads();
   const uint32_t cap = (uint32_t)(surv_cap < (uint64_t)kInactive ? surv_cap : kInactive);
-  const ActiveSet as{bm + lane, prefix, rcur};
   if (spec && !s_spec_miss && ctrl->total_surv <= surv_half) {
     // warp w reads the candidates of the histogram pass's warp w
     const uint32_t w = threadIdx.x >> 5;
     const uint32_t *wt = s_tab + w * kCandChunksPerWarp;
     const uint32_t cw = s_wcnt[w];
     const uint32_t cap_lo = (uint32_t)(surv_half < (uint64_t)cap ? surv_half : cap);
-    for (uint32_t i = lane; i < cw; i += 32) {
-      const K k[1] = {cand[(uint64_t)wt[i / kCandChunk] * kCandChunk + i % kCandChunk]};
-      if (filtered)
-        compact_filtered<K, 1>(k, h.base, h.shift, lut, as, surv, cap_lo);
-      else
-        compact_one<T, false>(k[0], h.base, h.shift, lut, cursor, surv, cap_lo);
-    }
+    for (uint32_t i = lane; i < cw; i += 32)
+      compact_one<T, false>(cand[(uint64_t)wt[i / kCandChunk] * kCandChunk + i % kCandChunk],
+                            h.base, h.shift, lut, cursor, surv, cap_lo);
     if (threadIdx.x == 0) atomicAdd(&ctrl->spec_ctas, 1u);
-  } else if (filtered) {
-    constexpr int PV = Traits<T>::kPerVec;
-    compact_body<T, UNROLL>(
-        x, n,
-        [&](const K(&kk)[PV], bool) { compact_filtered<K, PV>(kk, h.base, h.shift, lut, as, surv, cap); },
-        [&](K k) {
-          const K k1[1] = {k};
-          compact_filtered<K, 1>(k1, h.base, h.shift, lut, as, surv, cap);
-        });
   } else if (h.heavy) {
     constexpr int PV = Traits<T>::kPerVec;
     compact_body<T, UNROLL>(
@@ -2377,7 +2280,7 @@ __global__ void __launch_bounds__(1024, 1)
   for (uint32_t s = threadIdx.x; s < num_slots; s += blockDim.x) {
     if (seg_size[s] == 0) continue;
     const uint32_t b = seg_bucket[s];
-    if ((filtered ? rcur[rank_of(b)] : cursor[b]) != row[b]) s_bad = true;
+    if (cursor[b] != row[b]) s_bad = true;
   }
   __syncthreads();
   if (threadIdx.x == 0 && s_bad) atomicOr(&ctrl->status, ST_INTERNAL);

@@ -5,11 +5,13 @@
 
 #include <algorithm>
 #include <atomic>
+#include <type_traits>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "ggks_internal.h"
+#include "ggks_topk.cuh"
 
 namespace ggks {
 
@@ -265,11 +267,111 @@ static inline void set_windows(Ctrl *ci, const Req *hr, uint32_t num_req, uint64
   if (span > n / 16) ci->spec_nwin = 0;
 }
 
+// Top-k by a sampled threshold (ggks_topk.cuh): k_sample, k_tau, k_filter,
+// k_pick.  *missed: the candidates fell short (or did not fit), nothing is
+// answered, and the caller runs the pipeline; d_in then holds the device copy
+// of an ingested host vector.
+template <class InT>
+static int topk_threshold(Context &ctx, const InT *d_in, uint64_t n, uint32_t K, InT *d_out_user,
+                          const InT **host_results, cudaStream_t s, const InT *ingest,
+                          bool *missed) {
+  using Kt = typename Traits<InT>::K;
+  *missed = false;
+  const Plan p = make_plan<InT, InT>(ctx, n, K);
+  cudaError_t e = ensure_arena(ctx, p.total);
+  if (e != cudaSuccess) return from_cuda(e);
+  e = ensure_surv(ctx, (size_t)p.surv_cap * sizeof(Kt));
+  if (e != cudaSuccess) return from_cuda(e);
+  char *A = ctx.arena;
+  Ctrl *ctrl = reinterpret_cast<Ctrl *>(A + p.ctrl);
+  Kt *tau = reinterpret_cast<Kt *>(A + p.hdr);
+  Kt *samples = reinterpret_cast<Kt *>(A + p.samples);
+  uint32_t *slice_cnt = reinterpret_cast<uint32_t *>(A);
+  uint32_t *cand_cnt = reinterpret_cast<uint32_t *>(A + p.cand_cnt);
+  uint32_t *cand_tab = reinterpret_cast<uint32_t *>(A + p.cand_tab);
+  Kt *pool = reinterpret_cast<Kt *>(ctx.surv);
+  const uint64_t chunks64 = p.surv_cap / kCandChunk;
+  const uint32_t chunks = (uint32_t)(chunks64 < 0xFFFFFFFFull ? chunks64 : 0xFFFFFFFFull);
+  InT *d_out = d_out_user ? d_out_user : reinterpret_cast<InT *>(A + p.out);
+  const size_t out_span = p.ctrl - p.out;
+  e = ensure_pin(ctx, 256 + out_span + 256);
+  if (e != cudaSuccess) return from_cuda(e);
+  char *pin_up = ctx.pin;
+  char *pin_down = ctx.pin + 256;
+  Ctrl *h_ctrl = reinterpret_cast<Ctrl *>(pin_down + out_span);
+  std::memset(pin_up, 0, 256);  // a zeroed control block
+  e = cudaMemcpyAsync(ctrl, pin_up, 256, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return from_cuda(e);
+  cudaError_t le = cudaSuccess;
+  auto L = [&le](cudaError_t r) {
+    if (le == cudaSuccess) le = r;
+  };
+  const uint32_t lists = p.G * kCandWarps;
+  const int pick_smem = (int)pick_smem_bytes<Kt>();
+  L(set_smem_max<k_pick<Kt, InT>>(pick_smem));
+  bool ran[GGKS_NUM_PASSES] = {false, false, false, false, false, false};
+  {
+    PassTimer t(ctx, s, GGKS_PASS_SAMPLE);
+    L(launch(k_sample<InT>, p.sample_grid, 1024, 0, s, ingest ? ingest : d_in, n, p.S, 0x5EEDu,
+             samples, ctrl));
+    L(launch(k_tau<Kt>, p.sample_grid, 1024, 0, s, samples, p.S, ctrl, slice_cnt, n, K, tau));
+    ctx.stats.launches++;
+    ran[GGKS_PASS_SAMPLE] = true;
+  }
+  {
+    PassTimer t(ctx, s, GGKS_PASS_HIST);
+    L(launch(p.unroll8 ? k_filter<InT, 8> : k_filter<InT, 4>, p.G, 1024, 0, s,
+             ingest ? ingest : d_in, n, tau, pool, chunks, &ctrl->cand_next, cand_cnt, cand_tab,
+             ingest ? const_cast<InT *>(d_in) : nullptr, ctrl));
+    ran[GGKS_PASS_HIST] = true;
+  }
+  {
+    PassTimer t(ctx, s, GGKS_PASS_FINISH);
+    L(launch(k_pick<Kt, InT>, 1, 1024, pick_smem, s, pool, chunks, cand_cnt, cand_tab, lists, tau,
+             K, d_out, ctrl));
+    ran[GGKS_PASS_FINISH] = true;
+  }
+  e = le != cudaSuccess ? le : cudaGetLastError();
+  if (e != cudaSuccess) return from_cuda(e);
+  const bool want_host = host_results != nullptr;
+  if (want_host && !d_out_user)
+    e = cudaMemcpyAsync(pin_down, A + p.out, out_span + sizeof(Ctrl), cudaMemcpyDeviceToHost, s);
+  else
+    e = cudaMemcpyAsync(h_ctrl, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && want_host && d_out_user)
+    e = cudaMemcpyAsync(pin_down, d_out, (size_t)K * sizeof(InT), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return from_cuda(e);
+  collect_pass_times(ctx, ran);
+  const Ctrl c = *h_ctrl;
+  if (c.status & ST_FATAL) return (c.status & ST_TIMEOUT) ? GGKS_TIMEOUT : GGKS_INTERNAL;
+  if (c.status & ST_TOPK_MISS) {
+    *missed = true;
+    ctx.stats.topk_misses++;
+    return GGKS_OK;
+  }
+  ctx.stats.topk_threshold_calls++;
+  if (want_host) *host_results = reinterpret_cast<const InT *>(pin_down);
+  return GGKS_OK;
+}
+
 template <class InT, class OutT>
 int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint32_t num_req,
            OutT *d_out_user, const OutT **host_results, cudaStream_t s, const InT *ingest) {
   using K = typename Traits<InT>::K;
   if (ctx.depth > 12) return GGKS_INTERNAL;
+  // a top-k of at most kPickMax values from a vector larger than the sample:
+  // the threshold path, unless its candidates fall short
+  if constexpr (std::is_same<InT, OutT>::value) {
+    if (src.topk && ctx.depth == 0 && num_req <= kPickMax && n > 65536 &&
+        (uint64_t)num_req * 64 <= n && !src.topk_pipeline) {
+      bool missed = false;
+      const int st = topk_threshold<InT>(ctx, d_in, n, num_req, d_out_user, host_results, s,
+                                         ingest, &missed);
+      if (st != GGKS_OK || !missed) return st;
+      ingest = nullptr;  // the filter pass wrote the device copy
+    }
+  }
   const Plan p = make_plan<InT, OutT>(ctx, n, num_req);
   cudaError_t e = ensure_arena(ctx, p.total);
   if (e != cudaSuccess) return from_cuda(e);

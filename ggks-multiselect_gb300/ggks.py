@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(HERE, "libggks_gb300.so")
 OK, INVALID_ARG, OOM, CUDA_ERROR, TIMEOUT, INTERNAL, NO_DEVICE, UNSUPPORTED = range(8)
 FLAG_OUT_DEVICE = 1
 FLAG_AUTOTUNE = 2
+FLAG_TOPK_PIPELINE = 4
 NUM_PASSES = 6
 PASS_NAMES = ("sample", "hist", "scan", "plan", "compact", "finish")
 NUM_BATCH_PHASES = 5
@@ -53,7 +54,8 @@ class Stats(ctypes.Structure):
                 ("batch_calls", ctypes.c_uint64), ("batch_problems", ctypes.c_uint64),
                 ("batch_phase_ms", ctypes.c_double * NUM_BATCH_PHASES),
                 ("batch_grid", ctypes.c_uint64), ("spec_calls", ctypes.c_uint64),
-                ("spec_ctas", ctypes.c_uint64)]
+                ("spec_ctas", ctypes.c_uint64), ("topk_threshold_calls", ctypes.c_uint64),
+                ("topk_misses", ctypes.c_uint64)]
 
     def as_dict(self):
         return {"calls": self.calls, "launches": self.launches,
@@ -65,7 +67,8 @@ class Stats(ctypes.Structure):
                 "batch_calls": self.batch_calls, "batch_problems": self.batch_problems,
                 "batch_phase_ms": dict(zip(BATCH_PHASE_NAMES, list(self.batch_phase_ms))),
                 "batch_grid": self.batch_grid, "spec_calls": self.spec_calls,
-                "spec_ctas": self.spec_ctas}
+                "spec_ctas": self.spec_ctas, "topk_threshold_calls": self.topk_threshold_calls,
+                "topk_misses": self.topk_misses}
 
 
 DTYPE_CODES = {np.dtype(np.float32): 0, np.dtype(np.float64): 1, np.dtype(np.uint32): 2}
@@ -299,9 +302,12 @@ def multiselect_ptr(d_ptr, n, dtype, k, ctx=None, stream=None, out=None, out_dev
     return out
 
 
-def topk_ptr(d_ptr, n, dtype, K, ctx=None, stream=None, out=None, out_device_ptr=None):
+def topk_ptr(d_ptr, n, dtype, K, ctx=None, stream=None, out=None, out_device_ptr=None,
+             pipeline=False):
+    """The K largest of the device vector at d_ptr, descending.  pipeline=True
+    forces the histogram / compaction pipeline (same results)."""
     dtype = np.dtype(dtype)
-    flags = 0
+    flags = FLAG_TOPK_PIPELINE if pipeline else 0
     if out_device_ptr is not None:
         flags |= FLAG_OUT_DEVICE
         optr = out_device_ptr
@@ -347,11 +353,13 @@ def multiselect_host(h_vec, k, ctx=None, stream=None, out=None):
     return out
 
 
-def topk_host(h_vec, K, ctx=None, stream=None, out=None):
+def topk_host(h_vec, K, ctx=None, stream=None, out=None, pipeline=False):
+    """The K largest of a host vector (copied to the device inside the call),
+    descending.  pipeline=True forces the histogram / compaction pipeline."""
     h_vec = np.ascontiguousarray(h_vec)
     if out is None:
         out = np.empty(int(K), dtype=h_vec.dtype)
-    o = _opts(ctx, stream)
+    o = _opts(ctx, stream, FLAG_TOPK_PIPELINE if pipeline else 0)
     st = getattr(lib(), "ggks_topk_host_" + _SFX[h_vec.dtype])(
         h_vec.ctypes.data, h_vec.size, int(K), out.ctypes.data, ctypes.byref(o))
     _check(st, "topk_host")

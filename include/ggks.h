@@ -59,6 +59,10 @@ typedef struct ggks_opts {
 
 /* opts->flags: the output pointer is device memory (no device-to-host copy). */
 #define GGKS_FLAG_OUT_DEVICE 1u
+/* opts->flags for ggks_topk_*: run the histogram / compaction pipeline even
+ * where the threshold path applies (K <= 4096, n > 65536, 64 K <= n); the
+ * results are the same. */
+#define GGKS_FLAG_TOPK_PIPELINE 4u
 
 /* ------------------------------------------------------------------------ */
 /* Multiselect                                                               */
@@ -330,6 +334,8 @@ typedef struct ggks_stats {
                                          candidates (top-k, few clustered k's) */
   uint64_t spec_ctas;                 /* compaction CTAs that read those candidates
                                          in place of their share of the vector */
+  uint64_t topk_threshold_calls;      /* top-k calls answered by the threshold path */
+  uint64_t topk_misses;               /* threshold attempts that fell back to the pipeline */
 } ggks_stats;
 
 /* phase indices of ggks_stats.batch_phase_ms (one persistent launch; each

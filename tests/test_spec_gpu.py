@@ -1,7 +1,8 @@
 """Speculative compaction on the GPU: when the requested ranks cluster (top-k,
 one k, k's near both ends), the histogram pass also keeps the elements of the
 buckets the sample predicts, and compaction reads those in place of the
-vector.  Every result is compared bit for bit with the oracle (sort-and-choose,
+vector.  (Top-k calls here force the pipeline: small K otherwise take the
+threshold path, tests/test_topk_threshold_gpu.py.)  Every result is compared bit for bit with the oracle (sort-and-choose,
 multiselectTimingFunctions.cu:51-95 / :156-177), including the cases where the
 prediction misses or a CTA's candidates overflow and compaction falls back to
 the vector."""
@@ -67,7 +68,7 @@ def test_topk_reads_candidates(g, orc, dtype, dist, n, K):
     import ggks_problems as gp
     x = gp.generate(dtype, dist, n, seed=K + 1)
     d = DeviceArray(x)
-    got, st = run(g, g.topk_ptr, d.ptr, n, x.dtype, K)
+    got, st = run(g, g.topk_ptr, d.ptr, n, x.dtype, K, pipeline=True)
     assert_same(got, orc.topk(x, K, threads=8), f"topk {dtype}/{dist}/{n}/{K}")
     assert st["spec_calls"] == 1
     if dist != "uniform16":  # 2^16 values: the top buckets may hold one key each
@@ -132,7 +133,7 @@ def test_presorted_candidates_fill_few_ctas(g, orc):
     x = np.sort(gp.uniform_f32(n, 14))
     d = DeviceArray(x)
     for K in (1024, 65536):
-        got, st = run(g, g.topk_ptr, d.ptr, n, x.dtype, K)
+        got, st = run(g, g.topk_ptr, d.ptr, n, x.dtype, K, pipeline=True)
         assert_same(got, orc.topk(x, K, 8), f"sorted K={K}")
         assert st["spec_calls"] == 1
         assert st["spec_ctas"] == min(n // 65536, 152)
@@ -154,7 +155,7 @@ def test_speculation_with_survivor_overflow(g, orc):
     x[spread] = r.random(spread.size) * 2.0
     x[pos] = r.random(pos.size) * 2.0
     d = DeviceArray(x)
-    got, st = run(g, g.topk_ptr, d.ptr, n, np.float64, 100)
+    got, st = run(g, g.topk_ptr, d.ptr, n, np.float64, 100, pipeline=True)
     assert_same(got, orc.topk(x, 100, 8), "cluster top-k")
     assert st["spec_calls"] == 1 and st["spec_ctas"] == 0
     assert st["retries"] > 0
@@ -165,6 +166,6 @@ def test_host_vector_topk_speculates(g, orc):
     device copy and keeps the candidates."""
     import ggks_problems as gp
     x = gp.normal_f32(1 << 22, 15)
-    assert_same(g.topk_host(x, 2048), orc.topk(x, 2048, 8), "host topk")
+    assert_same(g.topk_host(x, 2048, pipeline=True), orc.topk(x, 2048, 8), "host topk")
     ks = np.array([7, 1 << 21], dtype=np.uint32)
     assert_same(g.multiselect_host(x, ks), orc.multiselect(x, ks), "host two k's")
