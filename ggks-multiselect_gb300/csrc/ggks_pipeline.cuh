@@ -287,11 +287,8 @@ static int topk_threshold(Context &ctx, const InT *d_in, uint64_t n, uint32_t K,
   Kt *tau = reinterpret_cast<Kt *>(A + p.hdr);
   Kt *samples = reinterpret_cast<Kt *>(A + p.samples);
   uint32_t *slice_cnt = reinterpret_cast<uint32_t *>(A);
-  uint32_t *cand_cnt = reinterpret_cast<uint32_t *>(A + p.cand_cnt);
-  uint32_t *cand_tab = reinterpret_cast<uint32_t *>(A + p.cand_tab);
-  Kt *pool = reinterpret_cast<Kt *>(ctx.surv);
-  const uint64_t chunks64 = p.surv_cap / kCandChunk;
-  const uint32_t chunks = (uint32_t)(chunks64 < 0xFFFFFFFFull ? chunks64 : 0xFFFFFFFFull);
+  Kt *arr = reinterpret_cast<Kt *>(ctx.surv);  // the candidate array
+  const uint64_t arr_cap = p.surv_cap;
   InT *d_out = d_out_user ? d_out_user : reinterpret_cast<InT *>(A + p.out);
   const size_t out_span = p.ctrl - p.out;
   e = ensure_pin(ctx, 256 + out_span + 256);
@@ -306,9 +303,11 @@ static int topk_threshold(Context &ctx, const InT *d_in, uint64_t n, uint32_t K,
   auto L = [&le](cudaError_t r) {
     if (le == cudaSuccess) le = r;
   };
-  const uint32_t lists = p.G * kCandWarps;
   const int pick_smem = (int)pick_smem_bytes<Kt>();
+  const int filt_smem = (int)(kCandWarps * kFiltBuf * sizeof(Kt));
   L(set_smem_max<k_pick<Kt, InT>>(pick_smem));
+  L(set_smem_max<k_filter<InT, 8>>(filt_smem));
+  L(set_smem_max<k_filter<InT, 4>>(filt_smem));
   bool ran[GGKS_NUM_PASSES] = {false, false, false, false, false, false};
   {
     PassTimer t(ctx, s, GGKS_PASS_SAMPLE);
@@ -320,15 +319,15 @@ static int topk_threshold(Context &ctx, const InT *d_in, uint64_t n, uint32_t K,
   }
   {
     PassTimer t(ctx, s, GGKS_PASS_HIST);
-    L(launch(p.unroll8 ? k_filter<InT, 8> : k_filter<InT, 4>, p.G, 1024, 0, s,
-             ingest ? ingest : d_in, n, tau, pool, chunks, &ctrl->cand_next, cand_cnt, cand_tab,
+    L(launch(p.unroll8 ? k_filter<InT, 8> : k_filter<InT, 4>, p.G, 1024, filt_smem, s,
+             ingest ? ingest : d_in, n, tau, arr, arr_cap, &ctrl->cand_next,
              ingest ? const_cast<InT *>(d_in) : nullptr, ctrl));
     ran[GGKS_PASS_HIST] = true;
   }
   {
     PassTimer t(ctx, s, GGKS_PASS_FINISH);
-    L(launch(k_pick<Kt, InT>, 1, 1024, pick_smem, s, pool, chunks, cand_cnt, cand_tab, lists, tau,
-             K, d_out, ctrl));
+    L(launch(k_pick<Kt, InT>, 1, 1024, pick_smem, s, arr, arr_cap, &ctrl->cand_next, tau, K,
+             d_out, ctrl));
     ran[GGKS_PASS_FINISH] = true;
   }
   e = le != cudaSuccess ? le : cudaGetLastError();

@@ -15,15 +15,15 @@
 //             about Binomial(S, 1 - K / n); six standard deviations plus four
 //             below its mean) and takes the sample key of that rank as the
 //             threshold tau;
-//   k_filter  streams the vector once: each key >= tau goes to its warp's
-//             candidate list (chunks of the pool), nothing else is written;
+//   k_filter  streams the vector once: each key >= tau is appended to one
+//             contiguous candidate array, nothing else is written;
 //   k_pick    one CTA: a 4096-bin histogram of the candidates over their key
 //             range, the bin holding the K-th largest, a gather of every
 //             candidate from that bin up into shared memory, a bitonic sort,
 //             and the K largest out in descending order.
-// Correctness never rests on the prediction: k_pick checks that the lists are
-// complete and hold at least K keys, and that the gathered keys fit; else it
-// flags ST_TOPK_MISS and the caller runs the pipeline instead.
+// Correctness never rests on the prediction: k_pick checks that every
+// candidate was kept and that there are at least K, and that the gathered
+// keys fit; else it flags ST_TOPK_MISS and the caller runs the pipeline.
 #pragma once
 
 #include "ggks_device.cuh"
@@ -119,10 +119,9 @@ __global__ void __launch_bounds__(1024) k_tau(const K *__restrict__ samples, uin
     }
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
-      if (s0 + u * blockDim.x < S && (uint32_t)((xs[u] - kmin) >> fsh) == jf) {
-        const uint32_t at = atomicAdd(&s_cnt, 1u);
-        if (at < kTauBuf) buf[at] = xs[u];
-      }
+      const bool in = s0 + u * blockDim.x < S && (uint32_t)((xs[u] - kmin) >> fsh) == jf;
+      const uint32_t at = warp_append(&s_cnt, in);
+      if (in && at < kTauBuf) buf[at] = xs[u];
     }
   }
   __syncthreads();
@@ -147,17 +146,54 @@ __global__ void __launch_bounds__(1024) k_tau(const K *__restrict__ samples, uin
 }
 
 // ---------------------------------------------------------------------------
-// k_filter: one pass, keys >= tau into per-warp candidate lists
+// k_filter: one pass, keys >= tau appended to one contiguous array
 // ---------------------------------------------------------------------------
-// Same tiles and lists as k_hist's speculative candidates (cand_put_warp):
-// warp w of CTA c leaves its count in cand_cnt[c * kCandWarps + w] and its
-// chunk table in cand_tab.  INGEST: x is a mapped host vector, also written to
-// copy_to (the device copy, same alignment modulo 16 bytes).
+// Each warp collects its candidates in a 256-key buffer in shared memory and
+// moves a buffer that could fill up to the candidate array with one atomic on
+// the array's length (cand_next); at the end the CTA's warps move what is left
+// with one atomic for the whole CTA.  The candidates are thus one contiguous
+// array [0, C), which k_pick reads with coalesced loads (one SM gathering
+// scattered 4-byte candidates from per-warp lists was bound by its outstanding
+// misses: 43 us for 20 000 keys).  Keys past the array's capacity are counted
+// but not written (k_pick then reports a miss).  INGEST: x is a mapped host
+// vector, also written to copy_to (the device copy, same alignment modulo 16
+// bytes).
+constexpr uint32_t kFiltBuf = 256;  // keys of one warp's buffer
+
+template <class K>
+struct FiltWarp {
+  K *buf;           // this warp's kFiltBuf keys in shared memory
+  uint32_t cnt = 0;  // keys in buf (warp-uniform)
+  K *arr;           // the candidate array
+  uint64_t cap;     // its capacity
+  uint32_t *len;    // its length (global)
+  // moves the buffer to the array (the whole warp calls this)
+  __device__ __forceinline__ void flush() {
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(len, cnt);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    __syncwarp();
+    for (uint32_t i = lane; i < cnt; i += 32)
+      if ((uint64_t)base + i < cap) arr[base + i] = buf[i];
+    __syncwarp();
+    cnt = 0;
+  }
+  // every lane calls this with its key and whether it keeps it
+  __device__ __forceinline__ void put(K k, bool keep) {
+    const uint32_t m = __ballot_sync(0xffffffffu, keep);
+    if (!m) return;
+    if (cnt > kFiltBuf - 32) flush();
+    const uint32_t lane = threadIdx.x & 31;
+    if (keep) buf[cnt + __popc(m & ((1u << lane) - 1u))] = k;
+    cnt += __popc(m);
+  }
+};
+
 template <class T, int UNROLL, bool INGEST>
 __device__ __forceinline__ void filter_body(const T *__restrict__ x, uint64_t n,
                                             typename Traits<T>::K t, T *__restrict__ copy_to,
-                                            const CandPool<typename Traits<T>::K> &cp,
-                                            CandList &cl, uint32_t *wtab) {
+                                            FiltWarp<typename Traits<T>::K> &fw) {
   using K = typename Traits<T>::K;
   using V = typename Traits<T>::Vec;
   constexpr int PV = Traits<T>::kPerVec;
@@ -186,7 +222,7 @@ __device__ __forceinline__ void filter_body(const T *__restrict__ x, uint64_t n,
       // one vote per vector; the per-key votes only when a lane keeps one
       if (__any_sync(0xffffffffu, any)) {
 #pragma unroll
-        for (int e = 0; e < PV; ++e) cand_put_warp<K>(cp, k[e], k[e] >= t, cl, wtab);
+        for (int e = 0; e < PV; ++e) fw.put(k[e], k[e] >= t);
       }
     }
   }
@@ -204,7 +240,7 @@ __device__ __forceinline__ void filter_body(const T *__restrict__ x, uint64_t n,
       K k[PV];
       vec_keys<T>(vv, k);
 #pragma unroll
-      for (int e = 0; e < PV; ++e) cand_put_warp<K>(cp, k[e], valid && k[e] >= t, cl, wtab);
+      for (int e = 0; e < PV; ++e) fw.put(k[e], valid && k[e] >= t);
     }
     auto scalar = [&](uint64_t e0, uint64_t e1) {
       for (uint64_t eb = e0; eb < e1; eb += blockDim.x) {
@@ -216,7 +252,7 @@ __device__ __forceinline__ void filter_body(const T *__restrict__ x, uint64_t n,
           if (INGEST) copy_to[e] = v;
           k = Traits<T>::key(v);
         }
-        cand_put_warp<K>(cp, k, valid && k >= t, cl, wtab);
+        fw.put(k, valid && k >= t);
       }
     };
     scalar(0, sp.head);
@@ -224,188 +260,132 @@ __device__ __forceinline__ void filter_body(const T *__restrict__ x, uint64_t n,
   }
 }
 
+// Grid and tiles as k_hist; 1024 threads; dynamic shared memory
+// kCandWarps * kFiltBuf keys.  arr[0 .. cap) receives the candidates and
+// *len (zero on entry) their count.
 template <class T, int UNROLL>
 __global__ void __launch_bounds__(1024, 1)
     k_filter(const T *__restrict__ x, uint64_t n, const typename Traits<T>::K *tau,
-             typename Traits<T>::K *__restrict__ pool, uint32_t pool_chunks, uint32_t *cand_next,
-             uint32_t *__restrict__ cand_cnt, uint32_t *__restrict__ cand_tab,
+             typename Traits<T>::K *__restrict__ arr, uint64_t cap, uint32_t *len,
              T *__restrict__ copy_to, const Ctrl *ctrl) {
   pdl_start();
   using K = typename Traits<T>::K;
+  extern __shared__ uint4 smem_raw[];
   __shared__ uint32_t s_wcnt[kCandWarps];
-  __shared__ uint32_t s_tab[kCandWarps * kCandChunksPerWarp];
+  __shared__ uint32_t s_base;
   if (ctrl->status & ST_FATAL) return;
   const K t = *tau;
-  CandPool<K> cp;
-  cp.pool = pool;
-  cp.chunks = pool_chunks;
-  cp.next = cand_next;
-  CandList cl;
-  const uint32_t warp = threadIdx.x >> 5;
-  uint32_t *wt = s_tab + warp * kCandChunksPerWarp;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  FiltWarp<K> fw;
+  fw.buf = reinterpret_cast<K *>(smem_raw) + warp * kFiltBuf;
+  fw.arr = arr;
+  fw.cap = cap;
+  fw.len = len;
   if (copy_to)
-    filter_body<T, UNROLL, true>(x, n, t, copy_to, cp, cl, wt);
+    filter_body<T, UNROLL, true>(x, n, t, copy_to, fw);
   else
-    filter_body<T, UNROLL, false>(x, n, t, nullptr, cp, cl, wt);
-  if ((threadIdx.x & 31) == 0) s_wcnt[warp] = cl.count;
+    filter_body<T, UNROLL, false>(x, n, t, nullptr, fw);
+  // what the warps hold: one atomic for the CTA
+  if (lane == 0) s_wcnt[warp] = fw.cnt;
   __syncthreads();
-  if (threadIdx.x < kCandWarps)
-    cand_cnt[(uint64_t)blockIdx.x * kCandWarps + threadIdx.x] = s_wcnt[threadIdx.x];
-  for (uint32_t i = threadIdx.x; i < kCandWarps * kCandChunksPerWarp; i += blockDim.x)
-    cand_tab[(uint64_t)blockIdx.x * kCandWarps * kCandChunksPerWarp + i] = s_tab[i];
+  if (threadIdx.x == 0) {
+    uint32_t tot = 0;
+    for (uint32_t w = 0; w < kCandWarps; ++w) {
+      const uint32_t c = s_wcnt[w];
+      s_wcnt[w] = tot;
+      tot += c;
+    }
+    s_base = tot ? atomicAdd(len, tot) : 0u;
+  }
+  __syncthreads();
+  const uint64_t base = (uint64_t)s_base + s_wcnt[warp];
+  for (uint32_t i = lane; i < fw.cnt; i += 32)
+    if (base + i < cap) arr[base + i] = fw.buf[i];
 }
 
 // ---------------------------------------------------------------------------
 // k_pick: the K largest of the candidates
 // ---------------------------------------------------------------------------
-// One CTA of 1024 threads.  lists = G * kCandWarps candidate lists (at most
-// kPickLists).  The candidates are numbered list after list (list offsets in
-// shared memory); thread t takes the contiguous numbers [C t / T, C (t+1) / T)
-// and walks its lists, with each list's first chunk index staged in shared
-// memory (later chunks, of lists holding more than kCandChunk keys, are read
-// from the chunk table).  When the C candidates fit the stage (kPickStage
-// keys) one walk copies them there and every later pass reads shared memory;
-// otherwise every pass walks the lists again.
-//
-// Dynamic shared memory: list offsets (kPickLists + 1 words), first chunks
-// (kPickLists), the histogram (kPickBins), the stage (kPickStage keys) and the
-// sort buffer (kPickCap keys).  out[i] = the (i + 1)-th largest, i < kk.
-constexpr uint32_t kPickLists = 4864;  // 152 CTAs x 32 warps
+// One CTA of 1024 threads over the contiguous candidate array arr[0, C)
+// (coalesced reads).  When C fits the stage (kStage keys) the candidates are
+// copied into shared memory once and every later pass reads them there.
+// Dynamic shared memory: the histogram and the bins' offsets (kPickBins words
+// each), the stage and the sort buffer (kPickCap keys).  out[i] = the (i + 1)-th largest, i < kk.
 template <class K>
 struct PickShape {
-  static constexpr uint32_t kStage = sizeof(K) == 4 ? 32768u : 12288u;
+  static constexpr uint32_t kStage = sizeof(K) == 4 ? 36864u : 14336u;
 };
+constexpr uint32_t kPickBinSort = 32;  // largest bin sorted by one thread
 template <class K>
 __host__ __device__ constexpr size_t pick_smem_bytes() {
-  return ((size_t)kPickLists * 2 + 1 + kPickBins) * sizeof(uint32_t) +
+  return (size_t)2 * kPickBins * sizeof(uint32_t) +
          ((size_t)PickShape<K>::kStage + kPickCap) * sizeof(K) + 16;
 }
 
 template <class K, class OutT>
 __global__ void __launch_bounds__(1024, 1)
-    k_pick(const K *__restrict__ pool, uint32_t pool_chunks, const uint32_t *__restrict__ cand_cnt,
-           const uint32_t *__restrict__ cand_tab, uint32_t lists, const K *tau, uint32_t kk,
+    k_pick(const K *__restrict__ arr, uint64_t cap, const uint32_t *len, const K *tau, uint32_t kk,
            OutT *__restrict__ out, Ctrl *ctrl) {
   pdl_start();
   constexpr uint32_t kStage = PickShape<K>::kStage;
   extern __shared__ uint4 smem_raw[];
-  uint32_t *loff = reinterpret_cast<uint32_t *>(smem_raw);  // kPickLists + 1
-  uint32_t *first = loff + kPickLists + 1;                   // kPickLists
-  uint32_t *hist = first + kPickLists;                       // kPickBins
-  K *stage = reinterpret_cast<K *>(
-      reinterpret_cast<uintptr_t>(hist + kPickBins + 3) & ~uintptr_t(15));
-  K *buf = stage + kStage;  // kPickCap
+  uint32_t *hist = reinterpret_cast<uint32_t *>(smem_raw);  // kPickBins
+  uint32_t *off = hist + kPickBins;                          // kPickBins
+  K *stage = reinterpret_cast<K *>(off + kPickBins);         // 16-byte aligned
+  K *buf = stage + kStage;                                   // kPickCap
   __shared__ uint32_t red32[33];
   __shared__ K redk[33];
-  __shared__ bool s_miss;
   __shared__ uint32_t s_j, s_above, s_cnt;
   const uint32_t tid = threadIdx.x, nt = blockDim.x;
   if (ctrl->status & ST_FATAL) return;
-  if (tid == 0) s_miss = lists > kPickLists;
-  __syncthreads();
-  if (s_miss) {
-    if (tid == 0) atomicOr(&ctrl->status, ST_TOPK_MISS);
-    return;
-  }
-  // list counts -> offsets (contiguous lists per thread); every list must be
-  // complete; first chunks staged
-  const uint32_t per = (lists + nt - 1) / nt;
-  uint32_t mysum = 0;
-  for (uint32_t q = 0; q < per; ++q) {
-    const uint32_t L = tid * per + q;
-    if (L >= lists) break;
-    const uint32_t c = __ldcg(cand_cnt + L);
-    const uint32_t nch = (c + kCandChunk - 1) / kCandChunk;
-    if (nch > kCandChunksPerWarp) {
-      s_miss = true;
-    } else {
-      for (uint32_t h = 0; h < nch; ++h) {
-        const uint32_t ch = __ldcg(cand_tab + (uint64_t)L * kCandChunksPerWarp + h);
-        if (ch >= pool_chunks) s_miss = true;
-        if (h == 0) first[L] = ch;
-      }
-    }
-    mysum += c;
-  }
-  uint32_t total;
-  uint32_t run = block_incl_scan(mysum, &total, red32) - mysum;
-  for (uint32_t q = 0; q < per; ++q) {
-    const uint32_t L = tid * per + q;
-    if (L >= lists) break;
-    loff[L] = run;
-    run += __ldcg(cand_cnt + L);
-  }
-  if (tid == 0) loff[lists] = total;
+  const uint32_t C = __ldcg(len);
+  const K t = *tau;
   for (uint32_t b = tid; b < kPickBins; b += nt) hist[b] = 0;
-  __syncthreads();
-  if (s_miss || total < kk) {
+  if ((uint64_t)C > cap || C < kk) {  // candidates lost past the capacity, or too few
     if (tid == 0) atomicOr(&ctrl->status, ST_TOPK_MISS);
     return;
   }
-  const uint32_t C = total;
-  // walk: fn(candidate number, key) for this thread's contiguous numbers, four
-  // loads in flight
-  auto walk = [&](auto &&fn) {
-    const uint32_t i0 = (uint32_t)((uint64_t)C * tid / nt);
-    const uint32_t i1 = (uint32_t)((uint64_t)C * (tid + 1) / nt);
-    if (i0 >= i1) return;
-    uint32_t lo = 0, hi = lists;  // the list holding i0: last L with loff[L] <= i0
-    while (hi - lo > 1) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (loff[mid] <= i0)
-        lo = mid;
-      else
-        hi = mid;
-    }
-    uint32_t L = lo;
-    for (uint32_t i = i0; i < i1; i += 4) {
-      uint64_t at[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const uint32_t idx = i + u;
-        at[u] = 0;
-        if (idx < i1) {
-          while (idx >= loff[L + 1]) ++L;
-          const uint32_t j = idx - loff[L];
-          const uint32_t ch = j < kCandChunk
-                                  ? first[L]
-                                  : __ldcg(cand_tab + (uint64_t)L * kCandChunksPerWarp + j / kCandChunk);
-          at[u] = (uint64_t)ch * kCandChunk + j % kCandChunk;
-        }
-      }
-      K kv[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) kv[u] = i + u < i1 ? __ldcg(pool + at[u]) : K(0);
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (i + u < i1) fn(i + u, kv[u]);
-    }
-  };
   const bool staged = C <= kStage;
-  // every candidate once: fn(key)
+  // every candidate once: fn(key); eight loads per thread in flight
   auto each = [&](auto &&fn) {
     if (staged) {
       for (uint32_t i = tid; i < C; i += nt) fn(stage[i]);
-    } else {
-      walk([&](uint32_t, K k) { fn(k); });
+      return;
+    }
+    for (uint32_t i0 = tid; i0 < C; i0 += 8 * nt) {
+      K kv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) kv[u] = i0 + u * nt < C ? __ldcg(arr + i0 + u * nt) : K(0);
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (i0 + u * nt < C) fn(kv[u]);
     }
   };
-  const K t = *tau;
   K mx = 0;
   if (staged) {
-    walk([&](uint32_t i, K k) {
-      stage[i] = k;
-      mx = k > mx ? k : mx;
-    });
+    for (uint32_t i0 = tid; i0 < C; i0 += 8 * nt) {
+      K kv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) kv[u] = i0 + u * nt < C ? __ldcg(arr + i0 + u * nt) : K(0);
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (i0 + u * nt < C) {
+          stage[i0 + u * nt] = kv[u];
+          mx = kv[u] > mx ? kv[u] : mx;
+        }
+    }
   } else {
-    walk([&](uint32_t, K k) { mx = k > mx ? k : mx; });
+    each([&](K k) { mx = k > mx ? k : mx; });
   }
   mx = block_reduce(mx, [](K p, K q) { return p > q ? p : q; }, redk);  // also orders the stage
   const int bl = bitlen<K>(mx - t);
   const uint32_t sh = bl > 12 ? (uint32_t)(bl - 12) : 0u;
   each([&](K k) { atomicAdd(&hist[min((uint32_t)((k - t) >> sh), kPickBins - 1u)], 1u); });
   __syncthreads();
-  // the bin holding the kk-th largest: counts from the top, 4 bins per thread
+  // the bin holding the kk-th largest: counts from the top, 4 bins per
+  // thread; off[b] = candidates in the bins above b (their place in
+  // descending order)
+  uint32_t maxc = 0;
   {
     uint32_t c4[4], sum = 0;
 #pragma unroll
@@ -418,15 +398,20 @@ __global__ void __launch_bounds__(1024, 1)
     uint32_t above = block_incl_scan(sum, &tot, red32) - sum;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
+      const uint32_t b = 4 * tid + q;
+      if (b < kPickBins) off[kPickBins - 1 - b] = above;
       if (above < kk && kk <= above + c4[q]) {
         s_j = kPickBins - 1 - (4 * tid + q);
         s_above = above;
       }
+      // a bin holding one of the kk largest and sorted here (not the
+      // kk-th's bin when it is one key wide)
+      if (above < kk && !(sh == 0 && kk <= above + c4[q])) maxc = max(maxc, c4[q]);
       above += c4[q];
     }
     if (tid == 0) s_cnt = 0;
   }
-  __syncthreads();
+  maxc = block_reduce(maxc, [](uint32_t p, uint32_t q) { return p > q ? p : q; }, red32);
   const uint32_t j = s_j, above = s_above;
   const uint32_t in_j = hist[j];
   // one key in bin j (a bin one key wide): only the bins above are gathered
@@ -436,15 +421,49 @@ __global__ void __launch_bounds__(1024, 1)
     if (tid == 0) atomicOr(&ctrl->status, ST_TOPK_MISS);
     return;
   }
+  // Bins of at most kPickBinSort keys: each key goes to its bin's place in
+  // descending order (the bin's count, counted down, numbers its keys), and
+  // one thread sorts each bin's few keys.  Otherwise the gathered keys are
+  // sorted together (bitonic).
+  const bool by_bin = maxc <= kPickBinSort;
   each([&](K k) {
     const uint32_t b = min((uint32_t)((k - t) >> sh), kPickBins - 1u);
-    if (single ? b > j : b >= j) buf[atomicAdd(&s_cnt, 1u)] = k;
+    const bool in = single ? b > j : b >= j;
+    if (by_bin) {
+      if (in) buf[off[b] + atomicSub(&hist[b], 1u) - 1u] = k;
+    } else {
+      const uint32_t at = warp_append(&s_cnt, in);
+      if (in) buf[at] = k;
+    }
   });
   __syncthreads();
-  const uint32_t cnt = s_cnt;  // == need
+  if (by_bin) {
+    // bins j .. kPickBins - 1 (j + 1 .. in the single-key case), each sorted
+    // descending in place by one thread (insertion sort)
+    for (uint32_t b = (single ? j + 1 : j) + tid; b < kPickBins; b += nt) {
+      const uint32_t lo = off[b];
+      const uint32_t hi = b ? off[b - 1] : need;
+      for (uint32_t q = lo + 1; q < hi; ++q) {
+        const K v = buf[q];
+        uint32_t r = q;
+        while (r > lo && buf[r - 1] < v) {
+          buf[r] = buf[r - 1];
+          --r;
+        }
+        buf[r] = v;
+      }
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < kk; i += nt) {
+      const K k = (single && i >= above) ? (K)(t + (K)j) : buf[i];
+      out[i] = Traits<OutT>::value(k);
+    }
+    return;
+  }
+  const uint32_t got = s_cnt;  // == need
   uint32_t P = 1;
-  while (P < cnt) P <<= 1;
-  for (uint32_t q = cnt + tid; q < P; q += nt) buf[q] = K(0);
+  while (P < got) P <<= 1;
+  for (uint32_t q = got + tid; q < P; q += nt) buf[q] = K(0);
   __syncthreads();
   if (P > 1) bitonic_sort_smem(buf, P);  // ascending; the padding sorts first
   // descending: the (i + 1)-th largest is buf[P - 1 - i]; in the single-key

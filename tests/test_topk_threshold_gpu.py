@@ -160,3 +160,16 @@ def test_threshold_topk_repeated_calls_one_context(g, orc):
     st = ctx.stats()
     assert st["topk_threshold_calls"] == 6
     ctx.close()
+
+
+def test_threshold_topk_far_outlier_sorts_together(g, orc):
+    """One key far above the rest stretches the pick's bins until nearly every
+    candidate shares the bottom bin: the gathered keys are sorted together
+    (bitonic) rather than bin by bin, and the answer is the same."""
+    import ggks_problems as gp
+    x = gp.uniform_f32(1 << 22, 17)
+    x[12345] = np.float32(1e30)
+    for K in (1, 32, 100):
+        got, st = _topk(g, x, K)
+        assert_same(got, orc.topk(x, K, 8), f"far outlier K={K}")
+        assert st["topk_threshold_calls"] == 1
