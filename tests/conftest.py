@@ -20,7 +20,15 @@ def pytest_configure(config):
 
 
 def golden_files():
-    return sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
+    """Known-answer and numpy cross-check fixtures (each holds its input)."""
+    return sorted(glob.glob(os.path.join(GOLDEN_DIR, "kat_*.npz"))
+                  + glob.glob(os.path.join(GOLDEN_DIR, "xcheck_*.npz")))
+
+
+def ref_files():
+    """Fixtures holding outputs of the reference itself (the input is
+    regenerated from its recipe; tests/golden/ref_inputs.py)."""
+    return sorted(glob.glob(os.path.join(GOLDEN_DIR, "ref_*.npz")))
 
 
 def load_golden(path):
