@@ -700,6 +700,8 @@ def run_served(torch, ggks, gp, dev, sptr, per_rate=4000):
                        "batch_phase_ms": {p: round(v, 2) for p, v in sst["batch_phase_ms"].items()},
                        "kernel_ms": round(sst["kernel_ms"], 2),
                        "lane_group_ms": round(sst["group_ms"], 2),
+                       "device_busy_ms": round(sst["device_busy_ms"], 2),
+                       "device_span_ms": round(sst["device_span_ms"], 2),
                        "mean_batch": round(sst["batched_requests"] / max(1, sst["batches"]), 2)},
             "sequential_plain": {"req_per_s": round(len(trace) / seq_span, 1),
                                  "p50_ms": pct(seq_lat, 50), "p99_ms": pct(seq_lat, 99)},

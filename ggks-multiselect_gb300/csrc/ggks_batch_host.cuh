@@ -240,25 +240,30 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
       if (r == cudaSuccess) r = cudaEventCreate(&ctx.bev1);
       if (r != cudaSuccess) return r;
     }
-    // a share of the co-resident CTAs when other batches may run at once,
-    // held until this launch has finished
-    uint32_t grid = grid_want, units = 0;
-    if (ctx.grid_budget) grid = ctx.grid_budget->acquire(grid_want, max_grid, &units);
-    struct Share {
-      GridBudget *b;
-      uint32_t u;
-      ~Share() {
-        if (b) b->release(u);
-      }
-    } share{ctx.grid_budget, units};
+    // with a chain (a server's lanes), the kernel is queued on the device
+    // right behind the newest batched kernel of any lane
+    const uint32_t grid = grid_want;
     ctx.stats.batch_grid = grid;
+    std::unique_lock<std::mutex> chain_lk;
+    if (ctx.chain) {
+      chain_lk = std::unique_lock<std::mutex>(ctx.chain->mu);
+      if (ctx.chain->last) {
+        if (cudaEventQuery(ctx.chain->last) == cudaErrorNotReady) ctx.chain->queued++;
+        const cudaError_t we = cudaStreamWaitEvent(s, ctx.chain->last, 0);
+        if (we != cudaSuccess) return we;
+      }
+    }
     cudaEventRecord(ctx.bev0, s);
     cudaError_t r = cudaLaunchCooperativeKernel((const void *)k_batch<T>, dim3(grid), dim3(kBThreads),
                                                 args, (size_t)smem, s);
     cudaEventRecord(ctx.bev1, s);
+    if (ctx.chain) {
+      if (r == cudaSuccess) ctx.chain->last = ctx.bev1;
+      chain_lk.unlock();
+    }
     ctx.stats.launches++;
     if (r != cudaSuccess) {
-      cudaStreamSynchronize(s);  // nothing of this launch may run once its share is returned
+      cudaStreamSynchronize(s);
       return r;
     }
     r = cudaMemcpyAsync(h_ctrl, ctrl, sizeof(BCtrl), cudaMemcpyDeviceToHost, s);
@@ -271,6 +276,9 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
     float ms = 0.f;
     if (r == cudaSuccess && cudaEventElapsedTime(&ms, ctx.bev0, ctx.bev1) == cudaSuccess)
       ms_total += ms;
+    if (r == cudaSuccess && ctx.time_base &&
+        cudaEventElapsedTime(&ctx.last_launch_t0, ctx.time_base, ctx.bev0) == cudaSuccess)
+      ctx.last_launch_t1 = ctx.last_launch_t0 + ms;
     return r;
   };
   e = launch();

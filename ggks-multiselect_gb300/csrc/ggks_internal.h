@@ -27,47 +27,17 @@ struct BatchTune {
   uint32_t tile = 1u << 18;
 };
 
-// Co-resident CTAs of one device, shared by batched launches that may be in
-// flight at the same time (the server's lanes).  A persistent launch waits on
-// grid barriers for all of its CTAs, so the grids in flight together must fit
-// on the device at once: a launch takes its share before it starts and gives
-// it back once it has finished.  Shares are counted in kUnits per device,
-// each kernel's grid measured against the CTAs it alone can keep resident.
-struct GridBudget {
-  static constexpr uint32_t kUnits = 1024;
+// Orders the batched launches of several contexts (a server's lanes) on the
+// device.  Under the mutex a launch makes its stream wait for the newest
+// launch's kernel-done event, launches with the whole co-resident grid, and
+// becomes the newest: the kernels run back to back with the whole device,
+// and each lane's planning, uploads, result copies and scatter overlap the
+// other lanes' kernels (a lane no longer waits on the host for another
+// lane's grid share).
+struct LaunchChain {
   std::mutex mu;
-  std::condition_variable cv;
-  uint32_t free_units = kUnits;
-  uint32_t floor_units = kUnits;  // a launch waits until this much is free (or all it wants)
-  uint32_t active = 0;            // launches holding a share
-  uint64_t concurrent = 0;        // launches started while another held a share
-  // Grid (<= want, >= 1) for a launch of a kernel that keeps max_grid CTAs
-  // resident on the device; *units receives the share taken.
-  uint32_t acquire(uint32_t want, uint32_t max_grid, uint32_t *units) {
-    auto need = [&](uint32_t g) {
-      return (uint32_t)(((uint64_t)g * kUnits + max_grid - 1) / max_grid);
-    };
-    const uint32_t floor_grid =
-        (uint32_t)std::max<uint64_t>(1, (uint64_t)max_grid * floor_units / kUnits);
-    const uint32_t first = std::min(want, floor_grid);
-    std::unique_lock<std::mutex> lk(mu);
-    cv.wait(lk, [&] { return free_units >= need(first); });
-    uint32_t g = (uint32_t)std::min<uint64_t>(want, (uint64_t)free_units * max_grid / kUnits);
-    g = std::max(g, first);
-    *units = need(g);
-    free_units -= *units;
-    if (active > 0) ++concurrent;
-    ++active;
-    return g;
-  }
-  void release(uint32_t units) {
-    {
-      std::lock_guard<std::mutex> lk(mu);
-      free_units += units;
-      --active;
-    }
-    cv.notify_all();
-  }
+  cudaEvent_t last = nullptr;  // kernel-done event of the newest launch (its context's)
+  uint64_t queued = 0;         // launches queued behind a kernel still in flight
 };
 
 // A context owns one device, one stream, a device arena (per-call scratch), a
@@ -103,7 +73,11 @@ struct Context {
   std::map<uint64_t, BatchTune> tuned;
   BatchTune last_tune;
   BatchTune pinned_tune{0, 0};  // div != 0: used for every batch (no autotuning)
-  GridBudget *grid_budget = nullptr;  // shared with other contexts' batched launches, if set
+  LaunchChain *chain = nullptr;  // shared with other contexts' batched launches, if set
+  // when set (a server's lanes), each batched launch's device interval in ms
+  // after this event, read once the launch has finished
+  cudaEvent_t time_base = nullptr;
+  float last_launch_t0 = 0.f, last_launch_t1 = 0.f;
 
   ggks_stats stats{};
   uint32_t profiling = 0;  // bit i: time pass i with CUDA events

@@ -15,11 +15,13 @@
 //              single request takes the single-vector pipeline, whose latency
 //              is lower), scatter the results to the callers' buffers and
 //              release the requests' device bytes.  Each lane has its own
-//              context (stream and workspace), so one lane plans and uploads
-//              its batch while another's runs, and their launches run on the
-//              device together: the persistent grids take shares of the
-//              co-resident CTAs (GridBudget), so every grid in flight is
-//              resident at once.
+//              context (stream and workspace).  The lanes' batched launches
+//              form one chain on the device (LaunchChain): each is queued
+//              behind the newest kernel of any lane and runs with the whole
+//              device as soon as that kernel ends, while the lanes' planning,
+//              control-block uploads, result copies and scatter overlap the
+//              running kernel -- the device goes from one batch's kernel to
+//              the next without a host round trip between them.
 // Requests that arrive while batches are on the GPU are admitted and uploaded
 // meanwhile and join the next batch.
 #include <algorithm>
@@ -69,8 +71,7 @@ struct Server {
   uint64_t cap = 0, used = 0, reserve = kDefaultReserve;
   uint32_t max_batch = 0;
   std::vector<std::unique_ptr<Lane>> lanes;
-  GridBudget budget;
-  std::atomic<uint32_t> groups_running{0};
+  LaunchChain chain;
   cudaStream_t copy_stream = nullptr;
   std::mutex mu;
   std::condition_variable cv_admit, cv_exec, cv_done;
@@ -82,6 +83,8 @@ struct Server {
   bool stopping = false;
   std::thread admit_thr;
   ggks_server_stats st{};
+  cudaEvent_t time_base = nullptr;                // recorded once at creation
+  std::vector<std::pair<float, float>> launch_ms;  // batched launches' device intervals
 };
 
 static size_t elem_size(int dtype) { return dtype == GGKS_DTYPE_F64 ? 8 : 4; }
@@ -220,6 +223,7 @@ static void run_group(Server *S, Context &ctx, std::vector<SReq *> &g) {
   {
     std::lock_guard<std::mutex> lk2(S->mu);
     S->st.kernel_ms += kms;
+    if (st == GGKS_OK) S->launch_ms.emplace_back(ctx.last_launch_t0, ctx.last_launch_t1);
   }
   for (size_t i = 0; i < g.size(); ++i) {
     if (st != GGKS_OK) {
@@ -252,17 +256,11 @@ static void complete(Server *S, cudaStream_t stream, std::vector<SReq *> &g, boo
   S->cv_admit.notify_one();
 }
 
-// runs one element type's group on a lane; counts it as concurrent when
-// another lane's group is on the device at the same time
+// runs one element type's group on a lane
 template <class T>
 static void run_counted(Server *S, Lane &L, std::vector<SReq *> &g) {
   const auto t0 = Clock::now();
-  if (S->groups_running.fetch_add(1) > 0) {
-    std::lock_guard<std::mutex> lk(S->mu);
-    S->st.concurrent_launches++;
-  }
   run_group<T>(S, L.ctx, g);
-  S->groups_running.fetch_sub(1);
   complete(S, L.ctx.stream, g, true);
   std::lock_guard<std::mutex> lk(S->mu);
   S->st.group_ms += std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
@@ -317,11 +315,22 @@ int ggks_server_create(const ggks_server_config *cfg, ggks_server **out) {
   for (uint32_t i = 0; i < nl && st == GGKS_OK; ++i) {
     S->lanes.emplace_back(new Lane());
     st = context_init(S->lanes.back()->ctx, cfg->device);
-    S->lanes.back()->ctx.grid_budget = &S->budget;
+    S->lanes.back()->ctx.chain = &S->chain;
   }
   if (st == GGKS_OK &&
       cudaStreamCreateWithFlags(&S->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
     st = GGKS_CUDA_ERROR;
+  // one time base for every lane's launch intervals
+  if (st == GGKS_OK && (cudaEventCreate(&S->time_base) != cudaSuccess ||
+                        cudaEventRecord(S->time_base, S->copy_stream) != cudaSuccess ||
+                        cudaEventSynchronize(S->time_base) != cudaSuccess))
+    st = GGKS_CUDA_ERROR;
+  if (st == GGKS_OK)
+    for (auto &L : S->lanes) L->ctx.time_base = S->time_base;
+  if (st != GGKS_OK) {
+    if (S->time_base) cudaEventDestroy(S->time_base);
+    if (S->copy_stream) cudaStreamDestroy(S->copy_stream);
+  }
   if (cur >= 0) cudaSetDevice(cur);
   if (st != GGKS_OK) {
     delete S;
@@ -331,8 +340,6 @@ int ggks_server_create(const ggks_server_config *cfg, ggks_server **out) {
   S->cap = cfg->hbm_cap_bytes;
   S->reserve = cfg->hbm_reserve_bytes ? cfg->hbm_reserve_bytes : kDefaultReserve;
   S->max_batch = cfg->max_batch;
-  // a launch waits for an even share of the device (or all it wants)
-  S->budget.floor_units = GridBudget::kUnits / nl;
   S->admit_thr = std::thread(admit_loop, S);
   for (auto &L : S->lanes) L->thr = std::thread(lane_loop, S, L.get());
   *out = reinterpret_cast<ggks_server *>(S);
@@ -359,6 +366,7 @@ int ggks_server_destroy(ggks_server *srv) {
   cudaGetDevice(&cur);
   cudaSetDevice(S->device);
   if (S->copy_stream) cudaStreamDestroy(S->copy_stream);
+  if (S->time_base) cudaEventDestroy(S->time_base);
   if (cur >= 0) cudaSetDevice(cur);
   delete S;
   return GGKS_OK;
@@ -426,11 +434,31 @@ int ggks_server_get_stats(ggks_server *srv, ggks_server_stats *out) {
   if (!srv || !out) return GGKS_INVALID_ARG;
   Server *S = reinterpret_cast<Server *>(srv);
   ggks_server_stats st;
+  std::vector<std::pair<float, float>> iv;
   {
     std::lock_guard<std::mutex> lk(S->mu);
     st = S->st;
     st.in_flight_bytes = S->used;
+    iv = S->launch_ms;
   }
+  {
+    std::lock_guard<std::mutex> lk(S->chain.mu);
+    st.concurrent_launches = S->chain.queued;
+  }
+  // device time covered by at least one batched launch
+  std::sort(iv.begin(), iv.end());
+  double busy = 0.0, end = -1e300;
+  for (const auto &p : iv) {
+    if (p.first > end) {
+      busy += p.second - p.first;
+      end = p.second;
+    } else if (p.second > end) {
+      busy += p.second - end;
+      end = p.second;
+    }
+  }
+  st.device_busy_ms = busy;
+  st.device_span_ms = iv.empty() ? 0.0 : end - iv.front().first;
   // the lanes' batched phases and recursions, read under each lane's lock
   st.recursions = 0;
   for (int ph = 0; ph < GGKS_NUM_BATCH_PHASES; ++ph) st.batch_phase_ms[ph] = 0.0;

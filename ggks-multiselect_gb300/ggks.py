@@ -94,13 +94,16 @@ class ServerStats(ctypes.Structure):
         "uploads", "upload_bytes", "peak_bytes", "in_flight_bytes", "concurrent_launches",
         "hbm_waits", "admit_budget_bytes", "single_calls", "recursions")] + [
         ("batch_phase_ms", ctypes.c_double * NUM_BATCH_PHASES), ("kernel_ms", ctypes.c_double),
-        ("group_ms", ctypes.c_double)]
+        ("group_ms", ctypes.c_double), ("device_busy_ms", ctypes.c_double),
+        ("device_span_ms", ctypes.c_double)]
 
     def as_dict(self):
         d = {f: int(getattr(self, f)) for f, t in self._fields_ if t is ctypes.c_uint64}
         d["batch_phase_ms"] = dict(zip(BATCH_PHASE_NAMES, list(self.batch_phase_ms)))
         d["kernel_ms"] = float(self.kernel_ms)
         d["group_ms"] = float(self.group_ms)
+        d["device_busy_ms"] = float(self.device_busy_ms)
+        d["device_span_ms"] = float(self.device_span_ms)
         return d
 
 

@@ -278,7 +278,8 @@ typedef struct ggks_server_stats {
   uint64_t uploads, upload_bytes; /* host vectors copied at admission */
   uint64_t peak_bytes;       /* largest admitted device bytes */
   uint64_t in_flight_bytes;  /* admitted device bytes now */
-  uint64_t concurrent_launches; /* launches started while another lane's batch ran */
+  uint64_t concurrent_launches; /* batched launches queued on the device behind another
+                                   lane's kernel still in flight */
   uint64_t hbm_waits;        /* admissions held back by the device's free memory */
   uint64_t admit_budget_bytes; /* the admission budget at the last admission */
   uint64_t single_calls;     /* lone requests of a type run on the single-vector pipeline */
@@ -286,6 +287,8 @@ typedef struct ggks_server_stats {
   double batch_phase_ms[GGKS_NUM_BATCH_PHASES]; /* device time per batch phase, all lanes */
   double kernel_ms;          /* device time of the batched launches, all lanes */
   double group_ms;           /* lane wall time per element-type group (plan, run, results) */
+  double device_busy_ms;     /* union of the batched launches' device intervals, all lanes */
+  double device_span_ms;     /* first batched launch's start to the last one's end */
 } ggks_server_stats;
 
 int ggks_server_create(const ggks_server_config *cfg, ggks_server **out);

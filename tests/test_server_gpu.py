@@ -139,10 +139,11 @@ def test_server_concurrent_submitters(g, orc):
 
 
 def test_server_lanes_overlap(g, orc):
-    """With two lanes and small batches under load, one lane's batch is on the
-    device while another lane plans and launches its own: the server counts
-    launches that started while another lane's batch ran.  Every result
-    equals the oracle's."""
+    """With two lanes and small batches under load, one lane's kernel runs
+    while the other lane plans, uploads and queues its own launch behind it
+    on the device: the server counts launches queued behind a kernel still in
+    flight, and the device time covered by batched kernels fits inside their
+    span.  Every result equals the oracle's."""
     reqs = _mixed_requests(5, 160, max_log2=21)
     devs = [DeviceArray(x) for x, _, _ in reqs]
     srv = g.Server(0, hbm_cap_bytes=16 << 30, max_batch=6, lanes=2)
@@ -157,19 +158,27 @@ def test_server_lanes_overlap(g, orc):
     assert st["completed"] == len(reqs)
     assert st["batches"] >= len(reqs) // 6
     assert st["concurrent_launches"] > 0
+    assert 0 < st["device_busy_ms"] <= st["device_span_ms"] + 1e-3
 
 
 def test_server_admission_by_free_device_memory(g, orc):
     """The admission budget follows the device's free memory: with a reserve
     that leaves only 512 MB of it to the server, 16 host-vector requests of
     64 MB wait for earlier ones to finish (hbm_waits) although the
-    cap would admit them all, and every result is exact.  A request that could
-    never fit -- the reserve larger than the free memory, nothing admitted --
-    fails with GGKS_OOM instead of waiting forever."""
+    cap would admit them all, and every result is exact.  The vectors are in
+    pinned host memory, so an upload does not hold the admission thread: it
+    reaches the eighth request (7 x 68 MB charged) while the first is still
+    uploading, and that one must wait.  A request that could never fit -- the
+    reserve larger than the free memory, nothing admitted -- fails with
+    GGKS_OOM instead of waiting forever."""
     import torch
 
     import ggks_problems as gp
-    xs = [gp.generate("f32", "uniform", 1 << 24, seed=40 + i) for i in range(16)]
+    xs = []
+    for i in range(16):
+        h = torch.empty(1 << 24, dtype=torch.float32, pin_memory=True).numpy()
+        h[:] = gp.generate("f32", "uniform", 1 << 24, seed=40 + i)
+        xs.append(h)
     ks = [gp.k_distinct(x.size, 64, i) for i, x in enumerate(xs)]
     torch.cuda.synchronize()
     free = torch.cuda.mem_get_info()[0]
