@@ -13,14 +13,28 @@
 //              (the single-vector builder) with 2^nsl_bits slices.
 //   2 hist     queue over (problem, tile) items: a tile is a contiguous range
 //              of one problem; its shared-memory histogram becomes one row of
-//              counts (rows of a problem's tiles are consecutive).
+//              counts (rows of a problem's tiles are consecutive).  Tiles of a
+//              speculating problem also keep the keys inside the problem's
+//              candidate window in the tile's candidate area.
 //   3 plan     queue over problems: the problem's rows become their exclusive
 //              prefix over its tiles (column sums = bucket counts), a block
 //              scan gives the bucket prefix, requested ranks map to buckets
 //              and slots, the slots' survivors get a range of the shared
 //              survivor buffer from a bump allocator, request lists per slot.
 //   4 compact  queue over the same (problem, tile) items: cursors start at the
-//              tile's prefix row, one shared atomic per element.
+//              tile's prefix row, one shared atomic per element; a tile of a
+//              speculating problem whose slots all lie inside the window
+//              reads its complete candidate list instead of its elements.
+//
+// Speculation (top-k and other requests whose ranks cluster): the host sends
+// the problem's rank window; phase 1 takes from the sample a key tau_lo below
+// the window's lowest rank and a key tau_hi above its highest, with four
+// standard deviations of the sample's rank error (counted in sampled chunks)
+// and two chunks to spare, and phase 3 checks that every slot's bucket lies
+// strictly between the buckets of tau_lo and tau_hi (buckets are monotone in
+// the key, so every key of those buckets is then a candidate).  A tile whose
+// list overflowed its area, or a problem whose slots fall outside, reads the
+// elements as before: correctness never rests on the sample.
 //   5 finish   queue over the large slots: finish_slot (the single-vector
 //              finisher), a whole CTA each; then a queue over the small slots
 //              (at most warp_cap keys, the common case), one warp each.
@@ -65,6 +79,9 @@ struct BProb {
   uint32_t req_off, num_req;  // requests [req_off, req_off + num_req); slots use the same range
   uint32_t nb_max, nsl_bits;
   uint32_t S, ntiles;
+  uint32_t spec;              // 1: keep candidates in [rank spec_lo, rank spec_hi]
+  uint32_t spec_lo, spec_hi;  // ascending ranks (0-based) the requests fall in
+  uint32_t pad;
 };
 
 // splitter-table header and plan results of one problem (device-written)
@@ -72,14 +89,19 @@ struct BHdr {
   uint64_t base;
   uint64_t surv_off;
   uint32_t shift, nb, heavy, num_slots;
-  uint32_t dup;  // tiles track whether each bucket holds a single key
-  uint32_t pad[3];
+  uint32_t dup;      // tiles track whether each bucket holds a single key
+  uint32_t spec_on;  // phase 1 set the candidate window [tau_lo, tau_hi]
+  uint32_t spec_ok;  // phase 3: every slot's bucket lies strictly inside it
+  uint32_t pad;
+  uint64_t tau_lo, tau_hi;  // keys; tau_lo 0 / tau_hi the largest key: open end
 };
 
 // one (problem, tile) work item (host-written)
 struct BTile {
   uint64_t begin, end;  // elements [begin, end) of problem prob
   uint32_t prob, rank;  // rank of the tile among its problem's tiles
+  uint64_t cand_off;    // key index of the tile's candidate area (speculating problems)
+  uint32_t cand_cap, pad;
 };
 
 struct BCtrl {
@@ -89,7 +111,7 @@ struct BCtrl {
   uint32_t deferred_count;
   uint32_t n_big, n_small;  // slots finished by a whole CTA / by one warp
   uint32_t small_pop;       // warp queue of the small slots
-  uint32_t pad;
+  uint32_t spec_tiles;      // compaction tiles that read their candidates
   uint64_t surv_top;    // survivor bump allocator
   uint64_t cap_needed;  // survivors wanted when they did not fit
   uint64_t t_ns[kBPhases + 1];  // %globaltimer at the start and after each phase (CTA 0)
@@ -121,6 +143,8 @@ struct BArgs {
   void *surv;             // key array
   uint32_t *deferred;
   void *out;              // output values
+  void *cand;             // key array: the tiles' candidate areas
+  uint32_t *cand_cnt;     // per tile: candidates seen (may exceed the area)
   BCtrl *ctrl;
 };
 
@@ -226,8 +250,57 @@ __device__ __forceinline__ BHdr load_hdr(const BHdr *h) {
   r.nb = w.y;
   r.heavy = w.z;
   r.num_slots = w.w;
-  r.dup = __ldcg(&h->dup);
+  const uint4 w2 = __ldcg(reinterpret_cast<const uint4 *>(&h->dup));
+  r.dup = w2.x;
+  r.spec_on = w2.y;
+  r.spec_ok = w2.z;
+  r.tau_lo = ldcg_u(&h->tau_lo);
+  r.tau_hi = ldcg_u(&h->tau_hi);
   return r;
+}
+
+// The r-th smallest (0-based, r < S) of keys[0, S) in shared memory, by the
+// whole CTA: MSD radix select, eight bits a round.  cnt: 256 shared words;
+// sel: 2 shared words.  Every thread returns the key.
+template <class K>
+__device__ K cta_select_rank(const K *keys, uint32_t S, uint32_t r, uint32_t *cnt, uint32_t *sel) {
+  const uint32_t tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
+  K prefix = 0, mask = 0;
+  for (int sh = 8 * (int)sizeof(K) - 8; sh >= 0; sh -= 8) {
+    for (uint32_t i = tid; i < 256; i += nt) cnt[i] = 0;
+    __syncthreads();
+    for (uint32_t i = tid; i < S; i += nt) {
+      const K k = keys[i];
+      if ((k & mask) == prefix) atomicAdd(&cnt[(uint32_t)(k >> sh) & 255u], 1u);
+    }
+    __syncthreads();
+    if (tid < 32) {
+      uint32_t c[8], sum = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        c[j] = cnt[8 * lane + j];
+        sum += c[j];
+      }
+      const uint32_t incl = warp_incl_scan(sum);
+      uint32_t acc = incl - sum;
+      if (acc <= r && r < incl) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          if (r >= acc && r < acc + c[j]) {
+            sel[0] = 8 * lane + j;
+            sel[1] = r - acc;
+          }
+          acc += c[j];
+        }
+      }
+    }
+    __syncthreads();
+    prefix |= (K)sel[0] << sh;
+    mask |= (K)255 << sh;
+    r = sel[1];
+    __syncthreads();
+  }
+  return prefix;
 }
 
 // One warp finishes a segment of at most warp_cap<K>() keys: the keys are
@@ -335,6 +408,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
   __shared__ uint32_t s_lb[2];
   __shared__ LutHeader<K> s_hdr;
   __shared__ bool s_bad;
+  __shared__ uint32_t s_rcnt[256], s_rsel[2], s_ccnt;
   BCtrl *ctrl = A.ctrl;
   const uint32_t tid = threadIdx.x, nt = blockDim.x;
   K *surv = reinterpret_cast<K *>(A.surv);
@@ -342,6 +416,8 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
   K *seg_hi = reinterpret_cast<K *>(A.seg_hi);
   OutT *out = reinterpret_cast<OutT *>(A.out);
   if (blockIdx.x == 0 && tid == 0) ctrl->t_ns[0] = global_ns();
+  // candidate counts start at zero (phase 2 adds to them after the barrier)
+  for (uint32_t t = blockIdx.x * nt + tid; t < A.num_tiles; t += gridDim.x * nt) A.cand_cnt[t] = 0;
 
   // ---------------- phase 1: splitter tables
   for (uint32_t p = queue_pop(&ctrl->queue[0], &s_item); p < A.num_probs;
@@ -391,6 +467,24 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
     build_lut_cta<K, kBSpt, true>(samples, P.S, lo, hi, P.nb_max, A.luts + P.lut_off, &s_hdr,
                                   (int)P.nsl_bits);
     __syncthreads();
+    // Speculation: the window's ends as sample ranks, moved outwards by four
+    // standard deviations of the number of sampled chunks below them
+    // (Binomial(chunks, rank / n)) plus two chunks, in chunk-sized units (a
+    // chunk's keys are neighbours, as correlated as sorted input makes them);
+    // an end beyond the samples leaves that side open.  A miss costs only the
+    // full compaction read.  The same float arithmetic in every thread.
+    K tau_lo = 0, tau_hi = KeyMax<K>::v;
+    const bool spec_on = P.spec && (uint64_t)P.S < P.n && !s_hdr.dup;
+    if (spec_on) {
+      constexpr uint32_t CH = 32 / sizeof(T);
+      const float fS = (float)P.S, fc = (float)(P.S / CH), fn = (float)P.n;
+      const float pl = (float)P.spec_lo / fn, ph = (float)((uint64_t)P.spec_hi + 1) / fn;
+      const float al = pl * fS - (float)CH * (4.0f * sqrtf(fc * pl * (1.0f - pl)) + 2.0f);
+      const float ah = ph * fS + (float)CH * (4.0f * sqrtf(fc * ph * (1.0f - ph)) + 2.0f);
+      if (al >= 1.0f) tau_lo = cta_select_rank<K>(samples, P.S, (uint32_t)al, s_rcnt, s_rsel);
+      if (ah <= fS - 2.0f)
+        tau_hi = cta_select_rank<K>(samples, P.S, (uint32_t)ah + 1u, s_rcnt, s_rsel);
+    }
 #ifdef GGKS_BATCH_TIMING
     if (tid == 0) {
       atomicAdd((unsigned long long *)&ctrl->dbg_a, (unsigned long long)(c1 - c0));
@@ -406,7 +500,11 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       h.heavy = s_hdr.heavy;
       h.num_slots = 0;
       h.dup = (s_hdr.dup && P.nb_max * sizeof(K) <= kBRepBytes) ? 1u : 0u;
-      h.pad[0] = h.pad[1] = h.pad[2] = 0;
+      h.spec_on = spec_on ? 1u : 0u;
+      h.spec_ok = 0;
+      h.pad = 0;
+      h.tau_lo = (uint64_t)tau_lo;
+      h.tau_hi = (uint64_t)tau_hi;
       A.hdrs[p] = h;
     }
     // the bucket totals start at zero: the tiles of phase 2 add to them
@@ -433,6 +531,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         hist[b] = 0;
         if (H.dup) rep[b] = KeyMax<K>::v;
       }
+      if (tid == 0) s_ccnt = 0;
       __syncthreads();
       if (tid == 0) s_cur = tl.prob;
       const K base = (K)H.base;
@@ -455,6 +554,23 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
             }
           }
         });
+      } else if (H.spec_on) {
+        // count, and append the keys inside the window to the tile's
+        // candidate area: one unsigned compare per key, a shared atomic for
+        // each kept key (about one lane in a warp keeps one when it does, so
+        // a warp vote would buy nothing); the count goes on past the area's
+        // end, so the compaction phase can tell a complete list
+        const K tlo = (K)H.tau_lo, span = (K)H.tau_hi - (K)H.tau_lo;
+        K *cand = reinterpret_cast<K *>(A.cand) + tl.cand_off;
+        const uint32_t ccap = tl.cand_cap;
+        for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
+          const uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
+          if (BCHECK(ub < H.nb, 4, ub, H.nb)) atomicAdd(&hist[swz(ub)], 1u);
+          if ((K)(k - tlo) <= span) {
+            const uint32_t pos = atomicAdd(&s_ccnt, 1u);
+            if (pos < ccap) cand[pos] = k;
+          }
+        });
       } else {
         // also for heavy problems: the histogram's atomics return nothing, and
         // lanes adding to one counter cost no more than lanes adding to
@@ -467,6 +583,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         });
       }
       __syncthreads();
+      if (H.spec_on && tid == 0) A.cand_cnt[t] = s_ccnt;
       const uint64_t ro = P.row0 + (uint64_t)tl.rank * P.nb_max;
       if (!BCHECK(ro + H.nb <= A.row_words && H.nb <= P.nb_max, 5, ro, H.nb)) continue;
       // the tile's row, and its counts added to the problem's bucket totals
@@ -593,6 +710,12 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       const uint32_t sper = (tot_slots + nt - 1) / nt;
       const uint32_t s0 = min(tot_slots, tid * sper), s1 = min(tot_slots, s0 + sper);
       uint64_t my_surv = 0;
+      // speculation holds when every slot with survivors lies strictly between
+      // the buckets of the window's ends (an open end bounds nothing)
+      const bool lo_open = H.tau_lo == 0, hi_open = (K)H.tau_hi == KeyMax<K>::v;
+      const uint32_t b_tlo = lo_open ? 0u : bucket_of<K>((K)H.tau_lo, (K)H.base, H.shift, lut, nsl);
+      const uint32_t b_thi = hi_open ? 0u : bucket_of<K>((K)H.tau_hi, (K)H.base, H.shift, lut, nsl);
+      bool outside = false;
       for (uint32_t q = s0; q < s1; ++q) {
         const uint32_t g = P.req_off + q;
         const uint32_t b = __ldcg(A.seg_bucket + g);
@@ -606,6 +729,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
           klo = ldcg_u(reps + P.row0 + b);
         }
         const uint32_t cb = single ? 0u : __ldcg(cnt + b);
+        if (cb && ((!lo_open && b <= b_tlo) || (!hi_open && b >= b_thi))) outside = true;
         A.seg_size[g] = cb;
         seg_lo[g] = klo;
         seg_hi[g] = single ? klo : (knext > klo ? knext - K(1) : KeyMax<K>::v);
@@ -614,6 +738,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         A.fill[g] = 0;
         my_surv += cb;
       }
+      if (__syncthreads_or(outside) == 0 && H.spec_on && tid == 0) A.hdrs[p].spec_ok = 1u;
       uint64_t tot_surv;
       uint64_t off = block_incl_scan(my_surv, &tot_surv, red64) - my_surv;
       if (tid == 0) {
@@ -752,7 +877,20 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       const uint32_t cap = (uint32_t)(room < (uint64_t)kInactive ? room : kInactive);
       const K base = (K)H.base;
       const uint32_t shift = H.shift;
-      if (H.heavy) {
+      const uint32_t ncand = H.spec_ok ? __ldcg(A.cand_cnt + t) : 0xFFFFFFFFu;
+      if (H.spec_ok && ncand <= tl.cand_cap) {
+        // the tile's complete candidate list holds every key of its slots'
+        // buckets (phase 3's check): read it in place of the elements
+        const K *cand = reinterpret_cast<const K *>(A.cand) + tl.cand_off;
+        for (uint32_t i = tid; i < ncand; i += nt) {
+          const K k = ldcg_u(cand + i);
+          const uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
+          if (!BCHECK(ub < H.nb, 9, ub, H.nb)) continue;
+          const uint32_t pos = atomicAdd(&cursor[swz(ub)], 1u);
+          st_global_if(sp + pos, k, pos < cap);
+        }
+        if (tid == 0) atomicAdd(&ctrl->spec_tiles, 1u);
+      } else if (H.heavy) {
         // Sorted runs and few distinct keys: the cursor atomics return
         // positions, which lanes of one address receive one at a time, so
         // lanes of a warp sharing a bucket take one atomic (match.any) and

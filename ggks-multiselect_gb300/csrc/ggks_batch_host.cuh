@@ -3,6 +3,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -96,6 +97,22 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
     b.ntiles = (uint32_t)((b.n + tile - 1) / tile);
     b.req_off = in.k_off[p];
     b.num_req = nr;
+    // speculation: requests whose ascending ranks span at most n / 32 (a top-k,
+    // k's close together) of a problem larger than eight samples' worth
+    {
+      uint64_t rmin = ~0ull, rmax = 0;
+      for (uint32_t i = 0; i < nr; ++i) {
+        const uint64_t k = in.k ? in.k[in.k_off[p] + i] : (uint64_t)i + 1;
+        const uint64_t r = b.n - k;
+        rmin = std::min(rmin, r);
+        rmax = std::max(rmax, r);
+      }
+      if (b.n > 8ull * kBMaxS && rmax - rmin + 1 <= b.n / 32) {
+        b.spec = 1;
+        b.spec_lo = (uint32_t)rmin;
+        b.spec_hi = (uint32_t)rmax;
+      }
+    }
     b.lut_off = lut_words;
     lut_words += ((1u << nsl_bits) + 1 + 3) & ~3u;
     b.cnt_off = cnt_words;
@@ -124,6 +141,26 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   std::stable_sort(tiles.begin(), tiles.end(), [](const BTile &a, const BTile &b) {
     return (a.end - a.begin) > (b.end - b.begin);
   });
+  // candidate areas of speculating problems' tiles: the window and the
+  // thresholds' margins (as the kernel places them) spread over the tiles in
+  // proportion to their length, with half again and 256 keys to spare; a tile
+  // that sees more reads its elements in the compaction phase
+  uint64_t cand_words = 0;
+  for (BTile &t : tiles) {
+    const BProb &b = probs[t.prob];
+    t.cand_off = cand_words;
+    t.cand_cap = 0;
+    if (!b.spec) continue;
+    constexpr double CH = 32.0 / sizeof(T);
+    const double S = b.S, fc = b.S / CH, n = (double)b.n;
+    auto margin = [&](double q) { return CH * (4.0 * std::sqrt(fc * q * (1.0 - q)) + 2.0) + 1.0; };
+    const double pl = b.spec_lo / n, ph = (b.spec_hi + 1.0) / n;
+    const double expect = (b.spec_hi - b.spec_lo + 1.0) + (margin(pl) + margin(ph)) * n / S;
+    const double len = (double)(t.end - t.begin);
+    const uint64_t cap = std::min<uint64_t>(t.end - t.begin, (uint64_t)(expect * len / n * 1.5) + 256);
+    t.cand_cap = (uint32_t)((cap + 3) & ~3ull);
+    cand_words += t.cand_cap;
+  }
 
   // ---- workspace: [ctrl | probs | tiles | reqs] is uploaded in one copy
   const size_t A = 256;
@@ -150,6 +187,7 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   const size_t o_klist = arr(R, sizeof(Req)), o_deferred = arr(R, 4);
   const size_t o_big = arr(R, 4), o_small = arr(R, 4);
   const size_t o_out = arr(R, sizeof(T));
+  const size_t o_cand = arr(cand_words, sizeof(K)), o_ccnt = arr(num_tiles, 4);
   const size_t total = o;
 
   cudaError_t e = ensure_buffer(ctx, &ctx.barena, &ctx.barena_bytes, total);
@@ -219,6 +257,8 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   a.small_list = reinterpret_cast<uint32_t *>(D + o_small);
   a.deferred = reinterpret_cast<uint32_t *>(D + o_deferred);
   a.out = d_out;
+  a.cand = D + o_cand;
+  a.cand_cnt = reinterpret_cast<uint32_t *>(D + o_ccnt);
   a.ctrl = ctrl;
 
 
@@ -312,6 +352,7 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
     for (int ph = 0; ph < kBPhases; ++ph)
       if (c.t_ns[ph + 1] >= c.t_ns[ph]) ctx.stats.batch_phase_ms[ph] += (c.t_ns[ph + 1] - c.t_ns[ph]) * 1e-6;
     ctx.stats.survivors += c.surv_top;
+    ctx.stats.batch_spec_tiles += c.spec_tiles;
     if (c.status & ST_DEFERRED) {
       // slots whose needed bins exceed shared memory: select each again on
       // its survivor keys (recursively, single-vector path)

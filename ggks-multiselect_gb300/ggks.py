@@ -55,7 +55,7 @@ class Stats(ctypes.Structure):
                 ("batch_phase_ms", ctypes.c_double * NUM_BATCH_PHASES),
                 ("batch_grid", ctypes.c_uint64), ("spec_calls", ctypes.c_uint64),
                 ("spec_ctas", ctypes.c_uint64), ("topk_threshold_calls", ctypes.c_uint64),
-                ("topk_misses", ctypes.c_uint64)]
+                ("topk_misses", ctypes.c_uint64), ("batch_spec_tiles", ctypes.c_uint64)]
 
     def as_dict(self):
         return {"calls": self.calls, "launches": self.launches,
@@ -68,7 +68,7 @@ class Stats(ctypes.Structure):
                 "batch_phase_ms": dict(zip(BATCH_PHASE_NAMES, list(self.batch_phase_ms))),
                 "batch_grid": self.batch_grid, "spec_calls": self.spec_calls,
                 "spec_ctas": self.spec_ctas, "topk_threshold_calls": self.topk_threshold_calls,
-                "topk_misses": self.topk_misses}
+                "topk_misses": self.topk_misses, "batch_spec_tiles": self.batch_spec_tiles}
 
 
 DTYPE_CODES = {np.dtype(np.float32): 0, np.dtype(np.float64): 1, np.dtype(np.uint32): 2}

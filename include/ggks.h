@@ -339,6 +339,8 @@ typedef struct ggks_stats {
                                          in place of their share of the vector */
   uint64_t topk_threshold_calls;      /* top-k calls answered by the threshold path */
   uint64_t topk_misses;               /* threshold attempts that fell back to the pipeline */
+  uint64_t batch_spec_tiles;          /* batched compaction tiles that read their candidates
+                                         in place of their elements */
 } ggks_stats;
 
 /* phase indices of ggks_stats.batch_phase_ms (one persistent launch; each
