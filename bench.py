@@ -658,20 +658,40 @@ def run_served(torch, ggks, gp, dev, sptr, per_rate=4000):
             seq_lat.append(time.perf_counter() - ta)
         seq_span = (t0 + trace[-1]["t"] + seq_lat[-1]) - t0
 
-        # ---- served: submit at arrival times, wait in order
+        # ---- served: submit at arrival times, wait in order.  Every request
+        # (its ggks_request, k list and output buffer) is built before the
+        # clock starts, so the submitter only waits for each arrival time and
+        # makes the C call: the offered rate is the trace's, not the rate at
+        # which Python can build requests.
         srv = ggks.Server(dev.index or 0, hbm_cap_bytes=64 << 30)
         tickets = [None] * len(trace)
         sub_t = [0.0] * len(trace)
+        sub_at = [0.0] * len(trace)
+        prepared = []
+        for i, q in enumerate(trace):
+            dt = q["dtype"]
+            karr = None if q["k"] is None else np.ascontiguousarray(q["k"], dtype=np.uint32)
+            req = ggks.Request(ggks.DTYPE_CODES[np.dtype(DT[dt])],
+                               ggks.REQ_TOPK if karr is None else 0,
+                               ctypes.c_void_p(ptrs[dt][q["vec"]]), sizes[dt][q["vec"]],
+                               karr.ctypes.data if karr is not None else None,
+                               q["K"] if karr is None else karr.size, 0)
+            prepared.append((req, karr, ctypes.c_void_p(bufs[i][1].ctypes.data),
+                             ctypes.c_uint64()))
+        fsub = L.ggks_server_submit
 
         def submitter():
             for i, q in enumerate(trace):
                 ta = t1 + q["t"]
                 while time.perf_counter() < ta:
                     pass
-                dt = q["dtype"]
-                sub_t[i] = time.perf_counter() - ta
-                tickets[i] = srv.submit(ptrs[dt][q["vec"]], sizes[dt][q["vec"]], DT[dt],
-                                        k=q["k"], K=q["K"], out=bufs[i][1])
+                req, _, optr, tk = prepared[i]
+                now = time.perf_counter()
+                sub_t[i] = now - ta
+                sub_at[i] = now
+                if fsub(srv.handle, ctypes.byref(req), optr, ctypes.byref(tk)) != 0:
+                    raise RuntimeError("server submit failed")
+                tickets[i] = tk.value
 
         t1 = time.perf_counter() + 0.01
         th = threading.Thread(target=submitter)
@@ -686,11 +706,13 @@ def run_served(torch, ggks, gp, dev, sptr, per_rate=4000):
         sst = srv.stats()
         srv.close()
         srv_span = max(q["t"] + lat for q, lat in zip(trace, srv_lat))
+        sub_span = sub_at[-1] - sub_at[0]
         exact = all(np.array_equal(a.view(np.uint8), b.view(np.uint8)) for a, b in bufs)
         all_exact &= exact
         out["rates"][str(rate)] = {
             "offered_req_per_s": rate,
             "served": {"req_per_s": round(len(trace) / srv_span, 1),
+                       "submitted_req_per_s": round((len(trace) - 1) / max(sub_span, 1e-9), 1),
                        "p50_ms": pct(srv_lat, 50), "p99_ms": pct(srv_lat, 99),
                        "GB/s": round(in_bytes / srv_span / 1e9, 1),
                        "batches": sst["batches"], "launches": sst["launches"],

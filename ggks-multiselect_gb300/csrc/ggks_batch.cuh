@@ -46,6 +46,8 @@
 // ld.global.cg (L2), never through a possibly stale L1 line.
 #pragma once
 
+#include <type_traits>
+
 #include "ggks_device.cuh"
 
 namespace ggks {
@@ -81,7 +83,7 @@ struct BProb {
   uint32_t S, ntiles;
   uint32_t spec;              // 1: keep candidates in [rank spec_lo, rank spec_hi]
   uint32_t spec_lo, spec_hi;  // ascending ranks (0-based) the requests fall in
-  uint32_t pad;
+  uint32_t flt;               // a uint32 batch's float32 problem: keys in float order
 };
 
 // splitter-table header and plan results of one problem (device-written)
@@ -394,6 +396,33 @@ __device__ __forceinline__ void for_range(const T *__restrict__ x, uint64_t a, u
   }
 }
 
+// A uint32 batch also carries float32 problems (flt): both have 32-bit keys,
+// so float32 and uint32 requests share one launch; a float32 problem's keys
+// take the float order (its outputs are keys, turned back into floats by the
+// host).  Key of element i of a problem's vector:
+template <class T>
+__device__ __forceinline__ typename Traits<T>::K load_key(const void *x, uint64_t i, uint32_t flt) {
+  if constexpr (std::is_same<T, uint32_t>::value) {
+    const uint32_t b = reinterpret_cast<const uint32_t *>(x)[i];
+    return flt ? Traits<float>::key_bits(b) : b;
+  } else {
+    return Traits<T>::key(reinterpret_cast<const T *>(x)[i]);
+  }
+}
+
+// for_range over a problem's vector in its own key order
+template <class T, class F>
+__device__ __forceinline__ void for_range_p(const void *x, uint32_t flt, uint64_t a, uint64_t b,
+                                            F &&f) {
+  if constexpr (std::is_same<T, uint32_t>::value) {
+    if (flt) {
+      for_range<float>(reinterpret_cast<const float *>(x), a, b, f);
+      return;
+    }
+  }
+  for_range<T>(reinterpret_cast<const T *>(x), a, b, f);
+}
+
 template <class T>
 __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
   using K = typename Traits<T>::K;
@@ -426,13 +455,12 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
     const long long c0 = clock64();
 #endif
     const BProb P = A.probs[p];
-    const T *x = reinterpret_cast<const T *>(P.x);
     K *samples = reinterpret_cast<K *>(sm);
     K lo = KeyMax<K>::v, hi = 0;
     if ((uint64_t)P.S >= P.n) {
       // small problem: every element is a sample
       for (uint32_t i = tid; i < P.S; i += nt) {
-        const K k = Traits<T>::key(x[i]);
+        const K k = load_key<T>(P.x, i, P.flt);
         samples[i] = k;
         lo = k < lo ? k : lo;
         hi = k > hi ? k : hi;
@@ -448,7 +476,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         const uint64_t pos = (((uint64_t)hash32(c * 0x9E3779B9u + 0x5EEDu) * slots) >> 32) * CH;
         K k[CH];
 #pragma unroll
-        for (uint32_t e = 0; e < CH; ++e) k[e] = Traits<T>::key(x[pos + e]);
+        for (uint32_t e = 0; e < CH; ++e) k[e] = load_key<T>(P.x, pos + e, P.flt);
 #pragma unroll
         for (uint32_t e = 0; e < CH; ++e) {
           samples[c * CH + e] = k[e];
@@ -539,7 +567,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       if (H.dup) {
         // count, and keep the bucket's first key; a second distinct key (or
         // the largest key, which marks an empty entry) sets the mixed bit
-        for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
+        for_range_p<T>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool) {
           const uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
           if (!BCHECK(ub < H.nb, 2, ub, H.nb)) return;
           const uint32_t b = swz(ub);
@@ -563,7 +591,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         const K tlo = (K)H.tau_lo, span = (K)H.tau_hi - (K)H.tau_lo;
         K *cand = reinterpret_cast<K *>(A.cand) + tl.cand_off;
         const uint32_t ccap = tl.cand_cap;
-        for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
+        for_range_p<T>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool) {
           const uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
           if (BCHECK(ub < H.nb, 4, ub, H.nb)) atomicAdd(&hist[swz(ub)], 1u);
           if ((K)(k - tlo) <= span) {
@@ -576,7 +604,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         // lanes adding to one counter cost no more than lanes adding to
         // different ones, so warp aggregation (compaction's) would only slow
         // this phase down
-        for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
+        for_range_p<T>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool) {
           const uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
           if (!BCHECK(ub < H.nb, 4, ub, H.nb)) return;
           atomicAdd(&hist[swz(ub)], 1u);
@@ -896,7 +924,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         // lanes of a warp sharing a bucket take one atomic (match.any) and
         // consecutive positions.  A key whose bucket fails the check (the call
         // is then failed) stays in the vote under bucket 0 but is not stored.
-        for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool full) {
+        for_range_p<T>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool full) {
           uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
           const bool ok = BCHECK(ub < H.nb, 9, ub, H.nb);
           if (!ok) ub = 0;
@@ -915,7 +943,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
           st_global_if(sp + pos, k, ok && pos < cap);
         });
       } else {
-        for_range<T>(reinterpret_cast<const T *>(P.x), tl.begin, tl.end, [&](K k, bool) {
+        for_range_p<T>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool) {
           uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
           if (!BCHECK(ub < H.nb, 9, ub, H.nb)) return;
           const uint32_t pos = atomicAdd(&cursor[swz(ub)], 1u);

@@ -7,6 +7,7 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "ggks_batch.cuh"
@@ -39,6 +40,8 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   using K = typename Traits<T>::K;
   const uint32_t bcap = sizeof(K) == 4 ? 4096u : 2048u;
   const uint32_t R = in.k_off[in.num_problems];
+  // float32 problems ride in uint32 batches only, with host outputs
+  if (in.is_float && (!std::is_same<T, uint32_t>::value || d_out_user)) return GGKS_INVALID_ARG;
 
   // co-resident grid: every CTA the SMs hold at once
   const int smem = batch_smem_bytes<T>();
@@ -97,6 +100,7 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
     b.ntiles = (uint32_t)((b.n + tile - 1) / tile);
     b.req_off = in.k_off[p];
     b.num_req = nr;
+    b.flt = in.is_float ? (in.is_float[p] ? 1u : 0u) : 0u;
     // speculation: requests whose ascending ranks span at most n / 32 (a top-k,
     // k's close together) of a problem larger than eight samples' worth
     {
@@ -296,6 +300,7 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
     cudaEventRecord(ctx.bev0, s);
     cudaError_t r = cudaLaunchCooperativeKernel((const void *)k_batch<T>, dim3(grid), dim3(kBThreads),
                                                 args, (size_t)smem, s);
+    ctx.last_launch_wall = std::chrono::steady_clock::now();
     cudaEventRecord(ctx.bev1, s);
     if (ctx.chain) {
       if (r == cudaSuccess) ctx.chain->last = ctx.bev1;
@@ -392,6 +397,14 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
       if (e != cudaSuccess) return from_cuda(e);
     }
     std::memcpy(h_out, h_res, out_bytes);
+    // float32 problems of a uint32 batch: keys back to float32 bits
+    if (in.is_float)
+      for (uint32_t p = 0; p < in.num_problems; ++p)
+        if (in.is_float[p])
+          for (uint32_t i = in.k_off[p]; i < in.k_off[p + 1]; ++i) {
+            uint32_t &v = reinterpret_cast<uint32_t *>(h_out)[i];
+            v ^= ((v >> 31) - 1u) | 0x80000000u;
+          }
   }
   if (kernel_ms) *kernel_ms = ms_total;
   ctx.stats.batch_calls++;

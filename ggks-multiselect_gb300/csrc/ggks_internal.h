@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <condition_variable>
 #include <cstddef>
 #include <cstdint>
@@ -78,6 +79,8 @@ struct Context {
   // after this event, read once the launch has finished
   cudaEvent_t time_base = nullptr;
   float last_launch_t0 = 0.f, last_launch_t1 = 0.f;
+  // host clock when the last batched kernel was launched
+  std::chrono::steady_clock::time_point last_launch_wall{};
 
   ggks_stats stats{};
   uint32_t profiling = 0;  // bit i: time pass i with CUDA events
@@ -135,6 +138,10 @@ struct BatchInput {
   uint32_t num_problems = 0;
   const uint32_t *k_off = nullptr;
   const uint32_t *k = nullptr;
+  // uint32 batches only, per problem (may be null): the vector holds float32
+  // values, selected in float order, whose outputs are float32 bits (host
+  // outputs only)
+  const uint8_t *is_float = nullptr;
 };
 
 // Run one batch in one cooperative launch (plus re-runs on survivor overflow

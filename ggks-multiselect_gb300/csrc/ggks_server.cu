@@ -10,8 +10,10 @@
 //              stream, and hands requests whose data is on the device to the
 //              lanes;
 //   lanes      (2 by default) each take every device-ready request (up to
-//              max_batch), run one batched selection per element type
-//              (select_batch: one persistent launch each; a type with a
+//              max_batch), run one batched selection for their float32 and
+//              uint32 requests together (32-bit keys; the float32 problems
+//              keep the float order) and one for their float64 requests
+//              (select_batch: one persistent launch each; a group of a
 //              single request takes the single-vector pipeline, whose latency
 //              is lower), scatter the results to the callers' buffers and
 //              release the requests' device bytes.  Each lane has its own
@@ -33,6 +35,7 @@
 #include <memory>
 #include <mutex>
 #include <thread>
+#include <type_traits>
 #include <unordered_map>
 #include <vector>
 
@@ -60,6 +63,8 @@ struct SReq {
 
 struct Lane {
   Context ctx;
+  Context ctx64;  // the float64 group's, while the 32-bit group runs on ctx
+  std::atomic<bool> ctx64_ready{false};
   std::thread thr;
 };
 
@@ -85,7 +90,28 @@ struct Server {
   ggks_server_stats st{};
   cudaEvent_t time_base = nullptr;                // recorded once at creation
   std::vector<std::pair<float, float>> launch_ms;  // batched launches' device intervals
+  // batch formation: when the device is expected to finish the batches handed
+  // out so far, and the device time per input byte of large batched launches
+  // (moving average; 0 until one has been measured)
+  Clock::time_point dev_free_est{};
+  double ns_per_byte = 0.0;
+  double prep_ns_per_req = 0.0;  // host time from taking a batch to its first launch, per request
+  // the device's free memory as last read, and when (admission reads it
+  // again after kFreeMemAge, or whenever a request does not fit)
+  uint64_t free_mem = 0;
+  Clock::time_point free_mem_t{};
 };
+
+constexpr auto kFreeMemAge = std::chrono::milliseconds(1);
+
+// a lane takes its batch this long, plus the measured host preparation of
+// as many requests as are ready, before the device is expected to run out of
+// queued work: time to plan and upload the batch and queue its launch
+constexpr auto kBatchLead = std::chrono::microseconds(150);
+// expected device time of a batched launch: a fixed part (its latency-bound
+// phases) and the slope measured on launches of at least kSlopeBytes
+constexpr double kLaunchFixedNs = 100e3;
+constexpr uint64_t kSlopeBytes = 64ull << 20;
 
 static size_t elem_size(int dtype) { return dtype == GGKS_DTYPE_F64 ? 8 : 4; }
 
@@ -97,12 +123,25 @@ static uint64_t charge_of(const SReq &r) {
 }
 
 // Admission budget: the cap, and no more than the device's free memory
-// (less the reserve) on top of the bytes already admitted.
-static uint64_t admit_budget(Server *S) {
-  size_t fr = 0, tot = 0;
+// (less the reserve) on top of the bytes already admitted.  The free memory
+// is read again when the last reading is older than kFreeMemAge or when
+// `fresh` (a request did not fit the budget); the bytes admitted since a
+// reading count against it through S->used.
+static uint64_t admit_budget(Server *S, bool fresh) {
+  const auto now = Clock::now();
   uint64_t hbm = S->cap;
-  if (cudaMemGetInfo(&fr, &tot) == cudaSuccess)
-    hbm = S->used + (fr > S->reserve ? (uint64_t)fr - S->reserve : 0ull);
+  if (fresh || now - S->free_mem_t > kFreeMemAge || S->free_mem_t == Clock::time_point{}) {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
+      // free memory net of what was admitted then, so that S->used adds back
+      S->free_mem = (uint64_t)fr + S->used;
+      S->free_mem_t = now;
+    } else {
+      S->free_mem_t = Clock::time_point{};
+    }
+  }
+  if (S->free_mem_t != Clock::time_point{})
+    hbm = S->free_mem > S->reserve ? S->free_mem - S->reserve : 0ull;
   const uint64_t b = std::min(S->cap, hbm);
   S->st.admit_budget_bytes = b;
   return b;
@@ -124,12 +163,12 @@ static void admit_loop(Server *S) {
     // admit in arrival order while the cap and the free memory allow; the
     // budget is taken once per round (cudaMemGetInfo), again when the head
     // does not fit it
-    uint64_t budget = admit_budget(S);
+    uint64_t budget = admit_budget(S, false);
     held = false;
     while (!S->pending.empty() && S->used + S->pending.front()->bytes <= S->cap) {
       SReq *r = S->pending.front();
       if (S->used + r->bytes > budget) {
-        budget = admit_budget(S);
+        budget = admit_budget(S, true);
         if (S->used + r->bytes > budget) {
           if (S->used == 0 && S->uploading.empty()) {
             // nothing admitted will free memory: it cannot fit
@@ -181,6 +220,22 @@ static void admit_loop(Server *S) {
   }
 }
 
+// a lone request: the single-vector pipeline has the lower latency
+template <class T>
+static void run_single(Context &ctx, SReq *r) {
+  const T *vec = static_cast<const T *>(r->host ? r->dvec : r->vec);
+  ReqSource src;
+  src.h_k = r->k.data();
+  const T *res = nullptr;
+  std::lock_guard<std::mutex> lk(ctx.mu);
+  r->status = select<T, T>(ctx, vec, r->n, src, (uint32_t)r->k.size(), nullptr, &res,
+                           ctx.stream, nullptr);
+  if (r->status == GGKS_OK) std::memcpy(r->out, res, r->k.size() * sizeof(T));
+}
+
+// One group: the float64 requests of a batch (T = double), or its float32 and
+// uint32 requests together (T = uint32_t: both have 32-bit keys, the float32
+// problems are flagged and keep the float order).
 template <class T>
 static void run_group(Server *S, Context &ctx, std::vector<SReq *> &g) {
   if (g.size() == 1) {
@@ -188,16 +243,11 @@ static void run_group(Server *S, Context &ctx, std::vector<SReq *> &g) {
       std::lock_guard<std::mutex> lk(S->mu);
       S->st.single_calls++;
     }
-    // a lone request: the single-vector pipeline has the lower latency
     SReq *r = g[0];
-    const T *vec = static_cast<const T *>(r->host ? r->dvec : r->vec);
-    ReqSource src;
-    src.h_k = r->k.data();
-    const T *res = nullptr;
-    std::lock_guard<std::mutex> lk(ctx.mu);
-    r->status = select<T, T>(ctx, vec, r->n, src, (uint32_t)r->k.size(), nullptr, &res,
-                             ctx.stream, nullptr);
-    if (r->status == GGKS_OK) std::memcpy(r->out, res, r->k.size() * sizeof(T));
+    if (r->dtype == GGKS_DTYPE_F32)
+      run_single<float>(ctx, r);
+    else
+      run_single<T>(ctx, r);
     return;
   }
   std::vector<const void *> vecs(g.size());
@@ -210,9 +260,16 @@ static void run_group(Server *S, Context &ctx, std::vector<SReq *> &g) {
     ks.insert(ks.end(), g[i]->k.begin(), g[i]->k.end());
   }
   std::vector<T> out(off.back());
+  std::vector<uint8_t> flt(g.size(), 0);
+  bool any_float = false;
+  for (size_t i = 0; i < g.size(); ++i) {
+    flt[i] = g[i]->dtype == GGKS_DTYPE_F32 ? 1 : 0;
+    any_float |= flt[i] != 0;
+  }
   BatchInput in;
   in.vecs = vecs.data();
   in.n = ns.data();
+  if (std::is_same<T, uint32_t>::value && any_float) in.is_float = flt.data();
   in.num_problems = (uint32_t)g.size();
   in.k_off = off.data();
   in.k = ks.data();
@@ -220,9 +277,26 @@ static void run_group(Server *S, Context &ctx, std::vector<SReq *> &g) {
   const BatchTune tune = ctx.pinned_tune.div ? ctx.pinned_tune : BatchTune{};
   float kms = 0.f;
   const int st = select_batch<T>(ctx, in, nullptr, out.data(), ctx.stream, tune, &kms);
+  uint64_t bytes = 0;
+  for (SReq *r : g) bytes += r->n * elem_size(r->dtype);
+  bool newest = false;  // no other lane's launch queued behind this one
+  {
+    std::lock_guard<std::mutex> lc(S->chain.mu);
+    newest = S->chain.last == ctx.bev1;
+  }
   {
     std::lock_guard<std::mutex> lk2(S->mu);
     S->st.kernel_ms += kms;
+    if (newest && S->dev_free_est > Clock::now()) {
+      // the device ran out of work sooner than expected: a lane holding its
+      // batch open takes it now
+      S->dev_free_est = Clock::now();
+      S->cv_exec.notify_all();
+    }
+    if (st == GGKS_OK && bytes >= kSlopeBytes) {
+      const double v = std::max(0.0, (double)kms * 1e6 - kLaunchFixedNs) / (double)bytes;
+      S->ns_per_byte = S->ns_per_byte == 0.0 ? v : 0.8 * S->ns_per_byte + 0.2 * v;
+    }
     if (st == GGKS_OK) S->launch_ms.emplace_back(ctx.last_launch_t0, ctx.last_launch_t1);
   }
   for (size_t i = 0; i < g.size(); ++i) {
@@ -256,12 +330,12 @@ static void complete(Server *S, cudaStream_t stream, std::vector<SReq *> &g, boo
   S->cv_admit.notify_one();
 }
 
-// runs one element type's group on a lane
+// runs one group on a context of a lane
 template <class T>
-static void run_counted(Server *S, Lane &L, std::vector<SReq *> &g) {
+static void run_counted(Server *S, Context &ctx, std::vector<SReq *> &g) {
   const auto t0 = Clock::now();
-  run_group<T>(S, L.ctx, g);
-  complete(S, L.ctx.stream, g, true);
+  run_group<T>(S, ctx, g);
+  complete(S, ctx.stream, g, true);
   std::lock_guard<std::mutex> lk(S->mu);
   S->st.group_ms += std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
 }
@@ -272,29 +346,88 @@ static void lane_loop(Server *S, Lane *L) {
   for (;;) {
     {
       std::unique_lock<std::mutex> lk(S->mu);
-      S->cv_exec.wait(lk, [&] {
-        return !S->ready.empty() ||
-               (S->stopping && S->pending.empty() && S->uploading.empty());
-      });
-      if (S->ready.empty()) {
-        S->cv_exec.notify_all();  // the other lanes stop too
-        return;
+      for (;;) {
+        S->cv_exec.wait(lk, [&] {
+          return !S->ready.empty() ||
+                 (S->stopping && S->pending.empty() && S->uploading.empty());
+        });
+        if (S->ready.empty()) {
+          S->cv_exec.notify_all();  // the other lanes stop too
+          return;
+        }
+        // Continuous batching: while the device still has queued work that
+        // lasts longer than it takes to plan and launch a batch, the batch
+        // is held open and requests arriving meanwhile join it (fewer,
+        // larger launches, each with its fixed phases); it is taken in time
+        // to keep the device fed, at once when the device is idle, full or
+        // the server is stopping.
+        const auto hold_until =
+            S->dev_free_est - kBatchLead -
+            std::chrono::nanoseconds((int64_t)(S->prep_ns_per_req * (double)S->ready.size()));
+        if (S->stopping || Clock::now() >= hold_until ||
+            (S->max_batch && S->ready.size() >= S->max_batch))
+          break;
+        S->cv_exec.wait_until(lk, hold_until);
       }
       batch.clear();
+      uint64_t bytes = 0;
       while (!S->ready.empty() && (S->max_batch == 0 || batch.size() < S->max_batch)) {
         batch.push_back(S->ready.front());
+        bytes += batch.back()->n * elem_size(batch.back()->dtype);
         S->ready.pop_front();
       }
+      // the device is expected to run this batch after the work already handed out
+      const auto start = std::max(Clock::now() + kBatchLead, S->dev_free_est);
+      if (S->ns_per_byte > 0.0)
+        S->dev_free_est =
+            start + std::chrono::nanoseconds((int64_t)(kLaunchFixedNs + S->ns_per_byte * (double)bytes));
       S->st.batches++;
       S->st.batched_requests += batch.size();
       S->st.max_batch_seen = std::max<uint64_t>(S->st.max_batch_seen, batch.size());
     }
-    std::vector<SReq *> g[3], failed;
-    for (SReq *r : batch) (r->status == GGKS_OK ? g[r->dtype] : failed).push_back(r);
+    // float32 and uint32 requests share one launch (32-bit keys); float64
+    // requests take their own
+    const auto t_take = Clock::now();
+    std::vector<SReq *> g32, g64, failed;
+    for (SReq *r : batch)
+      (r->status != GGKS_OK ? failed : r->dtype == GGKS_DTYPE_F64 ? g64 : g32).push_back(r);
     if (!failed.empty()) complete(S, L->ctx.stream, failed, false);
-    if (!g[GGKS_DTYPE_F32].empty()) run_counted<float>(S, *L, g[GGKS_DTYPE_F32]);
-    if (!g[GGKS_DTYPE_U32].empty()) run_counted<uint32_t>(S, *L, g[GGKS_DTYPE_U32]);
-    if (!g[GGKS_DTYPE_F64].empty()) run_counted<double>(S, *L, g[GGKS_DTYPE_F64]);
+    const auto launches0 = L->ctx.stats.launches;
+    // a float64 group runs at the same time on the lane's second context, so
+    // both groups' launches are queued on the device together
+    std::thread t64;
+    if (!g64.empty() && !g32.empty()) {
+      if (!L->ctx64_ready) {
+        if (context_init(L->ctx64, S->device) == GGKS_OK) {
+          L->ctx64.chain = &S->chain;
+          L->ctx64.time_base = S->time_base;
+          {
+            std::lock_guard<std::mutex> lk(L->ctx.mu);
+            L->ctx64.pinned_tune = L->ctx.pinned_tune;
+          }
+          L->ctx64_ready = true;
+        }
+      }
+      if (L->ctx64_ready) {
+        t64 = std::thread([S, L, &g64] {
+          cudaSetDevice(S->device);
+          run_counted<double>(S, L->ctx64, g64);
+        });
+      }
+    }
+    if (!g32.empty()) run_counted<uint32_t>(S, L->ctx, g32);
+    // host preparation of the first group, per request of the batch
+    if (L->ctx.stats.launches != launches0 && g32.size() > 1 && L->ctx.last_launch_wall > t_take) {
+      const double v =
+          std::chrono::duration<double, std::nano>(L->ctx.last_launch_wall - t_take).count() /
+          (double)batch.size();
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->prep_ns_per_req = S->prep_ns_per_req == 0.0 ? v : 0.8 * S->prep_ns_per_req + 0.2 * v;
+    }
+    if (t64.joinable())
+      t64.join();
+    else if (!g64.empty())
+      run_counted<double>(S, L->ctx, g64);
   }
 }
 
@@ -463,10 +596,14 @@ int ggks_server_get_stats(ggks_server *srv, ggks_server_stats *out) {
   st.recursions = 0;
   for (int ph = 0; ph < GGKS_NUM_BATCH_PHASES; ++ph) st.batch_phase_ms[ph] = 0.0;
   for (auto &L : S->lanes) {
-    std::lock_guard<std::mutex> lk(L->ctx.mu);
-    st.recursions += L->ctx.stats.recursions;
-    for (int ph = 0; ph < GGKS_NUM_BATCH_PHASES; ++ph)
-      st.batch_phase_ms[ph] += L->ctx.stats.batch_phase_ms[ph];
+    Context *cs[2] = {&L->ctx, L->ctx64_ready ? &L->ctx64 : nullptr};
+    for (Context *c : cs) {
+      if (!c) continue;
+      std::lock_guard<std::mutex> lk(c->mu);
+      st.recursions += c->stats.recursions;
+      for (int ph = 0; ph < GGKS_NUM_BATCH_PHASES; ++ph)
+        st.batch_phase_ms[ph] += c->stats.batch_phase_ms[ph];
+    }
   }
   *out = st;
   return GGKS_OK;
@@ -476,7 +613,9 @@ int ggks_server_set_tuning(ggks_server *srv, uint32_t div, uint32_t tile) {
   if (!srv) return GGKS_INVALID_ARG;
   Server *S = reinterpret_cast<Server *>(srv);
   for (auto &L : S->lanes) {
-    const int st = ggks_batch_set_tuning(reinterpret_cast<ggks_context *>(&L->ctx), div, tile);
+    int st = ggks_batch_set_tuning(reinterpret_cast<ggks_context *>(&L->ctx), div, tile);
+    if (st == GGKS_OK && L->ctx64_ready)
+      st = ggks_batch_set_tuning(reinterpret_cast<ggks_context *>(&L->ctx64), div, tile);
     if (st != GGKS_OK) return st;
   }
   return GGKS_OK;

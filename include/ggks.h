@@ -274,7 +274,8 @@ typedef struct ggks_server_stats {
   uint64_t batches;          /* batches formed */
   uint64_t batched_requests; /* requests over all batches */
   uint64_t max_batch_seen;
-  uint64_t launches;         /* batched selections run (one per element type per batch) */
+  uint64_t launches;         /* batched selections run (per batch: one for its float32 and
+                                uint32 requests together, one for its float64 ones) */
   uint64_t uploads, upload_bytes; /* host vectors copied at admission */
   uint64_t peak_bytes;       /* largest admitted device bytes */
   uint64_t in_flight_bytes;  /* admitted device bytes now */
