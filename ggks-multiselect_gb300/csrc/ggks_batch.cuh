@@ -10,7 +10,8 @@
 //
 //   1 table    queue over problems: up to kBMaxS keys sampled into shared
 //              memory, the problem's splitter table built by build_lut_cta
-//              (the single-vector builder) with 2^nsl_bits slices.
+//              (the single-vector builder) with 2^nsl_bits <= kBSlices slices;
+//              the tile phases hold it in shared memory once per bank.
 //   2 hist     queue over (problem, tile) items: a tile is a contiguous range
 //              of one problem; its shared-memory histogram becomes one row of
 //              counts (rows of a problem's tiles are consecutive).  Tiles of a
@@ -53,6 +54,15 @@
 namespace ggks {
 
 constexpr int kBThreads = 512;
+// slices of a problem's splitter table: few enough that the tile phases hold
+// the table once per bank (entry j of lane l's copy at word 32 j + l), so a
+// warp's 32 lookups take one shared-memory wavefront whatever slices its keys
+// hit (a single copy of up to 4096 slices took two to three)
+constexpr uint32_t kBSliceBits = 7;
+constexpr uint32_t kBSlices = 1u << kBSliceBits;
+constexpr uint32_t kBRepLut = (kBSlices + 1) * 32;  // words of the per-bank table
+// shared-memory words in front of the tile phases' histogram / cursors
+constexpr uint32_t kBTileLut = kBRepLut > kLutPadded ? kBRepLut : kLutPadded;
 constexpr int kBSpt = (int)kLutIdx / kBThreads;  // slices per thread in the table build
 constexpr uint32_t kBMaxNb = 8192;               // bucket budget of one problem
 constexpr uint32_t kBMaxS = 8192;                // samples of one problem (shared memory)
@@ -226,14 +236,15 @@ __device__ __forceinline__ uint32_t queue_pop(uint32_t *q, uint32_t *s_item) {
 // permutation inside every group of 32 entries.
 __device__ __forceinline__ uint32_t swz(uint32_t x) { return x ^ ((x >> 5) & 31u); }
 
-// bucket_of with the splitter table stored at swizzled positions
+// bucket_of with the splitter table held once per bank: lane_lut = table +
+// (lane index), entry j at lane_lut[32 j]
 template <class K>
-__device__ __forceinline__ uint32_t bucket_of_sw(K key, K base, uint32_t shift, const uint32_t *lut,
-                                                 uint32_t nsl) {
+__device__ __forceinline__ uint32_t bucket_of_lane(K key, K base, uint32_t shift,
+                                                   const uint32_t *lane_lut, uint32_t nsl) {
   const K d = key - base;  // wraps for key < base; that result is discarded
   const K idx = d >> shift;
   const uint32_t j = idx < (K)nsl ? (uint32_t)idx : nsl;
-  const uint32_t e = lut[swz(j)];
+  const uint32_t e = lane_lut[32 * j];
   const uint32_t b = (uint32_t)((int32_t)e >> 7) + shr_clamp(d, e & 127u);
   return key < base ? 0u : b;
 }
@@ -542,8 +553,9 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
 
   // ---------------- phase 2: one histogram row per tile
   if (tid == 0) s_cur = 0xFFFFFFFFu;  // problem whose table is in shared memory
-  uint32_t *lut = sm;
-  uint32_t *hist = sm + kLutPadded;
+  uint32_t *lut = sm;                     // the plan phase's single copy
+  const uint32_t *lane_lut = sm + (tid & 31);  // the tile phases' per-bank copies
+  uint32_t *hist = sm + kBTileLut;
   K *rep = reinterpret_cast<K *>(hist + kBMaxNb);
   K *reps = reinterpret_cast<K *>(A.reps);
   if (!(st & ST_FATAL)) {
@@ -554,7 +566,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       const BHdr H = load_hdr(A.hdrs + tl.prob);
       const uint32_t nsl = 1u << P.nsl_bits;
       if (s_cur != tl.prob)
-        for (uint32_t j = tid; j <= nsl; j += nt) lut[swz(j)] = __ldcg(A.luts + P.lut_off + j);
+        for (uint32_t w = tid; w < (nsl + 1) * 32; w += nt) sm[w] = __ldcg(A.luts + P.lut_off + (w >> 5));
       for (uint32_t b = tid; b < ((H.nb + 31) & ~31u); b += nt) {
         hist[b] = 0;
         if (H.dup) rep[b] = KeyMax<K>::v;
@@ -568,7 +580,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         // count, and keep the bucket's first key; a second distinct key (or
         // the largest key, which marks an empty entry) sets the mixed bit
         for_range_p<T>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool) {
-          const uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
+          const uint32_t ub = bucket_of_lane<K>(k, base, shift, lane_lut, nsl);
           if (!BCHECK(ub < H.nb, 2, ub, H.nb)) return;
           const uint32_t b = swz(ub);
           atomicAdd(&hist[b], 1u);
@@ -592,7 +604,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         K *cand = reinterpret_cast<K *>(A.cand) + tl.cand_off;
         const uint32_t ccap = tl.cand_cap;
         for_range_p<T>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool) {
-          const uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
+          const uint32_t ub = bucket_of_lane<K>(k, base, shift, lane_lut, nsl);
           if (BCHECK(ub < H.nb, 4, ub, H.nb)) atomicAdd(&hist[swz(ub)], 1u);
           if ((K)(k - tlo) <= span) {
             const uint32_t pos = atomicAdd(&s_ccnt, 1u);
@@ -605,7 +617,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         // different ones, so warp aggregation (compaction's) would only slow
         // this phase down
         for_range_p<T>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool) {
-          const uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
+          const uint32_t ub = bucket_of_lane<K>(k, base, shift, lane_lut, nsl);
           if (!BCHECK(ub < H.nb, 4, ub, H.nb)) return;
           atomicAdd(&hist[swz(ub)], 1u);
         });
@@ -868,7 +880,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       s_cur = 0xFFFFFFFFu;
       s_bad = false;
     }
-    uint32_t *cursor = sm + kLutPadded;
+    uint32_t *cursor = sm + kBTileLut;
     for (uint32_t t = queue_pop(&ctrl->queue[3], &s_item); t < A.num_tiles;
          t = queue_pop(&ctrl->queue[3], &s_item)) {
       const BTile tl = A.tiles[t];
@@ -876,7 +888,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
       const BHdr H = load_hdr(A.hdrs + tl.prob);
       const uint32_t nsl = 1u << P.nsl_bits;
       if (s_cur != tl.prob)
-        for (uint32_t j = tid; j <= nsl; j += nt) lut[swz(j)] = __ldcg(A.luts + P.lut_off + j);
+        for (uint32_t w = tid; w < (nsl + 1) * 32; w += nt) sm[w] = __ldcg(A.luts + P.lut_off + (w >> 5));
       for (uint32_t b = tid; b < ((H.nb + 31) & ~31u); b += nt) cursor[b] = kInactive;
       __syncthreads();
       if (tid == 0) s_cur = tl.prob;
@@ -912,7 +924,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         const K *cand = reinterpret_cast<const K *>(A.cand) + tl.cand_off;
         for (uint32_t i = tid; i < ncand; i += nt) {
           const K k = ldcg_u(cand + i);
-          const uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
+          const uint32_t ub = bucket_of_lane<K>(k, base, shift, lane_lut, nsl);
           if (!BCHECK(ub < H.nb, 9, ub, H.nb)) continue;
           const uint32_t pos = atomicAdd(&cursor[swz(ub)], 1u);
           st_global_if(sp + pos, k, pos < cap);
@@ -925,7 +937,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         // consecutive positions.  A key whose bucket fails the check (the call
         // is then failed) stays in the vote under bucket 0 but is not stored.
         for_range_p<T>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool full) {
-          uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
+          uint32_t ub = bucket_of_lane<K>(k, base, shift, lane_lut, nsl);
           const bool ok = BCHECK(ub < H.nb, 9, ub, H.nb);
           if (!ok) ub = 0;
           uint32_t pos;
@@ -944,7 +956,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         });
       } else {
         for_range_p<T>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool) {
-          uint32_t ub = bucket_of_sw<K>(k, base, shift, lut, nsl);
+          uint32_t ub = bucket_of_lane<K>(k, base, shift, lane_lut, nsl);
           if (!BCHECK(ub < H.nb, 9, ub, H.nb)) return;
           const uint32_t pos = atomicAdd(&cursor[swz(ub)], 1u);
           st_global_if(sp + pos, k, pos < cap);

@@ -29,7 +29,7 @@ static inline int batch_smem_bytes() {
   using K = typename Traits<T>::K;
   const size_t table = (size_t)kBMaxS * sizeof(K);
   const size_t plan = kLutPadded * 4 + (size_t)kBMaxNb * 5 + (size_t)kBPlanSlots * 8;
-  const size_t tiles = (kLutPadded + (size_t)kBMaxNb) * 4 + kBRepBytes;
+  const size_t tiles = (kBTileLut + (size_t)kBMaxNb) * 4 + kBRepBytes;
   const size_t fin = finish_smem_for<K>(sizeof(K) == 4 ? 4096u : 2048u);
   return (int)std::max(std::max(table, tiles), std::max(plan, fin));
 }
@@ -89,11 +89,12 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
     b.x = in.vecs[p];
     b.n = in.n[p];
     // buckets: about n / div elements each, a power of two in [4, kBMaxNb];
-    // half as many slices (the table needs nb_max >= slices + 2)
+    // half as many slices, at most kBSlices (the table needs nb_max >=
+    // slices + 2; the tile phases hold it once per bank)
     uint32_t nbm = pow2_ceil_u32((b.n + tune.div - 1) / tune.div);
     nbm = std::min(kBMaxNb, std::max(4u, nbm));
     uint32_t nsl_bits = 0;
-    while ((2u << nsl_bits) < nbm && nsl_bits < (uint32_t)kLutIdxBits) ++nsl_bits;
+    while ((2u << nsl_bits) < nbm && nsl_bits < kBSliceBits) ++nsl_bits;
     b.nb_max = nbm;
     b.nsl_bits = nsl_bits;
     b.S = (uint32_t)std::min<uint64_t>(b.n, kBMaxS);
