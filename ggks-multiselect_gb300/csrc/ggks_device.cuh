@@ -2163,7 +2163,13 @@ __host__ __device__ constexpr size_t compact_smem_bytes(uint32_t nb_max) {
 // atomic, cut the shared-memory wavefronts per warp of 32 keys from 5.3 to
 // 4.5 (atomics 4.0 -> 0.9), but the bitmap read, rank and predicated update
 // doubled the instructions per key (18.5 -> 40), and the pass became issue
-// bound: 2^27 keys took 194 us against 129 us.
+// bound: 2^27 keys took 194 us against 129 us.  A coarser gate -- per-bucket
+// cursors kept, a bitmap of 4096 bucket groups (8 buckets each) held once per
+// bank, the atomic and store only for keys of groups holding an active
+// bucket (24 % of them at 1001 spread k's) -- was slower too at 2^28: 325 us
+// branched (each key's returning atomic serialised behind its branch), 309 us
+// predicated, against 225 us; the third dependent shared-memory access per
+// key (table, gate, cursor) costs more than the conflicts it saves.
 //
 // Speculative compaction: when the histogram pass kept candidates (cand not
 // null, the table's spec on) and every segment's bucket is a kept one, CTA c's
