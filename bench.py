@@ -15,6 +15,12 @@ Metric: input GB/s per multiselect = n * sizeof(T) / time of one wrapper call
 metric through the host-vector entry point with the 1 GiB vector in pinned host
 memory, so the host-to-device copy is inside every step.
 
+"variants.reference_gpu": the reference's own kernels (built for sm_103a from
+its sources, oracle/ref_gpu.py) under a restatement of its host code, timed on
+this GPU as its timing adapter times them, on the headline input, the plain
+configuration and the float32 top-k input, beside this path's calls; their
+answers are compared with this path's.
+
 "batched": the batched workload -- 4096 resident float32 vectors of log-uniform
 lengths in [2^10, 2^22] with 1-64 k's each -- selected by one batched call (one
 persistent launch), against 4096 sequential ggks_multiselect_f32 calls on the
@@ -369,6 +375,8 @@ def run_ggks(args):
     variants = {}
     if not args.no_variants and rank == 0:
         variants = run_variants(torch, ggks, gp, ctx, stream, sptr, dev, args.log2n, parity)
+        variants["reference_gpu"] = run_reference_gpu(torch, ggks, gp, dev, x, k, ms_max,
+                                                      parity)
     batched = served = None
     if not args.no_batched and rank == 0:
         batched = run_batched(torch, ggks, gp, dev, sptr)
@@ -515,6 +523,90 @@ def run_variants(torch, ggks, gp, ctx, stream, sptr, dev, log2n, parity):
                                 "GB/s": round(x.nbytes / (ms * 1e-3) / 1e9, 1),
                                 "l2": "flushed before every call (256 MiB write, not timed)"}
     del d
+    return res
+
+
+def run_reference_gpu(torch, ggks, gp, dev, x, k, ours_ms, parity):
+    """The reference's own bucket multiselect on this GPU: its kernels
+    (bucketMultiselect.cu, compiled for sm_103a from its sources) under a
+    restatement of its host code (oracle/ref_gpu.py), on the headline input,
+    the plain configuration and the top-k configuration's float32 input.
+    Each call is timed as timeBucketMultiselect times it
+    (multiselectTimingFunctions.cu:100-122: CUDA events on the legacy stream
+    around the wrapper, its allocations and copies included), on a resident
+    vector; ``ours`` is this path's call on the same input.  The answers are
+    compared with this path's, outside the timed calls."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_gpu
+    why = ref_gpu.unavailable()
+    if why:
+        return {"unavailable": why}
+    ref_gpu.lib()
+    sms, mt = ref_gpu.device_shape()
+
+    def ref_calls(xv, kv, reps):
+        p = ref_gpu.padded_device_copy(xv)
+        ref_gpu.bucket_multiselect_device(p.data_ptr(), xv.size, kv, xv.dtype)  # warm-up
+        times, outs = [], None
+        for _ in range(reps):
+            outs, ms = ref_gpu.bucket_multiselect_device(p.data_ptr(), xv.size, kv, xv.dtype)
+            times.append(ms)
+        del p
+        torch.cuda.empty_cache()
+        return outs, statistics.median(times)
+
+    def ours_call(xv, kv, topk=None, reps=10):
+        carrier = xv.view(np.int32) if xv.dtype == np.uint32 else xv
+        d = torch.from_numpy(carrier).to(dev)
+        ctx = ggks.Context(dev.index or 0)
+
+        def f():
+            if topk:
+                return ggks.topk_ptr(d.data_ptr(), xv.size, xv.dtype, topk, ctx=ctx)
+            return ggks.multiselect_ptr(d.data_ptr(), xv.size, xv.dtype, kv, ctx=ctx)
+
+        for _ in range(3):
+            f()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        times = []
+        for _ in range(reps):
+            e0.record()
+            o = f()
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        ctx.close()
+        del d
+        return o, statistics.median(times)
+
+    res = {"kernels": "the reference's own (bucketMultiselect.cu:129-325) built for sm_103a",
+           "host": "phaseOne / generatePivots / bucketMultiselectWrapper restated "
+                   "(bucketMultiselect.cu:414-871), same launches, copies and allocations",
+           "launch_shape": {"blocks": sms, "threads": mt},
+           "timing": "CUDA events around one wrapper call on a resident vector (median); "
+                     "ours: the same around one synchronous call of this path"}
+    out, ms = ref_calls(x, k, 5)
+    ours, _ = ours_call(x, k, reps=3)
+    parity["reference_gpu_headline"] = same_bits(out, ours)
+    res["headline"] = {"n": x.size, "num_k": int(k.size), "ms": round(ms, 3),
+                       "GB/s": round(x.nbytes / (ms * 1e-3) / 1e9, 1), "ours_ms": round(ours_ms, 4),
+                       "speedup": round(ms / ours_ms, 1)}
+    xp, kp = gp.config_p()
+    out, ms = ref_calls(xp, kp, 20)
+    ours, oms = ours_call(xp, kp, reps=20)
+    parity["reference_gpu_plain_P"] = same_bits(out, ours)
+    res["plain_P_2^20_101k"] = {"ms": round(ms, 3), "ours_ms": round(oms, 4),
+                                "speedup": round(ms / oms, 1)}
+    xt = gp.config_t("f32_uniform")
+    topk = {}
+    for K in gp.T_KS:
+        out, ms = ref_calls(xt, np.arange(1, K + 1, dtype=np.uint32), 5)
+        ours, oms = ours_call(xt, None, topk=K)
+        parity[f"reference_gpu_topk_K{K}"] = same_bits(out, ours)
+        topk[str(K)] = {"ms": round(ms, 3), "ours_ms": round(oms, 4),
+                        "speedup": round(ms / oms, 1)}
+    res["topk_f32_uniform_2^26"] = topk
     return res
 
 
