@@ -293,6 +293,7 @@ static int api_multiselect(const T *vec, uint64_t n, const uint32_t *h_k, uint32
   const bool out_dev = opts && (opts->flags & GGKS_FLAG_OUT_DEVICE);
   ReqSource src;
   src.h_k = h_k;
+  src.no_small = opts && (opts->flags & GGKS_FLAG_NO_SMALL);
   const T *hres = nullptr;
   st = select<T, T>(*ctx, d_in, n, src, num_k, out_dev ? out : nullptr, out_dev ? nullptr : &hres, s,
                    ingest);
@@ -325,6 +326,7 @@ static int api_topk(const T *vec, uint64_t n, uint32_t K, T *out, const ggks_opt
   ReqSource src;
   src.topk = true;
   src.topk_pipeline = opts && (opts->flags & GGKS_FLAG_TOPK_PIPELINE);
+  src.no_small = opts && (opts->flags & (GGKS_FLAG_NO_SMALL | GGKS_FLAG_TOPK_PIPELINE));
   const T *hres = nullptr;
   st = select<T, T>(*ctx, d_in, n, src, K, out_dev ? out : nullptr, out_dev ? nullptr : &hres, s,
                    ingest);

@@ -195,6 +195,7 @@ struct Ctrl {
   uint32_t spec_on;    // the table keeps candidate buckets (k_lut)
   uint32_t spec_ctas;  // compaction CTAs that read candidates
   uint32_t cand_next;  // candidate chunks handed out (k_hist)
+  uint64_t t_ns[16];   // phase stamps of the small-vector kernel (GGKS_SMALL_TIMING builds)
 };
 
 template <class K>

@@ -115,6 +115,7 @@ struct ReqSource {
   const Req *d_reqs = nullptr;    // device requests (recursive levels)
   bool topk = false;              // ranks n-1 .. n-K into outputs 0 .. K-1
   bool topk_pipeline = false;     // a top-k that does not take the threshold path
+  bool no_small = false;          // never the one-launch small-vector path
 };
 
 // Run one selection.  Results land in d_out_user (device) or, when it is

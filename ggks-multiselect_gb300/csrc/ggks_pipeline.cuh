@@ -7,10 +7,12 @@
 #include <atomic>
 #include <type_traits>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
 #include "ggks_internal.h"
+#include "ggks_small.cuh"
 #include "ggks_topk.cuh"
 
 namespace ggks {
@@ -199,6 +201,62 @@ static cudaError_t launch(void (*kern)(P...), dim3 grid, dim3 block, size_t smem
   return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
 }
 
+// Launches k_small as one cluster of kSmCtas CTAs, plainly (no programmatic
+// serialization: it follows a copy).
+template <class... P, class... A>
+static cudaError_t launch_small(void (*kern)(P...), cudaStream_t s, A &&...args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kSmCtas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kSmCtas);
+  cfg.blockDim = dim3(kSmThreads);
+  cfg.dynamicSmemBytes = kSmBytes;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
+
+// Whether the current device can run k_small<InT, OutT> (once per device):
+// its shared memory and the cluster size (16 CTAs, a non-portable size that
+// must be allowed first) are set, and the occupancy calculator must find room
+// for one such cluster.  false: the small-vector path is not used there.
+template <class InT, class OutT>
+static bool small_ready() {
+  static std::atomic<int> state[kMaxDevices];  // 0 unknown, 1 ready, 2 unavailable
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return false;
+  const int st = state[dev].load(std::memory_order_acquire);
+  if (st) return st == 1;
+  auto kern = k_small<InT, OutT>;
+  bool ok = cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kSmBytes) == cudaSuccess &&
+            cudaFuncSetAttribute((const void *)kern,
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+  if (ok) {
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kSmCtas;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kSmCtas);
+    cfg.blockDim = dim3(kSmThreads);
+    cfg.dynamicSmemBytes = kSmBytes;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    ok = cudaOccupancyMaxActiveClusters(&clusters, (const void *)kern, &cfg) == cudaSuccess &&
+         clusters >= 1;
+  }
+  cudaGetLastError();  // a refused attribute or query leaves no error behind
+  state[dev].store(ok ? 1 : 2, std::memory_order_release);
+  return ok;
+}
+
 struct PassTimer {
   Context &ctx;
   cudaStream_t s;
@@ -354,11 +412,108 @@ static int topk_threshold(Context &ctx, const InT *d_in, uint64_t n, uint32_t K,
   return GGKS_OK;
 }
 
+// A small vector in one launch (ggks_small.cuh): host k lists or a top-k of
+// at most kSmMaxReq requests on a device vector of at most kSmMaxN
+// (kSmMaxTopkN for a top-k) elements.
+// *missed: the kernel met a case it leaves to the pipeline (nothing is
+// answered; the caller runs the pipeline, which writes every output again).
+// Arena: [slice counts | out | ctrl | requests]: the control block and the
+// requests go up in one copy, the outputs and the control block come back in
+// one.
+template <class InT, class OutT>
+static int select_small(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src,
+                        uint32_t num_req, OutT *d_out_user, const OutT **host_results,
+                        cudaStream_t s, bool *missed) {
+  using K = typename Traits<InT>::K;
+  *missed = false;
+  if (!small_ready<InT, OutT>()) {
+    *missed = true;
+    return GGKS_OK;
+  }
+  const size_t out_span = align_up((size_t)num_req * sizeof(OutT), 256);
+  const size_t o_out = kSliceCntBytes, o_ctrl = o_out + out_span, o_reqs = o_ctrl + 256;
+  const size_t o_chk = align_up(o_reqs + (size_t)num_req * sizeof(Req), 256);
+  const size_t up_bytes = 256 + (size_t)num_req * sizeof(Req);
+  cudaError_t e = ensure_arena(ctx, o_chk + (size_t)kSmNb * kSmCtas * sizeof(uint32_t));
+  if (e == cudaSuccess) e = ensure_surv(ctx, (size_t)n * sizeof(K));
+  const size_t down_off = align_up(up_bytes, 256);
+  if (e == cudaSuccess) e = ensure_pin(ctx, down_off + out_span + 256);
+  if (e != cudaSuccess) return from_cuda(e);
+  char *A = ctx.arena;
+  Ctrl *ctrl = reinterpret_cast<Ctrl *>(A + o_ctrl);
+  OutT *d_out = d_out_user ? d_out_user : reinterpret_cast<OutT *>(A + o_out);
+  char *pin_up = ctx.pin;
+  char *pin_down = ctx.pin + down_off;
+  Ctrl *h_ctrl = reinterpret_cast<Ctrl *>(pin_down + out_span);
+  // every call ends with a stream synchronisation: no earlier copy still
+  // reads the pinned buffer
+  std::memset(pin_up, 0, 256);
+  Req *hr = reinterpret_cast<Req *>(pin_up + 256);
+  for (uint32_t i = 0; i < num_req; ++i) {
+    hr[i].rank = src.topk ? (uint32_t)(n - 1 - i) : (uint32_t)(n - src.h_k[i]);
+    hr[i].out = i;
+  }
+  e = cudaMemcpyAsync(ctrl, pin_up, up_bytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return from_cuda(e);
+  {
+    PassTimer t(ctx, s, GGKS_PASS_SAMPLE);
+    e = launch_small(k_small<InT, OutT>, s, d_in, n, reinterpret_cast<const Req *>(A + o_reqs),
+                     num_req, d_out, reinterpret_cast<K *>(ctx.surv), ctx.surv_bytes / sizeof(K),
+                     reinterpret_cast<uint32_t *>(A + o_chk), ctrl);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return from_cuda(e);
+  const bool want_host = host_results != nullptr;
+  if (want_host && !d_out_user)
+    e = cudaMemcpyAsync(pin_down, A + o_out, out_span + sizeof(Ctrl), cudaMemcpyDeviceToHost, s);
+  else
+    e = cudaMemcpyAsync(h_ctrl, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && want_host && d_out_user)
+    e = cudaMemcpyAsync(pin_down, d_out, (size_t)num_req * sizeof(OutT), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return from_cuda(e);
+  bool ran[GGKS_NUM_PASSES] = {true, false, false, false, false, false};
+  collect_pass_times(ctx, ran);
+#ifdef GGKS_SMALL_TIMING
+  fprintf(stderr, "ggks small timing n=%llu req=%u:", (unsigned long long)n, num_req);
+  // stamp order: 0 start, 1 sampled, 2 table, 3 histograms, 8 totals, 9 scan,
+  // 10 barrier, 11 prefix, 12 requests, 13 cursors, 4 barrier, 5 compacted,
+  // 6 checked, 7 finished
+  static const int order[14] = {0, 1, 2, 3, 8, 9, 10, 11, 12, 13, 4, 5, 6, 7};
+  for (int i = 1; i < 14; ++i)
+    fprintf(stderr, " %.2f",
+            (double)(h_ctrl->t_ns[order[i]] - h_ctrl->t_ns[order[i - 1]]) * 1e-3);
+  fprintf(stderr, " us; first CTA start %.2f us before CTA 0, last CTA end %.2f us after\n",
+          (double)(h_ctrl->t_ns[0] - ~h_ctrl->t_ns[14]) * 1e-3,
+          (double)(h_ctrl->t_ns[15] - h_ctrl->t_ns[7]) * 1e-3);
+#endif
+  if (h_ctrl->status & ST_SMALL_MISS) {
+    *missed = true;
+    ctx.stats.small_misses++;
+    return GGKS_OK;
+  }
+  if (h_ctrl->status & ST_FATAL) return (h_ctrl->status & ST_TIMEOUT) ? GGKS_TIMEOUT : GGKS_INTERNAL;
+  ctx.stats.small_calls++;
+  if (want_host) *host_results = reinterpret_cast<const OutT *>(pin_down);
+  return GGKS_OK;
+}
+
 template <class InT, class OutT>
 int select(Context &ctx, const InT *d_in, uint64_t n, const ReqSource &src, uint32_t num_req,
            OutT *d_out_user, const OutT **host_results, cudaStream_t s, const InT *ingest) {
   using K = typename Traits<InT>::K;
   if (ctx.depth > 12) return GGKS_INTERNAL;
+  // a small device vector with host k's or a top-k: one launch, unless that
+  // kernel leaves the case to the pipeline
+  if constexpr (std::is_same<InT, OutT>::value) {
+    if (ctx.depth == 0 && !ingest && !src.no_small && (src.h_k || src.topk) && num_req >= 1 &&
+        num_req <= kSmMaxReq && n <= (src.topk ? kSmMaxTopkN : kSmMaxN)) {
+      bool missed = false;
+      const int st = select_small<InT, OutT>(ctx, d_in, n, src, num_req, d_out_user,
+                                             host_results, s, &missed);
+      if (st != GGKS_OK || !missed) return st;
+    }
+  }
   // a top-k of at most kPickMax values from a vector larger than the sample:
   // the threshold path, unless its candidates fall short
   if constexpr (std::is_same<InT, OutT>::value) {

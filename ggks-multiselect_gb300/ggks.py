@@ -25,6 +25,7 @@ OK, INVALID_ARG, OOM, CUDA_ERROR, TIMEOUT, INTERNAL, NO_DEVICE, UNSUPPORTED = ra
 FLAG_OUT_DEVICE = 1
 FLAG_AUTOTUNE = 2
 FLAG_TOPK_PIPELINE = 4
+FLAG_NO_SMALL = 8
 NUM_PASSES = 6
 PASS_NAMES = ("sample", "hist", "scan", "plan", "compact", "finish")
 NUM_BATCH_PHASES = 5
@@ -55,7 +56,8 @@ class Stats(ctypes.Structure):
                 ("batch_phase_ms", ctypes.c_double * NUM_BATCH_PHASES),
                 ("batch_grid", ctypes.c_uint64), ("spec_calls", ctypes.c_uint64),
                 ("spec_ctas", ctypes.c_uint64), ("topk_threshold_calls", ctypes.c_uint64),
-                ("topk_misses", ctypes.c_uint64), ("batch_spec_tiles", ctypes.c_uint64)]
+                ("topk_misses", ctypes.c_uint64), ("batch_spec_tiles", ctypes.c_uint64),
+                ("small_calls", ctypes.c_uint64), ("small_misses", ctypes.c_uint64)]
 
     def as_dict(self):
         return {"calls": self.calls, "launches": self.launches,
@@ -68,7 +70,8 @@ class Stats(ctypes.Structure):
                 "batch_phase_ms": dict(zip(BATCH_PHASE_NAMES, list(self.batch_phase_ms))),
                 "batch_grid": self.batch_grid, "spec_calls": self.spec_calls,
                 "spec_ctas": self.spec_ctas, "topk_threshold_calls": self.topk_threshold_calls,
-                "topk_misses": self.topk_misses, "batch_spec_tiles": self.batch_spec_tiles}
+                "topk_misses": self.topk_misses, "batch_spec_tiles": self.batch_spec_tiles,
+                "small_calls": self.small_calls, "small_misses": self.small_misses}
 
 
 DTYPE_CODES = {np.dtype(np.float32): 0, np.dtype(np.float64): 1, np.dtype(np.uint32): 2}
@@ -286,12 +289,15 @@ def set_profiling(ctx=None, on=True, passes=None):
 # ---------------------------------------------------------------------------
 
 
-def multiselect_ptr(d_ptr, n, dtype, k, ctx=None, stream=None, out=None, out_device_ptr=None):
+def multiselect_ptr(d_ptr, n, dtype, k, ctx=None, stream=None, out=None, out_device_ptr=None,
+                    small=True):
     """Multiselect of a device vector at d_ptr (n elements of dtype).
-    Returns a host array of len(k) values, or writes to out_device_ptr."""
+    Returns a host array of len(k) values, or writes to out_device_ptr.
+    small=False runs the pipeline where the one-launch small-vector path
+    (at most 2^20 elements and 1024 k's) would apply (same results)."""
     dtype = np.dtype(dtype)
     k = np.ascontiguousarray(k, dtype=np.uint32)
-    flags = 0
+    flags = 0 if small else FLAG_NO_SMALL
     if out_device_ptr is not None:
         flags |= FLAG_OUT_DEVICE
         optr = out_device_ptr
@@ -306,11 +312,13 @@ def multiselect_ptr(d_ptr, n, dtype, k, ctx=None, stream=None, out=None, out_dev
 
 
 def topk_ptr(d_ptr, n, dtype, K, ctx=None, stream=None, out=None, out_device_ptr=None,
-             pipeline=False):
+             pipeline=False, small=True):
     """The K largest of the device vector at d_ptr, descending.  pipeline=True
-    forces the histogram / compaction pipeline (same results)."""
+    forces the histogram / compaction pipeline; small=False keeps the threshold
+    path or the pipeline where the one-launch small-vector path (at most 2^18
+    elements, K <= 1024) would apply (same results)."""
     dtype = np.dtype(dtype)
-    flags = FLAG_TOPK_PIPELINE if pipeline else 0
+    flags = (FLAG_TOPK_PIPELINE if pipeline else 0) | (0 if small else FLAG_NO_SMALL)
     if out_device_ptr is not None:
         flags |= FLAG_OUT_DEVICE
         optr = out_device_ptr

@@ -25,6 +25,11 @@ CHECK_FLAGS = ["-DGGKS_BATCH_CHECKS"] if CHECKS else []
 if os.environ.get("GGKS_BATCH_TIMING") == "1":
     CHECKS = True
     CHECK_FLAGS.append("-DGGKS_BATCH_TIMING")
+# GGKS_SMALL_TIMING=1: the small-vector kernel stamps its phase boundaries
+# and the host prints them (diagnostic build, own object folder)
+if os.environ.get("GGKS_SMALL_TIMING") == "1":
+    CHECKS = True
+    CHECK_FLAGS.append("-DGGKS_SMALL_TIMING")
 if CHECKS:
     BUILD = os.path.join(HERE, "_build_" + "_".join(f[7:].lower() for f in CHECK_FLAGS))
 

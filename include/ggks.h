@@ -60,9 +60,14 @@ typedef struct ggks_opts {
 /* opts->flags: the output pointer is device memory (no device-to-host copy). */
 #define GGKS_FLAG_OUT_DEVICE 1u
 /* opts->flags for ggks_topk_*: run the histogram / compaction pipeline even
- * where the threshold path applies (K <= 4096, n > 65536, 64 K <= n); the
- * results are the same. */
+ * where the threshold path (K <= 4096, n > 65536, 64 K <= n) or the
+ * one-launch small-vector path applies; the results are the same. */
 #define GGKS_FLAG_TOPK_PIPELINE 4u
+/* opts->flags for ggks_multiselect_* / ggks_topk_*: run the pipeline even
+ * where the one-launch small-vector path applies (a device vector of at most
+ * 2^20 elements -- 2^18 for a top-k -- and at most 1024 k's); the results are
+ * the same. */
+#define GGKS_FLAG_NO_SMALL 8u
 
 /* ------------------------------------------------------------------------ */
 /* Multiselect                                                               */
@@ -342,6 +347,8 @@ typedef struct ggks_stats {
   uint64_t topk_misses;               /* threshold attempts that fell back to the pipeline */
   uint64_t batch_spec_tiles;          /* batched compaction tiles that read their candidates
                                          in place of their elements */
+  uint64_t small_calls;               /* calls answered by the one-launch small-vector path */
+  uint64_t small_misses;              /* small-vector attempts left to the pipeline */
 } ggks_stats;
 
 /* phase indices of ggks_stats.batch_phase_ms (one persistent launch; each

@@ -59,33 +59,46 @@ CASES = [
 ]
 
 
+# small: the one-launch small-vector path where it applies (at most 2^21
+# elements and 1024 k's), else the pipeline on the same inputs
+PATHS = [True, False]
+PATH_IDS = ["small", "pipeline"]
+
+
+@pytest.mark.parametrize("small", PATHS, ids=PATH_IDS)
 @pytest.mark.parametrize("dtype,dist,n", CASES, ids=[f"{a}-{b}-{c}" for a, b, c in CASES])
-def test_multiselect_vs_oracle(g, orc, dtype, dist, n):
+def test_multiselect_vs_oracle(g, orc, dtype, dist, n, small):
     import ggks_problems as gp
     x = gp.generate(dtype, dist, n, seed=n % 97)
     ks = np.concatenate([gp.k_pgrid(n, 101), gp.k_uniform_random(n, 400, 3),
                          gp.k_cluster(n, 45, 4), gp.k_sectioned(n, 64, 5), gp.k_normal(n, 50, 6)])
     d = DeviceArray(x)
-    got = g.multiselect_ptr(d.ptr, n, x.dtype, ks)
+    got = g.multiselect_ptr(d.ptr, n, x.dtype, ks, small=small)
     want = orc.multiselect(x, ks, threads=8)
     assert_same(got, want, f"{dtype}/{dist}/{n}")
 
 
+@pytest.mark.parametrize("small", PATHS, ids=PATH_IDS)
 @pytest.mark.parametrize("n", [1, 2, 3, 5, 31, 32, 33, 1023, 1024, 1025, 65535, 65536, 65537, 131073])
-def test_small_and_ragged_sizes(g, orc, n):
+def test_small_and_ragged_sizes(g, orc, n, small):
     import ggks_problems as gp
     for dtype, dist in (("f32", "normal"), ("f64", "uniform"), ("u32", "uniform16")):
         x = gp.generate(dtype, dist, n, seed=n)
+        # every k (in three calls of at most 1024 for the small path's limit)
         ks = np.arange(1, n + 1, dtype=np.uint32) if n <= 2048 else gp.k_pgrid(n, 101)
         d = DeviceArray(x)
-        assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks), orc.multiselect(x, ks),
-                    f"{dtype} n={n}")
+        want = orc.multiselect(x, ks)
+        for lo in range(0, ks.size, 1024):
+            assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks[lo:lo + 1024], small=small),
+                        want[lo:lo + 1024], f"{dtype} n={n}")
         K = min(n, 700)
-        assert_same(g.topk_ptr(d.ptr, n, x.dtype, K), orc.topk(x, K), f"topk {dtype} n={n}")
+        assert_same(g.topk_ptr(d.ptr, n, x.dtype, K, small=small), orc.topk(x, K),
+                    f"topk {dtype} n={n}")
 
 
+@pytest.mark.parametrize("small", PATHS, ids=PATH_IDS)
 @pytest.mark.parametrize("offset", [1, 2, 3])
-def test_unaligned_views(g, orc, offset):
+def test_unaligned_views(g, orc, offset, small):
     """Vectors that start off a 16-byte boundary take the scalar head path."""
     import ggks_problems as gp
     for dtype, dist in (("f32", "uniform"), ("u32", "uniform"), ("f64", "normal")):
@@ -93,8 +106,8 @@ def test_unaligned_views(g, orc, offset):
         x = gp.generate(dtype, dist, n, seed=offset)
         d = DeviceArray(x, pad_front=offset)
         ks = gp.k_pgrid(n, 101)
-        assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks), orc.multiselect(x, ks),
-                    f"{dtype} offset {offset}")
+        assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks, small=small),
+                    orc.multiselect(x, ks), f"{dtype} offset {offset}")
 
 
 TOPK = [("f32", "uniform", 1 << 22, 32), ("f32", "uniform", 1 << 22, 1024),
@@ -142,21 +155,25 @@ def test_duplicate_and_unsorted_ks(g, orc):
 
 def test_repeated_calls_one_context(g, orc):
     """Device state (per-slice sample counts at the workspace head, grid-barrier
-    counters, tickets) re-arms between calls of different shapes."""
+    counters, tickets) re-arms between calls of different shapes, with the
+    pipeline and the one-launch small-vector path taking turns."""
     import ggks_problems as gp
     ctx = g.Context(0)
-    prev = None
+    small_expected = 0
     for it, (dtype, dist, n) in enumerate([("f32", "uniform", 1 << 21), ("u32", "uniform", 5000),
                                            ("f64", "normal", 1 << 20), ("f32", "uniform", 1 << 21),
                                            ("f32", "cauchy", 123_457)] * 2):
         x = gp.generate(dtype, dist, n, seed=7)
         ks = gp.k_pgrid(n, 101)
         d = DeviceArray(x)
-        got = g.multiselect_ptr(d.ptr, n, x.dtype, ks, ctx=ctx)
+        small = it % 2 == 1
+        small_expected += small and n <= (1 << 20)
+        got = g.multiselect_ptr(d.ptr, n, x.dtype, ks, ctx=ctx, small=small)
         assert_same(got, orc.multiselect(x, ks), f"call {it}")
     st = ctx.stats()
     assert st["calls"] == 10
-    assert st["launches"] >= 60
+    assert st["small_calls"] == small_expected
+    assert st["launches"] >= 7 * (10 - small_expected) + small_expected
     ctx.close()
 
 
@@ -174,8 +191,8 @@ def test_single_key_buckets_tracked(g, orc, dtype):
     ks = gp.k_distinct(n, 1001, 5)
     d = DeviceArray(x)
     ctx = g.Context(0)
-    assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks, ctx=ctx), orc.multiselect(x, ks, 8),
-                "integer valued")
+    assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks, ctx=ctx, small=False),
+                orc.multiselect(x, ks, 8), "integer valued")
     assert ctx.stats()["survivors"] == 0
     y = x.copy()
     pick = np.nonzero(y == 200)[0][::3]
@@ -183,8 +200,11 @@ def test_single_key_buckets_tracked(g, orc, dtype):
         y[pick], dtype(300)), dtype(300)), dtype(300)), dtype(300)), dtype(300))
     d = DeviceArray(y)
     ctx.reset_stats()
+    assert_same(g.multiselect_ptr(d.ptr, n, y.dtype, ks, ctx=ctx, small=False),
+                orc.multiselect(y, ks, 8), "integer valued, one bucket with two keys")
+    # the small-vector path on the same inputs
     assert_same(g.multiselect_ptr(d.ptr, n, y.dtype, ks, ctx=ctx), orc.multiselect(y, ks, 8),
-                "integer valued, one bucket with two keys")
+                "integer valued, one bucket with two keys (small path)")
     ctx.close()
 
 
@@ -248,7 +268,7 @@ def test_oversized_segments_recurse(g, orc):
     ctx = g.Context(0)
     d = DeviceArray(base)
     ks = np.concatenate([gp.k_pgrid(n, 101), gp.k_distinct(n, 300, 1)])
-    got = g.multiselect_ptr(d.ptr, n, np.float64, ks, ctx=ctx)
+    got = g.multiselect_ptr(d.ptr, n, np.float64, ks, ctx=ctx, small=False)
     assert_same(got, orc.multiselect(base, ks, 8), "recursive f64 cluster")
     assert ctx.stats()["recursions"] > 0
     got = g.topk_ptr(d.ptr, n, np.float64, 20000, ctx=ctx)

@@ -47,6 +47,9 @@ def sampled_positions(n):
 
 
 def _topk(g, x, K, **kw):
+    """The threshold path where it applies (small=False: not the one-launch
+    small-vector path, which takes small vectors first)."""
+    kw.setdefault("small", False)
     ctx = g.Context(0)
     try:
         d = DeviceArray(x)
@@ -153,10 +156,11 @@ def test_threshold_topk_repeated_calls_one_context(g, orc):
                                        ("cauchy", 1 << 22, 1), ("normal", 1 << 21, 65536)] * 2):
         x = gp.generate("f32", dist, n, seed=it)
         d = DeviceArray(x)
-        assert_same(g.topk_ptr(d.ptr, n, x.dtype, K, ctx=ctx), orc.topk(x, K, 8), f"call {it}")
+        assert_same(g.topk_ptr(d.ptr, n, x.dtype, K, ctx=ctx, small=False), orc.topk(x, K, 8),
+                    f"call {it}")
         ks = gp.k_pgrid(n, 101)
-        assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks, ctx=ctx), orc.multiselect(x, ks, 8),
-                    f"multiselect {it}")
+        assert_same(g.multiselect_ptr(d.ptr, n, x.dtype, ks, ctx=ctx, small=False),
+                    orc.multiselect(x, ks, 8), f"multiselect {it}")
     st = ctx.stats()
     assert st["topk_threshold_calls"] == 6
     ctx.close()
