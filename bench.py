@@ -322,6 +322,11 @@ def run_ggks(args):
     st_all = ctx.stats()
     pass_ms = {p: st_all["pass_ms"][p] / max(1, st_all["pass_launches"][p]) for p in ggks.PASS_NAMES}
     dom = max(("hist", "compact"), key=lambda p: pass_ms[p])
+    # a vector small enough for the one-launch path has a single kernel
+    # (k_small), timed as the sample pass
+    small_path = st_all["small_calls"] > 0 and pass_ms[dom] == 0.0
+    if small_path:
+        dom = "sample"
     # inside the timed region CUDA events bracket the dominant pass only (an
     # event between two kernels gives up their overlapped launch); launch
     # counts cover the timed steps only
@@ -343,8 +348,9 @@ def run_ggks(args):
 
     peak, peak_kind = measured_peak()
     achieved = n * 4 / (stream_ms[dom] * 1e-3) / 1e9
-    traffic = read_traffic(dom)
-    roofline = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": round(achieved, 1),
+    traffic = read_traffic("small" if small_path else dom)
+    roofline = {"bound": "hbm", "kernel": "k_small" if small_path else f"k_{dom}",
+                "achieved": round(achieved, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind ==
                 "measured" else "fallback 6.8 TB/s",
