@@ -2351,6 +2351,50 @@ __device__ __forceinline__ K warp_bitonic32(K v) {
   return v;
 }
 
+// The r-th smallest (0-based, r < S) of keys[0, S) in shared memory, by the
+// whole CTA: MSD radix select, eight bits a round.  cnt: 256 shared words;
+// sel: 2 shared words.  Every thread returns the key.
+template <class K>
+__device__ K cta_select_rank(const K *keys, uint32_t S, uint32_t r, uint32_t *cnt, uint32_t *sel) {
+  const uint32_t tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
+  K prefix = 0, mask = 0;
+  for (int sh = 8 * (int)sizeof(K) - 8; sh >= 0; sh -= 8) {
+    for (uint32_t i = tid; i < 256; i += nt) cnt[i] = 0;
+    __syncthreads();
+    for (uint32_t i = tid; i < S; i += nt) {
+      const K k = keys[i];
+      if ((k & mask) == prefix) atomicAdd(&cnt[(uint32_t)(k >> sh) & 255u], 1u);
+    }
+    __syncthreads();
+    if (tid < 32) {
+      uint32_t c[8], sum = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        c[j] = cnt[8 * lane + j];
+        sum += c[j];
+      }
+      const uint32_t incl = warp_incl_scan(sum);
+      uint32_t acc = incl - sum;
+      if (acc <= r && r < incl) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          if (r >= acc && r < acc + c[j]) {
+            sel[0] = 8 * lane + j;
+            sel[1] = r - acc;
+          }
+          acc += c[j];
+        }
+      }
+    }
+    __syncthreads();
+    prefix |= (K)sel[0] << sh;
+    mask |= (K)255 << sh;
+    r = sel[1];
+    __syncthreads();
+  }
+  return prefix;
+}
+
 template <class K>
 __device__ __forceinline__ void bitonic_sort_smem(K *s, uint32_t P) {
   for (uint32_t k = 2; k <= P; k <<= 1) {

@@ -14,7 +14,8 @@
 //             probability (the rank of the K-th largest among S samples is
 //             about Binomial(S, 1 - K / n); six standard deviations plus four
 //             below its mean) and takes the sample key of that rank as the
-//             threshold tau;
+//             threshold tau (a radix select among the samples of the
+//             fine slice holding that rank);
 //   k_filter  streams the vector once: each key >= tau is appended to one
 //             contiguous candidate array, nothing else is written;
 //   k_pick    one CTA: a 4096-bin histogram of the candidates over their key
@@ -50,6 +51,7 @@ __global__ void __launch_bounds__(1024) k_tau(const K *__restrict__ samples, uin
   __shared__ uint32_t s_last, s_jf, s_r, s_cnt;
   __shared__ uint32_t ccnt[kLutIdx];
   __shared__ K buf[kTauBuf];
+  __shared__ uint32_t s_rcnt[256], s_rsel[2];
   const uint32_t tid = threadIdx.x;
   const uint32_t i = blockIdx.x * blockDim.x + tid;
   for (uint32_t j = tid; j < kLutIdx; j += blockDim.x) ccnt[j] = 0;
@@ -132,12 +134,9 @@ __global__ void __launch_bounds__(1024) k_tau(const K *__restrict__ samples, uin
   } else if (cnt > kTauBuf || r >= cnt) {
     t = kmin + ((K)jf << fsh);  // the fine slice's first key: a lower threshold
   } else {
-    uint32_t P = 1;
-    while (P < cnt) P <<= 1;
-    for (uint32_t q = cnt + tid; q < P; q += blockDim.x) buf[q] = KeyMax<K>::v;
-    __syncthreads();
-    bitonic_sort_smem(buf, P);
-    t = buf[r];
+    // the r-th smallest of the slice's samples by radix select (16 block
+    // barriers for 4-byte keys; a bitonic sort of up to 2048 keys took 66)
+    t = cta_select_rank<K>(buf, cnt, r, s_rcnt, s_rsel);
   }
   if (tid == 0) {
     *tau = t;
