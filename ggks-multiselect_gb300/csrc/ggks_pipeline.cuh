@@ -225,8 +225,13 @@ static cudaError_t launch_small(void (*kern)(P...), cudaStream_t s, A &&...args)
 // must be allowed first) are set, and the occupancy calculator must find room
 // for one such cluster.  false: the small-vector path is not used there.
 template <class InT, class OutT>
-static bool small_ready() {
+static std::atomic<int> *small_state() {
   static std::atomic<int> state[kMaxDevices];  // 0 unknown, 1 ready, 2 unavailable
+  return state;
+}
+template <class InT, class OutT>
+static bool small_ready() {
+  std::atomic<int> *state = small_state<InT, OutT>();
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return false;
   const int st = state[dev].load(std::memory_order_acquire);
@@ -461,7 +466,20 @@ static int select_small(Context &ctx, const InT *d_in, uint64_t n, const ReqSour
                      num_req, d_out, reinterpret_cast<K *>(ctx.surv), ctx.surv_bytes / sizeof(K),
                      reinterpret_cast<uint32_t *>(A + o_chk), ctrl);
   }
-  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    // a cluster launch the device refuses (its SMs held by other work in a
+    // way the occupancy query did not foresee): the pipeline runs instead,
+    // and this device no longer tries the small path
+    cudaGetLastError();
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < kMaxDevices)
+      small_state<InT, OutT>()[dev].store(2, std::memory_order_release);
+    e = cudaStreamSynchronize(s);  // the uploaded requests are no longer needed
+    if (e != cudaSuccess) return from_cuda(e);
+    *missed = true;
+    return GGKS_OK;
+  }
+  e = cudaGetLastError();
   if (e != cudaSuccess) return from_cuda(e);
   const bool want_host = host_results != nullptr;
   if (want_host && !d_out_user)
