@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(kSmThreads, 1)
   for_range<T>(x, a0, a1, [&](K k, bool) {
     atomicAdd(&hc[bucket_of_rep<K>(k, h.base, h.shift, lut)], 1u);
   });
-  cl.sync();  // 2: every histogram is complete
+  cl.sync();  // 1: every histogram is complete (and every CTA has started)
   GGKS_SMALL_STAMP(3);
 
   // ---------------- C: bucket totals and their global prefix
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(kSmThreads, 1)
   if (tid == 0) s_ctot = ctot;
   s_kcnt[tid] = 0;
   GGKS_SMALL_STAMP(9);
-  cl.sync();  // 3: every CTA's total is published
+  cl.sync();  // 2: every CTA's total is published
   GGKS_SMALL_STAMP(10);
   // the totals of the CTAs before this one: one remote load per lane of warp 0
   if (warp == 0) {
@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(kSmThreads, 1)
       s_slot[kSmThreads - 1u - atomicAdd(&s_nlarge, 1u)] = tid;
   }
   GGKS_SMALL_STAMP(13);
-  cl.sync();  // 4: every cursor is in place
+  cl.sync();  // 3: every cursor is in place
   GGKS_SMALL_STAMP(4);
 
   // ---------------- E: compaction of this CTA's share
@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(kSmThreads, 1)
       st_global_if(surv + pos, k, pos < cap);
     });
   }
-  cl.sync();  // 5: survivors written, cursors final
+  cl.sync();  // 4: survivors written, cursors final
   GGKS_SMALL_STAMP(5);
 
   // ---------------- F: check, then finish the requested buckets
@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(kSmThreads, 1)
       bad |= fin[c] != (c + 1 < kSmCtas ? start[c + 1] : pre + tot);
     if (bad) s_miss = true;
   }
-  cl.sync();  // 6: no shared memory of another CTA is read after this
+  cl.sync();  // 5: no shared memory of another CTA is read after this
   GGKS_SMALL_STAMP(6);
   if (!s_miss) {
     uint32_t *scratch = reinterpret_cast<uint32_t *>(smem_raw);
