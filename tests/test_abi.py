@@ -222,6 +222,19 @@ def test_python_structs_match_the_header(tmp_path):
             assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
 
 
+def test_python_flags_match_the_header():
+    """The option flags and status codes of ggks.py carry the values that
+    include/ggks.h defines."""
+    import re
+
+    import ggks
+    text = open(os.path.join(ROOT, "include", "ggks.h")).read()
+    defs = dict(re.findall(r"#define\s+GGKS_FLAG_(\w+)\s+(\d+)u", text))
+    assert {"OUT_DEVICE", "AUTOTUNE", "TOPK_PIPELINE", "NO_SMALL"} <= set(defs)
+    for name, val in defs.items():
+        assert getattr(ggks, "FLAG_" + name) == int(val), name
+
+
 def test_rank_windows_host_logic(tmp_path):
     """The host's rank windows for speculative compaction (set_windows in the
     pipeline header), built into a host program with nvcc and run without a
