@@ -698,6 +698,10 @@ def run_batched(torch, ggks, gp, dev, sptr, count=4096):
 # itself caps the served rate near 48k, so the ratio there is bounded by 50k over
 # the sequential rate; 100k, above the range, shows the server's capacity.
 SERVE_RATES = (1000, 5000, 20000, 50000, 100000)
+# requests per rate: 4000, and 12000 at the capacity point above the
+# configuration's range (with 4000, about 13 batches, one batch boundary
+# moved the measured capacity by up to 15 % between runs)
+SERVE_REQUESTS = {100000: 12000}
 
 
 def run_served(torch, ggks, gp, dev, sptr, per_rate=4000):
@@ -727,10 +731,11 @@ def run_served(torch, ggks, gp, dev, sptr, per_rate=4000):
                        "(K in [16,4096]); float32:uint32:float64 = 6:3:1 over a resident pool "
                        "of 80 vectors, lengths log-uniform in [2^12, 2^26], mixed distributions; "
                        "HBM admission cap 64 GB",
-           "requests_per_rate": per_rate, "rates": {}}
+           "requests_per_rate": {str(r): SERVE_REQUESTS.get(r, per_rate) for r in SERVE_RATES},
+           "rates": {}}
     all_exact = True
     for rate in SERVE_RATES:
-        trace = gp.serving_trace(sizes, rate, per_rate, seed=rate)
+        trace = gp.serving_trace(sizes, rate, SERVE_REQUESTS.get(rate, per_rate), seed=rate)
         bufs = []
         for q in trace:
             num = q["K"] if q["k"] is None else q["k"].size

@@ -107,7 +107,11 @@ constexpr auto kFreeMemAge = std::chrono::milliseconds(1);
 // a lane takes its batch this long, plus the measured host preparation of
 // as many requests as are ready, before the device is expected to run out of
 // queued work: time to plan and upload the batch and queue its launch
-constexpr auto kBatchLead = std::chrono::microseconds(150);
+constexpr auto kBatchLead = std::chrono::microseconds(400);
+// the device's queued work is taken as this fraction of its estimate: a batch
+// taken a little early only waits on the device, one taken late leaves the
+// device idle for its host preparation
+constexpr double kDevEstimateFactor = 0.8;
 // expected device time of a batched launch: a fixed part (its latency-bound
 // phases) and the slope measured on launches of at least kSlopeBytes
 constexpr double kLaunchFixedNs = 100e3;
@@ -380,7 +384,8 @@ static void lane_loop(Server *S, Lane *L) {
       const auto start = std::max(Clock::now() + kBatchLead, S->dev_free_est);
       if (S->ns_per_byte > 0.0)
         S->dev_free_est =
-            start + std::chrono::nanoseconds((int64_t)(kLaunchFixedNs + S->ns_per_byte * (double)bytes));
+            start + std::chrono::nanoseconds((int64_t)(kDevEstimateFactor *
+                                                       (kLaunchFixedNs + S->ns_per_byte * (double)bytes)));
       S->st.batches++;
       S->st.batched_requests += batch.size();
       S->st.max_batch_seen = std::max<uint64_t>(S->st.max_batch_seen, batch.size());
