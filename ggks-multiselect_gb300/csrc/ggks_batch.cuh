@@ -324,6 +324,162 @@ __device__ __forceinline__ void finish_warp(const K *__restrict__ src, uint32_t 
   __syncwarp();
 }
 
+// requests a warp answers by radix select (more: the segment is sorted)
+constexpr uint32_t kWarpSelReq = 4;
+constexpr uint32_t kWarpSelBins = 256;  // the select's histogram (one word per bin)
+
+// One warp answers m <= kWarpSelReq requests of a segment of size > 0 keys, all
+// in [lo, hi], by radix select instead of sorting the segment: a histogram of
+// (key - lo) in 256 bins, the bin of each requested rank, then only those
+// bins' keys gathered into buf (buf_cap keys), each bin sorted (32-key runs in
+// registers, the finish_warp merges above that), and each request read from
+// its bin.  hist: kWarpSelBins + kWarpSelReq shared words of this warp.
+// Returns false, having written nothing, when the needed bins do not fit buf
+// (keys spread unevenly over the bucket's range); the caller then sorts the
+// segment.  Every index into the per-request arrays is a compile-time one.
+template <class K, class OutT>
+__device__ __forceinline__ bool finish_warp_select(const K *__restrict__ src, uint32_t size, K lo,
+                                                   K hi, const Req *__restrict__ rq, uint32_t m,
+                                                   K *buf, uint32_t buf_cap, uint32_t *hist,
+                                                   OutT *__restrict__ out) {
+  const uint32_t lane = threadIdx.x & 31;
+  if (size >= 65536u) return false;  // ranks inside a bin travel in 16 bits
+  const int bl = bitlen<K>(hi - lo);
+  const uint32_t sh = bl > 8 ? (uint32_t)(bl - 8) : 0u;  // (hi - lo) >> sh < 256
+  auto bin_of = [&](K k) -> uint32_t {
+    const uint32_t b = (uint32_t)((K)(k - lo) >> sh);
+    return b < kWarpSelBins ? b : kWarpSelBins - 1u;  // keys lie in [lo, hi]: never clamped
+  };
+#pragma unroll
+  for (uint32_t q = 0; q < kWarpSelBins / 32; ++q) hist[q * 32 + lane] = 0;
+  __syncwarp();
+  for (uint32_t i = lane; i < size; i += 32) atomicAdd(&hist[bin_of(src[i])], 1u);
+  __syncwarp();
+  // exclusive prefix of the bins, lane l holding bins 8 l .. 8 l + 7
+  uint32_t c[8], sum = 0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    c[q] = hist[8 * lane + q];
+    sum += c[q];
+  }
+  const uint32_t run = warp_incl_scan(sum) - sum;
+  // each request's bin and rank inside it; its region of buf (a request
+  // whose bin an earlier request also needs shares that one's region)
+  uint32_t rb[kWarpSelReq], rr[kWarpSelReq], roff[kWarpSelReq], rcnt[kWarpSelReq],
+      rP[kWarpSelReq];
+  bool own[kWarpSelReq];
+  bool ok = true;
+  uint32_t used = 0;
+#pragma unroll
+  for (uint32_t j = 0; j < kWarpSelReq; ++j) {
+    rb[j] = 0xFFFFFFFFu;
+    rr[j] = 0;
+    roff[j] = 0;
+    rcnt[j] = 0;
+    rP[j] = 0;
+    own[j] = false;
+    if (j >= m) continue;
+    const uint32_t r = rq[j].rank;
+    uint32_t acc = run, hit = 0, at = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (c[q] && acc <= r && r < acc + c[q]) {
+        hit = 1;
+        at = ((8 * lane + q) << 16) | (r - acc);  // bin, rank inside it (< 2^16)
+      }
+      acc += c[q];
+    }
+    const uint32_t who = __ballot_sync(0xffffffffu, hit);
+    if (who == 0) {
+      ok = false;  // a rank outside the segment: leave it to the sort
+      continue;
+    }
+    at = __shfl_sync(0xffffffffu, at, __ffs(who) - 1);
+    rb[j] = at >> 16;
+    rr[j] = at & 0xFFFFu;
+    own[j] = true;
+#pragma unroll
+    for (uint32_t t = 0; t < j; ++t)
+      if (rb[t] == rb[j]) {
+        own[j] = false;
+        roff[j] = roff[t];
+      }
+    if (own[j]) {
+      rcnt[j] = hist[rb[j]];
+      uint32_t P = 32;
+      while (P < rcnt[j]) P <<= 1;
+      rP[j] = P;
+      roff[j] = used;
+      used += P;
+    }
+  }
+  if (!ok || used > buf_cap) return false;
+  // gather the needed bins' keys (per-bin counters after the histogram)
+  uint32_t *cur = hist + kWarpSelBins;
+  if (lane < kWarpSelReq) cur[lane] = 0;
+  __syncwarp();
+  for (uint32_t i0 = 0; i0 < size; i0 += 32) {
+    const uint32_t i = i0 + lane;
+    const K k = i < size ? src[i] : K(0);
+    const uint32_t b = i < size ? bin_of(k) : 0xFFFFFFFFu;
+#pragma unroll
+    for (uint32_t t = 0; t < kWarpSelReq; ++t) {
+      if (!own[t]) continue;
+      const bool mine = b == rb[t];
+      const uint32_t mm = __ballot_sync(0xffffffffu, mine);
+      if (mm == 0) continue;
+      const int leader = __ffs(mm) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(&cur[t], (uint32_t)__popc(mm));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (mine) buf[roff[t] + base + __popc(mm & ((1u << lane) - 1u))] = k;
+    }
+  }
+  __syncwarp();
+  // sort each needed bin in its region (the padding sorts last)
+#pragma unroll
+  for (uint32_t t = 0; t < kWarpSelReq; ++t) {
+    if (!own[t]) continue;
+    K *s = buf + roff[t];
+    const uint32_t P = rP[t];
+    for (uint32_t c0 = 0; c0 < P; c0 += 32) {
+      const K v = c0 + lane < rcnt[t] ? s[c0 + lane] : KeyMax<K>::v;
+      s[c0 + lane] = warp_bitonic32(v);
+    }
+    __syncwarp();
+    for (uint32_t k = 64; k <= P; k <<= 1) {
+      const uint32_t half = k >> 1;
+      for (uint32_t x = lane; x < (P >> 1); x += 32) {
+        const uint32_t a = ((x & ~(half - 1)) << 1) | (x & (half - 1));
+        const uint32_t b = a ^ (k - 1);
+        const K u = s[a], v = s[b];
+        if (u > v) {
+          s[a] = v;
+          s[b] = u;
+        }
+      }
+      __syncwarp();
+      for (uint32_t j = k >> 2; j > 0; j >>= 1) {
+        for (uint32_t x = lane; x < (P >> 1); x += 32) {
+          const uint32_t a = ((x & ~(j - 1)) << 1) | (x & (j - 1)), b = a + j;
+          const K u = s[a], v = s[b];
+          if (u > v) {
+            s[a] = v;
+            s[b] = u;
+          }
+        }
+        __syncwarp();
+      }
+    }
+  }
+  // answers: lane j answers request j
+#pragma unroll
+  for (uint32_t j = 0; j < kWarpSelReq; ++j)
+    if (j < m && lane == j) out[rq[j].out] = Traits<OutT>::value(buf[roff[j] + rr[j]]);
+  __syncwarp();
+  return true;
+}
+
 // Elements [a, b) of x (any alignment): scalar head up to a 16-byte boundary,
 // a 128-bit body with four vectors in flight per thread, a scalar tail.
 // f(key, full) is called once per element; full: all 32 lanes of the warp
@@ -973,6 +1129,9 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
     // barrier, so no thread of this CTA still uses the shared memory)
     const uint32_t lane = tid & 31;
     K *wbuf = reinterpret_cast<K *>(sm) + (size_t)(tid >> 5) * warp_cap<K>();
+    // the select's histogram, after every warp's buffer
+    uint32_t *whist = sm + (size_t)(nt / 32) * (kBWarpBytes / 4) +
+                      (size_t)(tid >> 5) * (kWarpSelBins + kWarpSelReq);
     while (true) {
       uint32_t i = 0;
       if (lane == 0) i = atomicAdd(&ctrl->small_pop, 1u);
@@ -998,8 +1157,15 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         }
       }
 #endif
-      finish_warp<K, OutT>(surv + ldcg_u(A.seg_off + g), __ldcg(A.seg_size + g), ldcg_u(seg_lo + g),
-                           A.klist + __ldcg(A.kstart + g), __ldcg(A.kcnt + g), wbuf, out);
+      // one to kWarpSelReq requests: radix select; more (a top-k's bucket),
+      // or needed bins that do not fit: the segment is sorted
+      const uint32_t sz = __ldcg(A.seg_size + g), kc = __ldcg(A.kcnt + g);
+      const Req *rq = A.klist + __ldcg(A.kstart + g);
+      const K *src = surv + ldcg_u(A.seg_off + g);
+      if (sz == 0 || kc > kWarpSelReq ||
+          !finish_warp_select<K, OutT>(src, sz, ldcg_u(seg_lo + g), ldcg_u(seg_hi + g), rq, kc,
+                                       wbuf, warp_cap<K>(), whist, out))
+        finish_warp<K, OutT>(src, sz, ldcg_u(seg_lo + g), rq, kc, wbuf, out);
     }
   }
   __syncthreads();

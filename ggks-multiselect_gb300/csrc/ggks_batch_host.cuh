@@ -30,7 +30,9 @@ static inline int batch_smem_bytes() {
   const size_t table = (size_t)kBMaxS * sizeof(K);
   const size_t plan = kLutPadded * 4 + (size_t)kBMaxNb * 5 + (size_t)kBPlanSlots * 8;
   const size_t tiles = (kBTileLut + (size_t)kBMaxNb) * 4 + kBRepBytes;
-  const size_t fin = finish_smem_for<K>(sizeof(K) == 4 ? 4096u : 2048u);
+  const size_t fin = std::max(finish_smem_for<K>(sizeof(K) == 4 ? 4096u : 2048u),
+                              (size_t)(kBThreads / 32) *
+                                  (kBWarpBytes + (kWarpSelBins + kWarpSelReq) * 4));
   return (int)std::max(std::max(table, tiles), std::max(plan, fin));
 }
 

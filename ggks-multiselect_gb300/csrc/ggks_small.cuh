@@ -29,7 +29,8 @@
 //      bucket's cursor (inactive cursors carry bit 31), a predicated store.
 //   F  the owners check that every CTA's cursor reached its end, then finish
 //      their requested buckets: a warp per bucket of at most small_warp_cap
-//      keys (finish_warp); the whole CTA for larger ones: a bitonic sort of
+//      keys (finish_warp_select for up to four requests, else finish_warp);
+//      the whole CTA for larger ones: a bitonic sort of
 //      the segment in shared memory up to small_sort_cap keys, finish_slot
 //      beyond.
 //
@@ -106,7 +107,8 @@ constexpr uint32_t kSmWarpBytes = 1024;
 static_assert(kSmHcOff % 16 == 0, "bucket words' alignment");
 static_assert((size_t)small_samples<uint32_t>() * 4 <= kSmBytes - kSmHcOff, "samples fit");
 static_assert((size_t)small_samples<uint64_t>() * 8 <= kSmBytes - kSmHcOff, "samples fit");
-static_assert(kSmThreads / 32 * kSmWarpBytes <= kSmBytes, "warp finishers' buffers fit");
+static_assert(kSmThreads / 32 * (kSmWarpBytes + (kWarpSelBins + kWarpSelReq) * 4) <= kSmBytes,
+              "warp finishers' buffers and histograms fit");
 static_assert(small_samples<uint64_t>() % (2 * kSmThreads) == 0, "whole pairs per thread");
 
 // segments of at most this many keys are finished by one warp
@@ -427,12 +429,19 @@ __global__ void __launch_bounds__(kSmThreads, 1)
     }
     __syncthreads();
     K *wbuf = reinterpret_cast<K *>(scratch) + (size_t)warp * small_warp_cap<K>();
+    uint32_t *whist = scratch + (size_t)(kSmThreads / 32) * (kSmWarpBytes / 4) +
+                      (size_t)warp * (kWarpSelBins + kWarpSelReq);
     for (uint32_t i = warp; i < nsmall; i += kSmThreads / 32) {
       const uint32_t t = s_slot[i];
       K lo, hi;
       range(r * kSmThreads + t, &lo, &hi);
-      finish_warp<K, OutT>(surv + s_pre[t], size_of(t), lo, s_klist + s_kstart[t], s_kcnt[t],
-                           wbuf, out);
+      const uint32_t size = size_of(t), m = s_kcnt[t];
+      const Req *rq = s_klist + s_kstart[t];
+      // up to kWarpSelReq requests: radix select, else (or when the needed
+      // bins do not fit) the segment is sorted
+      if (m > kWarpSelReq || !finish_warp_select<K, OutT>(surv + s_pre[t], size, lo, hi, rq, m,
+                                                           wbuf, small_warp_cap<K>(), whist, out))
+        finish_warp<K, OutT>(surv + s_pre[t], size, lo, rq, m, wbuf, out);
     }
   }
   __syncthreads();
