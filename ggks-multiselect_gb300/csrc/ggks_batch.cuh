@@ -37,8 +37,14 @@
 // list overflowed its area, or a problem whose slots fall outside, reads the
 // elements as before: correctness never rests on the sample.
 //   5 finish   queue over the large slots: finish_slot (the single-vector
-//              finisher), a whole CTA each; then a queue over the small slots
-//              (at most warp_cap keys, the common case), one warp each.
+//              finisher), a whole CTA each; then a warp queue over the
+//              mid-size slots with at most kWarpSelReq requests (radix select
+//              by one warp), then a warp queue over the small slots (at most
+//              warp_cap keys, the common case); after one more grid barrier,
+//              a CTA queue over the mid-size slots whose needed bins did not
+//              fit a warp's buffer.  A batch with fewer than kWselPerCta
+//              mid-size slots per CTA puts them in the first CTA queue
+//              instead, and skips that barrier.
 //
 // A grid-wide barrier with a bounded wait separates the phases; the grid is
 // launched cooperatively (all CTAs co-resident).  No CTA leaves early: a CTA
@@ -123,6 +129,8 @@ struct BCtrl {
   uint32_t deferred_count;
   uint32_t n_big, n_small;  // slots finished by a whole CTA / by one warp
   uint32_t small_pop;       // warp queue of the small slots
+  uint32_t n_wsel, wsel_pop;  // mid-size slots a warp selects in, and their queue
+  uint32_t n_retry, retry_pop;  // mid-size slots left to a whole CTA, and their queue
   uint32_t spec_tiles;      // compaction tiles that read their candidates
   uint64_t surv_top;    // survivor bump allocator
   uint64_t cap_needed;  // survivors wanted when they did not fit
@@ -151,7 +159,8 @@ struct BArgs {
   uint64_t *seg_off;
   void *seg_lo, *seg_hi;  // key arrays
   Req *klist;
-  uint32_t *big_list, *small_list;  // slot indices by finisher kind
+  uint32_t *big_list, *small_list, *wsel_list;  // slot indices by finisher kind
+  uint32_t *retry_list;  // mid-size slots whose warp select did not fit
   void *surv;             // key array
   uint32_t *deferred;
   void *out;              // output values
@@ -214,7 +223,7 @@ __device__ __forceinline__ uint32_t grid_barrier(BCtrl *c, uint32_t *s_status, i
       }
     }
     __threadfence();
-    if (blockIdx.x == 0) c->t_ns[phase] = global_ns();
+    if (blockIdx.x == 0 && phase >= 0) c->t_ns[phase] = global_ns();
     *s_status = ld_acquire_u32(&c->status);
   }
   __syncthreads();
@@ -327,6 +336,14 @@ __device__ __forceinline__ void finish_warp(const K *__restrict__ src, uint32_t 
 // requests a warp answers by radix select (more: the segment is sorted)
 constexpr uint32_t kWarpSelReq = 4;
 constexpr uint32_t kWarpSelBins = 256;  // the select's histogram (one word per bin)
+// Segments above warp_cap keys and up to this many, with at most kWarpSelReq
+// requests, are selected by one warp (two passes of size / 32 loads per lane)
+// instead of a whole CTA; larger ones keep the CTA.
+constexpr uint32_t kWarpSelMax = 16384;
+// A warp takes about ten times a CTA's time on such a segment, so warps take
+// them only when a batch has at least this many per CTA of the grid (a CTA
+// queue of fewer ends sooner); otherwise they join the CTA queue.
+constexpr uint32_t kWselPerCta = 16;
 
 // One warp answers m <= kWarpSelReq requests of a segment of size > 0 keys, all
 // in [lo, hi], by radix select instead of sorting the segment: a histogram of
@@ -353,7 +370,19 @@ __device__ __forceinline__ bool finish_warp_select(const K *__restrict__ src, ui
 #pragma unroll
   for (uint32_t q = 0; q < kWarpSelBins / 32; ++q) hist[q * 32 + lane] = 0;
   __syncwarp();
-  for (uint32_t i = lane; i < size; i += 32) atomicAdd(&hist[bin_of(src[i])], 1u);
+  // U loads in flight per lane in both passes over the segment
+  constexpr uint32_t U = sizeof(K) == 4 ? 8u : 4u;
+  for (uint32_t i0 = 0; i0 < size; i0 += 32 * U) {
+    K v[U];
+#pragma unroll
+    for (uint32_t u = 0; u < U; ++u) {
+      const uint32_t i = i0 + 32 * u + lane;
+      v[u] = i < size ? src[i] : K(0);
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < U; ++u)
+      if (i0 + 32 * u + lane < size) atomicAdd(&hist[bin_of(v[u])], 1u);
+  }
   __syncwarp();
   // exclusive prefix of the bins, lane l holding bins 8 l .. 8 l + 7
   uint32_t c[8], sum = 0;
@@ -413,26 +442,46 @@ __device__ __forceinline__ bool finish_warp_select(const K *__restrict__ src, ui
       used += P;
     }
   }
-  if (!ok || used > buf_cap) return false;
+  if (!ok) return false;
+  if (sh == 0) {
+    // bins one key wide (the bucket spans under 256 keys): each request's
+    // key is its bin's, however many copies the bin holds
+#pragma unroll
+    for (uint32_t j = 0; j < kWarpSelReq; ++j)
+      if (j < m && lane == j) out[rq[j].out] = Traits<OutT>::value((K)(lo + (K)rb[j]));
+    __syncwarp();
+    return true;
+  }
+  if (used > buf_cap) return false;
   // gather the needed bins' keys (per-bin counters after the histogram)
   uint32_t *cur = hist + kWarpSelBins;
   if (lane < kWarpSelReq) cur[lane] = 0;
   __syncwarp();
-  for (uint32_t i0 = 0; i0 < size; i0 += 32) {
-    const uint32_t i = i0 + lane;
-    const K k = i < size ? src[i] : K(0);
-    const uint32_t b = i < size ? bin_of(k) : 0xFFFFFFFFu;
+  for (uint32_t i0 = 0; i0 < size; i0 += 32 * U) {
+    K v[U];
 #pragma unroll
-    for (uint32_t t = 0; t < kWarpSelReq; ++t) {
-      if (!own[t]) continue;
-      const bool mine = b == rb[t];
-      const uint32_t mm = __ballot_sync(0xffffffffu, mine);
-      if (mm == 0) continue;
-      const int leader = __ffs(mm) - 1;
-      uint32_t base = 0;
-      if ((int)lane == leader) base = atomicAdd(&cur[t], (uint32_t)__popc(mm));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (mine) buf[roff[t] + base + __popc(mm & ((1u << lane) - 1u))] = k;
+    for (uint32_t u = 0; u < U; ++u) {
+      const uint32_t i = i0 + 32 * u + lane;
+      v[u] = i < size ? src[i] : K(0);
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < U; ++u) {
+      if (i0 + 32 * u >= size) break;  // the same for every lane
+      const uint32_t i = i0 + 32 * u + lane;
+      const K k = v[u];
+      const uint32_t b = i < size ? bin_of(k) : 0xFFFFFFFFu;
+#pragma unroll
+      for (uint32_t t = 0; t < kWarpSelReq; ++t) {
+        if (!own[t]) continue;
+        const bool mine = b == rb[t];
+        const uint32_t mm = __ballot_sync(0xffffffffu, mine);
+        if (mm == 0) continue;
+        const int leader = __ffs(mm) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(&cur[t], (uint32_t)__popc(mm));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (mine) buf[roff[t] + base + __popc(mm & ((1u << lane) - 1u))] = k;
+      }
     }
   }
   __syncwarp();
@@ -557,7 +606,7 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
   __shared__ uint32_t red32[33];
   __shared__ uint64_t red64[33];
   __shared__ uint64_t s_base;
-  __shared__ uint32_t s_lb[2];
+  __shared__ uint32_t s_lb[3];
   __shared__ LutHeader<K> s_hdr;
   __shared__ bool s_bad;
   __shared__ uint32_t s_rcnt[256], s_rsel[2], s_ccnt;
@@ -914,31 +963,6 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         A.seg_off[g] = off;
         off += __ldcg(A.seg_size + g);
       }
-      // finisher lists: small segments go to one warp each, the others to a
-      // whole CTA each
-      {
-        uint32_t my_small = 0;
-        for (uint32_t q = s0; q < s1; ++q)
-          my_small += __ldcg(A.seg_size + P.req_off + q) <= warp_cap<K>() ? 1u : 0u;
-        const uint32_t my_big = (s1 - s0) - my_small;
-        uint32_t tot_small, tot_big;
-        uint32_t rs = block_incl_scan(my_small, &tot_small, red32) - my_small;
-        uint32_t rb = block_incl_scan(my_big, &tot_big, red32) - my_big;
-        if (tid == 0) {
-          s_lb[0] = atomicAdd(&ctrl->n_small, tot_small);
-          s_lb[1] = atomicAdd(&ctrl->n_big, tot_big);
-        }
-        __syncthreads();
-        rs += s_lb[0];
-        rb += s_lb[1];
-        for (uint32_t q = s0; q < s1; ++q) {
-          const uint32_t g = P.req_off + q;
-          if (__ldcg(A.seg_size + g) <= warp_cap<K>())
-            A.small_list[rs++] = g;
-          else
-            A.big_list[rb++] = g;
-        }
-      }
       __syncthreads();
       // per-slot request counters: in the shared memory after the flags when
       // the slots fit (a top-k puts thousands of requests in a few slots),
@@ -968,6 +992,44 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
           if (in_smem) A.kcnt[P.req_off + q] = c;  // the finisher reads the counts
           A.kstart[P.req_off + q] = r2;
           r2 += c;
+        }
+      }
+      // finisher lists: small segments go to one warp each; mid-size ones
+      // with few requests to one warp's radix select; the others to a whole
+      // CTA each
+      {
+        auto kind = [&](uint32_t q) -> uint32_t {  // 0 small, 1 warp select, 2 CTA
+          const uint32_t sz = __ldcg(A.seg_size + P.req_off + q);
+          if (sz <= warp_cap<K>()) return 0u;
+          const uint32_t c = in_smem ? s_cnt[q] : __ldcg(A.kcnt + P.req_off + q);
+          return sz <= kWarpSelMax && c <= kWarpSelReq ? 1u : 2u;
+        };
+        uint32_t my[3] = {0, 0, 0};
+        for (uint32_t q = s0; q < s1; ++q) {
+          const uint32_t t = kind(q);
+          my[0] += t == 0u;
+          my[1] += t == 1u;
+          my[2] += t == 2u;
+        }
+        uint32_t tot[3], at[3];
+#pragma unroll
+        for (int t = 0; t < 3; ++t) at[t] = block_incl_scan(my[t], &tot[t], red32) - my[t];
+        if (tid == 0) {
+          s_lb[0] = atomicAdd(&ctrl->n_small, tot[0]);
+          s_lb[1] = atomicAdd(&ctrl->n_wsel, tot[1]);
+          s_lb[2] = atomicAdd(&ctrl->n_big, tot[2]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int t = 0; t < 3; ++t) at[t] += s_lb[t];
+        for (uint32_t q = s0; q < s1; ++q) {
+          const uint32_t g = P.req_off + q, t = kind(q);
+          if (t == 0u)
+            A.small_list[at[0]++] = g;
+          else if (t == 1u)
+            A.wsel_list[at[1]++] = g;
+          else
+            A.big_list[at[2]++] = g;
         }
       }
       __syncthreads();
@@ -1089,12 +1151,34 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
   st = grid_barrier(ctrl, &s_status, 4);
 
   // ---------------- phase 5: finish every slot
+  // one slot by the whole CTA; a slot whose needed bins exceed the shared
+  // memory goes to the host's recursion
+  auto cta_finish = [&](uint32_t g) {
+    // one vector per thread and chunk: the kernel's other phases already
+    // hold its register budget
+    const bool done = finish_slot<K, OutT, 1>(
+        surv + ldcg_u(A.seg_off + g), __ldcg(A.seg_size + g), ldcg_u(seg_lo + g), ldcg_u(seg_hi + g),
+        A.klist + __ldcg(A.kstart + g), __ldcg(A.kcnt + g), A.bcap, sm, out);
+    if (!done && tid == 0) {
+      const uint32_t d = atomicAdd(&ctrl->deferred_count, 1u);
+      A.deferred[d] = g;
+      atomicOr(&ctrl->status, ST_DEFERRED);
+    }
+  };
+  // mid-size slots by warps or, when the batch has few, by CTAs after the
+  // large ones.  The count is final since phase 3 and every CTA reads it,
+  // whatever the status: one choice for the grid, and so for the barrier
+  // that only the warps' fallback needs.
+  const uint32_t n_wsel_all = __ldcg(&ctrl->n_wsel);
+  const bool wsel_warps = n_wsel_all >= kWselPerCta * gridDim.x;
   if (!(st & (ST_FATAL | ST_OVERFLOW))) {
     const uint32_t n_big = __ldcg(&ctrl->n_big), n_small = __ldcg(&ctrl->n_small);
+    const uint32_t n_wsel = wsel_warps ? n_wsel_all : 0u;
+    const uint32_t n_cta = n_big + (wsel_warps ? 0u : n_wsel_all);
     // large segments first, a whole CTA each
-    for (uint32_t i = queue_pop(&ctrl->queue[4], &s_item); i < n_big;
+    for (uint32_t i = queue_pop(&ctrl->queue[4], &s_item); i < n_cta;
          i = queue_pop(&ctrl->queue[4], &s_item)) {
-      const uint32_t g = __ldcg(A.big_list + i);
+      const uint32_t g = i < n_big ? __ldcg(A.big_list + i) : __ldcg(A.wsel_list + (i - n_big));
       if (!BCHECK(i < A.num_req && g < A.num_req &&
                       ldcg_u(A.seg_off + g) + __ldcg(A.seg_size + g) <= A.surv_cap &&
                       __ldcg(A.kstart + g) + __ldcg(A.kcnt + g) <= A.num_req,
@@ -1114,24 +1198,51 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         }
       }
 #endif
-      // one vector per thread and chunk: the kernel's other phases already
-      // hold its register budget
-      const bool done = finish_slot<K, OutT, 1>(
-          surv + ldcg_u(A.seg_off + g), __ldcg(A.seg_size + g), ldcg_u(seg_lo + g), ldcg_u(seg_hi + g),
-          A.klist + __ldcg(A.kstart + g), __ldcg(A.kcnt + g), A.bcap, sm, out);
-      if (!done && tid == 0) {
-        const uint32_t d = atomicAdd(&ctrl->deferred_count, 1u);
-        A.deferred[d] = g;
-        atomicOr(&ctrl->status, ST_DEFERRED);
-      }
+      cta_finish(g);
     }
-    // then the small ones, one warp each (the queue pop above ended with a
-    // barrier, so no thread of this CTA still uses the shared memory)
+    // then the mid-size and the small ones, one warp each (the queue pop
+    // above ended with a barrier, so no thread of this CTA still uses the
+    // shared memory)
     const uint32_t lane = tid & 31;
     K *wbuf = reinterpret_cast<K *>(sm) + (size_t)(tid >> 5) * warp_cap<K>();
     // the select's histogram, after every warp's buffer
     uint32_t *whist = sm + (size_t)(nt / 32) * (kBWarpBytes / 4) +
                       (size_t)(tid >> 5) * (kWarpSelBins + kWarpSelReq);
+    // mid-size slots (the longer warp jobs) first: radix select, or to the
+    // CTA queue after the next barrier when the needed bins do not fit the
+    // warp's buffer
+    while (true) {
+      uint32_t i = 0;
+      if (lane == 0) i = atomicAdd(&ctrl->wsel_pop, 1u);
+      i = __shfl_sync(0xffffffffu, i, 0);
+      if (i >= n_wsel) break;
+      const uint32_t g = __ldcg(A.wsel_list + i);
+      if (!BCHECK(i < A.num_req && g < A.num_req && __ldcg(A.seg_size + g) > warp_cap<K>() &&
+                      __ldcg(A.seg_size + g) <= kWarpSelMax && __ldcg(A.kcnt + g) <= kWarpSelReq &&
+                      ldcg_u(A.seg_off + g) + __ldcg(A.seg_size + g) <= A.surv_cap &&
+                      __ldcg(A.kstart + g) + __ldcg(A.kcnt + g) <= A.num_req,
+                  15, i, g))
+        continue;
+#ifdef GGKS_BATCH_CHECKS
+      {
+        bool bad = false;
+        const uint32_t sz = __ldcg(A.seg_size + g), ks = __ldcg(A.kstart + g);
+        for (uint32_t j = lane; j < __ldcg(A.kcnt + g); j += 32) {
+          const Req e = A.klist[ks + j];
+          if (e.out >= A.num_req || e.rank >= sz) bad = true;
+        }
+        if (__any_sync(0xffffffffu, bad)) {
+          if (lane == 0) BCHECK(false, 16, g, sz);
+          continue;
+        }
+      }
+#endif
+      const bool done = finish_warp_select<K, OutT>(
+          surv + ldcg_u(A.seg_off + g), __ldcg(A.seg_size + g), ldcg_u(seg_lo + g),
+          ldcg_u(seg_hi + g), A.klist + __ldcg(A.kstart + g), __ldcg(A.kcnt + g), wbuf,
+          warp_cap<K>(), whist, out);
+      if (!done && lane == 0) A.retry_list[atomicAdd(&ctrl->n_retry, 1u)] = g;
+    }
     while (true) {
       uint32_t i = 0;
       if (lane == 0) i = atomicAdd(&ctrl->small_pop, 1u);
@@ -1166,6 +1277,19 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
           !finish_warp_select<K, OutT>(src, sz, ldcg_u(seg_lo + g), ldcg_u(seg_hi + g), rq, kc,
                                        wbuf, warp_cap<K>(), whist, out))
         finish_warp<K, OutT>(src, sz, ldcg_u(seg_lo + g), rq, kc, wbuf, out);
+    }
+  }
+  // the mid-size slots no warp could answer, a whole CTA each
+  if (wsel_warps) {
+    st = grid_barrier(ctrl, &s_status, -1);
+    if (!(st & (ST_FATAL | ST_OVERFLOW))) {
+      const uint32_t n_retry = __ldcg(&ctrl->n_retry);
+      for (uint32_t i = queue_pop(&ctrl->retry_pop, &s_item); i < n_retry;
+           i = queue_pop(&ctrl->retry_pop, &s_item)) {
+        const uint32_t g = __ldcg(A.retry_list + i);
+        if (!BCHECK(i < A.num_req && g < A.num_req, 17, i, g)) continue;
+        cta_finish(g);
+      }
     }
   }
   __syncthreads();

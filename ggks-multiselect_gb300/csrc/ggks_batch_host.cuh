@@ -171,6 +171,7 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
 
   // ---- workspace: [ctrl | probs | tiles | reqs] is uploaded in one copy
   const size_t A = 256;
+  static_assert(sizeof(BCtrl) <= A, "the control block fills one aligned slot");
   size_t o = 0;
   auto arr = [&](size_t elems, size_t esz) {
     const size_t at = o;
@@ -192,7 +193,8 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
                o_kcnt = arr(R, 4), o_kcur = arr(R, 4), o_fill = arr(R, 4);
   const size_t o_seg_off = arr(R, 8), o_seg_lo = arr(R, sizeof(K)), o_seg_hi = arr(R, sizeof(K));
   const size_t o_klist = arr(R, sizeof(Req)), o_deferred = arr(R, 4);
-  const size_t o_big = arr(R, 4), o_small = arr(R, 4);
+  const size_t o_big = arr(R, 4), o_small = arr(R, 4), o_wsel = arr(R, 4),
+               o_retry = arr(R, 4);
   const size_t o_out = arr(R, sizeof(T));
   const size_t o_cand = arr(cand_words, sizeof(K)), o_ccnt = arr(num_tiles, 4);
   const size_t total = o;
@@ -262,6 +264,8 @@ int select_batch(Context &ctx, const BatchInput &in, T *d_out_user, T *h_out, cu
   a.klist = reinterpret_cast<Req *>(D + o_klist);
   a.big_list = reinterpret_cast<uint32_t *>(D + o_big);
   a.small_list = reinterpret_cast<uint32_t *>(D + o_small);
+  a.wsel_list = reinterpret_cast<uint32_t *>(D + o_wsel);
+  a.retry_list = reinterpret_cast<uint32_t *>(D + o_retry);
   a.deferred = reinterpret_cast<uint32_t *>(D + o_deferred);
   a.out = d_out;
   a.cand = D + o_cand;

@@ -283,3 +283,49 @@ def test_batch_many_slots_and_large_topk(g, orc):
     g.batch_set_tuning(ctx, 256, 1 << 20)
     _check_batch(g, orc, [a, b], [ka, kb], np.float32, "many slots", ctx=ctx)
     ctx.close()
+
+
+@pytest.mark.parametrize("spread", [300, 6000])
+def test_batch_mid_size_segments(g, orc, spread):
+    """Vectors of 2^23-2^24 elements put 1000-4000 keys in a bucket (8192
+    buckets a problem at most): a slot with at most four requests is answered
+    by one warp's radix select, one with five or more by a whole CTA.  The
+    k's: spread ranks (one request a slot), groups of three and of five
+    adjacent ranks, and ranks on a dense cluster (3000 copies of one value:
+    its bin does not fit the warp's buffer, so a CTA finishes the slot after
+    the warps); heavy duplicates, whose bins are one key wide.  300 spread
+    k's a problem leave the batch's mid-size slots to CTAs, 6000 give the
+    warps enough of them."""
+    import ggks_problems as gp
+    r = np.random.default_rng(23)
+
+    def ks_for(n, seed):
+        rr = np.random.default_rng(seed)
+        sp = gp.k_distinct(n, spread, seed)
+        base = rr.integers(10, n - 10, 40)
+        threes = (base[:20, None] + np.arange(3)).ravel()
+        fives = (base[20:, None] + np.arange(5)).ravel()
+        return np.concatenate([sp, threes, fives, [1, n]]).astype(np.uint32)
+
+    n = 1 << 23
+    a = gp.generate("f32", "normal", n, seed=1)
+    c = r.random(n).astype(np.float32)
+    c[r.choice(n, 3000, replace=False)] = np.float32(0.5)
+    below = int(np.count_nonzero(c < 0.5))
+    # two requests on the cluster (a warp tries, its CTA finishes), and the
+    # same vector with nine requests on and around it (a CTA's slot)
+    kc2 = np.concatenate([ks_for(n, 3), [n - below, n - below - 1500]])
+    kc9 = np.concatenate([n - below - np.array([0, 1, 1500, 2999]),
+                          n - below - 3000 + np.arange(-2, 1), n - below + np.arange(1, 3)])
+    _check_batch(g, orc, [a, c, c], [ks_for(n, 2), kc2.astype(np.uint32), kc9.astype(np.uint32)],
+                 np.float32, "mid f32")
+    u = gp.generate("u32", "uniform", 1 << 24, seed=4)
+    # 256 copies of each value of [0, 2^16): buckets of a few values, whose
+    # bins are one key wide (answered from the bin, however many copies)
+    v = gp.generate("u32", "uniform16", 1 << 24, seed=10)
+    _check_batch(g, orc, [u, v], [ks_for(u.size, 5), ks_for(v.size, 11)], np.uint32, "mid u32")
+    w = gp.generate("f32", "uint_valued", 1 << 23, seed=12)
+    _check_batch(g, orc, [w], [ks_for(w.size, 13)], np.float32, "mid integer-valued f32")
+    d = gp.generate("f64", "cauchy", n, seed=6)
+    e = gp.generate("f64", "normal", 3 << 21, seed=7)
+    _check_batch(g, orc, [d, e], [ks_for(n, 8), ks_for(e.size, 9)], np.float64, "mid f64")
