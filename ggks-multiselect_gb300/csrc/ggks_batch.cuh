@@ -76,6 +76,10 @@ constexpr int kBPhases = 5;
 constexpr uint64_t kBMinTile = 1u << 16;  // smallest tile the host picks for a small batch
 constexpr int kBColBatch = 4;  // tile rows per lane and load step of the plan phase's single-key scan
 constexpr uint32_t kBWarpBytes = 2048;  // shared memory of one warp-finisher buffer
+// 128-bit vectors in flight per thread in the plain counting loop of the
+// tile phases and the plain compaction loop of uint32 and float64 batches
+// (the other tile loops keep four)
+constexpr int kBTileVecs = 8;
 constexpr uint32_t kBRepBytes = 32768;  // per-bucket first keys of a tile (dup problems)
 // slots whose request counters fit in the plan phase's spare shared memory
 // (after the table, the bucket prefix and the flags: 81936 - 57360 bytes)
@@ -530,11 +534,11 @@ __device__ __forceinline__ bool finish_warp_select(const K *__restrict__ src, ui
 }
 
 // Elements [a, b) of x (any alignment): scalar head up to a 16-byte boundary,
-// a 128-bit body with four vectors in flight per thread, a scalar tail.
+// a 128-bit body with U vectors in flight per thread, a scalar tail.
 // f(key, full) is called once per element; full: all 32 lanes of the warp
 // make the same call (the unrolled body), so warp-collective operations are
 // allowed.
-template <class T, class F>
+template <class T, int U = 4, class F>
 __device__ __forceinline__ void for_range(const T *__restrict__ x, uint64_t a, uint64_t b, F &&f) {
   using K = typename Traits<T>::K;
   using V = typename Traits<T>::Vec;
@@ -546,14 +550,14 @@ __device__ __forceinline__ void for_range(const T *__restrict__ x, uint64_t a, u
   for (uint64_t e = a + threadIdx.x; e < va; e += blockDim.x) f(Traits<T>::key(x[e]), false);
   for (uint64_t e = vb + threadIdx.x; e < b; e += blockDim.x) f(Traits<T>::key(x[e]), false);
   const V *xv = reinterpret_cast<const V *>(x + va);
-  const uint64_t step = 4ull * blockDim.x;
+  const uint64_t step = (uint64_t)U * blockDim.x;
   uint64_t v0 = 0;
   for (; v0 + step <= nvec; v0 += step) {
-    V vv[4];
+    V vv[U];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) vv[u] = ldg_stream(xv + v0 + (uint64_t)u * blockDim.x + threadIdx.x);
+    for (int u = 0; u < U; ++u) vv[u] = ldg_stream(xv + v0 + (uint64_t)u * blockDim.x + threadIdx.x);
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < U; ++u) {
       K k[PV];
       vec_keys<T>(vv[u], k);
 #pragma unroll
@@ -583,16 +587,16 @@ __device__ __forceinline__ typename Traits<T>::K load_key(const void *x, uint64_
 }
 
 // for_range over a problem's vector in its own key order
-template <class T, class F>
+template <class T, int U = 4, class F>
 __device__ __forceinline__ void for_range_p(const void *x, uint32_t flt, uint64_t a, uint64_t b,
                                             F &&f) {
   if constexpr (std::is_same<T, uint32_t>::value) {
     if (flt) {
-      for_range<float>(reinterpret_cast<const float *>(x), a, b, f);
+      for_range<float, U>(reinterpret_cast<const float *>(x), a, b, f);
       return;
     }
   }
-  for_range<T>(reinterpret_cast<const T *>(x), a, b, f);
+  for_range<T, U>(reinterpret_cast<const T *>(x), a, b, f);
 }
 
 template <class T>
@@ -776,8 +780,8 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
         // also for heavy problems: the histogram's atomics return nothing, and
         // lanes adding to one counter cost no more than lanes adding to
         // different ones, so warp aggregation (compaction's) would only slow
-        // this phase down
-        for_range_p<T>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool) {
+        // this phase down.  Eight vectors in flight per thread.
+        for_range_p<T, kBTileVecs>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool) {
           const uint32_t ub = bucket_of_lane<K>(k, base, shift, lane_lut, nsl);
           if (!BCHECK(ub < H.nb, 4, ub, H.nb)) return;
           atomicAdd(&hist[swz(ub)], 1u);
@@ -1129,7 +1133,10 @@ __global__ void __launch_bounds__(kBThreads, 2) k_batch(BArgs A) {
           st_global_if(sp + pos, k, ok && pos < cap);
         });
       } else {
-        for_range_p<T>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool) {
+        // eight vectors in flight, four for float batches (whose kernel
+        // spills 256 bytes of loads with eight)
+        constexpr int CV = std::is_same<T, float>::value ? 4 : kBTileVecs;
+        for_range_p<T, CV>(P.x, P.flt, tl.begin, tl.end, [&](K k, bool) {
           uint32_t ub = bucket_of_lane<K>(k, base, shift, lane_lut, nsl);
           if (!BCHECK(ub < H.nb, 9, ub, H.nb)) return;
           const uint32_t pos = atomicAdd(&cursor[swz(ub)], 1u);
