@@ -67,6 +67,9 @@ __global__ void __launch_bounds__(1024) k_tau(const K *__restrict__ samples, uin
     const uint32_t c = ccnt[j];
     if (c) atomicAdd(&slice_cnt[j], c);
   }
+  // every thread's counts before the CTA reports done (the fence below is
+  // cumulative over what the barrier ordered)
+  __syncthreads();
   if (tid == 0) {
     __threadfence();
     s_last = (atomicAdd(&ctrl->sample_done, 1u) == gridDim.x - 1) ? 1u : 0u;
