@@ -27,6 +27,8 @@
 // keys fit; else it flags ST_TOPK_MISS and the caller runs the pipeline.
 #pragma once
 
+#include <type_traits>
+
 #include "ggks_device.cuh"
 
 namespace ggks {
@@ -112,23 +114,42 @@ __global__ void __launch_bounds__(1024) k_tau(const K *__restrict__ samples, uin
   }
   __syncthreads();
   const uint32_t jf = s_jf, r = s_r;
-  // the samples of that fine slice; their r-th smallest is tau (16 loads per
-  // thread in flight before their compares: a load and a shared atomic in
-  // one loop body would complete one at a time)
-  for (uint32_t s0 = tid; s0 < S; s0 += 16 * blockDim.x) {
-    K xs[16];
+  // the samples of that fine slice; their r-th smallest is tau.  Eight
+  // 128-bit loads per thread in flight before their compares (a load and a
+  // shared atomic in one loop body would complete one at a time): 65 536
+  // four-byte samples take two rounds.  The sample array starts 256-byte aligned; keys
+  // past its last whole vector are read one by one.
+  using SV = typename std::conditional<sizeof(K) == 4, uint4, ulonglong2>::type;
+  constexpr uint32_t PV = 16 / sizeof(K);
+  const uint32_t nv = S / PV;
+  const SV *sv = reinterpret_cast<const SV *>(samples);
+  auto take = [&](K key, bool valid) {
+    const bool in = valid && (uint32_t)((key - kmin) >> fsh) == jf;
+    const uint32_t at = warp_append(&s_cnt, in);
+    if (in && at < kTauBuf) buf[at] = key;
+  };
+  for (uint32_t v0 = tid; v0 < nv; v0 += 8 * blockDim.x) {
+    SV xs[8];
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const uint32_t q = s0 + u * blockDim.x;
-      xs[u] = q < S ? __ldcg(samples + q) : kmin;
+    for (int u = 0; u < 8; ++u) {
+      const uint32_t q = v0 + u * blockDim.x;
+      if (q < nv) xs[u] = __ldcg(sv + q);
     }
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const bool in = s0 + u * blockDim.x < S && (uint32_t)((xs[u] - kmin) >> fsh) == jf;
-      const uint32_t at = warp_append(&s_cnt, in);
-      if (in && at < kTauBuf) buf[at] = xs[u];
+    for (int u = 0; u < 8; ++u) {
+      const bool ok = v0 + u * blockDim.x < nv;
+      if constexpr (sizeof(K) == 4) {
+        take(ok ? (K)xs[u].x : kmin, ok);
+        take(ok ? (K)xs[u].y : kmin, ok);
+        take(ok ? (K)xs[u].z : kmin, ok);
+        take(ok ? (K)xs[u].w : kmin, ok);
+      } else {
+        take(ok ? (K)xs[u].x : kmin, ok);
+        take(ok ? (K)xs[u].y : kmin, ok);
+      }
     }
   }
+  for (uint32_t q = nv * PV + tid; q < S; q += blockDim.x) take(__ldcg(samples + q), true);
   __syncthreads();
   const uint32_t cnt = s_cnt;
   K t;
