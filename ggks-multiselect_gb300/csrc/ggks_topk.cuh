@@ -123,10 +123,13 @@ __global__ void __launch_bounds__(1024) k_tau(const K *__restrict__ samples, uin
   constexpr uint32_t PV = 16 / sizeof(K);
   const uint32_t nv = S / PV;
   const SV *sv = reinterpret_cast<const SV *>(samples);
+  // the slice holds a few dozen samples: a lane that finds one takes its
+  // place with its own shared atomic (no vote per key)
   auto take = [&](K key, bool valid) {
-    const bool in = valid && (uint32_t)((key - kmin) >> fsh) == jf;
-    const uint32_t at = warp_append(&s_cnt, in);
-    if (in && at < kTauBuf) buf[at] = key;
+    if (valid && (uint32_t)((key - kmin) >> fsh) == jf) {
+      const uint32_t at = atomicAdd(&s_cnt, 1u);
+      if (at < kTauBuf) buf[at] = key;
+    }
   };
   for (uint32_t v0 = tid; v0 < nv; v0 += 8 * blockDim.x) {
     SV xs[8];
